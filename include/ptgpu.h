@@ -1,0 +1,199 @@
+/*
+ * ptgpu.h -- C ABI of the GB300 timestep engine for ProjecTracer-style tracer convection.
+ *
+ * The reference (Fortran 90 + OpenMP) has no plugin interface: its hot-path subroutines take no
+ * arguments and exchange data through the module globals of basics.f90 and arrays.f90.  The entry
+ * points below replace the bodies of those subroutines; a Fortran driver binds them with
+ * iso_c_binding (the binding is shown in INTEGRATION.md).  Each declaration cites the reference
+ * routine it replaces (file:line inside ProjecTracer_Source/).
+ *
+ * Conventions
+ *  - Every function returns 0 (PT_OK) or a negative PT_ERR_* code; pt_last_error() describes it.
+ *  - Grid arrays cross the boundary in Fortran column-major order (x index i fastest) with the
+ *    reference's ghost extents; the pointer is the element at the lowest ghost index.  The extents
+ *    of each array are given by pt_field_extent().
+ *  - Tracer arrays are plain FP64 vectors of length ntr in tracer-ID order.
+ *  - The library owns all device memory; no caller pointer is retained after a call returns.
+ *  - One context per process; call from one host thread.
+ */
+#ifndef PTGPU_H
+#define PTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_OK 0
+#define PT_ERR_CONFIG (-1)               /* unsupported or inconsistent configuration */
+#define PT_ERR_TRACER_OUT_OF_DOMAIN (-2) /* composition.f90:1007-1010 ("Tracer advected outside of domain") */
+#define PT_ERR_MG_DIVERGED (-3)          /* iterative_solver.f90:438-447 (residual > 1e10 x reference) */
+#define PT_ERR_MG_MAX_CYCLES (-4)        /* iterative_solver.f90:325-334 (too many multigrid cycles) */
+#define PT_ERR_SINGULAR_COARSE (-5)      /* DGBTRF INFO>0 on the coarsest grid (unchecked in the reference) */
+#define PT_ERR_CUDA (-6)                 /* a CUDA runtime call failed */
+#define PT_ERR_STATE (-7)                /* call out of order (e.g. pt_step before pt_upload_state) */
+#define PT_ERR_ITER_CAP (-8)             /* a data-dependent smoother loop hit its iteration cap */
+#define PT_ERR_ARG (-9)                  /* bad argument (null pointer, size, field id) */
+#define PT_ERR_NOT_FINITE (-10)          /* NaN/Inf detected in a residual */
+
+/* Precision of the stream-function solve (spec extension; not in the reference). */
+#define PT_PREC_FP64 0  /* plain FP64 multigrid: the reference algorithm on the GPU */
+#define PT_PREC_MIXED 1 /* FP32 smoothing/transfers, FP64 residual + defect correction, FP64 coarse LU */
+
+/* Initial-guess mode of the stream-function solve (spec extension). */
+#define PT_GUESS_PREVIOUS 0 /* previous psi (the reference's warm start, iterative_solver.f90:134) */
+#define PT_GUESS_ZERO 1
+#define PT_GUESS_UNET 2
+
+/*
+ * Run configuration: the &inputs, &Rayleigh_numbers, &heating_conductivity and &viscosity namelist
+ * values on the hot path (basics.f90:54-66), plus Tbot_iso/Ttop_iso (basics.f90:352-353; the
+ * reference only sets them in initial_temperature, so a restart run must pass them explicitly) and
+ * the &gpu extension group.  Supported subset: order=4, uniform grid (gridX=gridZ=0), Database=2,
+ * ntype<=1 with continuous C (iC_continuous=1), temperature tracers (tracer=1), RK4 (torder=4) with
+ * RK_update=1, multigrid with the RKC1 smoother (iterate=1, MG=1, RKC1=1, splitting=0), Newtonian
+ * viscosity (non_Newtonian=0, plastic=0), constant internal heating (iheattype=0), CFL=0.
+ */
+typedef struct pt_config {
+    /* grid (&inputs) */
+    int32_t nx, nz;      /* cells in x and z; nodes are (nx+1)*(nz+1) */
+    int32_t order;       /* must be 4 */
+    int32_t grids;       /* max multigrid levels (2..6); optimize_grid may lower it */
+    int32_t mingrid;     /* min coarse size for optimize_grid */
+    int32_t Nmulti;      /* RKC1 passes per level visit */
+    int32_t vis_iter;    /* Richardson passes before restricting viscosity */
+    int32_t max_cycles;  /* multigrid cycle cap */
+    int32_t nstageS;     /* RKC1 stages */
+    int32_t comp;        /* 0 or 1: composition tracers */
+    int32_t Tbot;        /* 0 isothermal, 1 insulating bottom */
+    int32_t Vbc;         /* 0 free-slip, 1 rigid top/bottom */
+    int32_t ivis;        /* 0 isoviscous, 1 eta(T,z), 2 eta(T,C,z) */
+    int32_t iheattype;   /* must be 0 */
+    int32_t precision;   /* PT_PREC_* (&gpu group) */
+    int32_t guess_mode;  /* PT_GUESS_* (&gpu group) */
+    int64_t ntr;         /* number of tracers */
+    double aspect;
+    double tolerance;      /* multigrid residual ratio target */
+    double eig_ratio;      /* (kept for namelist fidelity; unused with RKC1) */
+    double dampingS, c_2, c_1;
+    double courant, courantT, courantC, courant_stream;
+    double RaT, RaC;       /* RaC(1) */
+    double H, Htype;       /* H and Htype(1) */
+    double conduct_factor; /* conduct_factor(1) */
+    double visP, visT, delta_visT, eig_ratio_min, visC, delta_visC;
+    double Tbot_iso, Ttop_iso;
+    double dent;           /* reference height for the entrainment statistic */
+    double inner_tol;      /* mixed precision: FP32 inner-solve reduction per refinement (0 = default 1e-4) */
+} pt_config;
+
+/* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */
+enum pt_field_id {
+    PT_F_T = 0,       /* T(-3:nx+3,-3:nz+3)         grid temperature            arrays.f90:649 */
+    PT_F_TRATIO = 1,  /* Tratio(-3:nx+3,-3:nz+3)    projected tracer T          arrays.f90:656 */
+    PT_F_TVIS = 2,    /* Tvis(-3:nx+3,-3:nz+3)      smoothed T for viscosity    arrays.f90:655 */
+    PT_F_TBUOY = 3,   /* Tbuoy(-3:nx+3,-3:nz+3)     T for buoyancy              arrays.f90:655 */
+    PT_F_CNEW = 4,    /* Cnew(1,-5:nx+5,-5:nz+5)    projected composition       arrays.f90:658 */
+    PT_F_CVIS = 5,    /* Cvis(1,-5:nx+5,-5:nz+5)                                arrays.f90:655 */
+    PT_F_CBUOY = 6,   /* Cbuoy(1,-5:nx+5,-5:nz+5)                               arrays.f90:655 */
+    PT_F_SF = 7,      /* SF(-3:nx+3,-3:nz+3)        stream function psi         arrays.f90:649 */
+    PT_F_U = 8,       /* u(-3:nx+3,-3:nz+3)                                     arrays.f90:649 */
+    PT_F_W = 9,       /* w(-3:nx+3,-3:nz+3)                                     arrays.f90:649 */
+    PT_F_VIS = 10,    /* vis_grid(-3:nx+3,-3:nz+3,1) smoothed viscosity (get only) arrays.f90:665 */
+    PT_F_NEMPTY = 11, /* nempty(0:nx,0:nz) int32 tracer count per dual cell (get only) */
+    PT_F_RHS = 12,    /* RHS(1:nx-1,1:nz-1,1) buoyancy (get only)               arrays.f90:662 */
+    PT_F_TRACER_R = 20, /* rtr(1:ntr) */
+    PT_F_TRACER_S = 21, /* str(1:ntr) */
+    PT_F_TRACER_T = 22, /* Ttr(1:ntr) */
+    PT_F_TRACER_C = 23  /* Ctr(1:ntr) */
+};
+
+/* Per-step solver telemetry (logged by the reference to stdout at iterative_solver.f90:197,338). */
+typedef struct pt_solve_info {
+    int32_t cycles;       /* multigrid cycles (FP64) or total inner cycles (mixed) */
+    int32_t refinements;  /* defect-correction passes (mixed), 0 for FP64 */
+    int32_t n_eta;        /* viscosity-smoother passes on level 1 (smoother.f90:521) */
+    int32_t n_temp;       /* temperature-smoother iterations of the last projection (smoother.f90:654) */
+    double resid_ratio;   /* final mean|r| / mean|RHS| on level 1 (FP64) */
+    double eig_fine;      /* min eigenvalue ratio on level 1 (smoother.f90:520) */
+    double ms;            /* device time of the solve in milliseconds */
+} pt_solve_info;
+
+/* Columns of stats.dat (basics.f90:427-428) for comp=1 / tracer=1, ntype=1. */
+typedef struct pt_stats {
+    double time, Tavg, vrms, Nu, Nu_bot, RaT_avg, mobility, strain_max, q1, q2, q3, q4;
+    int32_t empty_cells, tracer_min, tracer_max, pad;
+    double Cavg, entrainment;
+} pt_stats_row;
+
+/* Replaces the start-up part of main.f90:168-230 that sizes and allocates the arrays
+ * (compute_basics basics.f90:204-333, storage basics.f90:70-202, multigrid_setup
+ * multigrid_cycle.f90:1-99, FD_coefficients main.f90:499-642, derivative_eigenvalues
+ * energy.f90:632-744, eigenvalue_prep iterative_solver.f90:1232-1362, Chebyshev_prep_stream
+ * Chebyshev.f90:182-210).  Allocates all device buffers. */
+int pt_init(const pt_config* cfg);
+
+/* Releases everything pt_init allocated. */
+int pt_finalize(void);
+
+/* Text for the last non-zero return code of this thread. */
+const char* pt_last_error(void);
+
+/* Multigrid levels chosen by optimize_grid (iterative_solver.f90:1-61) after pt_init. */
+int pt_grids(void);
+
+/* Extents of a field: lo/hi index in x and z (for tracer fields, lo_x=1, hi_x=ntr, z unused).
+ * Element size in bytes is returned in *elem_bytes (8, or 4 for PT_F_NEMPTY). */
+int pt_field_extent(int field, int32_t* lo_x, int32_t* hi_x, int32_t* lo_z, int32_t* hi_z,
+                    int32_t* elem_bytes);
+
+/* Copy a host array in (Fortran layout as in pt_field_extent) / out of the device state. */
+int pt_set_field(int field, const void* host);
+int pt_get_field(int field, void* host);
+
+/* Restart read (grid.f90:46-104 with restart=1, add_layer=0) plus the post-read steps of
+ * main.f90:204-210: host arrays in the layout of the Trestart / restart_tracers records
+ * (xg,zg,T,Cnew,SF and rtr,str,Ctr,Ttr).  Applies the T, psi and C boundary conditions, projects
+ * the tracers (tracers_to_corners without smoothing), then runs smoother_time_T(T), smoother_time
+ * and load_conductivity_array.  xg/zg are checked against the uniform grid.  Sets time=0. */
+int pt_upload_state(const double* xg, const double* zg, const double* T, const double* Cnew,
+                    const double* SF, const double* rtr, const double* str, const double* Ctr,
+                    const double* Ttr);
+
+/* Download of the restart records written by print_restart (main.f90:457-496). */
+int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* str, double* Ctr,
+                      double* Ttr);
+
+/* Velocity solve at the top of a time step (main.f90:246-259): multigrid
+ * (iterative_solver.f90:124-341) then compute_velocities (momentum.f90:655-710).
+ * info may be NULL. */
+int pt_solve_psi(pt_solve_info* info);
+
+/* One call of energy_time (energy.f90:181-556): RK4 over the tracers with the velocity
+ * re-solved at stages 2-4 (RK_update=1) and the tracer->grid projection after each stage.
+ * Advances time by dt.  dt_out and info may be NULL; info accumulates the three inner solves. */
+int pt_step(double* dt_out, pt_solve_info* info);
+
+/* stats (basics.f90:363-462) on the current state: the stats.dat columns. */
+int pt_stats(pt_stats_row* out);
+
+/* tracers_to_corners (composition.f90:923-1087) on the current tracer state, with the given
+ * empty-corner fallback field T0 (Fortran layout of PT_F_T; NULL = current Tratio) and
+ * smoothing on/off (smooth_vis, basics.f90:315). */
+int pt_tracers_to_corners(const double* T0, int smooth_vis);
+
+/* Current simulation time and the RK4 time step of stability_RK4 (energy.f90:756-810). */
+int pt_time(double* time, double* dt);
+
+/* Chooses the initial guess of the next solves (PT_GUESS_*).  weights_path names a U-Net
+ * weight file for PT_GUESS_UNET (NULL otherwise). */
+int pt_set_guess_mode(int mode, const char* weights_path);
+
+/* Device time of the last call of each phase, in milliseconds: [0] advection kernels,
+ * [1] projection, [2] psi solve, [3] smoothers, [4] derivative tables; sums since pt_init. */
+int pt_phase_times(double* ms5);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PTGPU_H */

@@ -1,0 +1,203 @@
+"""Run configuration: the ``pt_config`` struct of include/ptgpu.h as a ctypes mirror.
+
+``PtConfig.from_namelist`` maps the reference's namelist (basics.f90:54-66) onto the struct;
+``workload(name)`` builds the five benchmark configurations (grid, Rayleigh numbers, viscosity
+law, tracer density) with the reference's shipped solver settings (inputs.nml) where the
+configuration does not say otherwise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+from .namelist import read_namelist
+
+PT_PREC_FP64 = 0
+PT_PREC_MIXED = 1
+PT_GUESS_PREVIOUS = 0
+PT_GUESS_ZERO = 1
+PT_GUESS_UNET = 2
+
+
+class PtConfig(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32),
+        ("nz", ctypes.c_int32),
+        ("order", ctypes.c_int32),
+        ("grids", ctypes.c_int32),
+        ("mingrid", ctypes.c_int32),
+        ("Nmulti", ctypes.c_int32),
+        ("vis_iter", ctypes.c_int32),
+        ("max_cycles", ctypes.c_int32),
+        ("nstageS", ctypes.c_int32),
+        ("comp", ctypes.c_int32),
+        ("Tbot", ctypes.c_int32),
+        ("Vbc", ctypes.c_int32),
+        ("ivis", ctypes.c_int32),
+        ("iheattype", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("guess_mode", ctypes.c_int32),
+        ("ntr", ctypes.c_int64),
+        ("aspect", ctypes.c_double),
+        ("tolerance", ctypes.c_double),
+        ("eig_ratio", ctypes.c_double),
+        ("dampingS", ctypes.c_double),
+        ("c_2", ctypes.c_double),
+        ("c_1", ctypes.c_double),
+        ("courant", ctypes.c_double),
+        ("courantT", ctypes.c_double),
+        ("courantC", ctypes.c_double),
+        ("courant_stream", ctypes.c_double),
+        ("RaT", ctypes.c_double),
+        ("RaC", ctypes.c_double),
+        ("H", ctypes.c_double),
+        ("Htype", ctypes.c_double),
+        ("conduct_factor", ctypes.c_double),
+        ("visP", ctypes.c_double),
+        ("visT", ctypes.c_double),
+        ("delta_visT", ctypes.c_double),
+        ("eig_ratio_min", ctypes.c_double),
+        ("visC", ctypes.c_double),
+        ("delta_visC", ctypes.c_double),
+        ("Tbot_iso", ctypes.c_double),
+        ("Ttop_iso", ctypes.c_double),
+        ("dent", ctypes.c_double),
+        ("inner_tol", ctypes.c_double),
+    ]
+
+    @staticmethod
+    def defaults() -> "PtConfig":
+        """Solver settings of the reference's shipped inputs.nml (velocity-solver block)."""
+        c = PtConfig()
+        c.order = 4
+        c.grids = 6
+        c.mingrid = 4
+        c.Nmulti = 1
+        c.vis_iter = 12
+        c.max_cycles = 1000
+        c.nstageS = 35
+        c.comp = 1
+        c.Tbot = 0
+        c.Vbc = 0
+        c.ivis = 0
+        c.iheattype = 0
+        c.precision = PT_PREC_FP64
+        c.guess_mode = PT_GUESS_PREVIOUS
+        c.aspect = 1.0
+        c.tolerance = 1e-3
+        c.eig_ratio = 1.0
+        c.dampingS = 1000.0
+        c.c_2 = 0.95
+        c.c_1 = 0.9
+        c.courant = 0.99
+        c.courantT = 0.99
+        c.courantC = 0.99
+        c.courant_stream = 0.99
+        c.RaT = 1e5
+        c.RaC = 0.0
+        c.H = 0.0
+        c.Htype = 0.0
+        c.conduct_factor = 1.0
+        c.visP = 1.0
+        c.visT = 1.0
+        c.delta_visT = 2.0
+        c.eig_ratio_min = 2.0
+        c.visC = 1.0
+        c.delta_visC = 1.0
+        c.Tbot_iso = 1.0
+        c.Ttop_iso = 0.0
+        c.dent = 0.5
+        c.inner_tol = 0.0
+        return c
+
+    @staticmethod
+    def from_namelist(path: str, ntr: int | None = None) -> "PtConfig":
+        return PtConfig.from_groups(read_namelist(path), ntr)
+
+    @staticmethod
+    def from_groups(g: dict, ntr: int | None = None) -> "PtConfig":
+        c = PtConfig.defaults()
+        inp = g.get("inputs", {})
+        for key in ("nx", "nz", "order", "grids", "mingrid", "Nmulti", "vis_iter", "max_cycles",
+                    "nstageS", "comp", "Tbot", "Vbc"):
+            if key.lower() in inp:
+                setattr(c, key, int(inp[key.lower()]))
+        for key in ("aspect", "tolerance", "eig_ratio", "dampingS", "c_2", "c_1", "courant",
+                    "courantT", "courantC", "courant_stream", "dent"):
+            if key.lower() in inp:
+                setattr(c, key, float(inp[key.lower()]))
+        ray = g.get("rayleigh_numbers", {})
+        c.RaT = float(ray.get("rat", c.RaT))
+        c.RaC = float(ray.get("rac(1)", c.RaC))
+        heat = g.get("heating_conductivity", {})
+        c.iheattype = int(heat.get("iheattype", 0))
+        c.H = float(heat.get("h", 0.0))
+        c.conduct_factor = float(heat.get("conduct_factor(1)", 1.0))
+        c.Htype = float(heat.get("htype(1)", 0.0))
+        vis = g.get("viscosity", {})
+        c.ivis = int(vis.get("ivis", 0))
+        for key in ("visP", "visT", "delta_visT", "eig_ratio_min"):
+            if key.lower() in vis:
+                setattr(c, key, float(vis[key.lower()]))
+        c.visC = float(vis.get("visc(1)", 1.0))
+        c.delta_visC = float(vis.get("delta_visc(1)", 1.0))
+        gpu = g.get("gpu", {})
+        c.precision = int(gpu.get("precision", c.precision))
+        c.guess_mode = int(gpu.get("guess_mode", c.guess_mode))
+        c.inner_tol = float(gpu.get("inner_tol", 0.0))
+        tpc = int(inp.get("tpc", 0))
+        c.ntr = ntr if ntr is not None else (c.nx + 1) * (c.nz + 1) * tpc
+        return c
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+    def copy(self) -> "PtConfig":
+        c = PtConfig()
+        ctypes.pointer(c)[0] = self
+        return c
+
+
+WORKLOADS = {
+    # 128x128, isoviscous, Ra_T=1e5, Ra_C=0, H=0, 20 tracers per cell, Courant 0.5, 100 steps
+    "C1": dict(nx=128, nz=128, aspect=1.0, RaT=1e5, RaC=0.0, comp=0, ivis=0, visT=1.0, visP=1.0,
+               tpc=20, courant=0.5, tolerance=1e-8, steps=100),
+    # 256x128, thermochemical, eta = exp(-ln(1e3) T), 30 tracers per cell, 500 steps
+    "C2": dict(nx=256, nz=128, aspect=2.0, RaT=1e6, RaC=5e5, comp=1, ivis=1, visT=1e3, visP=1.0,
+               tpc=30, courant=0.5, tolerance=1e-8, steps=500),
+    # 1024x512, eta = exp(-ln(1e5) T + ln(10)(1-z)), 32 tracers per cell, 200 steps, 1e-8
+    "C3": dict(nx=1024, nz=512, aspect=2.0, RaT=1e7, RaC=2e6, comp=1, ivis=1, visT=1e5, visP=10.0,
+               tpc=32, courant=0.5, tolerance=1e-8, steps=200),
+    # 512x256 learned-guess configuration (Ra_T and contrast sampled per run)
+    "C4": dict(nx=512, nz=256, aspect=2.0, RaT=1e6, RaC=2e5, comp=1, ivis=1, visT=1e2, visP=1.0,
+               tpc=16, courant=0.5, tolerance=1e-8, steps=1),
+    # 2048x1024, Ra_T=1e8, Ra_C=2e7, contrast 1e6, 30 tracers per cell, H=5, 100 steps
+    "C5": dict(nx=2048, nz=1024, aspect=2.0, RaT=1e8, RaC=2e7, comp=1, ivis=1, visT=1e5, visP=10.0,
+               tpc=30, courant=0.5, tolerance=1e-8, steps=100, H=5.0),
+}
+
+
+def workload(name: str, scale: float = 1.0, precision: int = PT_PREC_FP64) -> tuple[PtConfig, dict]:
+    """Configuration for a named workload; ``scale`` < 1 shrinks the grid by powers of two
+    (used for CPU-sized parity cases of the same physics)."""
+    w = dict(WORKLOADS[name])
+    c = PtConfig.defaults()
+    div = 1
+    if scale < 1.0:
+        div = 2 ** int(round(-math.log2(scale)))
+    c.nx = w["nx"] // div
+    c.nz = w["nz"] // div
+    c.aspect = w["aspect"]
+    c.RaT = w["RaT"]
+    c.RaC = w["RaC"]
+    c.comp = w["comp"]
+    c.ivis = w["ivis"]
+    c.visT = w["visT"]
+    c.visP = w["visP"]
+    c.courant = w["courant"]
+    c.tolerance = w["tolerance"]
+    c.H = w.get("H", 0.0)
+    c.precision = precision
+    c.ntr = c.nx * c.nz * w["tpc"]
+    return c, w
