@@ -1,0 +1,449 @@
+// pt_api.cu -- the C ABI of include/ptgpu.h: context set-up, field exchange, the restart upload
+// and the time-step orchestration (energy_time, energy.f90:181-556) on one CUDA stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "pt_consts.cuh"
+
+namespace pt {
+
+Engine* g_eng = nullptr;
+thread_local std::string g_err;
+
+int upload_consts_fields(const Engine& E);
+int upload_consts_tracers(const Engine& E);
+int upload_consts_mg(const Engine& E);
+int upload_consts_mixed(const Engine& E);
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return 0;
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return PT_ERR_CUDA;
+}
+
+PhaseTimer::PhaseTimer(Engine& e, int s) : E(e), slot(s) {
+    if (E.ev0) cudaEventRecord(E.ev0, E.st);
+}
+PhaseTimer::~PhaseTimer() {
+    if (!E.ev0) return;
+    cudaEventRecord(E.ev1, E.st);
+    if (cudaEventSynchronize(E.ev1) == cudaSuccess) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+        E.phase_ms[slot] += ms;
+    }
+}
+
+static int dalloc(Engine& E, double** p, size_t n) {
+    CK(cudaMalloc(p, n * sizeof(double)));
+    CK(cudaMemsetAsync(*p, 0, n * sizeof(double), E.st));
+    E.bytes_allocated += n * sizeof(double);
+    return 0;
+}
+static int ialloc(Engine& E, int32_t** p, size_t n) {
+    CK(cudaMalloc(p, n * sizeof(int32_t)));
+    CK(cudaMemsetAsync(*p, 0, n * sizeof(int32_t), E.st));
+    E.bytes_allocated += n * sizeof(int32_t);
+    return 0;
+}
+
+static int engine_alloc(Engine& E) {
+    int rc;
+    const size_t n1 = E.g1.elems();
+    double** fine[] = {&E.T, &E.Tratio, &E.Tvis, &E.Tbuoy, &E.Cnew, &E.Cvis, &E.Cbuoy, &E.SF, &E.u, &E.w,
+                       &E.cond, &E.cond_r, &E.cond_s, &E.tsa, &E.Text, &E.T0, &E.C0, &E.scratch, &E.psi_keep};
+    for (auto p : fine)
+        if ((rc = dalloc(E, p, n1))) return rc;
+    for (int f = 0; f < 3; f++)
+        for (int j = 0; j < 3; j++)
+            if ((rc = dalloc(E, &E.der[f][j], n1))) return rc;
+    const int ncell = (E.K.nx + 1) * (E.K.nz + 1);
+    if ((rc = ialloc(E, &E.nempty, (size_t)ncell))) return rc;
+    if ((rc = dalloc(E, &E.red, (size_t)(4 * (E.K.nz + 1) + 64)))) return rc;
+    if ((rc = dalloc(E, &E.dscal, 32))) return rc;
+    CK(cudaMallocHost(&E.hscal, 64 * sizeof(double)));
+    CK(cudaMalloc(&E.derr, sizeof(int)));
+    CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
+    const size_t nt = (size_t)E.ntr;
+    double** trc[] = {&E.rtr, &E.str, &E.Ttr, &E.Ctr, &E.rtr0, &E.str0, &E.Ttr0,
+                      &E.rtr1, &E.str1, &E.Ttr1, &E.rtr2, &E.str2, &E.Ttr2};
+    for (auto p : trc)
+        if ((rc = dalloc(E, p, nt))) return rc;
+    if ((rc = ialloc(E, &E.tcell, nt))) return rc;
+    if ((rc = ialloc(E, &E.clist, nt))) return rc;
+    if ((rc = ialloc(E, &E.ccount, (size_t)ncell))) return rc;
+    if ((rc = ialloc(E, &E.cstart, (size_t)ncell))) return rc;
+    if ((rc = ialloc(E, &E.scan_tmp, (size_t)ncell + (size_t)ncell / 1024 + 64))) return rc;
+    if ((rc = dalloc(E, &E.cpart, (size_t)27 * ncell))) return rc;
+    if ((rc = mg_alloc(E))) return rc;
+    return 0;
+}
+
+static void engine_free(Engine& E) {
+    double** fine[] = {&E.T, &E.Tratio, &E.Tvis, &E.Tbuoy, &E.Cnew, &E.Cvis, &E.Cbuoy, &E.SF, &E.u, &E.w,
+                       &E.cond, &E.cond_r, &E.cond_s, &E.tsa, &E.Text, &E.T0, &E.C0, &E.scratch, &E.psi_keep,
+                       &E.red, &E.dscal, &E.cpart, &E.rtr, &E.str, &E.Ttr, &E.Ctr, &E.rtr0, &E.str0,
+                       &E.Ttr0, &E.rtr1, &E.str1, &E.Ttr1, &E.rtr2, &E.str2, &E.Ttr2, &E.Mc, &E.Bc, &E.RowB};
+    for (auto p : fine)
+        if (*p) { cudaFree(*p); *p = nullptr; }
+    for (int f = 0; f < 3; f++)
+        for (int j = 0; j < 3; j++)
+            if (E.der[f][j]) cudaFree(E.der[f][j]);
+    for (int l = 0; l < PT_MAXLEV; l++) {
+        double* arrs[] = {E.err[l], E.S0[l], E.S1[l], E.S2[l], E.RHS[l], E.res[l], E.dtst[l], E.ratio[l],
+                          E.vis[l], E.visst[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l],
+                          E.vxxmzz[l], E.vsm[l], E.visw[l]};
+        for (auto a : arrs)
+            if (a) cudaFree(a);
+        float* farrs[] = {E.ferr[l], E.fS1[l], E.fS2[l], E.fRHS[l], E.fres[l], E.fcoef[l]};
+        for (auto a : farrs)
+            if (a) cudaFree(a);
+    }
+    for (int q = PT_MAXLEV; q < 11; q++)
+        if (E.visw[q]) cudaFree(E.visw[q]);
+    int32_t* ia[] = {E.nempty, E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp};
+    for (auto a : ia)
+        if (a) cudaFree(a);
+    if (E.ipiv) cudaFree(E.ipiv);
+    if (E.derr) cudaFree(E.derr);
+    if (E.hscal) cudaFreeHost(E.hscal);
+    if (E.ev0) cudaEventDestroy(E.ev0);
+    if (E.ev1) cudaEventDestroy(E.ev1);
+    if (E.st) cudaStreamDestroy(E.st);
+}
+
+static Geo make_geo(int nx, int nz) {
+    Geo g;
+    g.nx = nx;
+    g.nz = nz;
+    g.pitch = ((nx + 2 * GH + 1) + 15) / 16 * 16;
+    return g;
+}
+
+static int need(int ok) { return ok ? 0 : fail(PT_ERR_STATE, "call pt_init (and pt_upload_state) first"); }
+
+// host (Fortran layout, ghost gh) <-> device (ghost GH, pitch)
+static int field_ghost(int id) {
+    switch (id) {
+        case PT_F_CNEW: case PT_F_CVIS: case PT_F_CBUOY: return 5;
+        default: return 3;
+    }
+}
+static double* field_ptr(Engine& E, int id) {
+    switch (id) {
+        case PT_F_T: return E.T;
+        case PT_F_TRATIO: return E.Tratio;
+        case PT_F_TVIS: return E.Tvis;
+        case PT_F_TBUOY: return E.Tbuoy;
+        case PT_F_CNEW: return E.Cnew;
+        case PT_F_CVIS: return E.Cvis;
+        case PT_F_CBUOY: return E.Cbuoy;
+        case PT_F_SF: return E.SF;
+        case PT_F_U: return E.u;
+        case PT_F_W: return E.w;
+        case PT_F_VIS: return E.vis[1];
+        case PT_F_RHS: return E.RHS[1];
+        case PT_F_TRACER_R: return E.rtr;
+        case PT_F_TRACER_S: return E.str;
+        case PT_F_TRACER_T: return E.Ttr;
+        case PT_F_TRACER_C: return E.Ctr;
+        default: return nullptr;
+    }
+}
+
+static int copy_grid(Engine& E, int id, void* host, bool to_device) {
+    double* d = field_ptr(E, id);
+    if (!d) return fail(PT_ERR_ARG, "unknown field id");
+    int gh = field_ghost(id), lo = -gh, hix = E.K.nx + gh, hiz = E.K.nz + gh;
+    if (id == PT_F_RHS) { lo = 1; hix = E.K.nx - 1; hiz = E.K.nz - 1; }
+    size_t w = (size_t)(hix - lo + 1), h = (size_t)(hiz - lo + 1);
+    double* dp = d + E.g1.at(lo, lo);
+    cudaError_t e;
+    if (to_device)
+        e = cudaMemcpy2DAsync(dp, E.g1.pitch * 8, host, w * 8, w * 8, h, cudaMemcpyHostToDevice, E.st);
+    else
+        e = cudaMemcpy2DAsync(host, w * 8, dp, E.g1.pitch * 8, w * 8, h, cudaMemcpyDeviceToHost, E.st);
+    CK(e);
+    CK(cudaStreamSynchronize(E.st));
+    return 0;
+}
+
+}  // namespace pt
+
+using namespace pt;
+
+extern "C" {
+
+const char* pt_last_error(void) { return g_err.c_str(); }
+
+int pt_init(const pt_config* cfg) {
+    if (!cfg) return fail(PT_ERR_ARG, "null config");
+    if (g_eng) pt_finalize();
+    Engine* E = new Engine();
+    E->cfg = *cfg;
+    E->ntr = cfg->ntr;
+    int rc = setup_constants(*E);
+    if (rc) { delete E; return rc; }
+    if (cfg->precision != PT_PREC_FP64 && cfg->precision != PT_PREC_MIXED) {
+        delete E;
+        return fail(PT_ERR_CONFIG, "precision must be PT_PREC_FP64 or PT_PREC_MIXED");
+    }
+    if ((int64_t)cfg->ntr > 2000000000LL) { delete E; return fail(PT_ERR_CONFIG, "ntr above 2e9 is not supported"); }
+    E->g1 = make_geo(cfg->nx, cfg->nz);
+    for (int l = 1; l <= E->grids; l++) E->gl[l] = make_geo(E->L[l].nx, E->L[l].nz);
+    if ((rc = cuda_check(cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking), "stream"))) { delete E; return rc; }
+    cudaEventCreate(&E->ev0);
+    cudaEventCreate(&E->ev1);
+    g_eng = E;
+    if ((rc = engine_alloc(*E)) || (rc = upload_consts_fields(*E)) || (rc = upload_consts_tracers(*E)) ||
+        (rc = upload_consts_mg(*E)) || (rc = upload_consts_mixed(*E))) {
+        std::string msg = g_err;
+        pt_finalize();
+        g_err = msg;
+        return rc;
+    }
+    rc = cuda_check(cudaStreamSynchronize(E->st), "init");
+    return rc;
+}
+
+int pt_finalize(void) {
+    if (!g_eng) return 0;
+    engine_free(*g_eng);
+    delete g_eng;
+    g_eng = nullptr;
+    return 0;
+}
+
+int pt_grids(void) { return g_eng ? g_eng->grids : 0; }
+
+int pt_field_extent(int field, int32_t* lo_x, int32_t* hi_x, int32_t* lo_z, int32_t* hi_z, int32_t* elem_bytes) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    Engine& E = *g_eng;
+    int32_t a = 0, b = 0, c = 0, d = 0, eb = 8;
+    if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) { a = 1; b = (int32_t)E.ntr; }
+    else if (field == PT_F_NEMPTY) { a = 0; b = E.K.nx; c = 0; d = E.K.nz; eb = 4; }
+    else if (field == PT_F_RHS) { a = 1; b = E.K.nx - 1; c = 1; d = E.K.nz - 1; }
+    else if (field_ptr(E, field)) { int g = field_ghost(field); a = -g; b = E.K.nx + g; c = -g; d = E.K.nz + g; }
+    else return fail(PT_ERR_ARG, "unknown field id");
+    if (lo_x) *lo_x = a;
+    if (hi_x) *hi_x = b;
+    if (lo_z) *lo_z = c;
+    if (hi_z) *hi_z = d;
+    if (elem_bytes) *elem_bytes = eb;
+    return 0;
+}
+
+int pt_set_field(int field, const void* host) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (!host) return fail(PT_ERR_ARG, "null pointer");
+    Engine& E = *g_eng;
+    if (field == PT_F_NEMPTY || field == PT_F_VIS || field == PT_F_RHS) return fail(PT_ERR_ARG, "field is read-only");
+    if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) {
+        CK(cudaMemcpy(field_ptr(E, field), host, sizeof(double) * (size_t)E.ntr, cudaMemcpyHostToDevice));
+        return 0;
+    }
+    return copy_grid(E, field, const_cast<void*>(host), true);
+}
+
+int pt_get_field(int field, void* host) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (!host) return fail(PT_ERR_ARG, "null pointer");
+    Engine& E = *g_eng;
+    CK(cudaStreamSynchronize(E.st));
+    if (field == PT_F_NEMPTY) {
+        CK(cudaMemcpy(host, E.nempty, sizeof(int32_t) * (size_t)(E.K.nx + 1) * (E.K.nz + 1), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+    if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) {
+        CK(cudaMemcpy(host, field_ptr(E, field), sizeof(double) * (size_t)E.ntr, cudaMemcpyDeviceToHost));
+        return 0;
+    }
+    return copy_grid(E, field, host, false);
+}
+
+int pt_upload_state(const double* xg, const double* zg, const double* T, const double* Cnew, const double* SF,
+                    const double* rtr, const double* str, const double* Ctr, const double* Ttr) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    Engine& E = *g_eng;
+    if (!xg || !zg || !T || !SF || !rtr || !str || !Ttr || (E.cfg.comp && (!Cnew || !Ctr)))
+        return fail(PT_ERR_ARG, "null pointer in restart arrays");
+    const int nx = E.K.nx, nz = E.K.nz;
+    for (int i = 0; i <= nx; i++)
+        if (std::fabs(xg[i + 6] - E.K.dr * i) > 1e-12 * E.K.aspect)
+            return fail(PT_ERR_CONFIG, "xg is not the uniform grid (stretched grids are not supported)");
+    for (int k = 0; k <= nz; k++)
+        if (std::fabs(zg[k + 6] - E.K.ds * k) > 1e-12) return fail(PT_ERR_CONFIG, "zg is not the uniform grid");
+    int rc;
+    double* zero_these[] = {E.T, E.Tratio, E.Tvis, E.Tbuoy, E.Cnew, E.Cvis, E.Cbuoy, E.SF, E.u, E.w};
+    for (auto p : zero_these) CK(cudaMemsetAsync(p, 0, E.g1.elems() * 8, E.st));
+    for (int l = 1; l <= E.grids; l++) CK(cudaMemsetAsync(E.err[l], 0, E.gl[l].elems() * 8, E.st));
+    if ((rc = copy_grid(E, PT_F_T, const_cast<double*>(T), true))) return rc;
+    if ((rc = copy_grid(E, PT_F_SF, const_cast<double*>(SF), true))) return rc;
+    if (E.cfg.comp && (rc = copy_grid(E, PT_F_CNEW, const_cast<double*>(Cnew), true))) return rc;
+    const size_t nb = sizeof(double) * (size_t)E.ntr;
+    CK(cudaMemcpyAsync(E.rtr, rtr, nb, cudaMemcpyHostToDevice, E.st));
+    CK(cudaMemcpyAsync(E.str, str, nb, cudaMemcpyHostToDevice, E.st));
+    CK(cudaMemcpyAsync(E.Ttr, Ttr, nb, cudaMemcpyHostToDevice, E.st));
+    if (E.cfg.comp) CK(cudaMemcpyAsync(E.Ctr, Ctr, nb, cudaMemcpyHostToDevice, E.st));
+    // grid.f90:67-73: boundary conditions on the restart fields
+    if ((rc = enforce_bcs_T(E, E.T))) return rc;
+    if ((rc = enforce_bcs_stream(E, 1, E.SF))) return rc;
+    if (E.cfg.comp && (rc = enforce_bcs_C(E, E.Cnew))) return rc;
+    // grid.f90:93-95: projection without smoothing, then main.f90:205-209
+    if ((rc = project(E, E.rtr, E.str, E.Ttr, E.T, 0))) return rc;
+    if ((rc = smoother_time_T(E, E.T))) return rc;
+    if (E.cfg.comp && (rc = smoother_time_C(E))) return rc;
+    if ((rc = load_conductivity(E))) return rc;
+    E.time = 0.0;
+    E.have_mass = 0;
+    E.uploaded = 1;
+    CK(cudaStreamSynchronize(E.st));
+    return 0;
+}
+
+int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* str, double* Ctr, double* Ttr) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    int rc;
+    if (T && (rc = pt_get_field(PT_F_T, T))) return rc;
+    if (Cnew && (rc = pt_get_field(PT_F_CNEW, Cnew))) return rc;
+    if (SF && (rc = pt_get_field(PT_F_SF, SF))) return rc;
+    if (rtr && (rc = pt_get_field(PT_F_TRACER_R, rtr))) return rc;
+    if (str && (rc = pt_get_field(PT_F_TRACER_S, str))) return rc;
+    if (Ctr && (rc = pt_get_field(PT_F_TRACER_C, Ctr))) return rc;
+    if (Ttr && (rc = pt_get_field(PT_F_TRACER_T, Ttr))) return rc;
+    return 0;
+}
+
+static int solve_psi(Engine& E, pt_solve_info* info) {
+    int rc;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, E.st);
+    if (E.cfg.guess_mode == PT_GUESS_ZERO) CK(cudaMemsetAsync(E.SF, 0, E.g1.elems() * 8, E.st));
+    rc = (E.cfg.precision == PT_PREC_MIXED) ? multigrid_mixed(E, info) : multigrid(E, info);
+    if (!rc) rc = compute_velocities(E);
+    cudaEventRecord(b, E.st);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (info) {
+        info->ms += ms;
+        info->n_temp = E.n_temp;
+        info->refinements += E.refinements;
+    }
+    return rc;
+}
+
+int pt_solve_psi(pt_solve_info* info) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    if (info) std::memset(info, 0, sizeof *info);
+    return solve_psi(*g_eng, info);
+}
+
+static int stage_tables(Engine& E) {
+    int rc;
+    if ((rc = load_tracer_space(E))) return rc;
+    return compute_derivatives(E, E.tsa, 2);
+}
+static int velocity_tables(Engine& E) {
+    int rc;
+    if ((rc = compute_derivatives(E, E.u, 0))) return rc;
+    return compute_derivatives(E, E.w, 1);
+}
+
+int pt_step(double* dt_out, pt_solve_info* info) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    Engine& E = *g_eng;
+    if (info) std::memset(info, 0, sizeof *info);
+    int rc;
+    if ((rc = stability_dt(E, &E.dt))) return rc;
+    const int comp = E.cfg.comp;
+    const size_t nb = sizeof(double) * (size_t)E.ntr;
+    if (comp && (rc = copy_field(E, E.C0, E.Cnew))) return rc;
+    if ((rc = copy_field(E, E.T0, E.Tratio))) return rc;
+    CK(cudaMemcpyAsync(E.Ttr0, E.Ttr, nb, cudaMemcpyDeviceToDevice, E.st));
+    CK(cudaMemcpyAsync(E.rtr0, E.rtr, nb, cudaMemcpyDeviceToDevice, E.st));
+    CK(cudaMemcpyAsync(E.str0, E.str, nb, cudaMemcpyDeviceToDevice, E.st));
+    // stage 1
+    if ((rc = stage_tables(E)) || (rc = velocity_tables(E)) || (rc = rk_stage(E, 1))) return rc;
+    // stages 2-4: project the stage positions, re-solve psi, advance
+    const double* sr[3] = {E.rtr1, E.rtr2, E.rtr1};
+    const double* ss[3] = {E.str1, E.str2, E.str1};
+    const double* sT[3] = {E.Ttr1, E.Ttr2, E.Ttr1};
+    for (int st = 2; st <= 4; st++) {
+        if (comp && st > 2 && (rc = copy_field(E, E.Cnew, E.C0))) return rc;
+        if ((rc = project(E, sr[st - 2], ss[st - 2], sT[st - 2], E.T0, 1))) return rc;
+        if ((rc = stage_tables(E))) return rc;
+        if ((rc = solve_psi(E, info))) return rc;
+        if ((rc = velocity_tables(E)) || (rc = rk_stage(E, st))) return rc;
+    }
+    // wrap-up
+    if (comp && (rc = copy_field(E, E.Cnew, E.C0))) return rc;
+    if ((rc = project(E, E.rtr, E.str, E.Ttr, E.T0, 1))) return rc;
+    if ((rc = copy_field(E, E.T, E.Tratio))) return rc;
+    E.time = E.time + E.dt;
+    if (dt_out) *dt_out = E.dt;
+    if (info) info->n_temp = E.n_temp;
+    CK(cudaStreamSynchronize(E.st));
+    return 0;
+}
+
+int pt_stats(pt_stats_row* out) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    if (!out) return fail(PT_ERR_ARG, "null pointer");
+    return stats(*g_eng, out);
+}
+
+int pt_tracers_to_corners(const double* T0, int smooth_vis) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    Engine& E = *g_eng;
+    int rc;
+    if (T0) {
+        if ((rc = copy_grid(E, PT_F_TRATIO, const_cast<double*>(T0), true))) return rc;
+    }
+    rc = project(E, E.rtr, E.str, E.Ttr, E.Tratio, smooth_vis);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(E.st), "projection");
+    return rc;
+}
+
+int pt_time(double* time, double* dt) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (time) *time = g_eng->time;
+    if (dt) {
+        int rc = stability_dt(*g_eng, &g_eng->dt);
+        if (rc) return rc;
+        *dt = g_eng->dt;
+    }
+    return 0;
+}
+
+int pt_set_guess_mode(int mode, const char* weights_path) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (mode != PT_GUESS_PREVIOUS && mode != PT_GUESS_ZERO && mode != PT_GUESS_UNET)
+        return fail(PT_ERR_ARG, "unknown guess mode");
+    if (mode == PT_GUESS_UNET) {
+        (void)weights_path;
+        return fail(PT_ERR_CONFIG, "U-Net guess is not available in this build");
+    }
+    g_eng->cfg.guess_mode = mode;
+    return 0;
+}
+
+int pt_phase_times(double* ms5) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (!ms5) return fail(PT_ERR_ARG, "null pointer");
+    for (int q = 0; q < 5; q++) ms5[q] = g_eng->phase_ms[q];
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+// pt_internal.h -- device state and kernel interfaces of libptgpu (not part of the C ABI).
+//
+// Grid layout in HBM: every grid array (physical fields on the fine grid and the multigrid level
+// arrays) stores node (i,k) at  p[(i+GH) + (k+GH)*pitch]  with a uniform ghost width GH=5 and a
+// row pitch rounded up to 16 doubles (128 B), x fastest as in the reference's column-major
+// arrays.  Ghost width 5 covers the widest reference extent (spanT=5 for C, conductivity and the
+// extended T); fields with 3 ghosts simply leave the outer two unused.
+// Tracers are structure-of-arrays FP64 vectors in tracer-ID order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ptgpu.h"
+
+#define GH 5
+#define PT_MAXLEV 8
+
+namespace pt {
+
+struct Geo {
+    int nx, nz, pitch;
+    size_t elems() const { return (size_t)pitch * (size_t)(nz + 2 * GH + 1); }
+    __host__ __device__ inline size_t at(int i, int k) const {
+        return (size_t)(i + GH) + (size_t)(k + GH) * (size_t)pitch;
+    }
+};
+
+// constants of one multigrid level (uniform grid: eigenvalue symbols are per-level scalars)
+struct LevConst {
+    int nx, nz;
+    double dr, ds, dr2, ds2, dr3, ds3, dr4, ds4, drds, drds2, dr2ds, dr2ds2;
+    double SR1, SR2, SR4, SR5, SR6, SI1, SI2, SI4, SI5, SI6;
+    double dt_vis;
+};
+
+// stencils and scalars shared by the kernels (copied to __constant__ memory)
+struct Consts {
+    double D1[7], D2[7], D3[7], D4[7];
+    double Dm[5][7];  // D(1..4,-3:3)
+    double Drs[5][5], Drss[5][5], Drrs[5][5], Drrss[5][5];  // [i+2][k+2]
+    double D1so[3], D2so[3], Drsso[3][3];                    // [i+1][k+1]
+    double SM1[7][7], SM2[7][7], SM4[7][7], SM5[7][7], SM6[7][7];  // [di+3][dk+3]
+    double mewt[64], mew[64], vv[64], cc[64];
+    double dr, ds, dr2, ds2, inv_dr, inv_ds, aspect;
+    double dr_pow[4], ds_pow[4], fact[4];
+    int exact_div;  // dr and ds are powers of two: x/dr == x*inv_dr exactly
+    double two_over_D20;
+    double Tbot_iso, Ttop_iso, H, Htype, conduct_factor;
+    double RaT, RaC, lvisT, lvisP, lvisC;
+    int nx, nz, comp, Tbot, Vbc, ivis;
+};
+
+struct Engine {
+    pt_config cfg;
+    Consts K;
+    LevConst L[PT_MAXLEV];
+    int grids = 0, nsteps = 0, multi[64];
+    double RKC1_stability = 0, delta_T = 2, delta_C = 2, dts = 0;
+    double Tr_base = 0, Trr_base = 0, Trrr_base = 0, Trrrr_base = 0, Trs_base = 0, Trrs_base = 0,
+           Trrss_base = 0, Tr_base_so = 0, Trr_base_so = 0;
+    int kl = 0, ku = 0, ngc = 0, kent = 0;
+    Geo g1;        // fine-grid geometry
+    Geo gl[PT_MAXLEV];
+    cudaStream_t st = nullptr;
+    // physical fields (fine geometry)
+    double *T = nullptr, *Tratio = nullptr, *Tvis = nullptr, *Tbuoy = nullptr, *Cnew = nullptr,
+           *Cvis = nullptr, *Cbuoy = nullptr, *SF = nullptr, *u = nullptr, *w = nullptr,
+           *cond = nullptr, *cond_r = nullptr, *cond_s = nullptr, *tsa = nullptr, *Text = nullptr,
+           *T0 = nullptr, *C0 = nullptr, *scratch = nullptr;
+    double* der[3][3] = {};  // derivative tables: [field u,w,tsa][order 1..3]
+    double* coef[3] = {};    // 16 Taylor coefficients per node per field (advection)
+    int32_t* nempty = nullptr;
+    // multigrid
+    double *err[PT_MAXLEV] = {}, *S0[PT_MAXLEV] = {}, *S1[PT_MAXLEV] = {}, *S2[PT_MAXLEV] = {},
+           *RHS[PT_MAXLEV] = {}, *res[PT_MAXLEV] = {}, *dtst[PT_MAXLEV] = {}, *ratio[PT_MAXLEV] = {},
+           *vis[PT_MAXLEV] = {}, *visst[PT_MAXLEV] = {}, *vx[PT_MAXLEV] = {}, *vz[PT_MAXLEV] = {},
+           *vxx[PT_MAXLEV] = {}, *vzz[PT_MAXLEV] = {}, *vxz[PT_MAXLEV] = {}, *vxxpzz[PT_MAXLEV] = {},
+           *vxxmzz[PT_MAXLEV] = {}, *vsm[PT_MAXLEV] = {}, *visw[PT_MAXLEV] = {};
+    // mixed precision mirrors
+    float *ferr[PT_MAXLEV] = {}, *fS1[PT_MAXLEV] = {}, *fS2[PT_MAXLEV] = {}, *fRHS[PT_MAXLEV] = {},
+          *fres[PT_MAXLEV] = {}, *fcoef[PT_MAXLEV] = {};
+    double* psi_keep = nullptr;
+    // coarse band LU
+    double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
+    int* ipiv = nullptr;
+    // reductions
+    double* red = nullptr;       // partial sums scratch
+    double* dscal = nullptr;     // device scalars
+    double* hscal = nullptr;     // pinned host mirror
+    int* derr = nullptr;         // device error word
+    // tracers
+    int64_t ntr = 0;
+    double *rtr = nullptr, *str = nullptr, *Ttr = nullptr, *Ctr = nullptr, *rtr0 = nullptr,
+           *str0 = nullptr, *Ttr0 = nullptr, *rtr1 = nullptr, *str1 = nullptr, *Ttr1 = nullptr,
+           *rtr2 = nullptr, *str2 = nullptr, *Ttr2 = nullptr;
+    int32_t *tcell = nullptr, *cstart = nullptr, *ccount = nullptr, *clist = nullptr;
+    double* cpart = nullptr;  // 27 partial sums per cell
+    int32_t* scan_tmp = nullptr;
+    // state
+    double time = 0, dt = 0;
+    int uploaded = 0;
+    double mass = 0;
+    int have_mass = 0;
+    int n_eta = 0, n_temp = 0, cycles = 0, refinements = 0;
+    double eig_fine = 0, resid_ratio = 0, res_ref[PT_MAXLEV] = {}, residual_mag1 = 0;
+    double phase_ms[5] = {};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t bytes_allocated = 0;
+};
+
+extern Engine* g_eng;
+extern thread_local std::string g_err;
+
+int fail(int code, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+#define CK(x)                                                \
+    do {                                                     \
+        int _rc = pt::cuda_check((x), #x);                   \
+        if (_rc) return _rc;                                 \
+    } while (0)
+#define CKL(what)                                            \
+    do {                                                     \
+        int _rc = pt::cuda_check(cudaGetLastError(), what);  \
+        if (_rc) return _rc;                                 \
+    } while (0)
+
+// host setup (pt_setup.cpp)
+int setup_constants(Engine& E);
+
+// constant upload (pt_fields.cu)
+int upload_consts(const Engine& E);
+
+// fine-grid field kernels (pt_fields.cu)
+int enforce_bcs_T(Engine& E, double* f);             // enforceBCs, energy.f90:558-592
+int enforce_bcs_C(Engine& E, double* f);             // enforceBCs_comp, composition.f90:1279-1292
+int enforce_bcs_stream(Engine& E, int level, double* f);  // iterative_solver.f90:1616-1664
+int smoother_time_T(Engine& E, const double* Tin);   // smoother.f90:638-672
+int smoother_time_C(Engine& E);                      // smoother.f90:582-636
+int load_conductivity(Engine& E);                    // energy.f90:59-86
+int load_tracer_space(Engine& E);                    // energy.f90:154-179 (+extendT 595-630)
+int compute_derivatives(Engine& E, const double* f, int which);  // composition.f90:1457-1478
+int compute_velocities(Engine& E);                   // momentum.f90:655-710
+int stability_dt(Engine& E, double* dt);             // energy.f90:756-810
+int stats(Engine& E, pt_stats_row* out);             // basics.f90:363-462
+int copy_field(Engine& E, double* dst, const double* src);
+
+// tracers (pt_tracers.cu)
+int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f,
+            int smooth);                              // composition.f90:923-1087
+int rk_stage(Engine& E, int stage);                   // energy.f90:258-536 tracer loops
+
+// multigrid (pt_mg.cu)
+int multigrid(Engine& E, pt_solve_info* info);        // iterative_solver.f90:124-341
+int mg_alloc(Engine& E);
+
+// mixed precision (pt_mixed.cu)
+int multigrid_mixed(Engine& E, pt_solve_info* info);
+
+// reductions (pt_fields.cu)
+int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitch, double* out);
+int reduce_max_smoothness(Engine& E, const double* f, double* out);
+
+// device timing
+struct PhaseTimer {
+    Engine& E;
+    int slot;
+    PhaseTimer(Engine& e, int s);
+    ~PhaseTimer();
+};
+
+}  // namespace pt

@@ -1,0 +1,777 @@
+// pt_mg.cu -- the variable-viscosity biharmonic stream-function solve (FP64): multigrid driver
+// (iterative_solver.f90:124-341) with the reference's level schedule, the viscosity pipeline
+// (compute_viscosity 560-634, smoother_vis smoother.f90:454-580, viscosity_gradients 472-558,
+// test_eigenvalues 1147-1211), the RKC1 smoother (iterate_stream 1418-1614), residual (415-470),
+// transfers (restrict 1107-1125, prolong 343-396) and the coarsest-grid banded LU
+// (Compute_Matrix_coarse 1701-1844 + DGBEQU/DGBTRF/DGBTRS) -- all on the device.
+//
+// The RKC1 stage kernel fuses stream_derivatives + stream_space + the three-term recurrence +
+// enforceBCs_stream: each thread evaluates the 10 stencil derivatives of S_{j-1} at its node
+// (separable 5x5/7-point stencils), writes S_j and the antisymmetric ghost images of S_j, so one
+// launch is one stage.  Error arrays keep the reference's quirk: error(:,:,2:grids) is never
+// reset, so a coarse visit starts from the previous coarse correction.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pt_consts.cuh"
+
+namespace pt {
+
+int upload_consts_mg(const Engine& E) { return upload_tu_consts(E); }
+
+struct VisSet {
+    double *vis, *vx, *vz, *vxx, *vzz, *vxz, *vxxpzz, *vxxmzz, *vsm, *ratio, *dtst;
+};
+
+static VisSet level_set(Engine& E, int l) {
+    return VisSet{E.vis[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l], E.vxxmzz[l],
+                  E.vsm[l], E.ratio[l], E.dtst[l]};
+}
+
+// ------------------------------------------------------------------ viscosity pipeline
+// visf, rheology.f90:2-23
+__global__ void k_visf(double* visst, const double* Tvis, const double* Cvis, Geo g) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    if (i > cK.nx) return;
+    double z = (double)k * cK.ds;
+    if (k == 0) z = 0.0;
+    if (k == cK.nz) z = 1.0;
+    double v;
+    if (cK.ivis == 1) v = exp(-Tvis[g.at(i, k)] * cK.lvisT + (1.0 - z) * cK.lvisP);
+    else if (cK.ivis == 2 && cK.comp == 1) {
+        double dot = 0.0 + Cvis[g.at(i, k)] * cK.lvisC;
+        v = exp(-Tvis[g.at(i, k)] * cK.lvisT - dot + (1.0 - z) * cK.lvisP);
+    } else v = 1.0;
+    visst[g.at(i, k)] = v;
+}
+
+// viscosityBCs (iterative_solver.f90:666-690): phase 1 column ghosts over all rows (the row
+// ghosts still hold the previous values there), phase 2 row ghosts for columns 0..nx.
+__global__ void k_visbc_cols(double* v, Geo g, int nx, int nz) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 6 * (nz + 7)) return;
+    int k = idx / 6 - 3, q = idx % 6;
+    int j = q % 3 + 1;
+    if (q < 3) v[g.at(-j, k)] = v[g.at(j, k)];
+    else v[g.at(nx + j, k)] = v[g.at(nx - j, k)];
+}
+__global__ void k_visbc_rows(double* v, Geo g, int nx, int nz) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 6 * (nx + 1)) return;
+    int i = idx / 6, q = idx % 6;
+    int j = q % 3 + 1;
+    if (q < 3) v[g.at(i, -j)] = v[g.at(i, j)];
+    else v[g.at(i, nz + j)] = v[g.at(i, nz - j)];
+}
+static int vis_bcs(Engine& E, double* v, int l) {
+    const Geo& g = E.gl[l];
+    k_visbc_cols<<<nblk(6 * (g.nz + 7), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
+    k_visbc_rows<<<nblk(6 * (g.nx + 1), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
+    CKL("vis_bcs");
+    return 0;
+}
+
+// viscosity_gradients, second-order stencils (uniform grid)
+__global__ void k_vis_grad(VisSet S, Geo g, int l, int full, int ivis) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    const LevConst& L = cL[l];
+    if (i > L.nx) return;
+    size_t o = g.at(i, k);
+    if (ivis == 0) {
+        S.vx[o] = 0; S.vz[o] = 0; S.vxx[o] = 0; S.vzz[o] = 0; S.vxz[o] = 0; S.vxxpzz[o] = 0; S.vxxmzz[o] = 0;
+        return;
+    }
+    const double* v = S.vis;
+    double xx = 0.0, zz = 0.0;
+    for (int j = -1; j <= 1; j++) xx = xx + cK.D2so[j + 1] * v[g.at(i + j, k)];
+    xx = xx / L.dr2;
+    for (int j = -1; j <= 1; j++) zz = zz + cK.D2so[j + 1] * v[g.at(i, k + j)];
+    zz = zz / L.ds2;
+    if (full) {
+        double xz = 0.0, x = 0.0, z = 0.0;
+        for (int k2 = -1; k2 <= 1; k2++)
+            for (int i2 = -1; i2 <= 1; i2++) xz = xz + cK.Drsso[i2 + 1][k2 + 1] * v[g.at(i + i2, k + k2)];
+        for (int j = -1; j <= 1; j++) x = x + cK.D1so[j + 1] * v[g.at(i + j, k)];
+        for (int j = -1; j <= 1; j++) z = z + cK.D1so[j + 1] * v[g.at(i, k + j)];
+        S.vxz[o] = xz / L.drds;
+        S.vx[o] = x / L.dr;
+        S.vz[o] = z / L.ds;
+        S.vxxmzz[o] = xx - zz;
+    }
+    S.vxx[o] = xx;
+    S.vzz[o] = zz;
+    S.vxxpzz[o] = xx + zz;
+    S.vsm[o] = L.dt_vis * (xx + zz);
+}
+
+// test_eigenvalues (RKC1 branch): ratio, local pseudo-time step, min ratio
+__global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double ctemp, unsigned long long* rmin) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    const LevConst& L = cL[l];
+    double ratio = 1.0e100;
+    if (i <= L.nx - 1) {
+        size_t o = g.at(i, k);
+        double vg = S.vis[o];
+        double eI = fabs(S.vxxpzz[o] * L.SI1) + vg * L.SI2 + fabs(S.vxz[o] * L.SI4) + fabs(S.vx[o] * L.SI5) +
+                    fabs(S.vz[o] * L.SI6);
+        double eR = S.vxxmzz[o] * L.SR1 + vg * L.SR2 + S.vxz[o] * L.SR4 + S.vx[o] * L.SR5 + S.vz[o] * L.SR6;
+        ratio = fabs(eR / eI);
+        S.ratio[o] = ratio;
+        double a = eR / ae, b = eI / be;
+        S.dtst[o] = ctemp * eR / (a * a + b * b);
+    }
+    double m = fmin(ratio, 1.0e100);
+    for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) atomicMin(rmin, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void k_vis_update(double* v, const double* vsm, Geo g, int nx, int nz, double c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    if (i > nx) return;
+    size_t o = g.at(i, k);
+    v[o] = v[o] + c * vsm[o];
+}
+
+static const double kPi = 3.1415926535897932;
+
+// smoother_vis (smoother.f90:454-580) on the arrays of set S at level l
+static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record) {
+    const Geo& g = E.gl[l];
+    const int nx = g.nx, nz = g.nz, ivis = E.cfg.ivis;
+    int rc;
+    if ((rc = vis_bcs(E, S.vis, l))) return rc;
+    int option, Niter;
+    double lb, la;
+    if (interpolate == 0) { option = 1; Niter = 3; lb = -3.0; la = -2.0; }
+    else { option = 0; Niter = E.cfg.vis_iter; lb = -2.0; la = -1.0; }
+    int Nvis_store = 0, nn_store = 1, n = 0, trigger = 0;
+    double ratio_min = 1.0e100;
+    const double ae = -E.RKC1_stability / 2.0, be = (double)E.cfg.nstageS;
+    const double ctemp = E.cfg.courant_stream * (E.RKC1_stability / (ae * ae));
+    dim3 gg(nblk(nx + 1, 128), nz + 1);
+    for (int guard = 0; guard < 100000; guard++) {
+        for (int nn = nn_store; nn <= Niter; nn++) {
+            k_vis_grad<<<gg, 128, 0, E.st>>>(S, g, l, Nvis_store != 0, ivis);
+            CKL("k_vis_grad");
+            if (interpolate == 0 && (Nvis_store >= 1 || ivis == 0)) {
+                unsigned long long* d = (unsigned long long*)E.dscal;
+                unsigned long long init = (unsigned long long)__builtin_bit_cast(long long, 1.0e100);
+                CK(cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, E.st));
+                dim3 ge(nblk(nx - 1, 128), nz - 1);
+                k_test_eig<<<ge, 128, 0, E.st>>>(S, g, l, ae, be, ctemp, d);
+                CKL("k_test_eig");
+                CK(cudaMemcpyAsync(E.hscal, d, 8, cudaMemcpyDeviceToHost, E.st));
+                CK(cudaStreamSynchronize(E.st));
+                ratio_min = E.hscal[0];
+            }
+            if (option == 1) {
+                if ((Nvis_store >= 1 && ratio_min > E.cfg.eig_ratio_min) || ivis == 0 || n > 20) {
+                    if (record) { E.eig_fine = ratio_min; E.n_eta = n; }
+                    trigger = 1;
+                    break;
+                }
+            } else if (interpolate == 0) {
+                if (ratio_min > E.cfg.eig_ratio || ivis == 0) { trigger = 1; nn_store = nn; break; }
+            } else if (Nvis_store >= 1 || ivis == 0) {
+                trigger = 1;
+                break;
+            }
+            int ntemp = Niter - nn + 1;
+            double c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
+            c = 0.99 * c;
+            k_vis_update<<<gg, 128, 0, E.st>>>(S.vis, S.vsm, g, nx, nz, c);
+            CKL("k_vis_update");
+            if ((rc = vis_bcs(E, S.vis, l))) return rc;
+        }
+        if (trigger) return 0;
+        Nvis_store++;
+        nn_store = 1;
+        if (option == 1) { Niter = 6; lb = -2.0; la = -1.0; }
+        n++;
+    }
+    return fail(PT_ERR_ITER_CAP, "viscosity smoother exceeded its iteration cap");
+}
+
+// restrict_coefficients / restrict: full weighting onto coarse interior nodes
+__global__ void k_restrict(double* out, const double* in, Geo gc, Geo gf, int nxc, int nzc) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i > nxc - 1) return;
+    int ii = 2 * i, kk = 2 * k;
+    double corners = (in[gf.at(ii - 1, kk - 1)] + in[gf.at(ii - 1, kk + 1)] + in[gf.at(ii + 1, kk + 1)] + in[gf.at(ii + 1, kk - 1)]) / 16.0;
+    double sides = (in[gf.at(ii - 1, kk)] + in[gf.at(ii, kk - 1)] + in[gf.at(ii + 1, kk)] + in[gf.at(ii, kk + 1)]) / 8.0;
+    double centre = in[gf.at(ii, kk)] / 4.0;
+    out[gc.at(i, k)] = corners + sides + centre;
+}
+
+// viscosityBCs_initialize (iterative_solver.f90:636-664)
+__global__ void k_visbc_init(double* v, const double* vf, Geo g, Geo gf, int nx, int nz, int nxf, int nzf) {
+    int W = nx + 7;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * (nz + 7)) return;
+    int i = idx % W - 3, k = idx / W - 3;
+    bool xin = (i >= 0 && i <= nx), zin = (k >= 0 && k <= nz);
+    if (xin && zin && i > 0 && i < nx && k > 0 && k < nz) return;  // interior: restricted values
+    int mi = mirror_idx(i, nx), mk = mirror_idx(k, nz);
+    // boundary value of the mirrored boundary node, taken from the finer level by injection
+    double val;
+    if (mk == 0) val = vf[gf.at(2 * mi, 0)];
+    else if (mk == nz) val = vf[gf.at(2 * mi, nzf)];
+    else if (mi == 0) val = vf[gf.at(0, 2 * mk)];
+    else if (mi == nx) val = vf[gf.at(nxf, 2 * mk)];
+    else val = v[g.at(mi, mk)];  // ghost of an interior node
+    v[g.at(i, k)] = val;
+}
+
+static int compute_viscosity(Engine& E, int level) {
+    int rc;
+    const Geo& g = E.gl[level];
+    if (level == 1) {
+        dim3 gg(nblk(g.nx + 1, 128), g.nz + 1);
+        k_visf<<<gg, 128, 0, E.st>>>(E.visst[1], E.Tvis, E.Cvis, g);
+        CKL("k_visf");
+        CK(cudaMemcpyAsync(E.vis[1], E.visst[1], g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+        return smoother_vis(E, 1, 0, level_set(E, 1), 1);
+    }
+    const int lf = level - 1;
+    const Geo& gf = E.gl[lf];
+    // smooth a work copy of the finer static viscosity (the reference smooths in place and
+    // restores the finer level's arrays afterwards)
+    VisSet W{E.visw[0], E.visw[1], E.visw[2], E.visw[3], E.visw[4], E.visw[5], E.visw[6], E.visw[7],
+             E.visw[8], E.visw[9], E.visw[10]};
+    CK(cudaMemcpyAsync(W.vis, E.visst[lf], gf.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    if ((rc = smoother_vis(E, lf, 1, W, 0))) return rc;
+    dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
+    k_restrict<<<gr, 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz);
+    int tot = (g.nx + 7) * (g.nz + 7);
+    k_visbc_init<<<nblk(tot, 128), 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz, gf.nx, gf.nz);
+    CKL("restrict_coefficients");
+    CK(cudaMemcpyAsync(E.visst[level], E.vis[level], g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    return smoother_vis(E, level, 0, level_set(E, level), 0);
+}
+
+// ------------------------------------------------------------------ RHS and residual norms
+__global__ void k_rhs1(double* RHS, const double* Tb, const double* Cb, Geo g, int comp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i > cK.nx - 1) return;
+    double v = 0.0;
+    if (cK.RaT != 0.0) {
+        double tr = 0.0;
+        for (int j = -2; j <= 2; j++) tr = tr + cK.D1[3 + j] * Tb[g.at(i + j, k)];
+        v = cK.RaT * (tr / cK.dr / 1.0);
+    }
+    if (comp) {
+        double cr = 0.0;
+        for (int j = -2; j <= 2; j++) cr = cr + cK.D1[3 + j] * Cb[g.at(i + j, k)];
+        v = v - cK.RaC * (cr / cK.dr / 1.0);
+    }
+    RHS[g.at(i, k)] = v;
+}
+
+static int compute_RHS(Engine& E, int level) {
+    const Geo& g = E.gl[level];
+    dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
+    if (level == 1) k_rhs1<<<gr, 128, 0, E.st>>>(E.RHS[1], E.Tbuoy, E.Cbuoy, g, E.cfg.comp);
+    else k_restrict<<<gr, 128, 0, E.st>>>(E.RHS[level], E.res[level - 1], g, E.gl[level - 1], g.nx, g.nz);
+    CKL("compute_RHS");
+    return 0;
+}
+
+static int mean_abs(Engine& E, const double* f, int level, double* host_out) {
+    const Geo& g = E.gl[level];
+    int rc = reduce_sum_abs_interior(E, f, g.nx, g.nz, g.pitch, E.dscal + 8);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    *host_out = E.hscal[0] / (double)(g.nx - 2) / (double)(g.nz - 2);
+    return 0;
+}
+
+// ------------------------------------------------------------------ RKC1 stage kernel
+struct StreamOp {
+    const double *vis, *vx, *vz, *vxz, *vxxmzz, *rhs, *dtst;
+};
+
+// -(stream operator - RHS) at node (i,k) of S (stream_derivatives + stream_space)
+__device__ __forceinline__ double stream_F(const double* __restrict__ S, Geo g, const LevConst& L,
+                                           const StreamOp& op, int i, int k, int ivis) {
+    // x and z lines through the node
+    double sx[7], sz[7];
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        sx[j] = S[g.at(i + j - 3, k)];
+        sz[j] = S[g.at(i, k + j - 3)];
+    }
+    double Sxx = 0, Sxxx = 0, Sxxxx = 0, Szz = 0, Szzz = 0, Szzzz = 0;
+#pragma unroll
+    for (int j = 1; j <= 5; j++) { Sxx += cK.D2[j] * sx[j]; Szz += cK.D2[j] * sz[j]; }
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        Sxxx += cK.D3[j] * sx[j]; Sxxxx += cK.D4[j] * sx[j];
+        Szzz += cK.D3[j] * sz[j]; Szzzz += cK.D4[j] * sz[j];
+    }
+    Sxx /= L.dr2; Sxxx /= L.dr3; Sxxxx /= L.dr4;
+    Szz /= L.ds2; Szzz /= L.ds3; Szzzz /= L.ds4;
+    // cross derivatives: x-derivatives of the 5 rows, combined in z
+    double Sxz = 0, Sxxz = 0, Sxzz = 0, Sxxzz = 0;
+#pragma unroll
+    for (int kk = -2; kk <= 2; kk++) {
+        double d1 = 0, d2 = 0;
+#pragma unroll
+        for (int ii = -2; ii <= 2; ii++) {
+            double v = (kk == 0) ? sx[ii + 3] : S[g.at(i + ii, k + kk)];
+            d1 += cK.D1[3 + ii] * v;
+            d2 += cK.D2[3 + ii] * v;
+        }
+        Sxz += cK.D1[3 + kk] * d1;
+        Sxzz += cK.D2[3 + kk] * d1;
+        Sxxz += cK.D1[3 + kk] * d2;
+        Sxxzz += cK.D2[3 + kk] * d2;
+    }
+    Sxz /= L.drds; Sxxz /= L.dr2ds; Sxzz /= L.drds2; Sxxzz /= L.dr2ds2;
+    size_t o = g.at(i, k);
+    double r;
+    double t2 = op.vis[o] * (Sxxxx + Szzzz + 2.0 * Sxxzz);
+    if (ivis == 0) r = t2 - op.rhs[o];
+    else {
+        double t1 = op.vxxmzz[o] * (Sxx - Szz);
+        double t4 = 4.0 * op.vxz[o] * Sxz;
+        double t5 = 2.0 * op.vx[o] * (Sxxx + Sxzz);
+        double t6 = 2.0 * op.vz[o] * (Szzz + Sxxz);
+        r = t1 + t2 + t4 + t5 + t6 - op.rhs[o];
+    }
+    return -r;
+}
+
+// writes value v of interior node (i,k) of out and its free-slip ghost images: the mirror
+// across a side wall flips the sign, across top/bottom it multiplies by sz (-1 free slip, +1 rigid)
+__device__ __forceinline__ void store_with_ghosts(double* out, Geo g, int i, int k, int nx, int nz, double v,
+                                                  double sz) {
+    int xs[3], zs[3];
+    double xf[3], zf[3];
+    int nxp = 0, nzp = 0;
+    xs[nxp] = i; xf[nxp++] = 1.0;
+    if (i <= 3) { xs[nxp] = -i; xf[nxp++] = -1.0; }
+    if (i >= nx - 3) { xs[nxp] = 2 * nx - i; xf[nxp++] = -1.0; }
+    zs[nzp] = k; zf[nzp++] = 1.0;
+    if (k <= 3) { zs[nzp] = -k; zf[nzp++] = sz; }
+    if (k >= nz - 3) { zs[nzp] = 2 * nz - k; zf[nzp++] = sz; }
+    for (int a = 0; a < nxp; a++)
+        for (int b = 0; b < nzp; b++) out[g.at(xs[a], zs[b])] = (xf[a] * zf[b]) * v;
+}
+
+// zero the boundary lines and their ghost images (done once per buffer per pass)
+__global__ void k_stream_zero_bnd(double* out, Geo g, int nx, int nz) {
+    int W = nx + 7;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * (nz + 7)) return;
+    int i = idx % W - 3, k = idx / W - 3;
+    if (i == 0 || i == nx || k == 0 || k == nz) out[g.at(i, k)] = 0.0;
+    else if ((i < 0 || i > nx) && (k == 0 || k == nz)) out[g.at(i, k)] = 0.0;
+}
+
+// one RKC1 stage: out = cS0*S0 + mew*S1 + v*S2 + (mewt*c)*dt*F(S1)   (stage 1: S0 + (mewt*c)*dt*F(S0))
+__global__ void __launch_bounds__(128) k_rkc_stage(double* __restrict__ out, const double* __restrict__ S1,
+                                                   const double* __restrict__ S2, const double* __restrict__ S0,
+                                                   StreamOp op, Geo g, int l, double cS0, double mew, double vv,
+                                                   double mewtc, int first, int ivis, double sz) {
+    const LevConst& L = cL[l];
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i > L.nx - 1) return;
+    double F = stream_F(S1, g, L, op, i, k, ivis);
+    size_t o = g.at(i, k);
+    double v;
+    if (first) v = S1[o] + mewtc * op.dtst[o] * F;
+    else v = cS0 * S0[o] + mew * S1[o] + vv * S2[o] + mewtc * op.dtst[o] * F;
+    store_with_ghosts(out, g, i, k, L.nx, L.nz, v, sz);
+}
+
+// residual = -(L S - RHS) on the interior (compute_residual)
+__global__ void k_residual(double* __restrict__ res, const double* __restrict__ S, StreamOp op, Geo g, int l, int ivis) {
+    const LevConst& L = cL[l];
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i > L.nx - 1) return;
+    res[g.at(i, k)] = stream_F(S, g, L, op, i, k, ivis);
+}
+
+// full free-slip ghost/boundary fill of a level array (enforceBCs_stream)
+__global__ void k_stream_bcs(double* S, Geo g, int nx, int nz, double sz) {
+    int W = nx + 7;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * (nz + 7)) return;
+    int i = idx % W - 3, k = idx / W - 3;
+    bool xin = (i > 0 && i < nx), zin = (k > 0 && k < nz);
+    if (xin && zin) return;
+    int mi = mirror_idx(i, nx), mk = mirror_idx(k, nz);
+    double v;
+    if (mi == 0 || mi == nx || mk == 0 || mk == nz) v = 0.0;
+    else {
+        double s = 1.0;
+        if (i < 0 || i > nx) s = -s;
+        if (k < 0 || k > nz) s = s * sz;
+        v = s * S[g.at(mi, mk)];
+    }
+    S[g.at(i, k)] = v;
+}
+
+int enforce_bcs_stream(Engine& E, int level, double* f) {
+    const Geo& g = E.gl[level];
+    int tot = (g.nx + 7) * (g.nz + 7);
+    k_stream_bcs<<<nblk(tot, 256), 256, 0, E.st>>>(f, g, g.nx, g.nz, E.cfg.Vbc == 0 ? -1.0 : 1.0);
+    CKL("k_stream_bcs");
+    return 0;
+}
+
+static StreamOp stream_op(Engine& E, int l) {
+    return StreamOp{E.vis[l], E.vx[l], E.vz[l], E.vxz[l], E.vxxmzz[l], E.RHS[l], E.dtst[l]};
+}
+
+// iterate_stream (RKC1 = 1, splitting = 0) + compute_residual; returns mean|r| in *mag if asked
+static int iterate_stream(Engine& E, int l, int want_mag, double* mag) {
+    const Geo& g = E.gl[l];
+    const int N = E.cfg.nstageS, Niter = E.cfg.Nmulti, ivis = E.cfg.ivis;
+    const double sz = E.cfg.Vbc == 0 ? -1.0 : 1.0;
+    StreamOp op = stream_op(E, l);
+    dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
+    int tot = (g.nx + 7) * (g.nz + 7);
+    double* buf[3] = {E.S0[l], E.S1[l], E.S2[l]};
+    for (int q = 0; q < 3; q++) k_stream_zero_bnd<<<nblk(tot, 256), 256, 0, E.st>>>(buf[q], g, g.nx, g.nz);
+    for (int n = 1; n <= Niter; n++) {
+        int ntemp = Niter - n + 1;
+        double temp = (E.cfg.Nmulti > 1) ? (E.cfg.c_2 - E.cfg.c_1) * (double)(ntemp - 1) / (double)(1 - Niter) : 0.0;
+        double c = temp + E.cfg.c_2;
+        const double* S0 = E.err[l];
+        // stage 1
+        int cur = 0;
+        k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[cur], S0, nullptr, nullptr, op, g, l, 0, 0, 0, E.K.mewt[1] * c, 1, ivis, sz);
+        const double* Sm1 = buf[cur];
+        const double* Sm2 = S0;
+        for (int j = 2; j <= N; j++) {
+            int nxt = (cur + 1) % 3;
+            if (buf[nxt] == Sm2) nxt = (nxt + 1) % 3;
+            k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[nxt], Sm1, Sm2, S0, op, g, l, E.K.cc[j], E.K.mew[j], E.K.vv[j],
+                                               E.K.mewt[j] * c, 0, ivis, sz);
+            Sm2 = Sm1;
+            Sm1 = buf[nxt];
+            cur = nxt;
+        }
+        CKL("k_rkc_stage");
+        CK(cudaMemcpyAsync(E.err[l], Sm1, g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    }
+    k_residual<<<gs, 128, 0, E.st>>>(E.res[l], E.err[l], op, g, l, ivis);
+    CKL("k_residual");
+    if (want_mag) return mean_abs(E, E.res[l], l, mag);
+    return 0;
+}
+
+// prolong (iterative_solver.f90:343-396): bilinear coarse correction added to the finer level
+__global__ void k_prolong(double* F, const double* C, Geo gf, Geo gc, int nxf, int nzf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i > nxf - 1) return;
+    double add;
+    if (!(i & 1) && !(k & 1)) add = C[gc.at(i / 2, k / 2)];
+    else if (!(i & 1)) add = (C[gc.at(i / 2, (k - 1) / 2)] + C[gc.at(i / 2, (k + 1) / 2)]) / 2.0;
+    else if (!(k & 1)) add = (C[gc.at((i - 1) / 2, k / 2)] + C[gc.at((i + 1) / 2, k / 2)]) / 2.0;
+    else
+        add = (C[gc.at((i - 1) / 2, (k - 1) / 2)] + C[gc.at((i + 1) / 2, (k - 1) / 2)] +
+               C[gc.at((i + 1) / 2, (k + 1) / 2)] + C[gc.at((i - 1) / 2, (k + 1) / 2)]) / 4.0;
+    size_t o = gf.at(i, k);
+    F[o] = F[o] + add;
+}
+
+static int prolong(Engine& E, int lc) {
+    const int lf = lc - 1;
+    const Geo &gf = E.gl[lf], &gc = E.gl[lc];
+    dim3 gp(nblk(gf.nx - 1, 128), gf.nz - 1);
+    k_prolong<<<gp, 128, 0, E.st>>>(E.err[lf], E.err[lc], gf, gc, gf.nx, gf.nz);
+    CKL("k_prolong");
+    return enforce_bcs_stream(E, lf, E.err[lf]);
+}
+
+// ------------------------------------------------------------------ coarsest level
+// Compute_Matrix_coarse (analysis=0) rows in LAPACK band storage, one thread per row
+__global__ void k_coarse_matrix(double* M, Geo g, int l, int kl, int ku, int n, double* RowB, int Vbc, int ivis,
+                                const double* vis, const double* vx, const double* vz, const double* vxz,
+                                const double* vxxmzz, int* err) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (p > n) return;
+    const LevConst& L = cL[l];
+    const int nxc = L.nx, nzc = L.nz, N = nzc + 1, ldab = 2 * kl + ku + 1, kk1 = kl + ku + 1;
+    const int reach[7] = {0, 2, 2, 3, 2, 2, 0};
+    int ip = (p - 1) / N, kp = (p - 1) % N;
+#define MB(row, col) M[(size_t)((row) - 1) + (size_t)((col) - 1) * (size_t)ldab]
+    for (int q = (p - kl > 1 ? p - kl : 1); q <= (p + ku < n ? p + ku : n); q++) MB(kk1 + p - q, q) = 0.0;
+    if (ip > 0 && ip < nxc && kp > 0 && kp < nzc) {
+        size_t o = g.at(ip, kp);
+        double a1 = vxxmzz[o], a2 = vis[o], a4 = vxz[o], a5 = vx[o], a6 = vz[o];
+        for (int pass = 0; pass < 2; pass++)
+            for (int j = -3; j <= 3; j++) {
+                int iq = j + ip;
+                for (int kq = kp - reach[j + 3]; kq <= kp + reach[j + 3]; kq++) {
+                    bool inside = (iq >= 0 && iq <= nxc && kq >= 0 && kq <= nzc);
+                    if ((pass == 0) != inside) continue;
+                    int di = iq - ip + 3, dk = kq - kp + 3;
+                    double v = (ivis == 0) ? a2 * cK.SM2[di][dk]
+                                           : a1 * cK.SM1[di][dk] + a2 * cK.SM2[di][dk] + a4 * cK.SM4[di][dk] +
+                                                 a5 * cK.SM5[di][dk] + a6 * cK.SM6[di][dk];
+                    if (pass == 0) {
+                        int q = N * iq + kq + 1;
+                        MB(kk1 + p - q, q) = v;
+                    } else {
+                        int iiq = iq, kkq = kq, sv = 1;
+                        if (iq < 0) { iiq = -iq; sv = -sv; }
+                        else if (iq > nxc) { iiq = 2 * nxc - iq; sv = -sv; }
+                        if (kq < 0) { kkq = -kq; if (Vbc == 0) sv = -sv; }
+                        else if (kq > nzc) { kkq = 2 * nzc - kq; if (Vbc == 0) sv = -sv; }
+                        int q = N * iiq + kkq + 1;
+                        MB(kk1 + p - q, q) = MB(kk1 + p - q, q) + (sv == -1 ? -v : v);
+                    }
+                }
+            }
+    } else {
+        MB(kk1, p) = 1.0;
+    }
+    // row equilibration (DGBEQU row factors) and scaling
+    double rmax = 0.0;
+    for (int q = (p - kl > 1 ? p - kl : 1); q <= (p + ku < n ? p + ku : n); q++) rmax = fmax(rmax, fabs(MB(kk1 + p - q, q)));
+    if (rmax == 0.0) { atomicOr(err, 2); rmax = 1.0; }
+    const double smlnum = 2.2250738585072014e-308;
+    double rf = 1.0 / fmin(fmax(rmax, smlnum), 1.0 / smlnum);
+    RowB[p - 1] = rf;
+    for (int q = (p - kl > 1 ? p - kl : 1); q <= (p + ku < n ? p + ku : n); q++) MB(kk1 + p - q, q) = rf * MB(kk1 + p - q, q);
+#undef MB
+}
+
+// DGBTF2: unblocked band LU with partial pivoting, one CTA (band in global memory / L2)
+__global__ void __launch_bounds__(1024) k_band_lu(double* ab, int* ipiv, int n, int kl, int ku, int* err) {
+    const int ldab = 2 * kl + ku + 1, kv = ku + kl;
+    __shared__ int s_jp, s_ju, s_nz;
+    const int tid = threadIdx.x, nt = blockDim.x;
+#define AB(r, c) ab[(size_t)((r) - 1) + (size_t)((c) - 1) * (size_t)ldab]
+    for (int j = ku + 2; j <= (kv < n ? kv : n); j++)
+        for (int i = kv - j + 2 + tid; i <= kl; i += nt) AB(i, j) = 0.0;
+    if (tid == 0) s_ju = 1;
+    __syncthreads();
+    for (int j = 1; j <= n; j++) {
+        if (j + kv <= n)
+            for (int i = 1 + tid; i <= kl; i += nt) AB(i, j + kv) = 0.0;
+        const int km = kl < n - j ? kl : n - j;
+        // pivot: first index of the maximum |a| in AB(kv+1..kv+1+km, j)
+        if (tid < 32) {
+            double best = -1.0;
+            int bi = 1 << 30;
+            for (int i = 1 + tid; i <= km + 1; i += 32) {
+                double a = fabs(AB(kv + i, j));
+                if (a > best) { best = a; bi = i; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (tid == 0) {
+                s_jp = bi;
+                ipiv[j - 1] = bi + j - 1;
+                s_nz = (AB(kv + bi, j) != 0.0);
+                if (s_nz) {
+                    int jue = j + ku + bi - 1 < n ? j + ku + bi - 1 : n;
+                    if (jue > s_ju) s_ju = jue;
+                } else {
+                    atomicCAS(err, 0, j);
+                }
+            }
+        }
+        __syncthreads();
+        const int jp = s_jp, ju = s_ju;
+        if (s_nz) {
+            if (jp != 1) {
+                for (int t = tid; t <= ju - j; t += nt) {
+                    size_t a0 = (size_t)(kv + jp - 1) + (size_t)(j - 1) * ldab + (size_t)t * (ldab - 1);
+                    size_t b0 = (size_t)kv + (size_t)(j - 1) * ldab + (size_t)t * (ldab - 1);
+                    double x = ab[a0];
+                    ab[a0] = ab[b0];
+                    ab[b0] = x;
+                }
+                __syncthreads();
+            }
+            if (km > 0) {
+                const double rp = 1.0 / AB(kv + 1, j);
+                for (int i = 1 + tid; i <= km; i += nt) AB(kv + 1 + i, j) = AB(kv + 1 + i, j) * rp;
+                __syncthreads();
+                const int ncol = ju - j;
+                for (int e = tid; e < ncol * km; e += nt) {
+                    int jj = e / km + 1, i = e % km + 1;
+                    double y = ab[(size_t)(kv - 1) + (size_t)j * ldab + (size_t)(jj - 1) * (ldab - 1)];
+                    if (y != 0.0) {
+                        size_t a0 = (size_t)kv + (size_t)j * ldab + (size_t)(jj - 1) * (ldab - 1) + (size_t)(i - 1);
+                        ab[a0] = ab[a0] + AB(kv + 1 + i, j) * (-1.0 * y);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+#undef AB
+}
+
+// DGBTRS (no transpose) + DTBSV upper, one warp; b is staged in shared memory
+__global__ void k_band_solve(const double* ab, const int* ipiv, double* bg, int n, int kl, int ku) {
+    extern __shared__ double b[];
+    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1, lane = threadIdx.x;
+    for (int q = lane; q < n; q += 32) b[q] = bg[q];
+    __syncwarp();
+#define AB(r, c) ab[(size_t)((r) - 1) + (size_t)((c) - 1) * (size_t)ldab]
+    for (int j = 1; j <= n - 1; j++) {
+        int lm = kl < n - j ? kl : n - j;
+        int l = ipiv[j - 1];
+        if (l != j && lane == 0) { double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
+        __syncwarp();
+        double bj = b[j - 1];
+        if (bj != 0.0) {
+            double temp = -1.0 * bj;
+            for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + AB(kd + i, j) * temp;
+        }
+        __syncwarp();
+    }
+    const int k = kl + ku, kp1 = k + 1;
+    for (int j = n; j >= 1; j--) {
+        double bj = b[j - 1];
+        if (bj != 0.0) {
+            double x = bj / AB(kp1, j);
+            __syncwarp();
+            if (lane == 0) b[j - 1] = x;
+            int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+            for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * AB(l + i, j);
+        }
+        __syncwarp();
+    }
+#undef AB
+    for (int q = lane; q < n; q += 32) bg[q] = b[q];
+}
+
+__global__ void k_coarse_rhs(double* B, const double* RHS, const double* RowB, Geo g, int nxc, int nzc) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int N = nzc + 1, n = (nxc + 1) * N;
+    if (p > n) return;
+    int ip = (p - 1) / N, kp = (p - 1) % N;
+    B[p - 1] = (ip > 0 && ip < nxc && kp > 0 && kp < nzc) ? RHS[g.at(ip, kp)] * RowB[p - 1] : 0.0;
+}
+__global__ void k_coarse_scatter(double* E, const double* B, Geo g, int nxc, int nzc) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int N = nzc + 1, n = (nxc + 1) * N;
+    if (p > n) return;
+    E[g.at((p - 1) / N, (p - 1) % N)] = B[p - 1];
+}
+
+static int coarse_factor(Engine& E) {
+    const int L = E.grids, n = E.ngc;
+    CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
+    k_coarse_matrix<<<nblk(n, 128), 128, 0, E.st>>>(E.Mc, E.gl[L], L, E.kl, E.ku, n, E.RowB, E.cfg.Vbc,
+                                                    E.cfg.ivis, E.vis[L], E.vx[L], E.vz[L], E.vxz[L], E.vxxmzz[L], E.derr);
+    k_band_lu<<<1, 1024, 0, E.st>>>(E.Mc, E.ipiv, n, E.kl, E.ku, E.derr);
+    CKL("coarse LU");
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    if (h) return fail(PT_ERR_SINGULAR_COARSE, "coarse banded LU: zero row or pivot");
+    return 0;
+}
+
+static int coarse_solve(Engine& E) {
+    const int L = E.grids, n = E.ngc;
+    const Geo& g = E.gl[L];
+    k_coarse_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.RHS[L], E.RowB, g, g.nx, g.nz);
+    k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
+    k_coarse_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.err[L], E.Bc, g, g.nx, g.nz);
+    CKL("coarse solve");
+    return enforce_bcs_stream(E, L, E.err[L]);
+}
+
+// ------------------------------------------------------------------ driver
+int mg_setup_solve(Engine& E) {
+    int rc;
+    CK(cudaMemcpyAsync(E.err[1], E.SF, E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    if ((rc = compute_RHS(E, 1))) return rc;
+    if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
+    for (int level = 1; level <= E.grids; level++)
+        if ((rc = compute_viscosity(E, level))) return rc;
+    if (E.time == 0.0 || E.cfg.ivis > 0)
+        if ((rc = coarse_factor(E))) return rc;
+    return 0;
+}
+
+int multigrid(Engine& E, pt_solve_info* info) {
+    int rc;
+    PhaseTimer tm(E, 2);
+    if ((rc = mg_setup_solve(E))) return rc;
+    const int grids = E.grids, nsteps = E.nsteps;
+    const int* multi = E.multi;
+    int q = 1;
+    double mag1 = 0.0;
+    for (;;) {
+        bool conv = false;
+        for (int p = 1; p <= nsteps; p++) {
+            const int level = multi[p];
+            if (multi[p - 1] < multi[p]) {
+                if ((rc = compute_RHS(E, level))) return rc;
+                if (p <= grids && q == 1 && level == 1) {
+                    if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
+                }
+            }
+            if (level < grids) {
+                if ((rc = iterate_stream(E, level, level == 1 && p == 1, &mag1))) return rc;
+                if (level == 1 && p == 1) {
+                    if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite multigrid residual");
+                    if (mag1 > 1.0e10 * E.res_ref[1])
+                        return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
+                }
+            } else {
+                if ((rc = coarse_solve(E))) return rc;
+            }
+            if (level == 1 && mag1 / E.res_ref[1] <= E.cfg.tolerance) { conv = true; break; }
+            if (multi[p + 1] < multi[p])
+                if ((rc = prolong(E, level))) return rc;
+        }
+        if (conv) break;
+        q++;
+        if (q > E.cfg.max_cycles) return fail(PT_ERR_MG_MAX_CYCLES, "Multigrid Convergence Problem: Too Many Multigrid Cycles Needed");
+    }
+    E.cycles = q;
+    E.residual_mag1 = mag1;
+    E.resid_ratio = mag1 / E.res_ref[1];
+    CK(cudaMemcpyAsync(E.SF, E.err[1], E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    if (info) {
+        info->cycles += q;
+        info->resid_ratio = E.resid_ratio;
+        info->n_eta = E.n_eta;
+        info->eig_fine = E.eig_fine;
+    }
+    return 0;
+}
+
+int mg_alloc(Engine& E) {
+    auto alloc = [&](double** p, size_t n) -> int {
+        CK(cudaMalloc(p, n * sizeof(double)));
+        CK(cudaMemsetAsync(*p, 0, n * sizeof(double), E.st));
+        E.bytes_allocated += n * sizeof(double);
+        return 0;
+    };
+    for (int l = 1; l <= E.grids; l++) {
+        size_t n = E.gl[l].elems();
+        double** arrs[] = {&E.err[l], &E.S0[l], &E.S1[l], &E.S2[l], &E.RHS[l], &E.res[l], &E.dtst[l], &E.ratio[l],
+                           &E.vis[l], &E.visst[l], &E.vx[l], &E.vz[l], &E.vxx[l], &E.vzz[l], &E.vxz[l],
+                           &E.vxxpzz[l], &E.vxxmzz[l], &E.vsm[l]};
+        for (auto a : arrs)
+            if (int rc = alloc(a, n)) return rc;
+    }
+    for (int q = 0; q < 11; q++)
+        if (int rc = alloc(&E.visw[q], E.gl[1].elems())) return rc;
+    int ldab = 2 * E.kl + E.ku + 1;
+    if (int rc = alloc(&E.Mc, (size_t)ldab * E.ngc)) return rc;
+    if (int rc = alloc(&E.Bc, E.ngc)) return rc;
+    if (int rc = alloc(&E.RowB, E.ngc)) return rc;
+    CK(cudaMalloc(&E.ipiv, sizeof(int) * E.ngc));
+    return 0;
+}
+
+}  // namespace pt

@@ -1,0 +1,320 @@
+// pt_tracers.cu -- tracer kernels: the RK4 stage loops of energy_time (energy.f90:258-536)
+// with the Taylor interpolation of interpolate (composition.f90:1359-1393), and the tracer->grid
+// projection tracers_to_corners_iC_continuous (composition.f90:942-1087).
+//
+// Projection, GB300 form: a counting sort of tracer IDs by cell (cell = nint of the position),
+// a per-cell sort of the IDs, per-cell partial sums of T*S, C*S and S for the 3x3 target nodes
+// in ascending ID order, then per node a fixed-order sum of the 9 partials.  Counts and cell
+// indices are integers (bit-exact); every floating-point sum has a fixed association, so the
+// result is deterministic and equals the oracle's canonical order bit for bit (the arithmetic
+// uses explicit round-to-nearest intrinsics, no contraction).
+#include <cstdio>
+
+#include "pt_consts.cuh"
+
+namespace pt {
+
+int upload_consts_tracers(const Engine& E) { return upload_tu_consts(E); }
+
+__device__ __forceinline__ int cell_index(double x, double inv, double h, int exact) {
+    double q = exact ? x * inv : x / h;
+    return (int)llround(q);
+}
+
+// ---------------------------------------------------------------- projection
+__global__ void k_cells(const double* __restrict__ r, const double* __restrict__ s, int64_t n,
+                        int32_t* __restrict__ cell, int32_t* __restrict__ count, int* err) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double rr = r[t], ss = s[t];
+    if (!(rr >= 0.0 && rr <= cK.aspect && ss >= 0.0 && ss <= 1.0)) {
+        atomicOr(err, 1);  // composition.f90:1007-1010
+        cell[t] = -1;
+        return;
+    }
+    int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div);
+    int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div);
+    int c = i + (cK.nx + 1) * k;
+    cell[t] = c;
+    atomicAdd(&count[c], 1);
+}
+
+// exclusive scan of int32 counts: block scan, scan of block totals, add offsets
+__global__ void k_scan_block(const int32_t* in, int32_t* out, int32_t* totals, int n) {
+    __shared__ int32_t ws[32];
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    int v = gid < n ? in[gid] : 0;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int y = (lane < (int)(blockDim.x >> 5)) ? ws[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += z;
+        }
+        ws[lane] = y;
+    }
+    __syncthreads();
+    int base = wid > 0 ? ws[wid - 1] : 0;
+    if (gid < n) out[gid] = base + x - v;
+    if (threadIdx.x == blockDim.x - 1) totals[blockIdx.x] = base + x;
+}
+__global__ void k_scan_totals(int32_t* totals, int nb) {
+    if (threadIdx.x != 0) return;
+    int acc = 0;
+    for (int b = 0; b < nb; b++) {
+        int v = totals[b];
+        totals[b] = acc;
+        acc += v;
+    }
+}
+__global__ void k_scan_add(int32_t* out, const int32_t* totals, int n) {
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < n) out[gid] += totals[blockIdx.x];
+}
+
+__global__ void k_scatter(const int32_t* __restrict__ cell, int64_t n, const int32_t* __restrict__ start,
+                          int32_t* cursor, int32_t* __restrict__ list) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int c = cell[t];
+    if (c < 0) return;
+    int slot = start[c] + atomicAdd(&cursor[c], 1);
+    list[slot] = (int32_t)t;
+}
+
+// ascending tracer IDs inside each cell (insertion sort: cells hold a few dozen tracers)
+__global__ void k_sort_cells(int32_t* list, const int32_t* start, const int32_t* count, int ncell) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int b = start[c], n = count[c];
+    for (int a = 1; a < n; a++) {
+        int32_t key = list[b + a];
+        int j = a - 1;
+        while (j >= 0 && list[b + j] > key) {
+            list[b + j + 1] = list[b + j];
+            j--;
+        }
+        list[b + j + 1] = key;
+    }
+}
+
+__device__ __forceinline__ double shape1(double x, int i, double h, double inv, int exact) {
+    double d = fabs(__dsub_rn(x, __dmul_rn((double)i, h)));
+    double q = exact ? __dmul_rn(d, inv) : __ddiv_rn(d, h);
+    double a = __dsub_rn(1.0, q);
+    return a > 0.0 ? a : 0.0;
+}
+
+// per-cell partial sums for the 3x3 nodes around the cell; planes of ncell: [q*9 + dz*3 + dx]
+__global__ void k_cell_partials(const double* __restrict__ r, const double* __restrict__ s,
+                                const double* __restrict__ Tt, const double* __restrict__ Ct,
+                                const int32_t* __restrict__ list, const int32_t* __restrict__ start,
+                                const int32_t* __restrict__ count, int ncell, double* __restrict__ P,
+                                int comp) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int nx1 = cK.nx + 1;
+    int ci = c % nx1, ck = c / nx1;
+    double aT[9], aC[9], aS[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) { aT[q] = 0.0; aC[q] = 0.0; aS[q] = 0.0; }
+    int b = start[c], n = count[c];
+    for (int a = 0; a < n; a++) {
+        int32_t t = list[b + a];
+        double rr = r[t], ss = s[t], tv = Tt[t], cv = comp ? Ct[t] : 0.0;
+        double wx[3], wz[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            wx[d] = shape1(rr, ci + d - 1, cK.dr, cK.inv_dr, cK.exact_div);
+            wz[d] = shape1(ss, ck + d - 1, cK.ds, cK.inv_ds, cK.exact_div);
+        }
+#pragma unroll
+        for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++) {
+                double S = __dmul_rn(wx[dx], wz[dz]);
+                int q = dz * 3 + dx;
+                aT[q] = __dadd_rn(aT[q], __dmul_rn(tv, S));
+                aC[q] = __dadd_rn(aC[q], __dmul_rn(cv, S));
+                aS[q] = __dadd_rn(aS[q], S);
+            }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        P[(size_t)q * ncell + c] = aT[q];
+        P[(size_t)(9 + q) * ncell + c] = aC[q];
+        P[(size_t)(18 + q) * ncell + c] = aS[q];
+    }
+}
+
+// per node: fixed-order sum of the partials of the 3x3 surrounding cells, then the ratio
+__global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restrict__ count, int ncell,
+                            double* Tratio, double* Cnew, int32_t* nempty, Geo g, int comp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    const int nx = cK.nx, nz = cK.nz;
+    if (i > nx) return;
+    double sT = 0.0, sC = 0.0, sS = 0.0;
+    for (int ck = k - 1; ck <= k + 1; ck++)
+        for (int ci = i - 1; ci <= i + 1; ci++) {
+            if (ci < 0 || ci > nx || ck < 0 || ck > nz) continue;
+            int c = ci + (nx + 1) * ck;
+            int q = (k - ck + 1) * 3 + (i - ci + 1);
+            sT = __dadd_rn(sT, P[(size_t)q * ncell + c]);
+            sC = __dadd_rn(sC, P[(size_t)(9 + q) * ncell + c]);
+            sS = __dadd_rn(sS, P[(size_t)(18 + q) * ncell + c]);
+        }
+    int c = i + (nx + 1) * k;
+    nempty[c] = count[c];
+    if (sS > 0.0) {
+        Tratio[g.at(i, k)] = __ddiv_rn(sT, sS);
+        if (comp) Cnew[g.at(i, k)] = __ddiv_rn(sC, sS);
+    }
+}
+
+int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f, int smooth) {
+    const int nx = E.K.nx, nz = E.K.nz;
+    const int ncell = (nx + 1) * (nz + 1);
+    const int64_t n = E.ntr;
+    int rc;
+    PhaseTimer tm(E, 1);
+    if (T0f && T0f != E.Tratio) {
+        if ((rc = copy_field(E, E.Tratio, T0f))) return rc;
+    }
+    CK(cudaMemsetAsync(E.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+    CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
+    k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, E.tcell, E.ccount, E.derr);
+    int nb = (int)nblk(ncell, 1024);
+    k_scan_block<<<nb, 1024, 0, E.st>>>(E.ccount, E.cstart, E.scan_tmp, ncell);
+    k_scan_totals<<<1, 32, 0, E.st>>>(E.scan_tmp, nb);
+    k_scan_add<<<nb, 1024, 0, E.st>>>(E.cstart, E.scan_tmp, ncell);
+    int32_t* cursor = E.scan_tmp + nb + 32;
+    CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+    k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.cstart, cursor, E.clist);
+    k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(E.clist, E.cstart, E.ccount, ncell);
+    k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount, ncell,
+                                                        E.cpart, E.cfg.comp);
+    dim3 grid(nblk(nx + 1, 128), nz + 1);
+    k_node_sums<<<grid, 128, 0, E.st>>>(E.cpart, E.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
+    CKL("projection");
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    if (herr) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
+    if (E.cfg.comp) {
+        if ((rc = enforce_bcs_C(E, E.Cnew))) return rc;
+        if (smooth && (rc = smoother_time_C(E))) return rc;
+    }
+    if ((rc = enforce_bcs_T(E, E.Tratio))) return rc;
+    if (smooth && (rc = smoother_time_T(E, E.Tratio))) return rc;
+    return load_conductivity(E);
+}
+
+// ---------------------------------------------------------------- RK4 stage loops
+// interpolate (composition.f90:1359-1393): x-Taylor series (order 3) on the 7 rows around the
+// nearest node, z-derivatives of those values with the 7-point stencils, z-Taylor series.
+struct Tables {
+    const double *f, *d1, *d2, *d3;
+};
+
+__device__ __forceinline__ double interp(const Tables& tb, Geo g, int i, int k, double a1, double a2,
+                                         double a3, double b1, double b2, double b3) {
+    double fR[7];
+#pragma unroll
+    for (int jj = 0; jj < 7; jj++) {
+        size_t o = g.at(i, k + jj - 3);
+        double v = tb.f[o];
+        v = v + tb.d1[o] * a1;
+        v = v + tb.d2[o] * a2;
+        v = v + tb.d3[o] * a3;
+        fR[jj] = v;
+    }
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        s1 = s1 + cK.Dm[1][j] * fR[j];
+        s2 = s2 + cK.Dm[2][j] * fR[j];
+        s3 = s3 + cK.Dm[3][j] * fR[j];
+    }
+    s1 = s1 / cK.ds_pow[1];
+    s2 = s2 / cK.ds_pow[2];
+    s3 = s3 / cK.ds_pow[3];
+    double fi = fR[3];
+    fi = fi + s1 * b1;
+    fi = fi + s2 * b2;
+    fi = fi + s3 * b3;
+    return fi;
+}
+
+struct StageArgs {
+    Tables u, w, t;
+    const double *xr, *xs;      // interpolation positions
+    double *rtr, *str, *Ttr;    // accumulators k1 + 2k2 + 2k3 (+k4)
+    const double *r0, *s0, *T0; // step-start state
+    double *rn, *sn, *Tn;       // next stage position/temperature
+    double dtstage;
+    int stage;
+    int64_t n;
+};
+
+__global__ void __launch_bounds__(256) k_rk_stage(StageArgs A, Geo g) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    double r = A.xr[t], s = A.xs[t];
+    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div);
+    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div);
+    i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
+    k = min(max(k, 0), cK.nz);
+    double hr = r - (double)i * cK.dr, hs = s - (double)k * cK.ds;
+    double a1 = hr / cK.fact[1], a2 = hr * hr / cK.fact[2], a3 = hr * hr * hr / cK.fact[3];
+    double b1 = hs / cK.fact[1], b2 = hs * hs / cK.fact[2], b3 = hs * hs * hs / cK.fact[3];
+    double tr = interp(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
+    double ts = interp(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
+    double tT = interp(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
+    double r0 = A.r0[t], s0 = A.s0[t], T0 = A.T0[t];
+    switch (A.stage) {
+        case 1:  // energy.f90:288-299
+            A.rtr[t] = tr; A.str[t] = ts; A.Ttr[t] = tT;
+            A.rn[t] = r0 + A.dtstage * tr; A.sn[t] = s0 + A.dtstage * ts; A.Tn[t] = T0 + A.dtstage * tT;
+            break;
+        case 2:  // energy.f90:376-399
+        case 3:  // energy.f90:458-470
+            A.rtr[t] = A.rtr[t] + 2.0 * tr; A.str[t] = A.str[t] + 2.0 * ts; A.Ttr[t] = A.Ttr[t] + 2.0 * tT;
+            A.rn[t] = r0 + A.dtstage * tr; A.sn[t] = s0 + A.dtstage * ts; A.Tn[t] = T0 + A.dtstage * tT;
+            break;
+        default:  // stage 4, energy.f90:525-534
+            A.rtr[t] = r0 + A.dtstage * (A.rtr[t] + tr);
+            A.str[t] = s0 + A.dtstage * (A.str[t] + ts);
+            A.Ttr[t] = T0 + A.dtstage * (A.Ttr[t] + tT);
+            break;
+    }
+}
+
+int rk_stage(Engine& E, int stage) {
+    PhaseTimer tm(E, 0);
+    StageArgs A;
+    A.u = {E.u, E.der[0][0], E.der[0][1], E.der[0][2]};
+    A.w = {E.w, E.der[1][0], E.der[1][1], E.der[1][2]};
+    A.t = {E.tsa, E.der[2][0], E.der[2][1], E.der[2][2]};
+    A.rtr = E.rtr; A.str = E.str; A.Ttr = E.Ttr;
+    A.r0 = E.rtr0; A.s0 = E.str0; A.T0 = E.Ttr0;
+    A.n = E.ntr;
+    A.stage = stage;
+    switch (stage) {
+        case 1: A.xr = E.rtr0; A.xs = E.str0; A.rn = E.rtr1; A.sn = E.str1; A.Tn = E.Ttr1; A.dtstage = 0.5 * E.dt; break;
+        case 2: A.xr = E.rtr1; A.xs = E.str1; A.rn = E.rtr2; A.sn = E.str2; A.Tn = E.Ttr2; A.dtstage = 0.5 * E.dt; break;
+        case 3: A.xr = E.rtr2; A.xs = E.str2; A.rn = E.rtr1; A.sn = E.str1; A.Tn = E.Ttr1; A.dtstage = E.dt; break;
+        default: A.xr = E.rtr1; A.xs = E.str1; A.rn = nullptr; A.sn = nullptr; A.Tn = nullptr; A.dtstage = E.dt / 6.0; break;
+    }
+    k_rk_stage<<<nblk(E.ntr, 256), 256, 0, E.st>>>(A, E.g1);
+    CKL("k_rk_stage");
+    return 0;
+}
+
+}  // namespace pt

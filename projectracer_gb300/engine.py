@@ -1,0 +1,166 @@
+"""Python binding of the C ABI in include/ptgpu.h (the engine behind the Fortran drop-in).
+
+``Engine`` drives one GPU context exactly as the reference's time loop drives its subroutines
+(main.f90:245-300): ``upload`` = restart read, ``solve_psi`` = velocity solve at the top of a
+step, ``step`` = energy_time, ``stats`` = the stats.dat row.  There is no CPU implementation
+behind this module: if libptgpu.so is missing or no GPU is present the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from .config import PtConfig
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libptgpu.so")
+HEADER = os.path.join(HERE, "..", "include", "ptgpu.h")
+
+F_T, F_TRATIO, F_TVIS, F_TBUOY, F_CNEW, F_CVIS, F_CBUOY, F_SF, F_U, F_W, F_VIS, F_NEMPTY, F_RHS = range(13)
+F_TRACER_R, F_TRACER_S, F_TRACER_T, F_TRACER_C = 20, 21, 22, 23
+
+ERRORS = {-1: "PT_ERR_CONFIG", -2: "PT_ERR_TRACER_OUT_OF_DOMAIN", -3: "PT_ERR_MG_DIVERGED",
+          -4: "PT_ERR_MG_MAX_CYCLES", -5: "PT_ERR_SINGULAR_COARSE", -6: "PT_ERR_CUDA", -7: "PT_ERR_STATE",
+          -8: "PT_ERR_ITER_CAP", -9: "PT_ERR_ARG", -10: "PT_ERR_NOT_FINITE"}
+
+
+class PtError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("cycles", ctypes.c_int32), ("refinements", ctypes.c_int32), ("n_eta", ctypes.c_int32),
+                ("n_temp", ctypes.c_int32), ("resid_ratio", ctypes.c_double), ("eig_fine", ctypes.c_double),
+                ("ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class StatsRow(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("time", "Tavg", "vrms", "Nu", "Nu_bot", "RaT_avg", "mobility",
+                                                 "strain_max", "q1", "q2", "q3", "q4")] + \
+               [("empty_cells", ctypes.c_int32), ("tracer_min", ctypes.c_int32), ("tracer_max", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("Cavg", ctypes.c_double), ("entrainment", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad"}
+
+
+_LIB = None
+
+
+def header_symbols() -> list[str]:
+    """Entry points declared in include/ptgpu.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(pt_[a-z_0-9]+)\s*\(", text, re.M)))
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build() "
+                           "(python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(path)
+    vp, i32, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.pt_init.argtypes = [ctypes.POINTER(PtConfig)]
+    L.pt_last_error.restype = ctypes.c_char_p
+    L.pt_field_extent.argtypes = [i32] + [ctypes.POINTER(ctypes.c_int32)] * 5
+    L.pt_set_field.argtypes = [i32, vp]
+    L.pt_get_field.argtypes = [i32, vp]
+    L.pt_upload_state.argtypes = [vp] * 9
+    L.pt_download_state.argtypes = [vp] * 7
+    L.pt_solve_psi.argtypes = [ctypes.POINTER(SolveInfo)]
+    L.pt_step.argtypes = [ctypes.POINTER(f64), ctypes.POINTER(SolveInfo)]
+    L.pt_stats.argtypes = [ctypes.POINTER(StatsRow)]
+    L.pt_tracers_to_corners.argtypes = [vp, i32]
+    L.pt_time.argtypes = [ctypes.POINTER(f64), ctypes.POINTER(f64)]
+    L.pt_set_guess_mode.argtypes = [i32, ctypes.c_char_p]
+    L.pt_phase_times.argtypes = [ctypes.POINTER(f64)]
+    _LIB = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Engine:
+    """One engine context (the library keeps one per process)."""
+
+    def __init__(self, cfg: PtConfig):
+        self.L = load_library()
+        self.cfg = cfg.copy()
+        self._check(self.L.pt_init(ctypes.byref(self.cfg)))
+        self.nx, self.nz = cfg.nx, cfg.nz
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise PtError(rc, self.L.pt_last_error().decode())
+
+    def close(self):
+        self.L.pt_finalize()
+
+    def extent(self, field: int):
+        v = [ctypes.c_int32() for _ in range(5)]
+        self._check(self.L.pt_field_extent(field, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def get(self, field: int) -> np.ndarray:
+        lox, hix, loz, hiz, eb = self.extent(field)
+        if field >= F_TRACER_R:
+            out = np.empty(hix, dtype=np.float64)
+        else:
+            out = np.empty((hiz - loz + 1, hix - lox + 1), dtype=np.int32 if eb == 4 else np.float64)
+        self._check(self.L.pt_get_field(field, _ptr(out)))
+        return out
+
+    def set(self, field: int, arr: np.ndarray):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        self._check(self.L.pt_set_field(field, _ptr(arr)))
+
+    def upload(self, st: dict):
+        arrs = [np.ascontiguousarray(st[k], dtype=np.float64)
+                for k in ("xg", "zg", "T", "Cnew", "SF", "rtr", "str", "Ctr", "Ttr")]
+        self._check(self.L.pt_upload_state(*[_ptr(a) for a in arrs]))
+
+    def solve_psi(self) -> dict:
+        info = SolveInfo()
+        self._check(self.L.pt_solve_psi(ctypes.byref(info)))
+        return info.as_dict()
+
+    def step(self) -> tuple[float, dict]:
+        dt = ctypes.c_double()
+        info = SolveInfo()
+        self._check(self.L.pt_step(ctypes.byref(dt), ctypes.byref(info)))
+        return dt.value, info.as_dict()
+
+    def stats(self) -> dict:
+        row = StatsRow()
+        self._check(self.L.pt_stats(ctypes.byref(row)))
+        return row.as_dict()
+
+    def project(self, T0: np.ndarray | None = None, smooth: int = 1):
+        t0 = None if T0 is None else np.ascontiguousarray(T0, dtype=np.float64)
+        self._check(self.L.pt_tracers_to_corners(None if t0 is None else _ptr(t0), smooth))
+
+    def time(self) -> tuple[float, float]:
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.pt_time(ctypes.byref(t), ctypes.byref(dt)))
+        return t.value, dt.value
+
+    def set_guess_mode(self, mode: int, weights: str | None = None):
+        self._check(self.L.pt_set_guess_mode(mode, None if weights is None else weights.encode()))
+
+    def phase_times(self) -> list[float]:
+        v = (ctypes.c_double * 5)()
+        self._check(self.L.pt_phase_times(v))
+        return list(v)

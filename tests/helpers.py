@@ -1,0 +1,40 @@
+"""Shared set-up for parity tests: one configuration, one seeded state, oracle and engine."""
+from __future__ import annotations
+
+import numpy as np
+
+from projectracer_gb300.config import PtConfig, workload
+from projectracer_gb300.inputs import make_state
+
+
+def small_case(kind: str = "iso", nx: int = 64, nz: int = 64, tpc: int = 8, seed: int = 3) -> tuple[PtConfig, dict]:
+    """CPU-sized parity cases on the hot path's code branches.
+    iso:   isoviscous thermal convection (comp=0, ivis=0), the C1 physics
+    chem:  thermochemical, eta(T), composition layer (comp=1, ivis=1), C2-like at lower Ra
+    depth: eta(T,z) with internal heating (ivis=1, visP>1, H>0), C3/C5-like at lower Ra
+    """
+    if kind == "iso":
+        c, _ = workload("C1")
+        c.nx, c.nz = nx, nz
+    elif kind == "chem":
+        c, _ = workload("C2")
+        c.nx, c.nz = nx, nz
+        c.RaT, c.RaC, c.visT = 1e5, 5e4, 1e3
+        c.courant = 0.1
+    elif kind == "depth":
+        c, _ = workload("C3")
+        c.nx, c.nz = nx, nz
+        c.RaT, c.RaC, c.visT, c.visP, c.H = 1e5, 2e4, 1e3, 10.0, 1.0
+        c.courant = 0.05
+    else:
+        raise ValueError(kind)
+    c.ntr = nx * nz * tpc
+    st = make_state(c, seed, noise=1e-3 if kind != "iso" else 0.0)
+    return c, st
+
+
+def rel_err(a: np.ndarray, b: np.ndarray) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(a - b))) / scale

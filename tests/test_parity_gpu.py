@@ -1,0 +1,98 @@
+"""GPU engine vs the CPU oracle on identical seeded inputs, through the C ABI.
+
+Integer work (cell indices, tracer counts) and the projection / boundary-condition / smoother
+kernels are compared bit for bit (the oracle runs the projection in the engine's canonical
+summation order).  Floating-point results that pass through the FMA-contracted kernels (psi
+solve, tracer interpolation) are compared at the benchmark spec's tolerance of 1e-10 relative to the
+field's maximum (per single solve / step, typically 1e-13).
+"""
+import numpy as np
+import pytest
+
+from oracle.ptref import Oracle
+from projectracer_gb300 import engine as eng
+from tests.helpers import rel_err, small_case
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def pair(kind, **kw):
+    cfg, st = small_case(kind, **kw)
+    o = Oracle(cfg, iterate=1, nparts=0)
+    o.load_restart(st["xg"], st["zg"], st["T"], st["Cnew"], st["SF"], st["rtr"], st["str"], st["Ctr"], st["Ttr"])
+    e = eng.Engine(cfg)
+    e.upload(st)
+    return cfg, o, e
+
+
+@pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
+def test_upload_projection_bit_exact(kind):
+    cfg, o, e = pair(kind)
+    assert np.array_equal(e.get(eng.F_NEMPTY), o.get(11))
+    for fid in (eng.F_TRATIO, eng.F_TVIS, eng.F_TBUOY, eng.F_T):
+        g, r = e.get(fid), o.get(fid)
+        assert np.array_equal(g[1:-1, 1:-1] if fid != eng.F_T else g, r[1:-1, 1:-1] if fid != eng.F_T else r), fid
+    if cfg.comp:
+        assert np.array_equal(e.get(eng.F_CNEW), o.get(4))
+    e.close()
+
+
+@pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
+def test_solve_psi_matches_oracle(kind):
+    cfg, o, e = pair(kind)
+    info = e.solve_psi()
+    o.solve_psi()
+    assert info["cycles"] == int(o.scalar("cycles"))
+    assert rel_err(e.get(eng.F_SF), o.get(7)) < TOL
+    assert rel_err(e.get(eng.F_U), o.get(8)) < TOL
+    assert rel_err(e.get(eng.F_W), o.get(9)) < TOL
+    assert rel_err(e.get(eng.F_VIS)[3:-3, 3:-3], o.get(10)[3:-3, 3:-3]) < 1e-12
+    assert info["n_eta"] == int(o.scalar("n_eta"))
+    e.close()
+
+
+@pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
+def test_step_matches_oracle(kind):
+    cfg, o, e = pair(kind)
+    e.solve_psi()
+    o.solve_psi()
+    dt, info = e.step()
+    o.step()
+    assert dt == o.scalar("dt")
+    for fid, oid in ((eng.F_TRACER_R, 20), (eng.F_TRACER_S, 21), (eng.F_TRACER_T, 22)):
+        assert rel_err(e.get(fid), o.get(oid)) < TOL, fid
+    assert rel_err(e.get(eng.F_T), o.get(0)) < TOL
+    assert np.array_equal(e.get(eng.F_NEMPTY), o.get(11))
+    if cfg.comp:
+        assert rel_err(e.get(eng.F_CNEW), o.get(4)) < TOL
+    e.close()
+
+
+def test_stats_match_oracle():
+    cfg, o, e = pair("chem")
+    e.solve_psi()
+    o.solve_psi()
+    sg, so = e.stats(), o.stats()
+    for k in ("empty_cells", "tracer_min", "tracer_max"):
+        assert sg[k] == so[k]
+    for k in ("Tavg", "Nu", "Nu_bot", "q1", "q2", "q3", "q4", "Cavg", "entrainment"):
+        assert sg[k] == pytest.approx(so[k], rel=1e-13, abs=1e-300), k
+    for k in ("vrms", "mobility", "strain_max", "RaT_avg"):
+        assert sg[k] == pytest.approx(so[k], rel=TOL), k
+    e.close()
+
+
+def test_three_steps_stay_close():
+    cfg, o, e = pair("chem")
+    for _ in range(3):
+        e.solve_psi()
+        o.solve_psi()
+        e.step()
+        o.step()
+    sg, so = e.stats(), o.stats()
+    for k in ("Tavg", "vrms", "Nu", "Cavg"):
+        assert sg[k] == pytest.approx(so[k], rel=TOL), k
+    assert rel_err(e.get(eng.F_TRACER_R), o.get(20)) < TOL
+    e.close()
