@@ -1,0 +1,358 @@
+"""Benchmark: time steps per second of the tracer-convection hot path on GB300.
+
+One "step" is one time step of the reference's loop (main.f90:245-300): the psi solve at the top
+of the step (pt_solve_psi) and energy_time (pt_step: RK4 over all tracers with three more psi
+solves and four tracer->grid projections).  Inputs are seeded synthetic restart files of the
+workload (no dataset is involved); every step works on 1.7 GB of tracer state, far above the
+129 MB L2, so no cache flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload C3] [--precision mixed|fp64]
+  python bench.py --impl reference ...   (CPU restatement of the reference on the host cores)
+
+Multi-GPU: the path does not shard (no domain decomposition in the reference), so N ranks run N
+independent replicas ("replicas only"); value = N * steps / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "timesteps/s @1024x512,16M tracers; psi-solve ms at 1e-8 resid vs plain FP64 GPU"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Host-side barrier / max over ranks (gloo); the data path has no collective."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as tdist
+
+            tdist.init_process_group("gloo")
+            self.tdist = tdist
+
+    def barrier(self):
+        if self.world > 1:
+            self.tdist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.tdist.all_reduce(t, op=self.tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.tdist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        mhz, maxm, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                mhz.append(float(p[1]))
+                maxm = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        mhz.sort()
+        med = mhz[len(mhz) // 2] if mhz else None
+        return {"sm_mhz": med, "sm_max_mhz": maxm, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def bench_config(workload: str, precision: str):
+    from projectracer_gb300.config import PT_PREC_FP64, PT_PREC_MIXED, workload as wl
+
+    prec = PT_PREC_MIXED if precision == "mixed" else PT_PREC_FP64
+    cfg, w = wl(workload, 1.0, prec)
+    return cfg, w
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def cpu_baseline(workload: str, precision_unused: str, steps: int = 1) -> dict:
+    """The oracle (plain-C restatement of the reference, OpenMP over all host cores) on a bounded
+    sample: the same workload physics at 1/4 linear resolution (1/16 of nodes and tracers)."""
+    from oracle.ptref import Oracle, build
+    from projectracer_gb300.config import workload as wl
+    from projectracer_gb300.inputs import make_state
+
+    build()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cfg, w = wl(workload, 0.25)
+    apply_bench_solver(cfg, w, scale=0.25)
+    st = make_state(cfg, 3, noise=w.get("noise", 1e-3))
+    o = Oracle(cfg, iterate=1, nparts=cores)
+    o.load_restart(st["xg"], st["zg"], st["T"], st["Cnew"], st["SF"], st["rtr"], st["str"], st["Ctr"], st["Ttr"])
+    o.solve_psi()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.solve_psi()
+        o.step()
+    dt = (time.perf_counter() - t0) / steps
+    scale = 16.0
+    return {"value": 1.0 / (dt * scale), "unit": "timesteps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} step(s) of the workload at 1/4 linear scale ({cfg.nx}x{cfg.nz}, {cfg.ntr} tracers) "
+                      f"took {dt:.2f} s each; value scaled by the 16x node/tracer ratio",
+            "sample_seconds_per_step": dt}
+
+
+def apply_bench_solver(cfg, w, scale=1.0):
+    """Solver settings used for the benchmark workload (the reference has no
+    advective time-step limit for tracer runs, and its RKC1 multigrid needs the coarsest grid
+    to resolve the viscosity contrast)."""
+    cfg.courant = w.get("bench_courant", cfg.courant)
+    if "bench_grids" in w:
+        cfg.grids = w["bench_grids"] if scale >= 1.0 else max(2, w["bench_grids"] - 2)
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    import numpy as np  # noqa: F401
+
+    W = max(0, args.warmup)
+    res = cpu_baseline(args.workload, args.precision, steps=1) if W > 0 else None
+    times = []
+    for _ in range(args.steps):
+        r = cpu_baseline(args.workload, args.precision, steps=1)
+        times.append(r["sample_seconds_per_step"])
+    per = sum(times) / len(times)
+    value = 1.0 / (per * 16.0)
+    cfg, w = bench_config(args.workload, args.precision)
+    line = {"metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per * 16.0 * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"{args.workload} {cfg.nx}x{cfg.nz} {cfg.ntr} tracers",
+                       "l2_flush": "inputs larger than L2"},
+            "cpu_baseline": {"value": value, "unit": "timesteps/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    del res
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="C3")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import numpy as np
+
+    from projectracer_gb300 import engine as eng
+    from projectracer_gb300.inputs import make_state
+
+    dist = Dist(world)
+    cfg, w = bench_config(args.workload, args.precision)
+    apply_bench_solver(cfg, w)
+    st = make_state(cfg, 3 + rank, noise=w.get("noise", 1e-3))
+    e = eng.Engine(cfg)
+    e.upload(st)
+    W = max(3, args.warmup)
+    for _ in range(W):
+        e.solve_psi()
+        e.step()
+    # timed region: device-resident inputs
+    sampler = ClockSampler(local)
+    sampler.start()
+    e.prof_reset()
+    dist.barrier()
+    t0 = time.perf_counter()
+    cycles, solve_ms, nsolve = 0, 0.0, 0
+    for _ in range(args.steps):
+        i0 = e.solve_psi()
+        dt, i1 = e.step()
+        cycles += i0["cycles"] + i1["cycles"]
+        solve_ms += i0["ms"] + i1["ms"]
+        nsolve += 4
+    dist.barrier()
+    elapsed = dist.max(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    launches = e.launches()
+    value = world * args.steps / elapsed
+    # end to end through the C ABI with host buffers: per step the driver pushes its tracer
+    # arrays (pinned host memory) and reads back the restart records
+    e2e = end_to_end(e, eng, cfg, st, max(1, min(3, args.steps)), dist, world)
+    # kernel timing pass for the roofline (events bracket each timed kernel batch)
+    roof = roofline(e, eng, cfg)
+    line = {"metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": W, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+            "data": "synthetic",
+            "config": {"workload": f"{args.workload} {cfg.nx}x{cfg.nz} {cfg.ntr} tracers",
+                       "precision": args.precision, "tolerance": cfg.tolerance, "grids": e.L.pt_grids(),
+                       "courant": cfg.courant, "replicas": world, "l2_flush": "inputs larger than L2"},
+            "psi_solve_ms": solve_ms / max(1, nsolve), "mg_cycles_per_solve": cycles / max(1, nsolve),
+            "tracers_per_s": value * cfg.ntr, "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
+            "roofline": roof}
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args.workload, args.precision).items()
+                                    if k != "sample_seconds_per_step"}
+        except Exception as ex:  # the baseline is reported, not required for the GPU number
+            line["cpu_baseline"] = {"value": None, "unit": "timesteps/s", "cores": os.cpu_count(), "kind": "port",
+                                    "sample": f"failed: {ex}"}
+    e.close()
+    dist.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def end_to_end(e, eng, cfg, st, steps, dist, world):
+    import numpy as np
+
+    try:
+        import torch
+
+        def pinned(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    except Exception:  # pinned buffers are an optimisation of the host side only
+        def pinned(a):
+            return np.ascontiguousarray(a)
+    n = int(cfg.ntr)
+    h_r, h_s, h_T, h_C = (pinned(np.empty(n)) for _ in range(4))
+    h_r[:] = e.get(eng.F_TRACER_R)
+    h_s[:] = e.get(eng.F_TRACER_S)
+    h_T[:] = e.get(eng.F_TRACER_T)
+    h_C[:] = e.get(eng.F_TRACER_C)
+    lx, hx, lz, hz, _ = e.extent(eng.F_T)
+    grid_T = pinned(np.empty((hz - lz + 1, hx - lx + 1)))
+    grid_S = pinned(np.empty_like(grid_T))
+    lx, hx, lz, hz, _ = e.extent(eng.F_CNEW)
+    grid_C = pinned(np.empty((hz - lz + 1, hx - lx + 1)))
+    ptr = lambda a: a.ctypes.data_as(__import__("ctypes").c_void_p)  # noqa: E731
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for fid, a in ((eng.F_TRACER_R, h_r), (eng.F_TRACER_S, h_s), (eng.F_TRACER_T, h_T), (eng.F_TRACER_C, h_C)):
+            e._check(e.L.pt_set_field(fid, ptr(a)))
+        e.solve_psi()
+        e.step()
+        e._check(e.L.pt_download_state(ptr(grid_T), ptr(grid_C), ptr(grid_S), ptr(h_r), ptr(h_s), ptr(h_C), ptr(h_T)))
+    dist.barrier()
+    el = dist.max(time.perf_counter() - t0)
+    h2d = 4 * n * 8
+    d2h = 4 * n * 8 + (grid_T.size + grid_S.size + grid_C.size) * 8
+    return {"value": world * steps / el, "unit": "timesteps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps,
+            "note": "per step: tracer arrays host->device through pt_set_field, pt_solve_psi + pt_step, "
+                    "restart records device->host through pt_download_state"}
+
+
+def roofline(e, eng, cfg):
+    peaks = measured_peaks()
+    e.prof_reset()
+    e.prof_enable(True)
+    e.solve_psi()
+    e.step()
+    e.prof_enable(False)
+    nx, nz = cfg.nx, cfg.nz
+    interior = (nx - 1) * (nz - 1)
+    n = int(cfg.ntr)
+    # algorithmic bytes per launch of each timed kernel class
+    per_launch = {0: 88.0 * interior, 1: 44.0 * interior, 2: 96.0 * n, 3: 32.0 * n + 28.0 * (nx + 1) * (nz + 1)}
+    names = {0: "RKC1 stage, FP64, finest level", 1: "RKC1 stage, FP32, finest level",
+             2: "RK4 tracer stage (3 interpolations + update)", 3: "tracer->grid projection"}
+    best, kinds = None, {}
+    for kid in range(4):
+        cnt, ms = e.prof_kernel(kid)
+        if cnt:
+            kinds[names[kid]] = {"launches": cnt, "total_ms": ms, "avg_ms": ms / cnt}
+            if best is None or ms > best[2]:
+                best = (kid, cnt, ms)
+    if best is None:
+        return None
+    kid, cnt, ms = best
+    avg_s = ms / cnt * 1e-3
+    achieved = per_launch[kid] / avg_s / 1e9
+    return {"bound": "hbm", "kernel": names[kid], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)",
+            "traffic": None, "algorithmic_bytes_per_launch": per_launch[kid], "avg_launch_ms": avg_s * 1e3,
+            "timed_kernels": kinds}
+
+
+if __name__ == "__main__":
+    main()

@@ -41,6 +41,13 @@ extern "C" {
 #define PT_PREC_FP64 0  /* plain FP64 multigrid: the reference algorithm on the GPU */
 #define PT_PREC_MIXED 1 /* FP32 smoothing/transfers, FP64 residual + defect correction, FP64 coarse LU */
 
+/* Coarse-level initial guess inside a multigrid cycle.  The reference never resets
+ * error(:,:,2:grids) (zeroed once, main.f90:229), so each coarse visit starts from the previous
+ * coarse correction; PT_MG_CORRECTION starts each descent from zero (textbook correction scheme),
+ * which converges in fewer cycles and keeps converging where the reference's variant stalls. */
+#define PT_MG_REFERENCE 0
+#define PT_MG_CORRECTION 1
+
 /* Initial-guess mode of the stream-function solve (spec extension). */
 #define PT_GUESS_PREVIOUS 0 /* previous psi (the reference's warm start, iterative_solver.f90:134) */
 #define PT_GUESS_ZERO 1
@@ -84,7 +91,8 @@ typedef struct pt_config {
     double visP, visT, delta_visT, eig_ratio_min, visC, delta_visC;
     double Tbot_iso, Ttop_iso;
     double dent;           /* reference height for the entrainment statistic */
-    double inner_tol;      /* mixed precision: FP32 inner-solve reduction per refinement (0 = default 1e-4) */
+    int32_t mg_scheme;     /* PT_MG_* (&gpu group) */
+    int32_t reserved;
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

@@ -1,0 +1,35 @@
+/*
+ * ptgpu_prof.h -- measurement hooks of libptgpu (not part of the reference's interface; the
+ * reference times its phases with omp_get_wtime accumulators, basics.f90:27-31, printed at
+ * main.f90:305-346).  Used by the benchmark to time kernels with CUDA events on the library's
+ * own stream and to count kernel launches.
+ */
+#ifndef PTGPU_PROF_H
+#define PTGPU_PROF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* kernel classes timed when profiling is on */
+#define PT_KT_RKC_FP64_L1 0 /* one FP64 RKC1 smoother stage on the finest level */
+#define PT_KT_RKC_FP32_L1 1 /* one FP32 RKC1 smoother stage on the finest level (mixed precision) */
+#define PT_KT_RK_STAGE 2    /* one RK4 tracer stage (3 interpolations + update per tracer) */
+#define PT_KT_PROJECT 3     /* one tracer->grid projection (sort, partial sums, node sums) */
+
+/* Bracket every batch of launches of the timed kernel classes with CUDA events (adds one
+ * event synchronisation per batch). */
+int pt_prof_enable(int on);
+/* Zero the per-class counters and the kernel launch counter. */
+int pt_prof_reset(void);
+/* Launches and summed event time (ms) of a kernel class since the last reset. */
+int pt_prof_kernel(int id, int64_t* launches, double* total_ms);
+/* Number of kernels this library launched since the last reset. */
+int64_t pt_prof_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

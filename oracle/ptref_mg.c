@@ -541,6 +541,8 @@ int ref_multigrid(ptref_state* s) {
             int level = multi[p];
             if (multi[p - 1] < multi[p]) {
                 compute_RHS(s, level);
+                if (s->cfg.mg_scheme == PT_MG_CORRECTION && level > 1)
+                    memset(s->err[level].p, 0, sizeof(double) * (size_t)s->err[level].ld * (size_t)(s->err[level].nz + 7));
                 if (p <= grids && q == 1) compute_reference_residual(s, level);
             }
             if (level < grids) {

@@ -391,7 +391,7 @@ ptref_state* ptref_create(const pt_config* cfg, int iterate, int nparts) {
     ptref_state* s = (ptref_state*)calloc(1, sizeof(ptref_state));
     s->cfg = *cfg;
     s->iterate = iterate;
-    s->nparts = nparts < 1 ? 1 : nparts;
+    s->nparts = nparts < 0 ? 0 : nparts; /* 0 = canonical projection order */
     s->smooth_vis = 1;
     int nx = cfg->nx, nz = cfg->nz, grids = cfg->grids;
     smoothing_parameters(s);

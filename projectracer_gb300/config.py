@@ -18,6 +18,8 @@ PT_PREC_MIXED = 1
 PT_GUESS_PREVIOUS = 0
 PT_GUESS_ZERO = 1
 PT_GUESS_UNET = 2
+PT_MG_REFERENCE = 0
+PT_MG_CORRECTION = 1
 
 
 class PtConfig(ctypes.Structure):
@@ -63,7 +65,8 @@ class PtConfig(ctypes.Structure):
         ("Tbot_iso", ctypes.c_double),
         ("Ttop_iso", ctypes.c_double),
         ("dent", ctypes.c_double),
-        ("inner_tol", ctypes.c_double),
+        ("mg_scheme", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
     @staticmethod
@@ -108,7 +111,7 @@ class PtConfig(ctypes.Structure):
         c.Tbot_iso = 1.0
         c.Ttop_iso = 0.0
         c.dent = 0.5
-        c.inner_tol = 0.0
+        c.mg_scheme = PT_MG_REFERENCE
         return c
 
     @staticmethod
@@ -145,7 +148,7 @@ class PtConfig(ctypes.Structure):
         gpu = g.get("gpu", {})
         c.precision = int(gpu.get("precision", c.precision))
         c.guess_mode = int(gpu.get("guess_mode", c.guess_mode))
-        c.inner_tol = float(gpu.get("inner_tol", 0.0))
+        c.mg_scheme = int(gpu.get("mg_scheme", PT_MG_REFERENCE))
         tpc = int(inp.get("tpc", 0))
         c.ntr = ntr if ntr is not None else (c.nx + 1) * (c.nz + 1) * tpc
         return c

@@ -2,14 +2,17 @@
 // and the time-step orchestration (energy_time, energy.f90:181-556) on one CUDA stream.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
 #include "pt_consts.cuh"
+#include "../../include/ptgpu_prof.h"
 
 namespace pt {
 
 Engine* g_eng = nullptr;
+int64_t g_launches = 0;
 thread_local std::string g_err;
 
 int upload_consts_fields(const Engine& E);
@@ -38,6 +41,20 @@ PhaseTimer::~PhaseTimer() {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, E.ev0, E.ev1);
         E.phase_ms[slot] += ms;
+    }
+}
+
+KernelTimer::KernelTimer(Engine& e, int i, int count) : E(e), id(i), n(count) {
+    if (E.prof) cudaEventRecord(E.kev0, E.st);
+}
+KernelTimer::~KernelTimer() {
+    if (!E.prof) return;
+    cudaEventRecord(E.kev1, E.st);
+    if (cudaEventSynchronize(E.kev1) == cudaSuccess) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, E.kev0, E.kev1);
+        E.kms[id] += ms;
+        E.kcount[id] += n;
     }
 }
 
@@ -83,6 +100,7 @@ static int engine_alloc(Engine& E) {
     if ((rc = ialloc(E, &E.scan_tmp, (size_t)ncell + (size_t)ncell / 1024 + 64))) return rc;
     if ((rc = dalloc(E, &E.cpart, (size_t)27 * ncell))) return rc;
     if ((rc = mg_alloc(E))) return rc;
+    if (E.cfg.precision == PT_PREC_MIXED && (rc = mixed_alloc(E))) return rc;
     return 0;
 }
 
@@ -99,14 +117,15 @@ static void engine_free(Engine& E) {
     for (int l = 0; l < PT_MAXLEV; l++) {
         double* arrs[] = {E.err[l], E.S0[l], E.S1[l], E.S2[l], E.RHS[l], E.res[l], E.dtst[l], E.ratio[l],
                           E.vis[l], E.visst[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l],
-                          E.vxxmzz[l], E.vsm[l], E.visw[l]};
+                          E.vxxmzz[l], E.vsm[l]};
         for (auto a : arrs)
             if (a) cudaFree(a);
-        float* farrs[] = {E.ferr[l], E.fS1[l], E.fS2[l], E.fRHS[l], E.fres[l], E.fcoef[l]};
+        float* farrs[] = {E.ferr[l], E.fS0[l], E.fS1[l], E.fS2[l], E.fRHS[l], E.fres[l],
+                          E.fcoef[l][0], E.fcoef[l][1], E.fcoef[l][2], E.fcoef[l][3], E.fcoef[l][4], E.fcoef[l][5]};
         for (auto a : farrs)
             if (a) cudaFree(a);
     }
-    for (int q = PT_MAXLEV; q < 11; q++)
+    for (int q = 0; q < 11; q++)
         if (E.visw[q]) cudaFree(E.visw[q]);
     int32_t* ia[] = {E.nempty, E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp};
     for (auto a : ia)
@@ -116,6 +135,12 @@ static void engine_free(Engine& E) {
     if (E.hscal) cudaFreeHost(E.hscal);
     if (E.ev0) cudaEventDestroy(E.ev0);
     if (E.ev1) cudaEventDestroy(E.ev1);
+    if (E.gM1) cudaGraphExecDestroy(E.gM1);
+    if (E.gM2) cudaGraphExecDestroy(E.gM2);
+    if (E.gA) cudaGraphExecDestroy(E.gA);
+    if (E.gB) cudaGraphExecDestroy(E.gB);
+    if (E.kev0) cudaEventDestroy(E.kev0);
+    if (E.kev1) cudaEventDestroy(E.kev1);
     if (E.st) cudaStreamDestroy(E.st);
 }
 
@@ -126,6 +151,16 @@ static Geo make_geo(int nx, int nz) {
     g.pitch = ((nx + 2 * GH + 1) + 15) / 16 * 16;
     return g;
 }
+
+static bool trace_on() {
+    static int on = -1;
+    if (on < 0) on = getenv("PTGPU_TRACE") ? 1 : 0;
+    return on == 1;
+}
+#define TRACE(msg)                                          \
+    do {                                                    \
+        if (trace_on()) fprintf(stderr, "[ptgpu] %s\n", msg); \
+    } while (0)
 
 static int need(int ok) { return ok ? 0 : fail(PT_ERR_STATE, "call pt_init (and pt_upload_state) first"); }
 
@@ -186,6 +221,7 @@ const char* pt_last_error(void) { return g_err.c_str(); }
 int pt_init(const pt_config* cfg) {
     if (!cfg) return fail(PT_ERR_ARG, "null config");
     if (g_eng) pt_finalize();
+    TRACE("pt_init: constants");
     Engine* E = new Engine();
     E->cfg = *cfg;
     E->ntr = cfg->ntr;
@@ -196,12 +232,16 @@ int pt_init(const pt_config* cfg) {
         return fail(PT_ERR_CONFIG, "precision must be PT_PREC_FP64 or PT_PREC_MIXED");
     }
     if ((int64_t)cfg->ntr > 2000000000LL) { delete E; return fail(PT_ERR_CONFIG, "ntr above 2e9 is not supported"); }
+    TRACE("pt_init: geometry and stream");
     E->g1 = make_geo(cfg->nx, cfg->nz);
     for (int l = 1; l <= E->grids; l++) E->gl[l] = make_geo(E->L[l].nx, E->L[l].nz);
     if ((rc = cuda_check(cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking), "stream"))) { delete E; return rc; }
     cudaEventCreate(&E->ev0);
     cudaEventCreate(&E->ev1);
+    cudaEventCreate(&E->kev0);
+    cudaEventCreate(&E->kev1);
     g_eng = E;
+    TRACE("pt_init: device allocations and constants");
     if ((rc = engine_alloc(*E)) || (rc = upload_consts_fields(*E)) || (rc = upload_consts_tracers(*E)) ||
         (rc = upload_consts_mg(*E)) || (rc = upload_consts_mixed(*E))) {
         std::string msg = g_err;
@@ -210,6 +250,7 @@ int pt_init(const pt_config* cfg) {
         return rc;
     }
     rc = cuda_check(cudaStreamSynchronize(E->st), "init");
+    TRACE("pt_init: done");
     return rc;
 }
 
@@ -292,10 +333,12 @@ int pt_upload_state(const double* xg, const double* zg, const double* T, const d
     CK(cudaMemcpyAsync(E.str, str, nb, cudaMemcpyHostToDevice, E.st));
     CK(cudaMemcpyAsync(E.Ttr, Ttr, nb, cudaMemcpyHostToDevice, E.st));
     if (E.cfg.comp) CK(cudaMemcpyAsync(E.Ctr, Ctr, nb, cudaMemcpyHostToDevice, E.st));
+    TRACE("upload: boundary conditions");
     // grid.f90:67-73: boundary conditions on the restart fields
     if ((rc = enforce_bcs_T(E, E.T))) return rc;
     if ((rc = enforce_bcs_stream(E, 1, E.SF))) return rc;
     if (E.cfg.comp && (rc = enforce_bcs_C(E, E.Cnew))) return rc;
+    TRACE("upload: projection and smoothers");
     // grid.f90:93-95: projection without smoothing, then main.f90:205-209
     if ((rc = project(E, E.rtr, E.str, E.Ttr, E.T, 0))) return rc;
     if ((rc = smoother_time_T(E, E.T))) return rc;
@@ -438,6 +481,29 @@ int pt_set_guess_mode(int mode, const char* weights_path) {
     g_eng->cfg.guess_mode = mode;
     return 0;
 }
+
+int pt_prof_enable(int on) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    g_eng->prof = on ? 1 : 0;
+    return 0;
+}
+
+int pt_prof_reset(void) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    for (int q = 0; q < 8; q++) { g_eng->kcount[q] = 0; g_eng->kms[q] = 0.0; }
+    g_launches = 0;
+    return 0;
+}
+
+int pt_prof_kernel(int id, int64_t* launches, double* total_ms) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (id < 0 || id >= 8) return fail(PT_ERR_ARG, "kernel id out of range");
+    if (launches) *launches = g_eng->kcount[id];
+    if (total_ms) *total_ms = g_eng->kms[id];
+    return 0;
+}
+
+int64_t pt_prof_launches(void) { return g_launches; }
 
 int pt_phase_times(double* ms5) {
     if (int rc = need(g_eng != nullptr)) return rc;

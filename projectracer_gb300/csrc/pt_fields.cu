@@ -62,7 +62,7 @@ __global__ void k_bc_T(double* dst, const double* src, const double* Cvis, Geo g
 
 int enforce_bcs_T(Engine& E, double* f) {
     int tot = (E.K.nx + 7) * (E.K.nz + 7);
-    k_bc_T<<<nblk(tot, 256), 256, 0, E.st>>>(f, f, E.Cvis, E.g1, 3, 0);
+    PT_COUNT(), k_bc_T<<<nblk(tot, 256), 256, 0, E.st>>>(f, f, E.Cvis, E.g1, 3, 0);
     CKL("k_bc_T");
     return 0;
 }
@@ -101,8 +101,8 @@ __global__ void k_bc_C_cols(double* C, Geo g) {
 }
 
 int enforce_bcs_C(Engine& E, double* f) {
-    k_bc_C_rows<<<nblk((E.K.nx + 11) * 10, 256), 256, 0, E.st>>>(f, E.g1);
-    k_bc_C_cols<<<nblk(10 * (E.K.nz + 1), 256), 256, 0, E.st>>>(f, E.g1);
+    PT_COUNT(), k_bc_C_rows<<<nblk((E.K.nx + 11) * 10, 256), 256, 0, E.st>>>(f, E.g1);
+    PT_COUNT(), k_bc_C_cols<<<nblk(10 * (E.K.nz + 1), 256), 256, 0, E.st>>>(f, E.g1);
     CKL("bc_C");
     return 0;
 }
@@ -129,7 +129,7 @@ int reduce_max_smoothness(Engine& E, const double* f, double* out) {
     unsigned long long* d = (unsigned long long*)E.dscal;
     CK(cudaMemsetAsync(d, 0, 8, E.st));
     dim3 grid(nblk(E.K.nx, 128), E.K.nz - 1);
-    k_smoothness<<<grid, 128, 0, E.st>>>(f, E.g1, d);
+    PT_COUNT(), k_smoothness<<<grid, 128, 0, E.st>>>(f, E.g1, d);
     CKL("k_smoothness");
     CK(cudaMemcpyAsync(E.hscal, d, 8, cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
@@ -170,7 +170,7 @@ int smoother_time_T(Engine& E, const double* Tin) {
         if (diff < E.delta_T) { E.n_temp = n; return 0; }
         if (n >= cap) return fail(PT_ERR_ITER_CAP, "temperature smoother exceeded its iteration cap");
         dim3 grid(nblk(E.K.nx + 1, 128), E.K.nz + 1);
-        k_smooth_T<<<grid, 128, 0, E.st>>>(E.scratch, E.Tvis, E.g1, dts);
+        PT_COUNT(), k_smooth_T<<<grid, 128, 0, E.st>>>(E.scratch, E.Tvis, E.g1, dts);
         CKL("k_smooth_T");
         std::swap(E.scratch, E.Tvis);
         if ((rc = enforce_bcs_T(E, E.Tvis))) return rc;
@@ -214,9 +214,9 @@ __global__ void k_cond_grad(double* cr, double* cs, const double* cd, Geo g) {
 
 int load_conductivity(Engine& E) {
     int tot = (E.K.nx + 11) * (E.K.nz + 11);
-    k_cond<<<nblk(tot, 256), 256, 0, E.st>>>(E.cond, E.Cvis, E.g1);
+    PT_COUNT(), k_cond<<<nblk(tot, 256), 256, 0, E.st>>>(E.cond, E.Cvis, E.g1);
     tot = (E.K.nx + 7) * (E.K.nz + 7);
-    k_cond_grad<<<nblk(tot, 256), 256, 0, E.st>>>(E.cond_r, E.cond_s, E.cond, E.g1);
+    PT_COUNT(), k_cond_grad<<<nblk(tot, 256), 256, 0, E.st>>>(E.cond_r, E.cond_s, E.cond, E.g1);
     CKL("conductivity");
     return 0;
 }
@@ -249,9 +249,9 @@ __global__ void k_tracer_space(double* tsa, const double* X, const double* cd, c
 
 int load_tracer_space(Engine& E) {
     int tot = (E.K.nx + 11) * (E.K.nz + 11);
-    k_bc_T<<<nblk(tot, 256), 256, 0, E.st>>>(E.Text, E.Tratio, E.Cvis, E.g1, 5, 1);
+    PT_COUNT(), k_bc_T<<<nblk(tot, 256), 256, 0, E.st>>>(E.Text, E.Tratio, E.Cvis, E.g1, 5, 1);
     tot = (E.K.nx + 7) * (E.K.nz + 7);
-    k_tracer_space<<<nblk(tot, 256), 256, 0, E.st>>>(E.tsa, E.Text, E.cond, E.cond_r, E.cond_s, E.Cvis, E.g1);
+    PT_COUNT(), k_tracer_space<<<nblk(tot, 256), 256, 0, E.st>>>(E.tsa, E.Text, E.cond, E.cond_r, E.cond_s, E.Cvis, E.g1);
     CKL("tracer_space");
     return 0;
 }
@@ -279,7 +279,7 @@ __global__ void k_derivs(double* d1, double* d2, double* d3, const double* f, Ge
 
 int compute_derivatives(Engine& E, const double* f, int which) {
     dim3 grid(nblk(E.K.nx + 1, 128), E.K.nz + 7);
-    k_derivs<<<grid, 128, 0, E.st>>>(E.der[which][0], E.der[which][1], E.der[which][2], f, E.g1);
+    PT_COUNT(), k_derivs<<<grid, 128, 0, E.st>>>(E.der[which][0], E.der[which][1], E.der[which][2], f, E.g1);
     CKL("k_derivs");
     return 0;
 }
@@ -326,9 +326,9 @@ __global__ void k_vel_bc(double* u, double* w, Geo g) {
 
 int compute_velocities(Engine& E) {
     dim3 grid(nblk(E.K.nx + 1, 128), E.K.nz + 1);
-    k_vel_interior<<<grid, 128, 0, E.st>>>(E.u, E.w, E.SF, E.g1);
+    PT_COUNT(), k_vel_interior<<<grid, 128, 0, E.st>>>(E.u, E.w, E.SF, E.g1);
     int tot = (E.K.nx + 7) * (E.K.nz + 7);
-    k_vel_bc<<<nblk(tot, 256), 256, 0, E.st>>>(E.u, E.w, E.g1);
+    PT_COUNT(), k_vel_bc<<<nblk(tot, 256), 256, 0, E.st>>>(E.u, E.w, E.g1);
     CKL("velocities");
     return 0;
 }
@@ -361,7 +361,7 @@ int stability_dt(Engine& E, double* dt) {
     unsigned long long* d = (unsigned long long*)E.dscal;
     CK(cudaMemsetAsync(d, 0, 16, E.st));
     dim3 grid(nblk(K.nx + 1, 128), K.nz + 1);
-    k_eig_max<<<grid, 128, 0, E.st>>>(E.cond, E.cond_r, E.cond_s, E.g1, Tr_max, Ts_max, Trr_max, Tss_max, d);
+    PT_COUNT(), k_eig_max<<<grid, 128, 0, E.st>>>(E.cond, E.cond_r, E.cond_s, E.g1, Tr_max, Ts_max, Trr_max, Tss_max, d);
     CKL("k_eig_max");
     CK(cudaMemcpyAsync(E.hscal, d, 16, cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
@@ -473,9 +473,9 @@ int stats(Engine& E, pt_stats_row* o) {
     double* rows = E.red;
     int nz = E.K.nz;
     const double* C = E.cfg.comp ? E.Cnew : E.T;
-    k_stats_rows<<<nblk(nz + 1, 64), 64, 0, E.st>>>(E.T, C, E.u, E.w, E.cond, E.vis[1], E.g1, rows);
+    PT_COUNT(), k_stats_rows<<<nblk(nz + 1, 64), 64, 0, E.st>>>(E.T, C, E.u, E.w, E.cond, E.vis[1], E.g1, rows);
     double* out = rows + 4 * (nz + 1) + 8;
-    k_stats_tail<<<1, 32, 0, E.st>>>(rows, E.T, E.u, E.w, E.cond, E.err[1], E.nempty, E.g1, out, E.kent);
+    PT_COUNT(), k_stats_tail<<<1, 32, 0, E.st>>>(rows, E.T, E.u, E.w, E.cond, E.err[1], E.nempty, E.g1, out, E.kent);
     CKL("stats");
     CK(cudaMemcpyAsync(E.hscal, out, 17 * sizeof(double), cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
@@ -531,8 +531,8 @@ __global__ void k_sum_parts(const double* part, int n, double* out) {
 }
 
 int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitch, double* dout) {
-    k_rowsum_abs<<<nz - 1, 256, 0, E.st>>>(f, nx, pitch, E.red);
-    k_sum_parts<<<1, 1024, 0, E.st>>>(E.red, nz - 1, dout);
+    PT_COUNT(), k_rowsum_abs<<<nz - 1, 256, 0, E.st>>>(f, nx, pitch, E.red);
+    PT_COUNT(), k_sum_parts<<<1, 1024, 0, E.st>>>(E.red, nz - 1, dout);
     CKL("reduce_sum_abs");
     return 0;
 }

@@ -79,10 +79,14 @@ struct Engine {
            *RHS[PT_MAXLEV] = {}, *res[PT_MAXLEV] = {}, *dtst[PT_MAXLEV] = {}, *ratio[PT_MAXLEV] = {},
            *vis[PT_MAXLEV] = {}, *visst[PT_MAXLEV] = {}, *vx[PT_MAXLEV] = {}, *vz[PT_MAXLEV] = {},
            *vxx[PT_MAXLEV] = {}, *vzz[PT_MAXLEV] = {}, *vxz[PT_MAXLEV] = {}, *vxxpzz[PT_MAXLEV] = {},
-           *vxxmzz[PT_MAXLEV] = {}, *vsm[PT_MAXLEV] = {}, *visw[PT_MAXLEV] = {};
+           *vxxmzz[PT_MAXLEV] = {}, *vsm[PT_MAXLEV] = {};
+    double* visw[11] = {};  // work set for smoothing the finer level before restriction
     // mixed precision mirrors
-    float *ferr[PT_MAXLEV] = {}, *fS1[PT_MAXLEV] = {}, *fS2[PT_MAXLEV] = {}, *fRHS[PT_MAXLEV] = {},
-          *fres[PT_MAXLEV] = {}, *fcoef[PT_MAXLEV] = {};
+    float *ferr[PT_MAXLEV] = {}, *fS0[PT_MAXLEV] = {}, *fS1[PT_MAXLEV] = {}, *fS2[PT_MAXLEV] = {},
+          *fRHS[PT_MAXLEV] = {}, *fres[PT_MAXLEV] = {};
+    float* fcoef[PT_MAXLEV][6] = {};  // vis, vx, vz, vxz, vxxmzz, dt_stream in FP32
+    cudaGraphExec_t gM1 = nullptr, gM2 = nullptr;
+    int64_t nM1 = 0, nM2 = 0;
     double* psi_keep = nullptr;
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
@@ -110,9 +114,28 @@ struct Engine {
     double phase_ms[5] = {};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     size_t bytes_allocated = 0;
+    // measurement hooks (ptgpu_prof.h): kernel launch count and per-kernel event timing
+    int64_t launches = 0;
+    cudaGraphExec_t gA = nullptr, gB = nullptr;  // captured multigrid cycle (parts A and B)
+    int64_t nA = 0, nB = 0;
+    int prof = 0;
+    cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+    int64_t kcount[8] = {};
+    double kms[8] = {};
 };
 
 extern Engine* g_eng;
+extern int64_t g_launches;
+#define PT_COUNT() (++pt::g_launches)
+
+// brackets a batch of n launches of kernel class `id` with events when profiling is on
+struct KernelTimer {
+    Engine& E;
+    int id, n;
+    KernelTimer(Engine& e, int i, int count);
+    ~KernelTimer();
+};
+enum { KT_RKC_FP64_L1 = 0, KT_RKC_FP32_L1 = 1, KT_RK_STAGE = 2, KT_PROJECT = 3 };
 extern thread_local std::string g_err;
 
 int fail(int code, const std::string& msg);
@@ -159,6 +182,10 @@ int mg_alloc(Engine& E);
 
 // mixed precision (pt_mixed.cu)
 int multigrid_mixed(Engine& E, pt_solve_info* info);
+int mixed_alloc(Engine& E);
+int mg_setup_solve(Engine& E);
+int coarse_band_solve(Engine& E);
+int residual_level1(Engine& E);
 
 // reductions (pt_fields.cu)
 int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitch, double* out);

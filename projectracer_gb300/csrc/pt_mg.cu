@@ -66,8 +66,8 @@ __global__ void k_visbc_rows(double* v, Geo g, int nx, int nz) {
 }
 static int vis_bcs(Engine& E, double* v, int l) {
     const Geo& g = E.gl[l];
-    k_visbc_cols<<<nblk(6 * (g.nz + 7), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
-    k_visbc_rows<<<nblk(6 * (g.nx + 1), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
+    PT_COUNT(), k_visbc_cols<<<nblk(6 * (g.nz + 7), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
+    PT_COUNT(), k_visbc_rows<<<nblk(6 * (g.nx + 1), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
     CKL("vis_bcs");
     return 0;
 }
@@ -152,14 +152,14 @@ static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record)
     dim3 gg(nblk(nx + 1, 128), nz + 1);
     for (int guard = 0; guard < 100000; guard++) {
         for (int nn = nn_store; nn <= Niter; nn++) {
-            k_vis_grad<<<gg, 128, 0, E.st>>>(S, g, l, Nvis_store != 0, ivis);
+            PT_COUNT(), k_vis_grad<<<gg, 128, 0, E.st>>>(S, g, l, Nvis_store != 0, ivis);
             CKL("k_vis_grad");
             if (interpolate == 0 && (Nvis_store >= 1 || ivis == 0)) {
                 unsigned long long* d = (unsigned long long*)E.dscal;
                 unsigned long long init = (unsigned long long)__builtin_bit_cast(long long, 1.0e100);
                 CK(cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, E.st));
                 dim3 ge(nblk(nx - 1, 128), nz - 1);
-                k_test_eig<<<ge, 128, 0, E.st>>>(S, g, l, ae, be, ctemp, d);
+                PT_COUNT(), k_test_eig<<<ge, 128, 0, E.st>>>(S, g, l, ae, be, ctemp, d);
                 CKL("k_test_eig");
                 CK(cudaMemcpyAsync(E.hscal, d, 8, cudaMemcpyDeviceToHost, E.st));
                 CK(cudaStreamSynchronize(E.st));
@@ -180,7 +180,7 @@ static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record)
             int ntemp = Niter - nn + 1;
             double c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
             c = 0.99 * c;
-            k_vis_update<<<gg, 128, 0, E.st>>>(S.vis, S.vsm, g, nx, nz, c);
+            PT_COUNT(), k_vis_update<<<gg, 128, 0, E.st>>>(S.vis, S.vsm, g, nx, nz, c);
             CKL("k_vis_update");
             if ((rc = vis_bcs(E, S.vis, l))) return rc;
         }
@@ -228,7 +228,7 @@ static int compute_viscosity(Engine& E, int level) {
     const Geo& g = E.gl[level];
     if (level == 1) {
         dim3 gg(nblk(g.nx + 1, 128), g.nz + 1);
-        k_visf<<<gg, 128, 0, E.st>>>(E.visst[1], E.Tvis, E.Cvis, g);
+        PT_COUNT(), k_visf<<<gg, 128, 0, E.st>>>(E.visst[1], E.Tvis, E.Cvis, g);
         CKL("k_visf");
         CK(cudaMemcpyAsync(E.vis[1], E.visst[1], g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
         return smoother_vis(E, 1, 0, level_set(E, 1), 1);
@@ -242,9 +242,9 @@ static int compute_viscosity(Engine& E, int level) {
     CK(cudaMemcpyAsync(W.vis, E.visst[lf], gf.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     if ((rc = smoother_vis(E, lf, 1, W, 0))) return rc;
     dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
-    k_restrict<<<gr, 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz);
+    PT_COUNT(), k_restrict<<<gr, 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz);
     int tot = (g.nx + 7) * (g.nz + 7);
-    k_visbc_init<<<nblk(tot, 128), 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz, gf.nx, gf.nz);
+    PT_COUNT(), k_visbc_init<<<nblk(tot, 128), 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz, gf.nx, gf.nz);
     CKL("restrict_coefficients");
     CK(cudaMemcpyAsync(E.visst[level], E.vis[level], g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     return smoother_vis(E, level, 0, level_set(E, level), 0);
@@ -271,8 +271,8 @@ __global__ void k_rhs1(double* RHS, const double* Tb, const double* Cb, Geo g, i
 static int compute_RHS(Engine& E, int level) {
     const Geo& g = E.gl[level];
     dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
-    if (level == 1) k_rhs1<<<gr, 128, 0, E.st>>>(E.RHS[1], E.Tbuoy, E.Cbuoy, g, E.cfg.comp);
-    else k_restrict<<<gr, 128, 0, E.st>>>(E.RHS[level], E.res[level - 1], g, E.gl[level - 1], g.nx, g.nz);
+    if (level == 1) PT_COUNT(), k_rhs1<<<gr, 128, 0, E.st>>>(E.RHS[1], E.Tbuoy, E.Cbuoy, g, E.cfg.comp);
+    else PT_COUNT(), k_restrict<<<gr, 128, 0, E.st>>>(E.RHS[level], E.res[level - 1], g, E.gl[level - 1], g.nx, g.nz);
     CKL("compute_RHS");
     return 0;
 }
@@ -417,7 +417,7 @@ __global__ void k_stream_bcs(double* S, Geo g, int nx, int nz, double sz) {
 int enforce_bcs_stream(Engine& E, int level, double* f) {
     const Geo& g = E.gl[level];
     int tot = (g.nx + 7) * (g.nz + 7);
-    k_stream_bcs<<<nblk(tot, 256), 256, 0, E.st>>>(f, g, g.nx, g.nz, E.cfg.Vbc == 0 ? -1.0 : 1.0);
+    PT_COUNT(), k_stream_bcs<<<nblk(tot, 256), 256, 0, E.st>>>(f, g, g.nx, g.nz, E.cfg.Vbc == 0 ? -1.0 : 1.0);
     CKL("k_stream_bcs");
     return 0;
 }
@@ -426,41 +426,43 @@ static StreamOp stream_op(Engine& E, int l) {
     return StreamOp{E.vis[l], E.vx[l], E.vz[l], E.vxz[l], E.vxxmzz[l], E.RHS[l], E.dtst[l]};
 }
 
-// iterate_stream (RKC1 = 1, splitting = 0) + compute_residual; returns mean|r| in *mag if asked
-static int iterate_stream(Engine& E, int l, int want_mag, double* mag) {
+// iterate_stream (RKC1 = 1, splitting = 0) + compute_residual.  The last stage writes straight
+// into error(:,:,level): a stage reads S0 only at its own node, so the update is safe in place.
+// With want_sum the sum of |residual| is left in dscal[8] (no host synchronisation, so the
+// sequence can be captured in a CUDA graph).  The boundary lines of the stage buffers are zero
+// from allocation and are never written by the stage kernel.
+static int iterate_stream(Engine& E, int l, int want_sum) {
     const Geo& g = E.gl[l];
     const int N = E.cfg.nstageS, Niter = E.cfg.Nmulti, ivis = E.cfg.ivis;
     const double sz = E.cfg.Vbc == 0 ? -1.0 : 1.0;
     StreamOp op = stream_op(E, l);
     dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
-    int tot = (g.nx + 7) * (g.nz + 7);
     double* buf[3] = {E.S0[l], E.S1[l], E.S2[l]};
-    for (int q = 0; q < 3; q++) k_stream_zero_bnd<<<nblk(tot, 256), 256, 0, E.st>>>(buf[q], g, g.nx, g.nz);
     for (int n = 1; n <= Niter; n++) {
         int ntemp = Niter - n + 1;
         double temp = (E.cfg.Nmulti > 1) ? (E.cfg.c_2 - E.cfg.c_1) * (double)(ntemp - 1) / (double)(1 - Niter) : 0.0;
         double c = temp + E.cfg.c_2;
         const double* S0 = E.err[l];
-        // stage 1
+        KernelTimer kt(E, KT_RKC_FP64_L1, l == 1 ? N : 0);
         int cur = 0;
-        k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[cur], S0, nullptr, nullptr, op, g, l, 0, 0, 0, E.K.mewt[1] * c, 1, ivis, sz);
+        PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[cur], S0, nullptr, nullptr, op, g, l, 0, 0, 0, E.K.mewt[1] * c, 1, ivis, sz);
         const double* Sm1 = buf[cur];
         const double* Sm2 = S0;
         for (int j = 2; j <= N; j++) {
             int nxt = (cur + 1) % 3;
             if (buf[nxt] == Sm2) nxt = (nxt + 1) % 3;
-            k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[nxt], Sm1, Sm2, S0, op, g, l, E.K.cc[j], E.K.mew[j], E.K.vv[j],
+            double* out = (j == N) ? E.err[l] : buf[nxt];
+            PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(out, Sm1, Sm2, S0, op, g, l, E.K.cc[j], E.K.mew[j], E.K.vv[j],
                                                E.K.mewt[j] * c, 0, ivis, sz);
             Sm2 = Sm1;
-            Sm1 = buf[nxt];
+            Sm1 = out;
             cur = nxt;
         }
         CKL("k_rkc_stage");
-        CK(cudaMemcpyAsync(E.err[l], Sm1, g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     }
-    k_residual<<<gs, 128, 0, E.st>>>(E.res[l], E.err[l], op, g, l, ivis);
+    PT_COUNT(), k_residual<<<gs, 128, 0, E.st>>>(E.res[l], E.err[l], op, g, l, ivis);
     CKL("k_residual");
-    if (want_mag) return mean_abs(E, E.res[l], l, mag);
+    if (want_sum) return reduce_sum_abs_interior(E, E.res[l], g.nx, g.nz, g.pitch, E.dscal + 8);
     return 0;
 }
 
@@ -483,7 +485,7 @@ static int prolong(Engine& E, int lc) {
     const int lf = lc - 1;
     const Geo &gf = E.gl[lf], &gc = E.gl[lc];
     dim3 gp(nblk(gf.nx - 1, 128), gf.nz - 1);
-    k_prolong<<<gp, 128, 0, E.st>>>(E.err[lf], E.err[lc], gf, gc, gf.nx, gf.nz);
+    PT_COUNT(), k_prolong<<<gp, 128, 0, E.st>>>(E.err[lf], E.err[lc], gf, gc, gf.nx, gf.nz);
     CKL("k_prolong");
     return enforce_bcs_stream(E, lf, E.err[lf]);
 }
@@ -666,9 +668,9 @@ __global__ void k_coarse_scatter(double* E, const double* B, Geo g, int nxc, int
 static int coarse_factor(Engine& E) {
     const int L = E.grids, n = E.ngc;
     CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
-    k_coarse_matrix<<<nblk(n, 128), 128, 0, E.st>>>(E.Mc, E.gl[L], L, E.kl, E.ku, n, E.RowB, E.cfg.Vbc,
+    PT_COUNT(), k_coarse_matrix<<<nblk(n, 128), 128, 0, E.st>>>(E.Mc, E.gl[L], L, E.kl, E.ku, n, E.RowB, E.cfg.Vbc,
                                                     E.cfg.ivis, E.vis[L], E.vx[L], E.vz[L], E.vxz[L], E.vxxmzz[L], E.derr);
-    k_band_lu<<<1, 1024, 0, E.st>>>(E.Mc, E.ipiv, n, E.kl, E.ku, E.derr);
+    PT_COUNT(), k_band_lu<<<1, 1024, 0, E.st>>>(E.Mc, E.ipiv, n, E.kl, E.ku, E.derr);
     CKL("coarse LU");
     int h = 0;
     CK(cudaMemcpyAsync(&h, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
@@ -680,11 +682,27 @@ static int coarse_factor(Engine& E) {
 static int coarse_solve(Engine& E) {
     const int L = E.grids, n = E.ngc;
     const Geo& g = E.gl[L];
-    k_coarse_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.RHS[L], E.RowB, g, g.nx, g.nz);
-    k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
-    k_coarse_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.err[L], E.Bc, g, g.nx, g.nz);
+    PT_COUNT(), k_coarse_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.RHS[L], E.RowB, g, g.nx, g.nz);
+    PT_COUNT(), k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
+    PT_COUNT(), k_coarse_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.err[L], E.Bc, g, g.nx, g.nz);
     CKL("coarse solve");
     return enforce_bcs_stream(E, L, E.err[L]);
+}
+
+// helpers shared with the mixed-precision solver (pt_mixed.cu)
+int coarse_band_solve(Engine& E) {
+    const int n = E.ngc;
+    PT_COUNT(), k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
+    CKL("k_band_solve");
+    return 0;
+}
+
+int residual_level1(Engine& E) {
+    const Geo& g = E.gl[1];
+    dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
+    PT_COUNT(), k_residual<<<gs, 128, 0, E.st>>>(E.res[1], E.err[1], stream_op(E, 1), g, 1, E.cfg.ivis);
+    CKL("k_residual");
+    return reduce_sum_abs_interior(E, E.res[1], g.nx, g.nz, g.pitch, E.dscal + 8);
 }
 
 // ------------------------------------------------------------------ driver
@@ -700,39 +718,81 @@ int mg_setup_solve(Engine& E) {
     return 0;
 }
 
+// One multigrid cycle of the reference's schedule, split where the reference tests convergence
+// (after the level-1 smoothing pass, iterative_solver.f90:313-315).  Part A: level-1 smoothing,
+// residual and sum|r|.  Part B: the rest of the schedule (restrict, coarse visits, coarse solve,
+// prolong back to level 1).  Neither part synchronises, so both are captured as CUDA graphs.
+static int cycle_part(Engine& E, int part) {
+    int rc;
+    const int grids = E.grids, nsteps = E.nsteps;
+    const int* multi = E.multi;
+    if (part == 0) return iterate_stream(E, 1, 1);
+    for (int p = 2; p <= nsteps; p++) {
+        const int level = multi[p];
+        if (multi[p - 1] < multi[p]) {
+            if ((rc = compute_RHS(E, level))) return rc;
+            if (E.cfg.mg_scheme == PT_MG_CORRECTION && level > 1)
+                CK(cudaMemsetAsync(E.err[level], 0, E.gl[level].elems() * sizeof(double), E.st));
+        }
+        if (level < grids) {
+            if ((rc = iterate_stream(E, level, 0))) return rc;
+        } else if ((rc = coarse_solve(E))) {
+            return rc;
+        }
+        if (multi[p + 1] < multi[p] && (rc = prolong(E, level))) return rc;
+    }
+    return 0;
+}
+
+static int capture_part(Engine& E, int part, cudaGraphExec_t* exec, int64_t* nlaunch) {
+    cudaGraph_t graph = nullptr;
+    int64_t before = g_launches;
+    CK(cudaStreamBeginCapture(E.st, cudaStreamCaptureModeThreadLocal));
+    int rc = cycle_part(E, part);
+    cudaError_t e = cudaStreamEndCapture(E.st, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    CK(e);
+    CK(cudaGraphInstantiate(exec, graph, 0));
+    cudaGraphDestroy(graph);
+    *nlaunch = g_launches - before;
+    g_launches = before;
+    return 0;
+}
+
+static int run_part(Engine& E, int part) {
+    if (E.prof) return cycle_part(E, part);  // event timing needs the launches on the stream
+    cudaGraphExec_t& ex = part == 0 ? E.gA : E.gB;
+    int64_t& n = part == 0 ? E.nA : E.nB;
+    if (!ex) {
+        int rc = capture_part(E, part, &ex, &n);
+        if (rc) return rc;
+    }
+    CK(cudaGraphLaunch(ex, E.st));
+    g_launches += n;
+    return 0;
+}
+
 int multigrid(Engine& E, pt_solve_info* info) {
     int rc;
     PhaseTimer tm(E, 2);
     if ((rc = mg_setup_solve(E))) return rc;
-    const int grids = E.grids, nsteps = E.nsteps;
-    const int* multi = E.multi;
+    const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int q = 1;
     double mag1 = 0.0;
     for (;;) {
-        bool conv = false;
-        for (int p = 1; p <= nsteps; p++) {
-            const int level = multi[p];
-            if (multi[p - 1] < multi[p]) {
-                if ((rc = compute_RHS(E, level))) return rc;
-                if (p <= grids && q == 1 && level == 1) {
-                    if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
-                }
-            }
-            if (level < grids) {
-                if ((rc = iterate_stream(E, level, level == 1 && p == 1, &mag1))) return rc;
-                if (level == 1 && p == 1) {
-                    if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite multigrid residual");
-                    if (mag1 > 1.0e10 * E.res_ref[1])
-                        return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
-                }
-            } else {
-                if ((rc = coarse_solve(E))) return rc;
-            }
-            if (level == 1 && mag1 / E.res_ref[1] <= E.cfg.tolerance) { conv = true; break; }
-            if (multi[p + 1] < multi[p])
-                if ((rc = prolong(E, level))) return rc;
-        }
-        if (conv) break;
+        if ((rc = run_part(E, 0))) return rc;
+        CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+        CK(cudaStreamSynchronize(E.st));
+        mag1 = E.hscal[0] / (double)(E.gl[1].nx - 2) / (double)(E.gl[1].nz - 2);
+        (void)norm;
+        if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite multigrid residual");
+        if (mag1 > 1.0e10 * E.res_ref[1])
+            return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
+        if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
+        if ((rc = run_part(E, 1))) return rc;
         q++;
         if (q > E.cfg.max_cycles) return fail(PT_ERR_MG_MAX_CYCLES, "Multigrid Convergence Problem: Too Many Multigrid Cycles Needed");
     }
@@ -771,6 +831,9 @@ int mg_alloc(Engine& E) {
     if (int rc = alloc(&E.Bc, E.ngc)) return rc;
     if (int rc = alloc(&E.RowB, E.ngc)) return rc;
     CK(cudaMalloc(&E.ipiv, sizeof(int) * E.ngc));
+    const size_t smem = sizeof(double) * (size_t)E.ngc;
+    if (smem > 220 * 1024) return fail(PT_ERR_CONFIG, "coarsest grid too large for the banded solve");
+    CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
 }
 

@@ -184,24 +184,25 @@ int project(Engine& E, const double* r, const double* s, const double* Tt, const
     const int64_t n = E.ntr;
     int rc;
     PhaseTimer tm(E, 1);
+    KernelTimer kt(E, KT_PROJECT, 1);
     if (T0f && T0f != E.Tratio) {
         if ((rc = copy_field(E, E.Tratio, T0f))) return rc;
     }
     CK(cudaMemsetAsync(E.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
     CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
-    k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, E.tcell, E.ccount, E.derr);
+    PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, E.tcell, E.ccount, E.derr);
     int nb = (int)nblk(ncell, 1024);
-    k_scan_block<<<nb, 1024, 0, E.st>>>(E.ccount, E.cstart, E.scan_tmp, ncell);
-    k_scan_totals<<<1, 32, 0, E.st>>>(E.scan_tmp, nb);
-    k_scan_add<<<nb, 1024, 0, E.st>>>(E.cstart, E.scan_tmp, ncell);
+    PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(E.ccount, E.cstart, E.scan_tmp, ncell);
+    PT_COUNT(), k_scan_totals<<<1, 32, 0, E.st>>>(E.scan_tmp, nb);
+    PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(E.cstart, E.scan_tmp, ncell);
     int32_t* cursor = E.scan_tmp + nb + 32;
     CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
-    k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.cstart, cursor, E.clist);
-    k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(E.clist, E.cstart, E.ccount, ncell);
-    k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount, ncell,
+    PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.cstart, cursor, E.clist);
+    PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(E.clist, E.cstart, E.ccount, ncell);
+    PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount, ncell,
                                                         E.cpart, E.cfg.comp);
     dim3 grid(nblk(nx + 1, 128), nz + 1);
-    k_node_sums<<<grid, 128, 0, E.st>>>(E.cpart, E.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
+    PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(E.cpart, E.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
     CKL("projection");
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
@@ -312,7 +313,10 @@ int rk_stage(Engine& E, int stage) {
         case 3: A.xr = E.rtr2; A.xs = E.str2; A.rn = E.rtr1; A.sn = E.str1; A.Tn = E.Ttr1; A.dtstage = E.dt; break;
         default: A.xr = E.rtr1; A.xs = E.str1; A.rn = nullptr; A.sn = nullptr; A.Tn = nullptr; A.dtstage = E.dt / 6.0; break;
     }
-    k_rk_stage<<<nblk(E.ntr, 256), 256, 0, E.st>>>(A, E.g1);
+    {
+        KernelTimer kt(E, KT_RK_STAGE, 1);
+        PT_COUNT(), k_rk_stage<<<nblk(E.ntr, 256), 256, 0, E.st>>>(A, E.g1);
+    }
     CKL("k_rk_stage");
     return 0;
 }

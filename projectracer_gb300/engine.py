@@ -57,9 +57,14 @@ _LIB = None
 
 
 def header_symbols() -> list[str]:
-    """Entry points declared in include/ptgpu.h."""
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(pt_[a-z_0-9]+)\s*\(", text, re.M)))
+    """Entry points declared in include/*.h."""
+    inc = os.path.dirname(HEADER)
+    names = set()
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            names |= set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(pt_[a-z_0-9]+)\s*\(", text, re.M))
+    return sorted(names)
 
 
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
@@ -85,6 +90,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_time.argtypes = [ctypes.POINTER(f64), ctypes.POINTER(f64)]
     L.pt_set_guess_mode.argtypes = [i32, ctypes.c_char_p]
     L.pt_phase_times.argtypes = [ctypes.POINTER(f64)]
+    L.pt_prof_enable.argtypes = [i32]
+    L.pt_prof_kernel.argtypes = [i32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
+    L.pt_prof_launches.restype = ctypes.c_int64
     _LIB = L
     return L
 
@@ -159,6 +167,20 @@ class Engine:
 
     def set_guess_mode(self, mode: int, weights: str | None = None):
         self._check(self.L.pt_set_guess_mode(mode, None if weights is None else weights.encode()))
+
+    def prof_enable(self, on: bool = True):
+        self._check(self.L.pt_prof_enable(1 if on else 0))
+
+    def prof_reset(self):
+        self._check(self.L.pt_prof_reset())
+
+    def prof_kernel(self, kid: int) -> tuple[int, float]:
+        n, ms = ctypes.c_int64(), ctypes.c_double()
+        self._check(self.L.pt_prof_kernel(kid, ctypes.byref(n), ctypes.byref(ms)))
+        return n.value, ms.value
+
+    def launches(self) -> int:
+        return int(self.L.pt_prof_launches())
 
     def phase_times(self) -> list[float]:
         v = (ctypes.c_double * 5)()
