@@ -92,7 +92,8 @@ typedef struct pt_config {
     double Tbot_iso, Ttop_iso;
     double dent;           /* reference height for the entrainment statistic */
     int32_t mg_scheme;     /* PT_MG_* (&gpu group) */
-    int32_t reserved;
+    int32_t CFL;           /* &inputs CFL: 1 = velocity terms in the advective eigenvalue and
+                              dt <= 2/eigD_max (energy.f90:809, 859-866) */
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

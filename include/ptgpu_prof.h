@@ -28,6 +28,10 @@ int pt_prof_reset(void);
 int pt_prof_kernel(int id, int64_t* launches, double* total_ms);
 /* Number of kernels this library launched since the last reset. */
 int64_t pt_prof_launches(void);
+/* Device-timed region on the library's stream: end=0 records the start event and opens the NVTX
+ * range "pt_timed"; end=1 records the stop event, waits for it, closes the range and returns the
+ * elapsed milliseconds in *ms. */
+int pt_prof_region(int end, double* ms);
 
 #ifdef __cplusplus
 }

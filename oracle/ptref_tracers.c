@@ -404,7 +404,9 @@ int ref_project(ptref_state* s, const double* r, const double* sv, const double*
     return s->status;
 }
 
-/* stability_RK4, energy.f90:756-810 (eigA/eigD 850-875; tracer=1, CFL=0, torder=4) */
+/* stability_RK4, energy.f90:756-810 (eigA/eigD 850-875; tracer=1, torder=4, uniform grid: xr=zs=1,
+ * xrr=zss=0).  CFL=1 adds the velocities to the advective eigenvalue (859-866) and caps dt at
+ * 2/eigD_max (809). */
 static double stability_RK4(ptref_state* s) {
     int nx = s->nx, nz = s->nz;
     double Ts_max = s->Tr_base / s->ds, Tr_max = s->Tr_base / s->dr;
@@ -415,18 +417,21 @@ static double stability_RK4(ptref_state* s) {
         for (int k = 0; k <= nz; k++)
             for (int i = 0; i <= nx; i++) {
                 double cd = RF(s->conduct, i, k);
-                double eA = fabs(-cd * 0.0 / 1.0 + RF(s->conduct_r, i, k) / 1.0) * Tr_max +
-                            fabs(-cd * 0.0 / 1.0 + RF(s->conduct_s, i, k) / 1.0) * Ts_max;
+                double uu = s->cfg.CFL == 1 ? RF(s->u, i, k) : 0.0, ww = s->cfg.CFL == 1 ? RF(s->w, i, k) : 0.0;
+                double eA = fabs(-cd * 0.0 / 1.0 - uu / 1.0 + RF(s->conduct_r, i, k) / 1.0) * Tr_max +
+                            fabs(-cd * 0.0 / 1.0 - ww / 1.0 + RF(s->conduct_s, i, k) / 1.0) * Ts_max;
                 double eD = cd * (fabs(Trr_max / 1.0) + fabs(Tss_max / 1.0));
                 if (eA > eigA_max) eigA_max = eA;
                 if (eD > eigD_max) eigD_max = eD;
             }
         double dtA = 2.8 / eigA_max, dtD = 2.8 / eigD_max;
         dt = (eigA_max == 0.0) ? dtD : 1.0 / (1.0 / dtA + 1.0 / dtD);
+        dt = s->cfg.courant * dt;
+        if (s->cfg.CFL == 1 && 2.0 / eigD_max < dt) dt = 2.0 / eigD_max;
     } else {
         return ref_fail(s, PT_ERR_CONFIG, "RaT=0 (dt_manual) not supported"), 0.0;
     }
-    return s->cfg.courant * dt;
+    return dt;
 }
 
 static rfld fld_view(ptref_state* s, double* p, int g) {

@@ -1,5 +1,6 @@
 // pt_api.cu -- the C ABI of include/ptgpu.h: context set-up, field exchange, the restart upload
 // and the time-step orchestration (energy_time, energy.f90:181-556) on one CUDA stream.
+#include <nvtx3/nvToolsExt.h>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -131,6 +132,7 @@ static void engine_free(Engine& E) {
     for (auto a : ia)
         if (a) cudaFree(a);
     if (E.ipiv) cudaFree(E.ipiv);
+    if (E.Ginv) cudaFree(E.Ginv);
     if (E.derr) cudaFree(E.derr);
     if (E.hscal) cudaFreeHost(E.hscal);
     if (E.ev0) cudaEventDestroy(E.ev0);
@@ -140,6 +142,8 @@ static void engine_free(Engine& E) {
     if (E.gA) cudaGraphExecDestroy(E.gA);
     if (E.gB) cudaGraphExecDestroy(E.gB);
     if (E.kev0) cudaEventDestroy(E.kev0);
+    if (E.rev0) cudaEventDestroy(E.rev0);
+    if (E.rev1) cudaEventDestroy(E.rev1);
     if (E.kev1) cudaEventDestroy(E.kev1);
     if (E.st) cudaStreamDestroy(E.st);
 }
@@ -152,7 +156,7 @@ static Geo make_geo(int nx, int nz) {
     return g;
 }
 
-static bool trace_on() {
+bool trace_on() {
     static int on = -1;
     if (on < 0) on = getenv("PTGPU_TRACE") ? 1 : 0;
     return on == 1;
@@ -504,6 +508,27 @@ int pt_prof_kernel(int id, int64_t* launches, double* total_ms) {
 }
 
 int64_t pt_prof_launches(void) { return g_launches; }
+
+int pt_prof_region(int end, double* ms) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    Engine& E = *g_eng;
+    if (!E.rev0) {
+        CK(cudaEventCreate(&E.rev0));
+        CK(cudaEventCreate(&E.rev1));
+    }
+    if (!end) {
+        nvtxRangePushA("pt_timed");
+        CK(cudaEventRecord(E.rev0, E.st));
+        return 0;
+    }
+    CK(cudaEventRecord(E.rev1, E.st));
+    CK(cudaEventSynchronize(E.rev1));
+    nvtxRangePop();
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, E.rev0, E.rev1));
+    if (ms) *ms = f;
+    return 0;
+}
 
 int pt_phase_times(double* ms5) {
     if (int rc = need(g_eng != nullptr)) return rc;

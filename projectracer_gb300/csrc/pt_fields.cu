@@ -334,14 +334,18 @@ int compute_velocities(Engine& E) {
 }
 
 // stability_RK4 (energy.f90:756-810): eigenvalue maxima over the nodes
-__global__ void k_eig_max(const double* cd, const double* cr, const double* cs, Geo g, double Tr_max,
-                          double Ts_max, double Trr_max, double Tss_max, unsigned long long* out) {
+// eigA/eigD of energy.f90:850-875 on the uniform grid (xr = zs = 1, xrr = zss = 0); u, w are
+// nullptr unless CFL = 1
+__global__ void k_eig_max(const double* cd, const double* cr, const double* cs, const double* u, const double* w,
+                          Geo g, double Tr_max, double Ts_max, double Trr_max, double Tss_max,
+                          unsigned long long* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
     double eA = 0.0, eD = 0.0;
     if (i <= cK.nx) {
         size_t a = g.at(i, k);
         double c = cd[a];
-        eA = fabs(-c * 0.0 / 1.0 + cr[a] / 1.0) * Tr_max + fabs(-c * 0.0 / 1.0 + cs[a] / 1.0) * Ts_max;
+        const double uu = u ? u[a] : 0.0, ww = w ? w[a] : 0.0;
+        eA = fabs(-c * 0.0 / 1.0 - uu / 1.0 + cr[a] / 1.0) * Tr_max + fabs(-c * 0.0 / 1.0 - ww / 1.0 + cs[a] / 1.0) * Ts_max;
         eD = c * (fabs(Trr_max / 1.0) + fabs(Tss_max / 1.0));
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -361,7 +365,9 @@ int stability_dt(Engine& E, double* dt) {
     unsigned long long* d = (unsigned long long*)E.dscal;
     CK(cudaMemsetAsync(d, 0, 16, E.st));
     dim3 grid(nblk(K.nx + 1, 128), K.nz + 1);
-    PT_COUNT(), k_eig_max<<<grid, 128, 0, E.st>>>(E.cond, E.cond_r, E.cond_s, E.g1, Tr_max, Ts_max, Trr_max, Tss_max, d);
+    PT_COUNT(), k_eig_max<<<grid, 128, 0, E.st>>>(E.cond, E.cond_r, E.cond_s, E.cfg.CFL == 1 ? E.u : nullptr,
+                                                   E.cfg.CFL == 1 ? E.w : nullptr, E.g1, Tr_max, Ts_max, Trr_max,
+                                                   Tss_max, d);
     CKL("k_eig_max");
     CK(cudaMemcpyAsync(E.hscal, d, 16, cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
@@ -369,6 +375,7 @@ int stability_dt(Engine& E, double* dt) {
     double dtA = 2.8 / eA, dtD = 2.8 / eD;
     double v = (eA == 0.0) ? dtD : 1.0 / (1.0 / dtA + 1.0 / dtD);
     *dt = E.cfg.courant * v;
+    if (E.cfg.CFL == 1 && 2.0 / eD < *dt) *dt = 2.0 / eD;  // energy.f90:809
     return 0;
 }
 
@@ -504,11 +511,12 @@ int stats(Engine& E, pt_stats_row* o) {
 
 // --- deterministic sum of |f| over the interior (1..nx-1, 1..nz-1) of a level array ----------
 // pass 1: one block per row, fixed strided order + fixed tree; pass 2: one block over the rows.
-__global__ void k_rowsum_abs(const double* f, int nx, int pitch, double* part) {
+template <typename R>
+__global__ void k_rowsum_abs(const R* f, int nx, int pitch, double* part) {
     __shared__ double sh[256];
     int k = blockIdx.x + 1;
     double a = 0.0;
-    for (int i = 1 + threadIdx.x; i <= nx - 1; i += blockDim.x) a += fabs(f[(size_t)(i + GH) + (size_t)(k + GH) * pitch]);
+    for (int i = 1 + threadIdx.x; i <= nx - 1; i += blockDim.x) a += fabs((double)f[(size_t)(i + GH) + (size_t)(k + GH) * pitch]);
     sh[threadIdx.x] = a;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -530,11 +538,18 @@ __global__ void k_sum_parts(const double* part, int n, double* out) {
     if (threadIdx.x == 0) *out = sh[0];
 }
 
-int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitch, double* dout) {
-    PT_COUNT(), k_rowsum_abs<<<nz - 1, 256, 0, E.st>>>(f, nx, pitch, E.red);
+template <typename R>
+static int sum_abs_interior(Engine& E, const R* f, int nx, int nz, int pitch, double* dout) {
+    PT_COUNT(), k_rowsum_abs<R><<<nz - 1, 256, 0, E.st>>>(f, nx, pitch, E.red);
     PT_COUNT(), k_sum_parts<<<1, 1024, 0, E.st>>>(E.red, nz - 1, dout);
     CKL("reduce_sum_abs");
     return 0;
+}
+int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitch, double* dout) {
+    return sum_abs_interior(E, f, nx, nz, pitch, dout);
+}
+int reduce_sum_abs_interior(Engine& E, const float* f, int nx, int nz, int pitch, double* dout) {
+    return sum_abs_interior(E, f, nx, nz, pitch, dout);
 }
 
 }  // namespace pt

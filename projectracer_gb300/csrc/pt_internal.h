@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cstdio>
 #include <stdint.h>
 
 #include <string>
@@ -33,6 +34,8 @@ struct Geo {
 struct LevConst {
     int nx, nz;
     double dr, ds, dr2, ds2, dr3, ds3, dr4, ds4, drds, drds2, dr2ds, dr2ds2;
+    // reciprocals of the above (exact for the power-of-two spacings of a multigrid hierarchy)
+    double idr2, ids2, idr3, ids3, idr4, ids4, idrds, idrds2, idr2ds, idr2ds2;
     double SR1, SR2, SR4, SR5, SR6, SI1, SI2, SI4, SI5, SI6;
     double dt_vis;
 };
@@ -47,6 +50,7 @@ struct Consts {
     double mewt[64], mew[64], vv[64], cc[64];
     double dr, ds, dr2, ds2, inv_dr, inv_ds, aspect;
     double dr_pow[4], ds_pow[4], fact[4];
+    double inv_ds_pow[4], inv_fact[4];
     int exact_div;  // dr and ds are powers of two: x/dr == x*inv_dr exactly
     double two_over_D20;
     double Tbot_iso, Ttop_iso, H, Htype, conduct_factor;
@@ -90,6 +94,8 @@ struct Engine {
     double* psi_keep = nullptr;
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
+    double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
+    int ginv_cols = 32;
     int* ipiv = nullptr;
     // reductions
     double* red = nullptr;       // partial sums scratch
@@ -120,6 +126,7 @@ struct Engine {
     int64_t nA = 0, nB = 0;
     int prof = 0;
     cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+    cudaEvent_t rev0 = nullptr, rev1 = nullptr;  // pt_prof_region
     int64_t kcount[8] = {};
     double kms[8] = {};
 };
@@ -177,6 +184,7 @@ int project(Engine& E, const double* r, const double* s, const double* Tt, const
 int rk_stage(Engine& E, int stage);                   // energy.f90:258-536 tracer loops
 
 // multigrid (pt_mg.cu)
+bool trace_on();  // PTGPU_TRACE set in the environment
 int multigrid(Engine& E, pt_solve_info* info);        // iterative_solver.f90:124-341
 int mg_alloc(Engine& E);
 
@@ -184,11 +192,14 @@ int mg_alloc(Engine& E);
 int multigrid_mixed(Engine& E, pt_solve_info* info);
 int mixed_alloc(Engine& E);
 int mg_setup_solve(Engine& E);
+int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, const float* rhs32);
 int coarse_band_solve(Engine& E);
+int residual_level1_nosum(Engine& E);  // res[1] = RHS - A err[1] (FP64)
 int residual_level1(Engine& E);
 
 // reductions (pt_fields.cu)
 int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitch, double* out);
+int reduce_sum_abs_interior(Engine& E, const float* f, int nx, int nz, int pitch, double* out);
 int reduce_max_smoothness(Engine& E, const double* f, double* out);
 
 // device timing

@@ -310,8 +310,8 @@ __device__ __forceinline__ double stream_F(const double* __restrict__ S, Geo g, 
         Sxxx += cK.D3[j] * sx[j]; Sxxxx += cK.D4[j] * sx[j];
         Szzz += cK.D3[j] * sz[j]; Szzzz += cK.D4[j] * sz[j];
     }
-    Sxx /= L.dr2; Sxxx /= L.dr3; Sxxxx /= L.dr4;
-    Szz /= L.ds2; Szzz /= L.ds3; Szzzz /= L.ds4;
+    Sxx *= L.idr2; Sxxx *= L.idr3; Sxxxx *= L.idr4;  // reciprocals: see LevConst
+    Szz *= L.ids2; Szzz *= L.ids3; Szzzz *= L.ids4;
     // cross derivatives: x-derivatives of the 5 rows, combined in z
     double Sxz = 0, Sxxz = 0, Sxzz = 0, Sxxzz = 0;
 #pragma unroll
@@ -328,7 +328,7 @@ __device__ __forceinline__ double stream_F(const double* __restrict__ S, Geo g, 
         Sxxz += cK.D1[3 + kk] * d2;
         Sxxzz += cK.D2[3 + kk] * d2;
     }
-    Sxz /= L.drds; Sxxz /= L.dr2ds; Sxzz /= L.drds2; Sxxzz /= L.dr2ds2;
+    Sxz *= L.idrds; Sxxz *= L.idr2ds; Sxzz *= L.idrds2; Sxxzz *= L.idr2ds2;
     size_t o = g.at(i, k);
     double r;
     double t2 = op.vis[o] * (Sxxxx + Szzzz + 2.0 * Sxxzz);
@@ -651,6 +651,67 @@ __global__ void k_band_solve(const double* ab, const int* ipiv, double* bg, int 
     for (int q = lane; q < n; q += 32) bg[q] = b[q];
 }
 
+// Explicit inverse of the factored coarse matrix, G = (P L U)^{-1}: thread t of a block carries
+// column c = blockIdx.x * blockDim.x + t through the same forward/back substitution as
+// k_band_solve (DGBTRS restated) on the unit vector e_c.  The band entries are shared by all
+// threads of the block (broadcast loads), each column lives in shared memory, y[q * C + t].
+// G is stored row-major so the per-cycle coarse solve is a coalesced GEMV (k_coarse_apply).
+__global__ void k_band_inverse(const double* ab, const int* ipiv, double* G, int n, int kl, int ku) {
+    extern __shared__ double y[];
+    const int C = blockDim.x, t = threadIdx.x, c = blockIdx.x * C + t;
+    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1;
+    if (c >= n) return;  // no block-level synchronisation below: every thread owns its column
+#define AB(r, cc) ab[(size_t)((r) - 1) + (size_t)((cc) - 1) * (size_t)ldab]
+#define Y(q) y[(size_t)(q) * C + t]
+    for (int q = 0; q < n; q++) Y(q) = (q == c) ? 1.0 : 0.0;
+    for (int j = 1; j <= n - 1; j++) {
+        int lm = kl < n - j ? kl : n - j;
+        int l = ipiv[j - 1];
+        if (l != j) { double tt = Y(l - 1); Y(l - 1) = Y(j - 1); Y(j - 1) = tt; }
+        double bj = Y(j - 1);
+        if (bj != 0.0) {
+            double temp = -1.0 * bj;
+            for (int i = 1; i <= lm; i++) Y(j + i - 1) = Y(j + i - 1) + AB(kd + i, j) * temp;
+        }
+    }
+    const int k = kl + ku, kp1 = k + 1;
+    for (int j = n; j >= 1; j--) {
+        double bj = Y(j - 1);
+        if (bj != 0.0) {
+            double x = bj / AB(kp1, j);
+            Y(j - 1) = x;
+            int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+            for (int i = j - 1; i >= i0; i--) Y(i - 1) = Y(i - 1) - x * AB(l + i, j);
+        }
+    }
+    for (int q = 0; q < n; q++) G[(size_t)q * n + c] = Y(q);
+#undef Y
+#undef AB
+}
+
+// coarse solve through the explicit inverse: b = RowB * RHS on interior nodes (0 on the
+// boundary), x = G b (one warp per row, lanes stride the row, fixed-order shuffle reduction),
+// scattered into the level array.  R = float for the mixed-precision cycle.
+template <typename R>
+__global__ void __launch_bounds__(256) k_coarse_apply(R* Eout, const R* RHS, const double* G, const double* RowB, Geo g,
+                                                      int nxc, int nzc) {
+    extern __shared__ double bsh[];
+    const int N = nzc + 1, n = (nxc + 1) * N;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        int ip = q / N, kp = q % N;
+        bsh[q] = (ip > 0 && ip < nxc && kp > 0 && kp < nzc) ? (double)RHS[g.at(ip, kp)] * RowB[q] : 0.0;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int p = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (p >= n) return;
+    const double* row = G + (size_t)p * n;
+    double a = 0.0;
+    for (int q = lane; q < n; q += 32) a += row[q] * bsh[q];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) Eout[g.at(p / N, p % N)] = (R)a;
+}
+
 __global__ void k_coarse_rhs(double* B, const double* RHS, const double* RowB, Geo g, int nxc, int nzc) {
     int p = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int N = nzc + 1, n = (nxc + 1) * N;
@@ -676,12 +737,34 @@ static int coarse_factor(Engine& E) {
     CK(cudaMemcpyAsync(&h, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
     if (h) return fail(PT_ERR_SINGULAR_COARSE, "coarse banded LU: zero row or pivot");
+    if (E.Ginv) {
+        const int C = E.ginv_cols;
+        PT_COUNT(), k_band_inverse<<<nblk(n, C), C, sizeof(double) * (size_t)n * C, E.st>>>(E.Mc, E.ipiv, E.Ginv, n,
+                                                                                           E.kl, E.ku);
+        CKL("k_band_inverse");
+    }
+    return 0;
+}
+
+// x = G b into err[L] (FP64) or ferr[L] (FP32); needs E.Ginv
+int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, const float* rhs32) {
+    const int L = E.grids, n = E.ngc;
+    const Geo& g = E.gl[L];
+    const unsigned blocks = nblk(n, 8);
+    const size_t smem = sizeof(double) * (size_t)n;
+    if (out64) PT_COUNT(), k_coarse_apply<double><<<blocks, 256, smem, E.st>>>(out64, rhs64, E.Ginv, E.RowB, g, g.nx, g.nz);
+    else PT_COUNT(), k_coarse_apply<float><<<blocks, 256, smem, E.st>>>(out32, rhs32, E.Ginv, E.RowB, g, g.nx, g.nz);
+    CKL("k_coarse_apply");
     return 0;
 }
 
 static int coarse_solve(Engine& E) {
     const int L = E.grids, n = E.ngc;
     const Geo& g = E.gl[L];
+    if (E.Ginv && E.cfg.precision == PT_PREC_MIXED) {
+        if (int rc = coarse_apply(E, E.err[L], nullptr, E.RHS[L], nullptr)) return rc;
+        return enforce_bcs_stream(E, L, E.err[L]);
+    }
     PT_COUNT(), k_coarse_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.RHS[L], E.RowB, g, g.nx, g.nz);
     PT_COUNT(), k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
     PT_COUNT(), k_coarse_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.err[L], E.Bc, g, g.nx, g.nz);
@@ -694,6 +777,14 @@ int coarse_band_solve(Engine& E) {
     const int n = E.ngc;
     PT_COUNT(), k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
     CKL("k_band_solve");
+    return 0;
+}
+
+int residual_level1_nosum(Engine& E) {
+    const Geo& g = E.gl[1];
+    dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
+    PT_COUNT(), k_residual<<<gs, 128, 0, E.st>>>(E.res[1], E.err[1], stream_op(E, 1), g, 1, E.cfg.ivis);
+    CKL("k_residual");
     return 0;
 }
 
@@ -791,6 +882,7 @@ int multigrid(Engine& E, pt_solve_info* info) {
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite multigrid residual");
         if (mag1 > 1.0e10 * E.res_ref[1])
             return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
+        if (trace_on()) fprintf(stderr, "[ptgpu] cycle %d residual ratio %.4e\n", q, mag1 / E.res_ref[1]);
         if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
         if ((rc = run_part(E, 1))) return rc;
         q++;
@@ -834,6 +926,19 @@ int mg_alloc(Engine& E) {
     const size_t smem = sizeof(double) * (size_t)E.ngc;
     if (smem > 220 * 1024) return fail(PT_ERR_CONFIG, "coarsest grid too large for the banded solve");
     CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_coarse_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_coarse_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // explicit coarse inverse for the mixed-precision cycle: n^2 doubles, kept while it is small
+    // next to the level arrays (n <= 4096: <= 134 MB)
+    if (E.cfg.precision == PT_PREC_MIXED && E.ngc <= 4096) {
+        int C = 32;
+        while (C > 1 && sizeof(double) * (size_t)E.ngc * C > 200 * 1024) C /= 2;
+        E.ginv_cols = C;
+        CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
+        E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
+        CK(cudaFuncSetAttribute(k_band_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(double) * (size_t)E.ngc * C)));
+    }
     return 0;
 }
 

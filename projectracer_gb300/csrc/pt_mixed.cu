@@ -1,73 +1,80 @@
-// pt_mixed.cu -- mixed-precision stream-function solve (spec extension, no reference
-// counterpart): FP64 residual and defect correction around FP32 multigrid cycles.
+// pt_mixed.cu -- mixed-precision stream-function solve (no reference counterpart): FP32
+// multigrid cycles on the correction inside FP64 defect correction.
 //
-//   x = psi (FP64 warm start);  r = RHS - A x (FP64, the reference's stream_space residual)
-//   until mean|r| / mean|RHS| <= tolerance (the reference's convergence test, unchanged):
-//     one FP32 cycle of the reference's level schedule on A e = r, e = 0 on entry and at every
-//     descent (correction scheme): FP32 RKC1 smoothing with the FP64 pipeline's viscosity
-//     coefficients and local pseudo-time steps rounded to FP32, FP32 restriction/prolongation,
-//     coarsest level through the FP64 banded LU;  x += e (FP64);  r = RHS - A x (FP64).
-// The viscosity pipeline and the coarse LU are the FP64 ones (mg_setup_solve).  Each cycle is
-// two captured CUDA graphs: the FP64 residual + |r| sum, and the FP32 cycle + update.
+//   x = psi (FP64 warm start)
+//   repeat:  r = RHS - A x (FP64);  FP32 RKC1 smoothing of A e = r on level 1 from e = 0
+//            (increment form, see k_rkc_first_f);  x += e;  r = RHS - A x (FP64)
+//            stop when mean|r| / mean|RHS| <= tolerance: the reference's test, taken at the same
+//            point as in the FP64 cycle (after the level-1 smoothing), on the FP64 residual
+//            the rest of the reference's level schedule on a correction that restarts from zero
+//            on every descent (correction scheme), FP32 restriction/prolongation, the coarsest
+//            level through the FP64 banded LU;  x += P e_2 (FP64)
+// The viscosity pipeline and the coarse LU factors are the FP64 ones (mg_setup_solve); the
+// coefficient fields are rounded to FP32 once per solve.  Residuals that feed a coarser level use
+// FP64 arithmetic on the FP32 correction: for smooth modes the biharmonic stencil cancels by many
+// orders of magnitude on the fine levels.  Each iteration is two captured CUDA graphs.
 #include <cmath>
+#include <cstdlib>
 
 #include "pt_consts.cuh"
 
 namespace pt {
 
-int upload_consts_mixed(const Engine& E) { return upload_tu_consts(E); }
+// Per-level stencils with the grid spacing folded in (FP32 and FP64 copies): no division and no
+// FP64->FP32 conversion in the kernels (both run on the FP64 pipe of this part).
+//   Sxx = sum x2[j] S(i+j-2), Sxxx = sum x3[j] S(i+j-3), Sxxxx = sum x4[j] S(i+j-3), same in z;
+//   cross terms: d1_kk = sum_ii D1[ii] S(i+ii,k+kk), d2_kk = sum_ii D2[ii] S(i+ii,k+kk), then
+//   Sxz = sum o_xz[kk] d1_kk, Sxzz = sum o_xzz[kk] d1_kk, Sxxz = sum o_xxz[kk] d2_kk,
+//   Sxxzz = sum o_xxzz[kk] d2_kk  (the reference's stream_derivatives, folded)
+template <typename T>
+struct Stencil {
+    T x2[5], x3[7], x4[7], z2[5], z3[7], z4[7], i1[5], i2[5], o_xz[5], o_xzz[5], o_xxz[5], o_xxzz[5];
+};
+static __constant__ Stencil<float> cSF[PT_MAXLEV];
+static __constant__ Stencil<double> cSD[PT_MAXLEV];
+
+template <typename T>
+static void make_stencil(const Engine& E, int l, Stencil<T>& c) {
+    const Consts& K = E.K;
+    const LevConst& L = E.L[l];
+    for (int j = 0; j < 5; j++) {
+        c.x2[j] = (T)(K.D2[j + 1] / L.dr2);
+        c.z2[j] = (T)(K.D2[j + 1] / L.ds2);
+        c.i1[j] = (T)K.D1[j + 1];
+        c.i2[j] = (T)K.D2[j + 1];
+        c.o_xz[j] = (T)(K.D1[j + 1] / L.drds);
+        c.o_xzz[j] = (T)(K.D2[j + 1] / L.drds2);
+        c.o_xxz[j] = (T)(K.D1[j + 1] / L.dr2ds);
+        c.o_xxzz[j] = (T)(K.D2[j + 1] / L.dr2ds2);
+    }
+    for (int j = 0; j < 7; j++) {
+        c.x3[j] = (T)(K.D3[j] / L.dr3);
+        c.x4[j] = (T)(K.D4[j] / L.dr4);
+        c.z3[j] = (T)(K.D3[j] / L.ds3);
+        c.z4[j] = (T)(K.D4[j] / L.ds4);
+    }
+}
+
+int upload_consts_mixed(const Engine& E) {
+    if (int rc = upload_tu_consts(E)) return rc;
+    Stencil<float> sf[PT_MAXLEV] = {};
+    Stencil<double> sd[PT_MAXLEV] = {};
+    for (int l = 1; l <= E.grids && l < PT_MAXLEV; l++) {
+        make_stencil(E, l, sf[l]);
+        make_stencil(E, l, sd[l]);
+    }
+    CK(cudaMemcpyToSymbol(cSF, sf, sizeof sf));
+    CK(cudaMemcpyToSymbol(cSD, sd, sizeof sd));
+    return 0;
+}
 
 struct FOp {
     const float *vis, *vx, *vz, *vxz, *vxxmzz, *rhs, *dtst;
 };
-
-struct FLev {
-    float dr2, dr3, dr4, ds2, ds3, ds4, drds, dr2ds, drds2, dr2ds2;
+struct DOp {
+    const double *vis, *vx, *vz, *vxz, *vxxmzz, *rhs;
 };
 
-// -(A S - rhs) in FP32 at node (i,k)
-__device__ __forceinline__ float stream_F_f(const float* __restrict__ S, Geo g, const FLev& L, const FOp& op, int i,
-                                            int k, int ivis) {
-    float sx[7], sz[7];
-#pragma unroll
-    for (int j = 0; j < 7; j++) {
-        sx[j] = S[g.at(i + j - 3, k)];
-        sz[j] = S[g.at(i, k + j - 3)];
-    }
-    float Sxx = 0, Sxxx = 0, Sxxxx = 0, Szz = 0, Szzz = 0, Szzzz = 0;
-#pragma unroll
-    for (int j = 1; j <= 5; j++) { Sxx += (float)cK.D2[j] * sx[j]; Szz += (float)cK.D2[j] * sz[j]; }
-#pragma unroll
-    for (int j = 0; j < 7; j++) {
-        Sxxx += (float)cK.D3[j] * sx[j]; Sxxxx += (float)cK.D4[j] * sx[j];
-        Szzz += (float)cK.D3[j] * sz[j]; Szzzz += (float)cK.D4[j] * sz[j];
-    }
-    Sxx /= L.dr2; Sxxx /= L.dr3; Sxxxx /= L.dr4;
-    Szz /= L.ds2; Szzz /= L.ds3; Szzzz /= L.ds4;
-    float Sxz = 0, Sxxz = 0, Sxzz = 0, Sxxzz = 0;
-#pragma unroll
-    for (int kk = -2; kk <= 2; kk++) {
-        float d1 = 0, d2 = 0;
-#pragma unroll
-        for (int ii = -2; ii <= 2; ii++) {
-            float v = (kk == 0) ? sx[ii + 3] : S[g.at(i + ii, k + kk)];
-            d1 += (float)cK.D1[3 + ii] * v;
-            d2 += (float)cK.D2[3 + ii] * v;
-        }
-        Sxz += (float)cK.D1[3 + kk] * d1;
-        Sxzz += (float)cK.D2[3 + kk] * d1;
-        Sxxz += (float)cK.D1[3 + kk] * d2;
-        Sxxzz += (float)cK.D2[3 + kk] * d2;
-    }
-    Sxz /= L.drds; Sxxz /= L.dr2ds; Sxzz /= L.drds2; Sxxzz /= L.dr2ds2;
-    size_t o = g.at(i, k);
-    float r = op.vis[o] * (Sxxxx + Szzzz + 2.0f * Sxxzz);
-    if (ivis != 0) {
-        r += op.vxxmzz[o] * (Sxx - Szz) + 4.0f * op.vxz[o] * Sxz + 2.0f * op.vx[o] * (Sxxx + Sxzz) +
-             2.0f * op.vz[o] * (Szzz + Sxxz);
-    }
-    return -(r - op.rhs[o]);
-}
 
 __device__ __forceinline__ void store_ghosts_f(float* out, Geo g, int i, int k, int nx, int nz, float v, float sz) {
     int xs[3], zs[3];
@@ -83,76 +90,121 @@ __device__ __forceinline__ void store_ghosts_f(float* out, Geo g, int i, int k, 
         for (int b = 0; b < nzp; b++) out[g.at(xs[a], zs[b])] = (xf[a] * zf[b]) * v;
 }
 
-// one FP32 RKC1 stage; 2-D blocks so the 7x7 stencil reuses neighbours from L1
-__global__ void __launch_bounds__(256) k_rkc_stage_f(float* __restrict__ out, const float* __restrict__ S1,
-                                                     const float* __restrict__ S2, const float* __restrict__ S0,
-                                                     FOp op, Geo g, FLev L, int nx, int nz, float cS0, float mew,
-                                                     float vv, float mewtc, int first, int ivis, float sz) {
+template <typename T>
+__device__ __forceinline__ const Stencil<T>& stencil(int l);
+template <>
+__device__ __forceinline__ const Stencil<float>& stencil<float>(int l) { return cSF[l]; }
+template <>
+__device__ __forceinline__ const Stencil<double>& stencil<double>(int l) { return cSD[l]; }
+
+// A S (no right-hand side) at node (i,k) of the FP32 array S, in arithmetic T with the folded
+// stencils of level l (FP32: the smoother stages; FP64: residuals and F0)
+template <typename T, typename SIn = float, typename Op = FOp>
+__device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, const Op& op, int i, int k, int ivis) {
+    const Stencil<T>& C = stencil<T>(l);
+    T sx[7], sz[7];
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        sx[j] = (T)S[g.at(i + j - 3, k)];
+        sz[j] = (T)S[g.at(i, k + j - 3)];
+    }
+    T Sxx = 0, Sxxx = 0, Sxxxx = 0, Szz = 0, Szzz = 0, Szzzz = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) { Sxx += C.x2[j] * sx[j + 1]; Szz += C.z2[j] * sz[j + 1]; }
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        Sxxx += C.x3[j] * sx[j]; Sxxxx += C.x4[j] * sx[j];
+        Szzz += C.z3[j] * sz[j]; Szzzz += C.z4[j] * sz[j];
+    }
+    T Sxz = 0, Sxxz = 0, Sxzz = 0, Sxxzz = 0;
+#pragma unroll
+    for (int kk = 0; kk < 5; kk++) {
+        T d1 = 0, d2 = 0;
+#pragma unroll
+        for (int ii = 0; ii < 5; ii++) {
+            T v = (kk == 2) ? sx[ii + 1] : (T)S[g.at(i + ii - 2, k + kk - 2)];
+            d1 += C.i1[ii] * v;
+            d2 += C.i2[ii] * v;
+        }
+        Sxz += C.o_xz[kk] * d1;
+        Sxzz += C.o_xzz[kk] * d1;
+        Sxxz += C.o_xxz[kk] * d2;
+        Sxxzz += C.o_xxzz[kk] * d2;
+    }
+    size_t o = g.at(i, k);
+    T r = (T)op.vis[o] * (Sxxxx + Szzzz + (T)2 * Sxxzz);
+    if (ivis != 0)
+        r += (T)op.vxxmzz[o] * (Sxx - Szz) + (T)4 * (T)op.vxz[o] * Sxz + (T)2 * (T)op.vx[o] * (Sxxx + Sxzz) +
+             (T)2 * (T)op.vz[o] * (Szzz + Sxxz);
+    return r;
+}
+
+// RKC1 in increment form.  With Y_0 = e and D_j = Y_j - Y_0 the reference's recurrence
+//   Y_j = cc_j Y_0 + mew_j Y_{j-1} + vv_j Y_{j-2} + mewt_j c dt F(Y_{j-1}),  cc_j = 1 - mew_j - vv_j
+// becomes  D_j = mew_j D_{j-1} + vv_j D_{j-2} + mewt_j c dt (F0 - A D_{j-1}),  F0 = F(Y_0).
+// Stored in FP32, the increments carry rounding relative to |D| instead of |Y|: a 35-stage
+// Chebyshev recurrence amplifies per-stage rounding by O(s^2), which on the stored stage values
+// themselves swamps the correction after a prolongation.  F0 carries the same hazard (a constant
+// forcing integrated over the whole pseudo-time interval), so it is evaluated in FP64 arithmetic
+// from the FP32 Y_0; after a descent Y_0 = 0 and F0 is the right-hand side itself.
+template <bool ZERO>
+__global__ void __launch_bounds__(256) k_rkc_first_f(float* __restrict__ D1, float* __restrict__ F0,
+                                                     const float* __restrict__ Y0, FOp op, Geo g, int l, int nx,
+                                                     int nz, float mewtc, int ivis, float sz) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
-    float F = stream_F_f(S1, g, L, op, i, k, ivis);
     size_t o = g.at(i, k);
-    float v;
-    if (first) v = S1[o] + mewtc * op.dtst[o] * F;
-    else v = cS0 * S0[o] + mew * S1[o] + vv * S2[o] + mewtc * op.dtst[o] * F;
-    store_ghosts_f(out, g, i, k, nx, nz, v, sz);
+    float F = ZERO ? op.rhs[o] : (float)((double)op.rhs[o] - apply_A<double>(Y0, g, l, op, i, k, ivis));
+    F0[o] = F;
+    store_ghosts_f(D1, g, i, k, nx, nz, mewtc * op.dtst[o] * F, sz);
+}
+
+// stage j >= 2: out may alias Dm2 (each thread reads Dm2 only at its own interior node).
+// The last stage (Y0out != nullptr) writes Y0 + D_s into Y0out instead.
+__global__ void __launch_bounds__(256) k_rkc_stage_f(float* out, const float* __restrict__ Dm1, const float* Dm2,
+                                                     const float* __restrict__ F0, float* Y0out, FOp op, Geo g,
+                                                     int l, int nx, int nz, float mew, float vv, float mewtc,
+                                                     int ivis, float sz) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    size_t o = g.at(i, k);
+    float F = F0[o] - apply_A<float>(Dm1, g, l, op, i, k, ivis);
+    float d = mew * Dm1[o] + mewtc * op.dtst[o] * F;
+    if (Dm2) d += vv * Dm2[o];
+    if (Y0out) store_ghosts_f(Y0out, g, i, k, nx, nz, Y0out[o] + d, sz);
+    else store_ghosts_f(out, g, i, k, nx, nz, d, sz);
 }
 
 // Residual of the correction equation with FP64 arithmetic on the FP32 correction: for smooth
 // modes the biharmonic stencil cancels by orders of magnitude, which FP32 cannot resolve on the
 // fine levels; this residual is what the coarser levels see.
-__global__ void k_residual_f(float* __restrict__ res, const float* __restrict__ S, FOp op, Geo g, int l, int nx, int nz,
-                             int ivis) {
+__global__ void __launch_bounds__(256) k_residual_f(float* __restrict__ res, const float* __restrict__ S, FOp op, Geo g,
+                                                    int l, int nx, int nz, int ivis) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
-    const LevConst& L = cL[l];
-    double sx[7], sz[7];
-#pragma unroll
-    for (int j = 0; j < 7; j++) {
-        sx[j] = (double)S[g.at(i + j - 3, k)];
-        sz[j] = (double)S[g.at(i, k + j - 3)];
-    }
-    double Sxx = 0, Sxxx = 0, Sxxxx = 0, Szz = 0, Szzz = 0, Szzzz = 0;
-#pragma unroll
-    for (int j = 1; j <= 5; j++) { Sxx += cK.D2[j] * sx[j]; Szz += cK.D2[j] * sz[j]; }
-#pragma unroll
-    for (int j = 0; j < 7; j++) {
-        Sxxx += cK.D3[j] * sx[j]; Sxxxx += cK.D4[j] * sx[j];
-        Szzz += cK.D3[j] * sz[j]; Szzzz += cK.D4[j] * sz[j];
-    }
-    Sxx /= L.dr2; Sxxx /= L.dr3; Sxxxx /= L.dr4;
-    Szz /= L.ds2; Szzz /= L.ds3; Szzzz /= L.ds4;
-    double Sxz = 0, Sxxz = 0, Sxzz = 0, Sxxzz = 0;
-#pragma unroll
-    for (int kk = -2; kk <= 2; kk++) {
-        double d1 = 0, d2 = 0;
-#pragma unroll
-        for (int ii = -2; ii <= 2; ii++) {
-            double v = (kk == 0) ? sx[ii + 3] : (double)S[g.at(i + ii, k + kk)];
-            d1 += cK.D1[3 + ii] * v;
-            d2 += cK.D2[3 + ii] * v;
-        }
-        Sxz += cK.D1[3 + kk] * d1;
-        Sxzz += cK.D2[3 + kk] * d1;
-        Sxxz += cK.D1[3 + kk] * d2;
-        Sxxzz += cK.D2[3 + kk] * d2;
-    }
-    Sxz /= L.drds; Sxxz /= L.dr2ds; Sxzz /= L.drds2; Sxxzz /= L.dr2ds2;
     size_t o = g.at(i, k);
-    double r = (double)op.vis[o] * (Sxxxx + Szzzz + 2.0 * Sxxzz);
-    if (ivis != 0)
-        r += (double)op.vxxmzz[o] * (Sxx - Szz) + 4.0 * (double)op.vxz[o] * Sxz + 2.0 * (double)op.vx[o] * (Sxxx + Sxzz) +
-             2.0 * (double)op.vz[o] * (Szzz + Sxxz);
-    res[o] = (float)((double)op.rhs[o] - r);
+    res[o] = (float)((double)op.rhs[o] - apply_A<double>(S, g, l, op, i, k, ivis));
 }
 
-__global__ void k_restrict_f(float* out, const float* in, Geo gc, Geo gf, int nxc, int nzc) {
+// FP64 residual of the level-1 iterate, r = RHS - A x, with the folded FP64 stencil
+__global__ void __launch_bounds__(128) k_residual64(double* __restrict__ res, const double* __restrict__ x, DOp op, Geo g,
+                                                    int nx, int nz, int ivis) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    size_t o = g.at(i, k);
+    res[o] = op.rhs[o] - apply_A<double, double, DOp>(x, g, 1, op, i, k, ivis);
+}
+
+// full weighting (restrict, iterative_solver.f90:398-418) into FP32; R = double restricts the
+// FP64 level-1 residual directly
+template <typename R>
+__global__ void k_restrict_f(float* out, const R* in, Geo gc, Geo gf, int nxc, int nzc) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxc - 1) return;
     int ii = 2 * i, kk = 2 * k;
-    float corners = (in[gf.at(ii - 1, kk - 1)] + in[gf.at(ii - 1, kk + 1)] + in[gf.at(ii + 1, kk + 1)] + in[gf.at(ii + 1, kk - 1)]) * 0.0625f;
-    float sides = (in[gf.at(ii - 1, kk)] + in[gf.at(ii, kk - 1)] + in[gf.at(ii + 1, kk)] + in[gf.at(ii, kk + 1)]) * 0.125f;
-    out[gc.at(i, k)] = corners + sides + in[gf.at(ii, kk)] * 0.25f;
+    R corners = (in[gf.at(ii - 1, kk - 1)] + in[gf.at(ii - 1, kk + 1)] + in[gf.at(ii + 1, kk + 1)] + in[gf.at(ii + 1, kk - 1)]) * (R)0.0625;
+    R sides = (in[gf.at(ii - 1, kk)] + in[gf.at(ii, kk - 1)] + in[gf.at(ii + 1, kk)] + in[gf.at(ii, kk + 1)]) * (R)0.125;
+    out[gc.at(i, k)] = (float)(corners + sides + in[gf.at(ii, kk)] * (R)0.25);
 }
 
 __global__ void k_prolong_f(float* F, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
@@ -200,6 +252,22 @@ __global__ void k_res_to_f32(float* out, const double* in, size_t n) {
     if (q < n) out[q] = (float)in[q];
 }
 
+// x += e1 + P e2 on the interior in FP64: the last prolongation of a cycle (level 2 -> 1) fused
+// with the update, so the level-1 correction is never rounded to FP32 after it
+__global__ void k_prolong_add(double* x, const float* F, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
+    if (i > nxf - 1) return;
+    double add;
+    if (!(i & 1) && !(k & 1)) add = (double)C[gc.at(i / 2, k / 2)];
+    else if (!(i & 1)) add = ((double)C[gc.at(i / 2, (k - 1) / 2)] + (double)C[gc.at(i / 2, (k + 1) / 2)]) * 0.5;
+    else if (!(k & 1)) add = ((double)C[gc.at((i - 1) / 2, k / 2)] + (double)C[gc.at((i + 1) / 2, k / 2)]) * 0.5;
+    else
+        add = ((double)C[gc.at((i - 1) / 2, (k - 1) / 2)] + (double)C[gc.at((i + 1) / 2, (k - 1) / 2)] +
+               (double)C[gc.at((i + 1) / 2, (k + 1) / 2)] + (double)C[gc.at((i - 1) / 2, (k + 1) / 2)]) * 0.25;
+    size_t o = gf.at(i, k);
+    x[o] += (double)F[o] + add;
+}
+
 // x += e on the interior (FP64 accumulate of the FP32 correction)
 __global__ void k_add_correction(double* x, const float* e, Geo g, int nx, int nz) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
@@ -222,10 +290,25 @@ __global__ void k_coarse_scatter_f(float* e, const double* B, Geo g, int nxc, in
     e[g.at((p - 1) / N, (p - 1) % N)] = (float)B[p - 1];
 }
 
-static FLev flev(const LevConst& L) {
-    return FLev{(float)L.dr2, (float)L.dr3, (float)L.dr4, (float)L.ds2, (float)L.ds3, (float)L.ds4,
-                (float)L.drds, (float)L.dr2ds, (float)L.drds2, (float)L.dr2ds2};
+// FP64 level-1 residual (and optionally the sum of |r| into dscal[8])
+static int residual64(Engine& E, bool want_sum) {
+    const Geo& g = E.gl[1];
+    DOp op{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.RHS[1]};
+    dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
+    PT_COUNT(), k_residual64<<<grd, blk, 0, E.st>>>(E.res[1], E.err[1], op, g, g.nx, g.nz, E.cfg.ivis);
+    CKL("k_residual64");
+    if (want_sum) return reduce_sum_abs_interior(E, E.res[1], g.nx, g.nz, g.pitch, E.dscal + 8);
+    return 0;
 }
+
+static int add_correction(Engine& E) {
+    const Geo& g1 = E.gl[1];
+    PT_COUNT(), k_add_correction<<<dim3(nblk(g1.nx - 1, 128), g1.nz - 1), 128, 0, E.st>>>(E.err[1], E.ferr[1], g1, g1.nx,
+                                                                                           g1.nz);
+    CKL("k_add_correction");
+    return enforce_bcs_stream(E, 1, E.err[1]);
+}
+
 static FOp fop(Engine& E, int l) {
     float* const* c = E.fcoef[l];
     return FOp{c[0], c[1], c[2], c[3], c[4], E.fRHS[l], c[5]};
@@ -239,45 +322,54 @@ static int bcs_f(Engine& E, int l, float* f) {
     return 0;
 }
 
-// FP32 iterate_stream on the correction of level l (e starts at zero: correction scheme)
-static int smooth_f(Engine& E, int l) {
+// FP32 iterate_stream on the correction of level l, RKC1 in increment form (k_rkc_first_f).
+// zero: the correction is zero on entry (first visit after a descent); want_res: the residual is
+// needed (the next step descends).
+static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
     const Geo& g = E.gl[l];
     const int N = E.cfg.nstageS, ivis = E.cfg.ivis;
     const float sz = E.cfg.Vbc == 0 ? -1.f : 1.f;
     FOp op = fop(E, l);
-    FLev L = flev(E.L[l]);
     dim3 blk(32, 8), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 8));
-    float* buf[3] = {E.fS0[l], E.fS1[l], E.fS2[l]};
+    // FP64-arithmetic kernels (F0, residual) in 64-thread blocks: this part issues about two
+    // FP64 FMAs per clock per SM, so the coarse levels need every SM they can get
+    dim3 blk64(32, 2), grd64(nblk(g.nx - 1, 32), nblk(g.nz - 1, 2));
     float* e = E.ferr[l];
-    const double c = E.cfg.c_2;  // Nmulti passes: one pass with c = c_2 (Nmulti=1)
+    float* F0 = E.fS0[l];
+    const double c = E.cfg.c_2;  // Nmulti = 1: one pass with c = c_2
     for (int n = 1; n <= E.cfg.Nmulti; n++) {
         KernelTimer kt(E, KT_RKC_FP32_L1, l == 1 ? N : 0);
-        int cur = 0;
-        PT_COUNT(), k_rkc_stage_f<<<grd, blk, 0, E.st>>>(buf[cur], e, nullptr, nullptr, op, g, L, g.nx, g.nz, 0.f, 0.f, 0.f,
-                                                          (float)(E.K.mewt[1] * c), 1, ivis, sz);
-        const float* Sm1 = buf[cur];
-        const float* Sm2 = e;
+        float* Dm1 = E.fS1[l];
+        float* Dm2 = E.fS2[l];
+        auto first = (zero && n == 1) ? k_rkc_first_f<true> : k_rkc_first_f<false>;
+        const bool z = zero && n == 1;
+        PT_COUNT(), first<<<z ? grd : grd64, z ? blk : blk64, 0, E.st>>>(Dm1, F0, e, op, g, l, g.nx, g.nz, (float)(E.K.mewt[1] * c), ivis, sz);
         for (int j = 2; j <= N; j++) {
-            int nxt = (cur + 1) % 3;
-            if (buf[nxt] == Sm2) nxt = (nxt + 1) % 3;
-            float* out = (j == N) ? e : buf[nxt];
-            PT_COUNT(), k_rkc_stage_f<<<grd, blk, 0, E.st>>>(out, Sm1, Sm2, e, op, g, L, g.nx, g.nz, (float)E.K.cc[j],
-                                                              (float)E.K.mew[j], (float)E.K.vv[j],
-                                                              (float)(E.K.mewt[j] * c), 0, ivis, sz);
-            Sm2 = Sm1;
-            Sm1 = out;
-            cur = nxt;
+            const bool last = (j == N);
+            // D_{j-2} = D_0 = 0 at j = 2; the output overwrites D_{j-2}
+            PT_COUNT(), k_rkc_stage_f<<<grd, blk, 0, E.st>>>(Dm2, Dm1, j == 2 ? nullptr : Dm2, F0, last ? e : nullptr, op,
+                                                              g, l, g.nx, g.nz, (float)E.K.mew[j], (float)E.K.vv[j],
+                                                              (float)(E.K.mewt[j] * c), ivis, sz);
+            float* t = Dm1;
+            Dm1 = Dm2;
+            Dm2 = t;
         }
         CKL("k_rkc_stage_f");
     }
-    PT_COUNT(), k_residual_f<<<grd, blk, 0, E.st>>>(E.fres[l], e, op, g, l, g.nx, g.nz, ivis);
-    CKL("k_residual_f");
+    if (want_res) {
+        PT_COUNT(), k_residual_f<<<grd64, blk64, 0, E.st>>>(E.fres[l], e, op, g, l, g.nx, g.nz, ivis);
+        CKL("k_residual_f");
+    }
     return 0;
 }
 
 static int coarse_solve_f(Engine& E) {
     const int L = E.grids, n = E.ngc;
     const Geo& g = E.gl[L];
+    if (E.Ginv) {
+        if (int rc = coarse_apply(E, nullptr, E.ferr[L], nullptr, E.fRHS[L])) return rc;
+        return bcs_f(E, L, E.ferr[L]);
+    }
     PT_COUNT(), k_coarse_rhs_f<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.fRHS[L], E.RowB, g, g.nx, g.nz);
     int rc = coarse_band_solve(E);
     if (rc) return rc;
@@ -286,31 +378,50 @@ static int coarse_solve_f(Engine& E) {
     return bcs_f(E, L, E.ferr[L]);
 }
 
-// part 0: FP64 residual + sum; part 1: FP32 cycle on the correction + FP64 update
+// part 0: r = RHS - A x (FP64); FP32 pre-smoothing of A e = r on level 1 from e = 0; x += e;
+//         r = RHS - A x (FP64) and the sum of |r| for the convergence test -- the same test, at
+//         the same point (after the level-1 smoothing), as in the FP64 cycle;
+// part 1: the rest of the schedule on the correction, from the restriction of that FP64
+//         residual onwards; the closing prolongation (level 2 -> 1) is added to x in FP64.
 static int mixed_part(Engine& E, int part) {
     int rc;
-    if (part == 0) return residual_level1(E);
     const Geo& g1 = E.gl[1];
     const size_t n1 = g1.elems();
-    PT_COUNT(), k_res_to_f32<<<nblk(n1, 256), 256, 0, E.st>>>(E.fRHS[1], E.res[1], n1);
+    if (part == 0) {
+        if ((rc = residual64(E, false))) return rc;
+        PT_COUNT(), k_res_to_f32<<<nblk(n1, 256), 256, 0, E.st>>>(E.fRHS[1], E.res[1], n1);
+        CK(cudaMemsetAsync(E.ferr[1], 0, n1 * sizeof(float), E.st));
+        if ((rc = smooth_f(E, 1, true, false))) return rc;
+        if ((rc = add_correction(E))) return rc;
+        return residual64(E, true);
+    }
     const int grids = E.grids, nsteps = E.nsteps;
     const int* multi = E.multi;
-    for (int p = 1; p <= nsteps; p++) {
+    // the level-1 correction restarts from zero (the pre-smoothing is already in x); its RHS is
+    // the residual after the pre-smoothing, used only if the schedule revisits level 1
+    CK(cudaMemsetAsync(E.ferr[1], 0, n1 * sizeof(float), E.st));
+    PT_COUNT(), k_res_to_f32<<<nblk(n1, 256), 256, 0, E.st>>>(E.fRHS[1], E.res[1], n1);
+    for (int p = 2; p <= nsteps; p++) {
         const int l = multi[p];
         const Geo& g = E.gl[l];
-        const bool descend = (p == 1) || multi[p - 1] < multi[p];
+        const bool descend = multi[p - 1] < multi[p];
         if (descend) {
-            if (l > 1) {
-                const Geo& gf = E.gl[l - 1];
-                PT_COUNT(), k_restrict_f<<<dim3(nblk(g.nx - 1, 128), g.nz - 1), 128, 0, E.st>>>(E.fRHS[l], E.fres[l - 1], g, gf,
-                                                                                                 g.nx, g.nz);
-            }
+            const Geo& gf = E.gl[l - 1];
+            dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
+            if (l == 2) PT_COUNT(), k_restrict_f<double><<<gr, 128, 0, E.st>>>(E.fRHS[l], E.res[1], g, gf, g.nx, g.nz);
+            else PT_COUNT(), k_restrict_f<float><<<gr, 128, 0, E.st>>>(E.fRHS[l], E.fres[l - 1], g, gf, g.nx, g.nz);
             CK(cudaMemsetAsync(E.ferr[l], 0, g.elems() * sizeof(float), E.st));
         }
         if (l < grids) {
-            if ((rc = smooth_f(E, l))) return rc;
+            if ((rc = smooth_f(E, l, descend, multi[p + 1] > multi[p]))) return rc;
         } else if ((rc = coarse_solve_f(E))) {
             return rc;
+        }
+        if (multi[p + 1] < multi[p] && l == 2 && p == nsteps) {
+            PT_COUNT(), k_prolong_add<<<dim3(nblk(g1.nx - 1, 128), g1.nz - 1), 128, 0, E.st>>>(E.err[1], E.ferr[1], E.ferr[2],
+                                                                                              g1, g, g1.nx, g1.nz);
+            CKL("k_prolong_add");
+            return enforce_bcs_stream(E, 1, E.err[1]);
         }
         if (multi[p + 1] < multi[p]) {
             const Geo& gf = E.gl[l - 1];
@@ -319,10 +430,7 @@ static int mixed_part(Engine& E, int part) {
             if ((rc = bcs_f(E, l - 1, E.ferr[l - 1]))) return rc;
         }
     }
-    PT_COUNT(), k_add_correction<<<dim3(nblk(g1.nx - 1, 128), g1.nz - 1), 128, 0, E.st>>>(E.err[1], E.ferr[1], g1, g1.nx,
-                                                                                           g1.nz);
-    CKL("mixed cycle");
-    return enforce_bcs_stream(E, 1, E.err[1]);
+    return add_correction(E);
 }
 
 static int run_mixed(Engine& E, int part) {
@@ -372,18 +480,19 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite residual in the mixed-precision solve");
         if (mag1 > 1.0e10 * E.res_ref[1])
             return fail(PT_ERR_MG_DIVERGED, "mixed-precision solve: abnormally high residual");
+        if (trace_on()) fprintf(stderr, "[ptgpu] mixed cycle %d residual ratio %.4e\n", cycles, mag1 / E.res_ref[1]);
         if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
         if (cycles >= E.cfg.max_cycles)
             return fail(PT_ERR_MG_MAX_CYCLES, "mixed-precision solve: too many cycles");
         if ((rc = run_mixed(E, 1))) return rc;
         cycles++;
     }
-    E.cycles = cycles;
+    E.cycles = cycles + 1;  // level-1 smoothings, counted as in the FP64 cycle
     E.refinements = cycles;
     E.resid_ratio = mag1 / E.res_ref[1];
     CK(cudaMemcpyAsync(E.SF, E.err[1], E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     if (info) {
-        info->cycles += cycles;
+        info->cycles += cycles + 1;
         info->resid_ratio = E.resid_ratio;
         info->n_eta = E.n_eta;
         info->eig_fine = E.eig_fine;

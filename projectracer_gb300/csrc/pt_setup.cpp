@@ -254,6 +254,10 @@ int setup_constants(Engine& E) {
         K.dr_pow[j] = std::pow(K.dr, (double)j);
         K.ds_pow[j] = std::pow(K.ds, (double)j);
     }
+    for (int j = 0; j <= 3; j++) {
+        K.inv_ds_pow[j] = 1.0 / K.ds_pow[j];
+        K.inv_fact[j] = 1.0 / K.fact[j];
+    }
     K.two_over_D20 = 2.0 / K.D2[3];
     K.Tbot_iso = c.Tbot_iso; K.Ttop_iso = c.Ttop_iso;
     K.H = c.H; K.Htype = c.Htype; K.conduct_factor = c.conduct_factor;
@@ -276,6 +280,9 @@ int setup_constants(Engine& E) {
         L.dr3 = std::pow(L.dr, 3.0); L.ds3 = std::pow(L.ds, 3.0);
         L.dr4 = std::pow(L.dr, 4.0); L.ds4 = std::pow(L.ds, 4.0);
         L.drds = L.dr * L.ds; L.drds2 = L.dr * L.ds2; L.dr2ds = L.dr2 * L.ds; L.dr2ds2 = L.dr2 * L.ds2;
+        L.idr2 = 1.0 / L.dr2; L.ids2 = 1.0 / L.ds2; L.idr3 = 1.0 / L.dr3; L.ids3 = 1.0 / L.ds3;
+        L.idr4 = 1.0 / L.dr4; L.ids4 = 1.0 / L.ds4; L.idrds = 1.0 / L.drds; L.idrds2 = 1.0 / L.drds2;
+        L.idr2ds = 1.0 / L.dr2ds; L.idr2ds2 = 1.0 / L.dr2ds2;
         // symbols of the stream operator (real parts: even derivative counts, imaginary: odd)
         double Tss = -E.Trr_base / L.ds2, Tssss = E.Trrrr_base / L.ds4, Tsss = E.Trrr_base / L.ds3;
         double Trr = -E.Trr_base / L.dr2, Trrrr = E.Trrrr_base / L.dr4, Trrr = E.Trrr_base / L.dr3;

@@ -243,9 +243,11 @@ __device__ __forceinline__ double interp(const Tables& tb, Geo g, int i, int k, 
         s2 = s2 + cK.Dm[2][j] * fR[j];
         s3 = s3 + cK.Dm[3][j] * fR[j];
     }
-    s1 = s1 / cK.ds_pow[1];
-    s2 = s2 / cK.ds_pow[2];
-    s3 = s3 / cK.ds_pow[3];
+    // reciprocal multiplies: this part issues about two FP64 operations per clock per SM and a
+    // division costs many; with power-of-two spacings the reciprocals are exact
+    s1 = s1 * cK.inv_ds_pow[1];
+    s2 = s2 * cK.inv_ds_pow[2];
+    s3 = s3 * cK.inv_ds_pow[3];
     double fi = fR[3];
     fi = fi + s1 * b1;
     fi = fi + s2 * b2;
@@ -273,8 +275,8 @@ __global__ void __launch_bounds__(256) k_rk_stage(StageArgs A, Geo g) {
     i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
     k = min(max(k, 0), cK.nz);
     double hr = r - (double)i * cK.dr, hs = s - (double)k * cK.ds;
-    double a1 = hr / cK.fact[1], a2 = hr * hr / cK.fact[2], a3 = hr * hr * hr / cK.fact[3];
-    double b1 = hs / cK.fact[1], b2 = hs * hs / cK.fact[2], b3 = hs * hs * hs / cK.fact[3];
+    double a1 = hr * cK.inv_fact[1], a2 = hr * hr * cK.inv_fact[2], a3 = hr * hr * hr * cK.inv_fact[3];
+    double b1 = hs * cK.inv_fact[1], b2 = hs * hs * cK.inv_fact[2], b3 = hs * hs * hs * cK.inv_fact[3];
     double tr = interp(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
     double ts = interp(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
     double tT = interp(A.t, g, i, k, a1, a2, a3, b1, b2, b3);

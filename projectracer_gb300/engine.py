@@ -93,6 +93,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_prof_enable.argtypes = [i32]
     L.pt_prof_kernel.argtypes = [i32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
     L.pt_prof_launches.restype = ctypes.c_int64
+    L.pt_prof_region.argtypes = [i32, ctypes.POINTER(f64)]
     _LIB = L
     return L
 
@@ -178,6 +179,14 @@ class Engine:
         n, ms = ctypes.c_int64(), ctypes.c_double()
         self._check(self.L.pt_prof_kernel(kid, ctypes.byref(n), ctypes.byref(ms)))
         return n.value, ms.value
+
+    def region_begin(self):
+        self._check(self.L.pt_prof_region(0, None))
+
+    def region_end(self) -> float:
+        ms = ctypes.c_double()
+        self._check(self.L.pt_prof_region(1, ctypes.byref(ms)))
+        return ms.value
 
     def launches(self) -> int:
         return int(self.L.pt_prof_launches())

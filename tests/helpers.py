@@ -12,6 +12,8 @@ def small_case(kind: str = "iso", nx: int = 64, nz: int = 64, tpc: int = 8, seed
     iso:   isoviscous thermal convection (comp=0, ivis=0), the C1 physics
     chem:  thermochemical, eta(T), composition layer (comp=1, ivis=1), C2-like at lower Ra
     depth: eta(T,z) with internal heating (ivis=1, visP>1, H>0), C3/C5-like at lower Ra
+    c3:    the 1024x512 workload's physics (Ra_T=1e7, Ra_C=2e6, eta contrast 1e5 x depth 10) on a
+           small grid, with velocity-limited time steps (CFL=1) and the correction-scheme cycle
     """
     if kind == "iso":
         c, _ = workload("C1")
@@ -26,6 +28,17 @@ def small_case(kind: str = "iso", nx: int = 64, nz: int = 64, tpc: int = 8, seed
         c.nx, c.nz = nx, nz
         c.RaT, c.RaC, c.visT, c.visP, c.H = 1e5, 2e4, 1e3, 10.0, 1.0
         c.courant = 0.05
+        c.CFL = 0
+        c.mg_scheme = 0
+    elif kind == "c3":
+        from projectracer_gb300.config import PT_MG_CORRECTION
+
+        c, _ = workload("C3")
+        c.nx, c.nz = nx, nz
+        c.grids = 4
+        c.CFL = 1
+        c.courant = 0.5
+        c.mg_scheme = PT_MG_CORRECTION
     else:
         raise ValueError(kind)
     c.ntr = nx * nz * tpc

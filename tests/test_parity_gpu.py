@@ -138,3 +138,42 @@ def test_correction_scheme_solve_matches_oracle(kind):
     assert info["cycles"] == int(o.scalar("cycles"))
     assert rel_err(e.get(eng.F_SF), o.get(7)) < TOL
     e.close()
+
+
+def test_cfl_steps_match_oracle():
+    """The 1024x512 workload's physics on a 128x64 grid with velocity-limited time steps (CFL=1,
+    energy.f90:809 and 859-866): dt, tracers and T after two full steps."""
+    cfg, o, e = pair("c3", nx=128, nz=64)
+    for _ in range(2):
+        i0 = e.solve_psi()
+        o.solve_psi()
+        assert i0["cycles"] == int(o.scalar("cycles"))
+        dt, _ = e.step()
+        o.step()
+        assert abs(dt - o.scalar("dt")) <= TOL * o.scalar("dt")
+    for fid, oid in ((eng.F_TRACER_R, 20), (eng.F_TRACER_S, 21), (eng.F_TRACER_T, 22)):
+        assert rel_err(e.get(fid), o.get(oid)) < TOL, fid
+    assert rel_err(e.get(eng.F_T), o.get(0)) < TOL
+    assert rel_err(e.get(eng.F_SF), o.get(7)) < TOL
+    e.close()
+
+
+def test_mixed_precision_on_workload_physics():
+    """Mixed precision on the 1024x512 workload's physics (viscosity contrast 1e5 x 10 in depth):
+    same tolerance, same number of cycles as the FP64 correction-scheme solve, psi within 1e-6."""
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    cfg, st = small_case("c3", nx=128, nz=64)
+    e = eng.Engine(cfg)
+    e.upload(st)
+    i64 = e.solve_psi()
+    sf64 = e.get(eng.F_SF)
+    e.close()
+    cfg.precision = PT_PREC_MIXED
+    e = eng.Engine(cfg)
+    e.upload(st)
+    im = e.solve_psi()
+    assert im["resid_ratio"] <= cfg.tolerance
+    assert abs(im["cycles"] - i64["cycles"]) <= 1
+    assert rel_err(e.get(eng.F_SF), sf64) < 1e-6
+    e.close()
