@@ -233,7 +233,9 @@ def main():
     # timed region: device-resident inputs
     sampler = ClockSampler(local)
     sampler.start()
+    e.prof_enable(True)  # live kernel timing: event pairs inside the captured graphs, no extra syncs
     e.prof_reset()
+    ph0 = e.phase_times()
     dist.barrier()
     e.region_begin()  # CUDA event on the library's stream (the calls below return synchronised)
     t0 = time.perf_counter()
@@ -246,6 +248,9 @@ def main():
         nsolve += 4
     dev_s = e.region_end() * 1e-3
     host_s = time.perf_counter() - t0
+    ph1 = e.phase_times()
+    kinds = {kid: e.prof_kernel(kid) for kid in range(4)}
+    e.prof_enable(False)
     dist.barrier()
     elapsed = dist.max(dev_s)
     clocks = sampler.stop()
@@ -255,8 +260,10 @@ def main():
     # end to end through the C ABI with host buffers: per step the driver pushes its tracer
     # arrays (pinned host memory) and reads back the restart records
     e2e = end_to_end(e, eng, cfg, st, max(1, min(3, args.steps)), dist, world)
-    # kernel timing pass for the roofline (events bracket each timed kernel batch)
-    roof = roofline(e, eng, cfg)
+    roof = roofline(kinds, cfg)
+    phase_names = ("tracer_rk_stages", "projections", "psi_solves", "mg_setup", "mg_level1", "mg_coarse_levels",
+                   "grid_work", "coarse_factor")
+    phases = {nm: (ph1[q] - ph0[q]) / args.steps for q, nm in enumerate(phase_names)}
     # the plain FP64 GPU path from the same state: psi-solve ms at the same tolerance
     fp64 = None
     if args.precision == "mixed" and not args.no_fp64_compare:
@@ -274,7 +281,7 @@ def main():
                        "courant": cfg.courant, "replicas": world, "l2_flush": "inputs larger than L2"},
             "psi_solve_ms": solve_ms / max(1, nsolve), "mg_cycles_per_solve": cycles / max(1, nsolve),
             "tracers_per_s": value * cfg.ntr, "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
-            "roofline": roof}
+            "roofline": roof, "phase_ms_per_step": phases}
     if fp64 is not None:
         line["fp64_path"] = fp64
         line["psi_solve_speedup_vs_fp64"] = fp64["psi_solve_ms"] / max(1e-9, line["psi_solve_ms"])
@@ -367,36 +374,42 @@ def end_to_end(e, eng, cfg, st, steps, dist, world):
                     "restart records device->host through pt_download_state"}
 
 
-def roofline(e, eng, cfg):
-    peaks = measured_peaks()
-    e.prof_reset()
-    e.prof_enable(True)
-    e.solve_psi()
-    e.step()
-    e.prof_enable(False)
+KERNEL_NAMES = {0: "RKC1 stage, FP64, finest level", 1: "RKC1 stage, FP32, finest level",
+                2: "RK4 tracer stage (3 interpolations + update)", 3: "tracer->grid projection"}
+
+
+def algorithmic_bytes(kid: int, cfg) -> float:
+    """Bytes a launch must move at minimum (each array touched once):
+    FP64 stage: S_j-1 stencil, S_j-2, S_0, dtst, rhs, 5 coefficient fields, out = 11 x 8 B per node;
+    FP32 stage (increment form): D_j-1 stencil, D_j-2, F0, dtst, 5 coefficient fields, out = 10 x 4 B
+    per node (+4 B for Y0 on the last stage, not counted);
+    RK tracer stage: 2 stage positions, 3 step-start values, 3 accumulators read + written, 3 next
+    positions written = 14 x 8 B per tracer (the derivative tables, 12 x 8 B per node, are counted);
+    projection: position pair + T (+C) per tracer read twice (count, scatter), cell ids, the sorted
+    list and per-node sums: 32 B per tracer + 28 B per node."""
     nx, nz = cfg.nx, cfg.nz
     interior = (nx - 1) * (nz - 1)
-    n = int(cfg.ntr)
-    # algorithmic bytes per launch of each timed kernel class
-    per_launch = {0: 88.0 * interior, 1: 44.0 * interior, 2: 96.0 * n, 3: 32.0 * n + 28.0 * (nx + 1) * (nz + 1)}
-    names = {0: "RKC1 stage, FP64, finest level", 1: "RKC1 stage, FP32, finest level",
-             2: "RK4 tracer stage (3 interpolations + update)", 3: "tracer->grid projection"}
-    best, kinds = None, {}
-    for kid in range(4):
-        cnt, ms = e.prof_kernel(kid)
-        if cnt:
-            kinds[names[kid]] = {"launches": cnt, "total_ms": ms, "avg_ms": ms / cnt}
-            if best is None or ms > best[2]:
-                best = (kid, cnt, ms)
-    if best is None:
+    nodes = (nx + 1) * (nz + 1)
+    n = float(cfg.ntr)
+    return {0: 88.0 * interior, 1: 40.0 * interior, 2: 112.0 * n + 96.0 * nodes,
+            3: 32.0 * n + 28.0 * nodes}[kid]
+
+
+def roofline(kinds: dict, cfg) -> dict | None:
+    """Roofline of the kernel class with the largest share of the timed region, from the live
+    event timings (launch-averaged)."""
+    peaks = measured_peaks()
+    timed = {KERNEL_NAMES[k]: {"launches": c, "total_ms": ms, "avg_ms": ms / c} for k, (c, ms) in kinds.items() if c}
+    if not timed:
         return None
-    kid, cnt, ms = best
+    kid, (cnt, ms) = max(((k, v) for k, v in kinds.items() if v[0]), key=lambda kv: kv[1][1])
     avg_s = ms / cnt * 1e-3
-    achieved = per_launch[kid] / avg_s / 1e9
-    return {"bound": "hbm", "kernel": names[kid], "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)",
-            "traffic": None, "algorithmic_bytes_per_launch": per_launch[kid], "avg_launch_ms": avg_s * 1e3,
-            "timed_kernels": kinds}
+    per = algorithmic_bytes(kid, cfg)
+    achieved = per / avg_s / 1e9
+    return {"bound": "hbm", "kernel": KERNEL_NAMES[kid], "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)",
+            "traffic": None, "algorithmic_bytes_per_launch": per, "avg_launch_ms": avg_s * 1e3,
+            "timed_kernels": timed}
 
 
 if __name__ == "__main__":

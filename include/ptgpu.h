@@ -198,9 +198,12 @@ int pt_time(double* time, double* dt);
  * weight file for PT_GUESS_UNET (NULL otherwise). */
 int pt_set_guess_mode(int mode, const char* weights_path);
 
-/* Device time of the last call of each phase, in milliseconds: [0] advection kernels,
- * [1] projection, [2] psi solve, [3] smoothers, [4] derivative tables; sums since pt_init. */
-int pt_phase_times(double* ms5);
+/* Device time of each phase summed since pt_init, in milliseconds (8 entries): [0] tracer RK
+ * stages, [1] projections, [2] psi solves, [3] multigrid setup (viscosity pipeline, coarse
+ * matrix and factorisation), [4] level-1 part of the multigrid cycles, [5] coarser levels of the
+ * cycles, [6] grid work of a step (smoothers, conductivity, derivative tables, time step), [7]
+ * coarse matrix, banded LU and explicit inverse (included in [3]). */
+int pt_phase_times(double* ms8);
 
 #ifdef __cplusplus
 }

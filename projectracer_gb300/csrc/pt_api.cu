@@ -33,15 +33,37 @@ int cuda_check(cudaError_t e, const char* what) {
 }
 
 PhaseTimer::PhaseTimer(Engine& e, int s) : E(e), slot(s) {
-    if (E.ev0) cudaEventRecord(E.ev0, E.st);
+    if (E.pev[slot][0]) cudaEventRecord(E.pev[slot][0], E.st);
 }
 PhaseTimer::~PhaseTimer() {
-    if (!E.ev0) return;
-    cudaEventRecord(E.ev1, E.st);
-    if (cudaEventSynchronize(E.ev1) == cudaSuccess) {
+    if (!E.pev[slot][0]) return;
+    cudaEventRecord(E.pev[slot][1], E.st);
+    if (cudaEventSynchronize(E.pev[slot][1]) == cudaSuccess) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+        cudaEventElapsedTime(&ms, E.pev[slot][0], E.pev[slot][1]);
         E.phase_ms[slot] += ms;
+    }
+}
+
+// cudaEventRecordExternal makes the record a timing node of the captured graph (a plain record
+// during capture only expresses a dependency)
+GraphTimer::GraphTimer(Engine& e, int w, int count) : E(e), which(w), n(count) {
+    if (n) cudaEventRecordWithFlags(E.gev[which][0], E.st, cudaEventRecordExternal);
+}
+GraphTimer::~GraphTimer() {
+    if (!n) return;
+    cudaEventRecordWithFlags(E.gev[which][1], E.st, cudaEventRecordExternal);
+    E.gev_n[which] = n;
+}
+void harvest_graph_timer(Engine& E, int which) {
+    if (!E.prof || !E.gev_n[which]) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, E.gev[which][0], E.gev[which][1]) == cudaSuccess) {
+        const int id = which == 0 ? KT_RKC_FP64_L1 : KT_RKC_FP32_L1;
+        E.kms[id] += ms;
+        E.kcount[id] += E.gev_n[which];
+    } else {
+        (void)cudaGetLastError();  // a timing miss must not surface as the next launch's error
     }
 }
 
@@ -115,6 +137,9 @@ static void engine_free(Engine& E) {
     for (int f = 0; f < 3; f++)
         for (int j = 0; j < 3; j++)
             if (E.der[f][j]) cudaFree(E.der[f][j]);
+    for (int f = 0; f < 3; f++)
+        for (int j = 0; j < 4; j++)
+            if (E.fder[f][j]) cudaFree(E.fder[f][j]);
     for (int l = 0; l < PT_MAXLEV; l++) {
         double* arrs[] = {E.err[l], E.S0[l], E.S1[l], E.S2[l], E.RHS[l], E.res[l], E.dtst[l], E.ratio[l],
                           E.vis[l], E.visst[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l],
@@ -135,8 +160,12 @@ static void engine_free(Engine& E) {
     if (E.Ginv) cudaFree(E.Ginv);
     if (E.derr) cudaFree(E.derr);
     if (E.hscal) cudaFreeHost(E.hscal);
-    if (E.ev0) cudaEventDestroy(E.ev0);
-    if (E.ev1) cudaEventDestroy(E.ev1);
+    for (int q = 0; q < PT_NPHASE; q++)
+        for (int j = 0; j < 2; j++)
+            if (E.pev[q][j]) cudaEventDestroy(E.pev[q][j]);
+    for (int q = 0; q < 2; q++)
+        for (int j = 0; j < 2; j++)
+            if (E.gev[q][j]) cudaEventDestroy(E.gev[q][j]);
     if (E.gM1) cudaGraphExecDestroy(E.gM1);
     if (E.gM2) cudaGraphExecDestroy(E.gM2);
     if (E.gA) cudaGraphExecDestroy(E.gA);
@@ -240,8 +269,10 @@ int pt_init(const pt_config* cfg) {
     E->g1 = make_geo(cfg->nx, cfg->nz);
     for (int l = 1; l <= E->grids; l++) E->gl[l] = make_geo(E->L[l].nx, E->L[l].nz);
     if ((rc = cuda_check(cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking), "stream"))) { delete E; return rc; }
-    cudaEventCreate(&E->ev0);
-    cudaEventCreate(&E->ev1);
+    for (int q = 0; q < PT_NPHASE; q++)
+        for (int j = 0; j < 2; j++) cudaEventCreate(&E->pev[q][j]);
+    for (int q = 0; q < 2; q++)
+        for (int j = 0; j < 2; j++) cudaEventCreate(&E->gev[q][j]);
     cudaEventCreate(&E->kev0);
     cudaEventCreate(&E->kev1);
     g_eng = E;
@@ -286,6 +317,7 @@ int pt_field_extent(int field, int32_t* lo_x, int32_t* hi_x, int32_t* lo_z, int3
 }
 
 int pt_set_field(int field, const void* host) {
+    if (g_eng) g_eng->coarse_ready = false;  // new inputs: refactor the coarse operator
     if (int rc = need(g_eng != nullptr)) return rc;
     if (!host) return fail(PT_ERR_ARG, "null pointer");
     Engine& E = *g_eng;
@@ -351,6 +383,7 @@ int pt_upload_state(const double* xg, const double* zg, const double* T, const d
     E.time = 0.0;
     E.have_mass = 0;
     E.uploaded = 1;
+    E.coarse_ready = false;
     CK(cudaStreamSynchronize(E.st));
     return 0;
 }
@@ -398,14 +431,19 @@ int pt_solve_psi(pt_solve_info* info) {
 }
 
 static int stage_tables(Engine& E) {
+    PhaseTimer tm(E, PH_GRID);
     int rc;
     if ((rc = load_tracer_space(E))) return rc;
-    return compute_derivatives(E, E.tsa, 2);
+    if ((rc = compute_derivatives(E, E.tsa, 2))) return rc;
+    return tables_to_f32(E, 2, E.tsa);
 }
 static int velocity_tables(Engine& E) {
+    PhaseTimer tm(E, PH_GRID);
     int rc;
     if ((rc = compute_derivatives(E, E.u, 0))) return rc;
-    return compute_derivatives(E, E.w, 1);
+    if ((rc = compute_derivatives(E, E.w, 1))) return rc;
+    if ((rc = tables_to_f32(E, 0, E.u))) return rc;
+    return tables_to_f32(E, 1, E.w);
 }
 
 int pt_step(double* dt_out, pt_solve_info* info) {
@@ -530,10 +568,10 @@ int pt_prof_region(int end, double* ms) {
     return 0;
 }
 
-int pt_phase_times(double* ms5) {
+int pt_phase_times(double* ms8) {
     if (int rc = need(g_eng != nullptr)) return rc;
-    if (!ms5) return fail(PT_ERR_ARG, "null pointer");
-    for (int q = 0; q < 5; q++) ms5[q] = g_eng->phase_ms[q];
+    if (!ms8) return fail(PT_ERR_ARG, "null pointer");
+    for (int q = 0; q < PT_NPHASE; q++) ms8[q] = g_eng->phase_ms[q];
     return 0;
 }
 

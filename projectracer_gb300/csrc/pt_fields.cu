@@ -359,6 +359,7 @@ __global__ void k_eig_max(const double* cd, const double* cr, const double* cs, 
 }
 
 int stability_dt(Engine& E, double* dt) {
+    PhaseTimer tm(E, PH_GRID);
     const Consts& K = E.K;
     double Ts_max = E.Tr_base / K.ds, Tr_max = E.Tr_base / K.dr;
     double Tss_max = -E.Trr_base / K.ds2, Trr_max = -E.Trr_base / K.dr2;

@@ -20,6 +20,8 @@
 #define GH 5
 #define PT_MAXLEV 8
 
+enum { PH_RK = 0, PH_PROJECT, PH_SOLVE, PH_SETUP, PH_CYCLE_L1, PH_CYCLE_COARSE, PH_GRID, PH_FACTOR, PT_NPHASE };
+
 namespace pt {
 
 struct Geo {
@@ -76,6 +78,7 @@ struct Engine {
            *cond = nullptr, *cond_r = nullptr, *cond_s = nullptr, *tsa = nullptr, *Text = nullptr,
            *T0 = nullptr, *C0 = nullptr, *scratch = nullptr;
     double* der[3][3] = {};  // derivative tables: [field u,w,tsa][order 1..3]
+    float* fder[3][4] = {};  // mixed precision: FP32 [field][value, orders 1..3] for the RK stages
     double* coef[3] = {};    // 16 Taylor coefficients per node per field (advection)
     int32_t* nempty = nullptr;
     // multigrid
@@ -95,6 +98,8 @@ struct Engine {
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
+    bool coarse_ready = false;  // coarse factorisation valid for coarse_time (mixed precision)
+    double coarse_time = -1.0;
     int ginv_cols = 32;
     int* ipiv = nullptr;
     // reductions
@@ -117,8 +122,12 @@ struct Engine {
     int have_mass = 0;
     int n_eta = 0, n_temp = 0, cycles = 0, refinements = 0;
     double eig_fine = 0, resid_ratio = 0, res_ref[PT_MAXLEV] = {}, residual_mag1 = 0;
-    double phase_ms[5] = {};
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double phase_ms[PT_NPHASE] = {};
+    cudaEvent_t pev[PT_NPHASE][2] = {};  // one start/stop pair per phase slot (slots nest)
+    // events recorded inside the captured level-1 smoothing batch (graph nodes), read after the
+    // graph's synchronisation when profiling is on: [0] FP64 batch, [1] FP32 batch
+    cudaEvent_t gev[2][2] = {};
+    int gev_n[2] = {0, 0};
     size_t bytes_allocated = 0;
     // measurement hooks (ptgpu_prof.h): kernel launch count and per-kernel event timing
     int64_t launches = 0;
@@ -143,6 +152,15 @@ struct KernelTimer {
     ~KernelTimer();
 };
 enum { KT_RKC_FP64_L1 = 0, KT_RKC_FP32_L1 = 1, KT_RK_STAGE = 2, KT_PROJECT = 3 };
+// Event pair around the level-1 smoothing batch of a cycle; recorded into the CUDA graph when the
+// batch is captured, read by harvest_graph_timer after the graph has run.
+struct GraphTimer {
+    Engine& E;
+    int which, n;
+    GraphTimer(Engine& e, int w, int count);
+    ~GraphTimer();
+};
+void harvest_graph_timer(Engine& E, int which);
 extern thread_local std::string g_err;
 
 int fail(int code, const std::string& msg);
@@ -172,6 +190,7 @@ int smoother_time_T(Engine& E, const double* Tin);   // smoother.f90:638-672
 int smoother_time_C(Engine& E);                      // smoother.f90:582-636
 int load_conductivity(Engine& E);                    // energy.f90:59-86
 int load_tracer_space(Engine& E);                    // energy.f90:154-179 (+extendT 595-630)
+int tables_to_f32(Engine& E, int which, const double* f);  // FP32 copies for the mixed RK stage
 int compute_derivatives(Engine& E, const double* f, int which);  // composition.f90:1457-1478
 int compute_velocities(Engine& E);                   // momentum.f90:655-710
 int stability_dt(Engine& E, double* dt);             // energy.f90:756-810
@@ -202,7 +221,11 @@ int reduce_sum_abs_interior(Engine& E, const double* f, int nx, int nz, int pitc
 int reduce_sum_abs_interior(Engine& E, const float* f, int nx, int nz, int pitch, double* out);
 int reduce_max_smoothness(Engine& E, const double* f, double* out);
 
-// device timing
+// device timing.  Phase slots (pt_phase_times): PH_RK tracer RK stages, PH_PROJECT projections,
+// PH_SOLVE psi solves, PH_SETUP multigrid setup (viscosity pipeline, coarse matrix, LU, inverse),
+// PH_CYCLE_L1 level-1 part of the cycles, PH_CYCLE_COARSE the coarser levels, PH_GRID grid work
+// of a step (smoothers, conductivity, derivative tables, time step), PH_FACTOR the coarse matrix,
+// its LU and explicit inverse (part of PH_SETUP).
 struct PhaseTimer {
     Engine& E;
     int slot;

@@ -443,7 +443,7 @@ static int iterate_stream(Engine& E, int l, int want_sum) {
         double temp = (E.cfg.Nmulti > 1) ? (E.cfg.c_2 - E.cfg.c_1) * (double)(ntemp - 1) / (double)(1 - Niter) : 0.0;
         double c = temp + E.cfg.c_2;
         const double* S0 = E.err[l];
-        KernelTimer kt(E, KT_RKC_FP64_L1, l == 1 ? N : 0);
+        GraphTimer gt(E, 0, (l == 1 && want_sum) ? N : 0);
         int cur = 0;
         PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[cur], S0, nullptr, nullptr, op, g, l, 0, 0, 0, E.K.mewt[1] * c, 1, ivis, sz);
         const double* Sm1 = buf[cur];
@@ -727,6 +727,7 @@ __global__ void k_coarse_scatter(double* E, const double* B, Geo g, int nxc, int
 }
 
 static int coarse_factor(Engine& E) {
+    PhaseTimer tf(E, PH_FACTOR);
     const int L = E.grids, n = E.ngc;
     CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
     PT_COUNT(), k_coarse_matrix<<<nblk(n, 128), 128, 0, E.st>>>(E.Mc, E.gl[L], L, E.kl, E.ku, n, E.RowB, E.cfg.Vbc,
@@ -804,8 +805,18 @@ int mg_setup_solve(Engine& E) {
     if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
     for (int level = 1; level <= E.grids; level++)
         if ((rc = compute_viscosity(E, level))) return rc;
-    if (E.time == 0.0 || E.cfg.ivis > 0)
-        if ((rc = coarse_factor(E))) return rc;
+    if (E.time == 0.0 || E.cfg.ivis > 0) {
+        // The mixed-precision cycle uses the coarse solve as a preconditioner inside FP64 defect
+        // correction: its factorisation is refreshed once per time level (the top-of-step solve)
+        // and reused by the RK-stage solves of the step, whose viscosity differs by O(dt).  The
+        // FP64 cycle refactors every solve, as the reference does.
+        const bool reuse = E.cfg.precision == PT_PREC_MIXED && E.coarse_ready && E.coarse_time == E.time;
+        if (!reuse) {
+            if ((rc = coarse_factor(E))) return rc;
+            E.coarse_ready = true;
+            E.coarse_time = E.time;
+        }
+    }
     return 0;
 }
 
@@ -854,7 +865,6 @@ static int capture_part(Engine& E, int part, cudaGraphExec_t* exec, int64_t* nla
 }
 
 static int run_part(Engine& E, int part) {
-    if (E.prof) return cycle_part(E, part);  // event timing needs the launches on the stream
     cudaGraphExec_t& ex = part == 0 ? E.gA : E.gB;
     int64_t& n = part == 0 ? E.nA : E.nB;
     if (!ex) {
@@ -868,15 +878,21 @@ static int run_part(Engine& E, int part) {
 
 int multigrid(Engine& E, pt_solve_info* info) {
     int rc;
-    PhaseTimer tm(E, 2);
-    if ((rc = mg_setup_solve(E))) return rc;
+    PhaseTimer tm(E, PH_SOLVE);
+    {
+        PhaseTimer ts(E, PH_SETUP);
+        if ((rc = mg_setup_solve(E))) return rc;
+    }
     const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int q = 1;
     double mag1 = 0.0;
     for (;;) {
-        if ((rc = run_part(E, 0))) return rc;
-        CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
-        CK(cudaStreamSynchronize(E.st));
+        {
+            PhaseTimer tp(E, PH_CYCLE_L1);
+            if ((rc = run_part(E, 0))) return rc;
+            CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+        }
+        harvest_graph_timer(E, 0);
         mag1 = E.hscal[0] / (double)(E.gl[1].nx - 2) / (double)(E.gl[1].nz - 2);
         (void)norm;
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite multigrid residual");
@@ -884,7 +900,10 @@ int multigrid(Engine& E, pt_solve_info* info) {
             return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
         if (trace_on()) fprintf(stderr, "[ptgpu] cycle %d residual ratio %.4e\n", q, mag1 / E.res_ref[1]);
         if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
-        if ((rc = run_part(E, 1))) return rc;
+        {
+            PhaseTimer tp(E, PH_CYCLE_COARSE);
+            if ((rc = run_part(E, 1))) return rc;
+        }
         q++;
         if (q > E.cfg.max_cycles) return fail(PT_ERR_MG_MAX_CYCLES, "Multigrid Convergence Problem: Too Many Multigrid Cycles Needed");
     }

@@ -15,10 +15,38 @@
 // orders of magnitude on the fine levels.  Each iteration is two captured CUDA graphs.
 #include <cmath>
 #include <cstdlib>
+#include <utility>
 
 #include "pt_consts.cuh"
 
 namespace pt {
+
+// Programmatic dependent launch: every kernel of the mixed cycle starts by waiting for its
+// predecessor grid (griddepcontrol.wait returns once that grid has completed and its writes are
+// visible; it is a no-op for a kernel launched without the attribute) and then lets its own
+// successor be scheduled.  The successor's launch latency hides behind this kernel's run, which
+// matters on the coarse levels where each stage kernel lasts a couple of microseconds.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+static int launch_pdl(const char* what, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                      Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PT_COUNT();
+    return cuda_check(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...), what);
+}
 
 // Per-level stencils with the grid spacing folded in (FP32 and FP64 copies): no division and no
 // FP64->FP32 conversion in the kernels (both run on the FP64 pipe of this part).
@@ -146,15 +174,23 @@ __device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, co
 // Chebyshev recurrence amplifies per-stage rounding by O(s^2), which on the stored stage values
 // themselves swamps the correction after a prolongation.  F0 carries the same hazard (a constant
 // forcing integrated over the whole pseudo-time interval), so it is evaluated in FP64 arithmetic
-// from the FP32 Y_0; after a descent Y_0 = 0 and F0 is the right-hand side itself.
+// from the FP32 Y_0; after a descent Y_0 = 0 and F0 is the right-hand side itself (the ZERO
+// variant also clears Y_0's interior node, so no separate clearing pass is needed).
 template <bool ZERO>
 __global__ void __launch_bounds__(256) k_rkc_first_f(float* __restrict__ D1, float* __restrict__ F0,
-                                                     const float* __restrict__ Y0, FOp op, Geo g, int l, int nx,
+                                                     float* __restrict__ Y0, FOp op, Geo g, int l, int nx,
                                                      int nz, float mewtc, int ivis, float sz) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
     size_t o = g.at(i, k);
-    float F = ZERO ? op.rhs[o] : (float)((double)op.rhs[o] - apply_A<double>(Y0, g, l, op, i, k, ivis));
+    float F;
+    if (ZERO) {
+        F = op.rhs[o];
+        Y0[o] = 0.0f;  // the correction restarts from zero (its ghosts are written by the last stage)
+    } else {
+        F = (float)((double)op.rhs[o] - apply_A<double>(Y0, g, l, op, i, k, ivis));
+    }
     F0[o] = F;
     store_ghosts_f(D1, g, i, k, nx, nz, mewtc * op.dtst[o] * F, sz);
 }
@@ -165,6 +201,7 @@ __global__ void __launch_bounds__(256) k_rkc_stage_f(float* out, const float* __
                                                      const float* __restrict__ F0, float* Y0out, FOp op, Geo g,
                                                      int l, int nx, int nz, float mew, float vv, float mewtc,
                                                      int ivis, float sz) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
     size_t o = g.at(i, k);
@@ -180,6 +217,7 @@ __global__ void __launch_bounds__(256) k_rkc_stage_f(float* out, const float* __
 // fine levels; this residual is what the coarser levels see.
 __global__ void __launch_bounds__(256) k_residual_f(float* __restrict__ res, const float* __restrict__ S, FOp op, Geo g,
                                                     int l, int nx, int nz, int ivis) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
     size_t o = g.at(i, k);
@@ -189,6 +227,7 @@ __global__ void __launch_bounds__(256) k_residual_f(float* __restrict__ res, con
 // FP64 residual of the level-1 iterate, r = RHS - A x, with the folded FP64 stencil
 __global__ void __launch_bounds__(128) k_residual64(double* __restrict__ res, const double* __restrict__ x, DOp op, Geo g,
                                                     int nx, int nz, int ivis) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
     size_t o = g.at(i, k);
@@ -199,6 +238,7 @@ __global__ void __launch_bounds__(128) k_residual64(double* __restrict__ res, co
 // FP64 level-1 residual directly
 template <typename R>
 __global__ void k_restrict_f(float* out, const R* in, Geo gc, Geo gf, int nxc, int nzc) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxc - 1) return;
     int ii = 2 * i, kk = 2 * k;
@@ -208,6 +248,7 @@ __global__ void k_restrict_f(float* out, const R* in, Geo gc, Geo gf, int nxc, i
 }
 
 __global__ void k_prolong_f(float* F, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxf - 1) return;
     float add;
@@ -221,6 +262,7 @@ __global__ void k_prolong_f(float* F, const float* C, Geo gf, Geo gc, int nxf, i
 }
 
 __global__ void k_stream_bcs_f(float* S, Geo g, int nx, int nz, float sz) {
+    pdl_begin();
     int W = nx + 7;
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= W * (nz + 7)) return;
@@ -248,13 +290,15 @@ __global__ void k_coef_to_f32(float* v0, float* v1, float* v2, float* v3, float*
 }
 
 __global__ void k_res_to_f32(float* out, const double* in, size_t n) {
+    pdl_begin();
     size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) out[q] = (float)in[q];
 }
 
-// x += e1 + P e2 on the interior in FP64: the last prolongation of a cycle (level 2 -> 1) fused
-// with the update, so the level-1 correction is never rounded to FP32 after it
-__global__ void k_prolong_add(double* x, const float* F, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
+// x += P e2 on the interior in FP64: the closing prolongation of a cycle (level 2 -> 1) fused
+// with the update, so the level-1 correction is never rounded to FP32
+__global__ void k_prolong_add(double* x, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxf - 1) return;
     double add;
@@ -265,11 +309,12 @@ __global__ void k_prolong_add(double* x, const float* F, const float* C, Geo gf,
         add = ((double)C[gc.at((i - 1) / 2, (k - 1) / 2)] + (double)C[gc.at((i + 1) / 2, (k - 1) / 2)] +
                (double)C[gc.at((i + 1) / 2, (k + 1) / 2)] + (double)C[gc.at((i - 1) / 2, (k + 1) / 2)]) * 0.25;
     size_t o = gf.at(i, k);
-    x[o] += (double)F[o] + add;
+    x[o] += add;
 }
 
 // x += e on the interior (FP64 accumulate of the FP32 correction)
 __global__ void k_add_correction(double* x, const float* e, Geo g, int nx, int nz) {
+    pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nx - 1) return;
     size_t o = g.at(i, k);
@@ -295,17 +340,18 @@ static int residual64(Engine& E, bool want_sum) {
     const Geo& g = E.gl[1];
     DOp op{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.RHS[1]};
     dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
-    PT_COUNT(), k_residual64<<<grd, blk, 0, E.st>>>(E.res[1], E.err[1], op, g, g.nx, g.nz, E.cfg.ivis);
-    CKL("k_residual64");
+    if (int rc = launch_pdl("k_residual64", k_residual64, grd, blk, 0, E.st, E.res[1], (const double*)E.err[1], op, g, g.nx,
+                            g.nz, E.cfg.ivis))
+        return rc;
     if (want_sum) return reduce_sum_abs_interior(E, E.res[1], g.nx, g.nz, g.pitch, E.dscal + 8);
     return 0;
 }
 
 static int add_correction(Engine& E) {
     const Geo& g1 = E.gl[1];
-    PT_COUNT(), k_add_correction<<<dim3(nblk(g1.nx - 1, 128), g1.nz - 1), 128, 0, E.st>>>(E.err[1], E.ferr[1], g1, g1.nx,
-                                                                                           g1.nz);
-    CKL("k_add_correction");
+    if (int rc = launch_pdl("k_add_correction", k_add_correction, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0,
+                            E.st, E.err[1], (const float*)E.ferr[1], g1, g1.nx, g1.nz))
+        return rc;
     return enforce_bcs_stream(E, 1, E.err[1]);
 }
 
@@ -316,10 +362,8 @@ static FOp fop(Engine& E, int l) {
 
 static int bcs_f(Engine& E, int l, float* f) {
     const Geo& g = E.gl[l];
-    PT_COUNT(), k_stream_bcs_f<<<nblk((size_t)(g.nx + 7) * (g.nz + 7), 256), 256, 0, E.st>>>(f, g, g.nx, g.nz,
-                                                                                             E.cfg.Vbc == 0 ? -1.f : 1.f);
-    CKL("k_stream_bcs_f");
-    return 0;
+    return launch_pdl("k_stream_bcs_f", k_stream_bcs_f, dim3(nblk((size_t)(g.nx + 7) * (g.nz + 7), 256)), dim3(256), 0,
+                      E.st, f, g, g.nx, g.nz, E.cfg.Vbc == 0 ? -1.f : 1.f);
 }
 
 // FP32 iterate_stream on the correction of level l, RKC1 in increment form (k_rkc_first_f).
@@ -338,18 +382,22 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
     float* F0 = E.fS0[l];
     const double c = E.cfg.c_2;  // Nmulti = 1: one pass with c = c_2
     for (int n = 1; n <= E.cfg.Nmulti; n++) {
-        KernelTimer kt(E, KT_RKC_FP32_L1, l == 1 ? N : 0);
+        GraphTimer gt(E, 1, (l == 1 && zero) ? N : 0);
         float* Dm1 = E.fS1[l];
         float* Dm2 = E.fS2[l];
         auto first = (zero && n == 1) ? k_rkc_first_f<true> : k_rkc_first_f<false>;
         const bool z = zero && n == 1;
-        PT_COUNT(), first<<<z ? grd : grd64, z ? blk : blk64, 0, E.st>>>(Dm1, F0, e, op, g, l, g.nx, g.nz, (float)(E.K.mewt[1] * c), ivis, sz);
+        if (int rc = launch_pdl("k_rkc_first_f", first, z ? grd : grd64, z ? blk : blk64, 0, E.st, Dm1, F0, e, op, g, l,
+                                g.nx, g.nz, (float)(E.K.mewt[1] * c), ivis, sz))
+            return rc;
         for (int j = 2; j <= N; j++) {
             const bool last = (j == N);
             // D_{j-2} = D_0 = 0 at j = 2; the output overwrites D_{j-2}
-            PT_COUNT(), k_rkc_stage_f<<<grd, blk, 0, E.st>>>(Dm2, Dm1, j == 2 ? nullptr : Dm2, F0, last ? e : nullptr, op,
-                                                              g, l, g.nx, g.nz, (float)E.K.mew[j], (float)E.K.vv[j],
-                                                              (float)(E.K.mewt[j] * c), ivis, sz);
+            if (int rc = launch_pdl("k_rkc_stage_f", k_rkc_stage_f, grd, blk, 0, E.st, Dm2, (const float*)Dm1,
+                                    (const float*)(j == 2 ? nullptr : Dm2), (const float*)F0, last ? e : nullptr, op, g,
+                                    l, g.nx, g.nz, (float)E.K.mew[j], (float)E.K.vv[j], (float)(E.K.mewt[j] * c), ivis,
+                                    sz))
+                return rc;
             float* t = Dm1;
             Dm1 = Dm2;
             Dm2 = t;
@@ -357,8 +405,9 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
         CKL("k_rkc_stage_f");
     }
     if (want_res) {
-        PT_COUNT(), k_residual_f<<<grd64, blk64, 0, E.st>>>(E.fres[l], e, op, g, l, g.nx, g.nz, ivis);
-        CKL("k_residual_f");
+        if (int rc = launch_pdl("k_residual_f", k_residual_f, grd64, blk64, 0, E.st, E.fres[l], (const float*)e, op, g, l,
+                                g.nx, g.nz, ivis))
+            return rc;
     }
     return 0;
 }
@@ -389,52 +438,58 @@ static int mixed_part(Engine& E, int part) {
     const size_t n1 = g1.elems();
     if (part == 0) {
         if ((rc = residual64(E, false))) return rc;
-        PT_COUNT(), k_res_to_f32<<<nblk(n1, 256), 256, 0, E.st>>>(E.fRHS[1], E.res[1], n1);
-        CK(cudaMemsetAsync(E.ferr[1], 0, n1 * sizeof(float), E.st));
+        if ((rc = launch_pdl("k_res_to_f32", k_res_to_f32, dim3(nblk(n1, 256)), dim3(256), 0, E.st, E.fRHS[1],
+                             (const double*)E.res[1], n1)))
+            return rc;
         if ((rc = smooth_f(E, 1, true, false))) return rc;
         if ((rc = add_correction(E))) return rc;
         return residual64(E, true);
     }
     const int grids = E.grids, nsteps = E.nsteps;
     const int* multi = E.multi;
-    // the level-1 correction restarts from zero (the pre-smoothing is already in x); its RHS is
-    // the residual after the pre-smoothing, used only if the schedule revisits level 1
-    CK(cudaMemsetAsync(E.ferr[1], 0, n1 * sizeof(float), E.st));
-    PT_COUNT(), k_res_to_f32<<<nblk(n1, 256), 256, 0, E.st>>>(E.fRHS[1], E.res[1], n1);
     for (int p = 2; p <= nsteps; p++) {
         const int l = multi[p];
         const Geo& g = E.gl[l];
+        // the reference's schedules visit level 1 only at their first step; the pre-smoothing of
+        // part 0 is already in x, so the cycle's level-1 correction is the closing prolongation
+        if (l == 1) return fail(PT_ERR_CONFIG, "mixed-precision cycle: schedule revisits level 1");
         const bool descend = multi[p - 1] < multi[p];
         if (descend) {
             const Geo& gf = E.gl[l - 1];
             dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
-            if (l == 2) PT_COUNT(), k_restrict_f<double><<<gr, 128, 0, E.st>>>(E.fRHS[l], E.res[1], g, gf, g.nx, g.nz);
-            else PT_COUNT(), k_restrict_f<float><<<gr, 128, 0, E.st>>>(E.fRHS[l], E.fres[l - 1], g, gf, g.nx, g.nz);
-            CK(cudaMemsetAsync(E.ferr[l], 0, g.elems() * sizeof(float), E.st));
+            // the correction of level l restarts from zero: cleared by the first smoothing stage
+            // (or overwritten whole by the coarse solve)
+            if (l == 2)
+                rc = launch_pdl("k_restrict_f", k_restrict_f<double>, gr, dim3(128), 0, E.st, E.fRHS[l],
+                                (const double*)E.res[1], g, gf, g.nx, g.nz);
+            else
+                rc = launch_pdl("k_restrict_f", k_restrict_f<float>, gr, dim3(128), 0, E.st, E.fRHS[l],
+                                (const float*)E.fres[l - 1], g, gf, g.nx, g.nz);
+            if (rc) return rc;
         }
         if (l < grids) {
             if ((rc = smooth_f(E, l, descend, multi[p + 1] > multi[p]))) return rc;
         } else if ((rc = coarse_solve_f(E))) {
             return rc;
         }
-        if (multi[p + 1] < multi[p] && l == 2 && p == nsteps) {
-            PT_COUNT(), k_prolong_add<<<dim3(nblk(g1.nx - 1, 128), g1.nz - 1), 128, 0, E.st>>>(E.err[1], E.ferr[1], E.ferr[2],
-                                                                                              g1, g, g1.nx, g1.nz);
-            CKL("k_prolong_add");
-            return enforce_bcs_stream(E, 1, E.err[1]);
-        }
         if (multi[p + 1] < multi[p]) {
+            if (l == 2) {  // closing prolongation, added to x in FP64
+                if ((rc = launch_pdl("k_prolong_add", k_prolong_add, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0,
+                                     E.st, E.err[1], (const float*)E.ferr[2], g1, g, g1.nx, g1.nz)))
+                    return rc;
+                return enforce_bcs_stream(E, 1, E.err[1]);
+            }
             const Geo& gf = E.gl[l - 1];
-            PT_COUNT(), k_prolong_f<<<dim3(nblk(gf.nx - 1, 128), gf.nz - 1), 128, 0, E.st>>>(E.ferr[l - 1], E.ferr[l], gf, g,
-                                                                                             gf.nx, gf.nz);
+            if ((rc = launch_pdl("k_prolong_f", k_prolong_f, dim3(nblk(gf.nx - 1, 128), gf.nz - 1), dim3(128), 0, E.st,
+                                 E.ferr[l - 1], (const float*)E.ferr[l], gf, g, gf.nx, gf.nz)))
+                return rc;
             if ((rc = bcs_f(E, l - 1, E.ferr[l - 1]))) return rc;
         }
     }
-    return add_correction(E);
+    return fail(PT_ERR_CONFIG, "mixed-precision cycle: schedule does not return to level 1");
 }
 
 static int run_mixed(Engine& E, int part) {
-    if (E.prof) return mixed_part(E, part);
     cudaGraphExec_t& ex = part == 0 ? E.gM1 : E.gM2;
     int64_t& n = part == 0 ? E.nM1 : E.nM2;
     if (!ex) {
@@ -460,22 +515,28 @@ static int run_mixed(Engine& E, int part) {
 
 int multigrid_mixed(Engine& E, pt_solve_info* info) {
     int rc;
-    PhaseTimer tm(E, 2);
-    if ((rc = mg_setup_solve(E))) return rc;
-    for (int l = 1; l < E.grids; l++) {
-        size_t n = E.gl[l].elems();
-        float* const* f = E.fcoef[l];
-        PT_COUNT(), k_coef_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(f[0], f[1], f[2], f[3], f[4], f[5], E.vis[l], E.vx[l],
-                                                                  E.vz[l], E.vxz[l], E.vxxmzz[l], E.dtst[l], n);
+    PhaseTimer tm(E, PH_SOLVE);
+    {
+        PhaseTimer ts(E, PH_SETUP);
+        if ((rc = mg_setup_solve(E))) return rc;
+        for (int l = 1; l < E.grids; l++) {
+            size_t n = E.gl[l].elems();
+            float* const* f = E.fcoef[l];
+            PT_COUNT(), k_coef_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(f[0], f[1], f[2], f[3], f[4], f[5], E.vis[l], E.vx[l],
+                                                                      E.vz[l], E.vxz[l], E.vxxmzz[l], E.dtst[l], n);
+        }
+        CKL("k_coef_to_f32");
     }
-    CKL("k_coef_to_f32");
     const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int cycles = 0;
     double mag1 = 0.0;
     for (;;) {
-        if ((rc = run_mixed(E, 0))) return rc;
-        CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
-        CK(cudaStreamSynchronize(E.st));
+        {
+            PhaseTimer tp(E, PH_CYCLE_L1);
+            if ((rc = run_mixed(E, 0))) return rc;
+            CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+        }
+        harvest_graph_timer(E, 1);
         mag1 = E.hscal[0] / norm;
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite residual in the mixed-precision solve");
         if (mag1 > 1.0e10 * E.res_ref[1])
@@ -484,7 +545,10 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
         if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
         if (cycles >= E.cfg.max_cycles)
             return fail(PT_ERR_MG_MAX_CYCLES, "mixed-precision solve: too many cycles");
-        if ((rc = run_mixed(E, 1))) return rc;
+        {
+            PhaseTimer tp(E, PH_CYCLE_COARSE);
+            if ((rc = run_mixed(E, 1))) return rc;
+        }
         cycles++;
     }
     E.cycles = cycles + 1;  // level-1 smoothings, counted as in the FP64 cycle
@@ -501,6 +565,13 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
 }
 
 int mixed_alloc(Engine& E) {
+    for (int f = 0; f < 3; f++)
+        for (int j = 0; j < 4; j++) {
+            const size_t n = E.g1.elems();
+            CK(cudaMalloc(&E.fder[f][j], n * sizeof(float)));
+            CK(cudaMemsetAsync(E.fder[f][j], 0, n * sizeof(float), E.st));
+            E.bytes_allocated += n * sizeof(float);
+        }
     for (int l = 1; l <= E.grids; l++) {
         const size_t n = E.gl[l].elems();
         float** arrs[] = {&E.ferr[l], &E.fS0[l], &E.fS1[l], &E.fS2[l], &E.fRHS[l], &E.fres[l], &E.fcoef[l][0],

@@ -14,7 +14,17 @@
 
 namespace pt {
 
-int upload_consts_tracers(const Engine& E) { return upload_tu_consts(E); }
+// z-direction interpolation stencils with 1/ds^j folded in, FP32 (mixed-precision stage)
+static __constant__ float cDmf[4][7];
+
+int upload_consts_tracers(const Engine& E) {
+    if (int rc = upload_tu_consts(E)) return rc;
+    float d[4][7] = {};
+    for (int m = 1; m <= 3; m++)
+        for (int j = 0; j < 7; j++) d[m][j] = (float)(E.K.Dm[m][j] * E.K.inv_ds_pow[m]);
+    CK(cudaMemcpyToSymbol(cDmf, d, sizeof d));
+    return 0;
+}
 
 __device__ __forceinline__ int cell_index(double x, double inv, double h, int exact) {
     double q = exact ? x * inv : x / h;
@@ -183,7 +193,7 @@ int project(Engine& E, const double* r, const double* s, const double* Tt, const
     const int ncell = (nx + 1) * (nz + 1);
     const int64_t n = E.ntr;
     int rc;
-    PhaseTimer tm(E, 1);
+    PhaseTimer tm(E, PH_PROJECT);
     KernelTimer kt(E, KT_PROJECT, 1);
     if (T0f && T0f != E.Tratio) {
         if ((rc = copy_field(E, E.Tratio, T0f))) return rc;
@@ -299,8 +309,97 @@ __global__ void __launch_bounds__(256) k_rk_stage(StageArgs A, Geo g) {
     }
 }
 
+// ---------------------------------------------------------------- mixed-precision stage
+// The same stage with the Taylor interpolation in FP32 from FP32 copies of the velocity and
+// dT/dt tables: positions, step-start values and the RK accumulators stay FP64.  Interpolated
+// velocities carry a relative error of order 1e-7, below the psi solve's tolerance; the FP64
+// stage (k_rk_stage) is the reference-order path.
+struct FTables {
+    const float *f, *d1, *d2, *d3;
+};
+
+__device__ __forceinline__ float interp_f(const FTables& tb, Geo g, int i, int k, float a1, float a2, float a3,
+                                          float b1, float b2, float b3) {
+    float fR[7];
+#pragma unroll
+    for (int jj = 0; jj < 7; jj++) {
+        size_t o = g.at(i, k + jj - 3);
+        fR[jj] = tb.f[o] + tb.d1[o] * a1 + tb.d2[o] * a2 + tb.d3[o] * a3;
+    }
+    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        s1 += cDmf[1][j] * fR[j];
+        s2 += cDmf[2][j] * fR[j];
+        s3 += cDmf[3][j] * fR[j];
+    }
+    return fR[3] + s1 * b1 + s2 * b2 + s3 * b3;
+}
+
+struct StageArgsF {
+    FTables u, w, t;
+    const double *xr, *xs;
+    double *rtr, *str, *Ttr;
+    const double *r0, *s0, *T0;
+    double *rn, *sn, *Tn;
+    double dtstage;
+    int stage;
+    int64_t n;
+};
+
+__global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    double r = A.xr[t], s = A.xs[t];
+    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div);
+    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div);
+    i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
+    k = min(max(k, 0), cK.nz);
+    const float hr = (float)(r - (double)i * cK.dr), hs = (float)(s - (double)k * cK.ds);
+    const float a1 = hr, a2 = 0.5f * hr * hr, a3 = hr * hr * hr * (1.0f / 6.0f);
+    const float b1 = hs, b2 = 0.5f * hs * hs, b3 = hs * hs * hs * (1.0f / 6.0f);
+    const double tr = interp_f(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
+    const double ts = interp_f(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
+    const double tT = interp_f(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
+    const double r0 = A.r0[t], s0 = A.s0[t], T0 = A.T0[t];
+    switch (A.stage) {
+        case 1:
+            A.rtr[t] = tr; A.str[t] = ts; A.Ttr[t] = tT;
+            A.rn[t] = r0 + A.dtstage * tr; A.sn[t] = s0 + A.dtstage * ts; A.Tn[t] = T0 + A.dtstage * tT;
+            break;
+        case 2:
+        case 3:
+            A.rtr[t] = A.rtr[t] + 2.0 * tr; A.str[t] = A.str[t] + 2.0 * ts; A.Ttr[t] = A.Ttr[t] + 2.0 * tT;
+            A.rn[t] = r0 + A.dtstage * tr; A.sn[t] = s0 + A.dtstage * ts; A.Tn[t] = T0 + A.dtstage * tT;
+            break;
+        default:
+            A.rtr[t] = r0 + A.dtstage * (A.rtr[t] + tr);
+            A.str[t] = s0 + A.dtstage * (A.str[t] + ts);
+            A.Ttr[t] = T0 + A.dtstage * (A.Ttr[t] + tT);
+            break;
+    }
+}
+
+// FP32 copies of one interpolation table set (value and its three x-derivatives)
+__global__ void k_tables_to_f32(float* f, float* d1, float* d2, float* d3, const double* F, const double* D1,
+                                const double* D2, const double* D3, size_t n) {
+    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    f[q] = (float)F[q]; d1[q] = (float)D1[q]; d2[q] = (float)D2[q]; d3[q] = (float)D3[q];
+}
+
+int tables_to_f32(Engine& E, int which, const double* f) {
+    if (!E.fder[which][0]) return 0;
+    const size_t n = E.g1.elems();
+    PT_COUNT(), k_tables_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(E.fder[which][0], E.fder[which][1], E.fder[which][2],
+                                                                E.fder[which][3], f, E.der[which][0], E.der[which][1],
+                                                                E.der[which][2], n);
+    CKL("k_tables_to_f32");
+    return 0;
+}
+
 int rk_stage(Engine& E, int stage) {
-    PhaseTimer tm(E, 0);
+    PhaseTimer tm(E, PH_RK);
     StageArgs A;
     A.u = {E.u, E.der[0][0], E.der[0][1], E.der[0][2]};
     A.w = {E.w, E.der[1][0], E.der[1][1], E.der[1][2]};
@@ -315,7 +414,13 @@ int rk_stage(Engine& E, int stage) {
         case 3: A.xr = E.rtr2; A.xs = E.str2; A.rn = E.rtr1; A.sn = E.str1; A.Tn = E.Ttr1; A.dtstage = E.dt; break;
         default: A.xr = E.rtr1; A.xs = E.str1; A.rn = nullptr; A.sn = nullptr; A.Tn = nullptr; A.dtstage = E.dt / 6.0; break;
     }
-    {
+    if (E.fder[0][0]) {  // mixed precision: FP32 interpolation
+        auto ft = [&](int w) { return FTables{E.fder[w][0], E.fder[w][1], E.fder[w][2], E.fder[w][3]}; };
+        StageArgsF F{ft(0), ft(1), ft(2), A.xr, A.xs, A.rtr, A.str, A.Ttr, A.r0, A.s0, A.T0, A.rn, A.sn, A.Tn,
+                     A.dtstage, A.stage, A.n};
+        KernelTimer kt(E, KT_RK_STAGE, 1);
+        PT_COUNT(), k_rk_stage_f<<<nblk(E.ntr, 256), 256, 0, E.st>>>(F, E.g1);
+    } else {
         KernelTimer kt(E, KT_RK_STAGE, 1);
         PT_COUNT(), k_rk_stage<<<nblk(E.ntr, 256), 256, 0, E.st>>>(A, E.g1);
     }

@@ -192,6 +192,6 @@ class Engine:
         return int(self.L.pt_prof_launches())
 
     def phase_times(self) -> list[float]:
-        v = (ctypes.c_double * 5)()
+        v = (ctypes.c_double * 8)()
         self._check(self.L.pt_phase_times(v))
         return list(v)

@@ -177,3 +177,29 @@ def test_mixed_precision_on_workload_physics():
     assert abs(im["cycles"] - i64["cycles"]) <= 1
     assert rel_err(e.get(eng.F_SF), sf64) < 1e-6
     e.close()
+
+
+def test_mixed_step_close_to_fp64():
+    """A full mixed-precision step (FP32 multigrid inside FP64 defect correction, FP32 Taylor
+    interpolation, FP64 positions) against the plain FP64 step from the same state: the tracers
+    and T agree to the psi solve tolerance times the step's displacement."""
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    cfg, st = small_case("c3", nx=128, nz=64)
+    out = {}
+    for prec in (cfg.precision, PT_PREC_MIXED):
+        c = cfg.copy()
+        c.precision = prec
+        e = eng.Engine(c)
+        e.upload(st)
+        e.solve_psi()
+        dt, _ = e.step()
+        out[prec] = {f: e.get(f) for f in (eng.F_TRACER_R, eng.F_TRACER_S, eng.F_TRACER_T, eng.F_T)}
+        out[prec]["dt"] = dt
+        e.close()
+    a, b = out[cfg.precision], out[PT_PREC_MIXED]
+    assert abs(a["dt"] - b["dt"]) <= 1e-6 * a["dt"]
+    for f in (eng.F_TRACER_R, eng.F_TRACER_S):
+        assert rel_err(b[f], a[f]) < 1e-7, f
+    assert rel_err(b[eng.F_TRACER_T], a[eng.F_TRACER_T]) < 1e-6
+    assert rel_err(b[eng.F_T], a[eng.F_T]) < 1e-6
