@@ -48,6 +48,12 @@ extern "C" {
 #define PT_MG_REFERENCE 0
 #define PT_MG_CORRECTION 1
 
+/* Level schedule of the mixed-precision solve (the FP64 solve always runs the reference's
+ * schedule, multigrid_setup in iterative_solver.f90:1-122): PT_CYCLE_REFERENCE the reference's
+ * table for the level count (a W-type cycle), PT_CYCLE_V one descent and one ascent. */
+#define PT_CYCLE_REFERENCE 0
+#define PT_CYCLE_V 1
+
 /* Initial-guess mode of the stream-function solve (spec extension). */
 #define PT_GUESS_PREVIOUS 0 /* previous psi (the reference's warm start, iterative_solver.f90:134) */
 #define PT_GUESS_ZERO 1
@@ -94,6 +100,8 @@ typedef struct pt_config {
     int32_t mg_scheme;     /* PT_MG_* (&gpu group) */
     int32_t CFL;           /* &inputs CFL: 1 = velocity terms in the advective eigenvalue and
                               dt <= 2/eigD_max (energy.f90:809, 859-866) */
+    int32_t mg_cycle;      /* PT_CYCLE_*: level schedule of the mixed-precision solve (&gpu group) */
+    int32_t reserved;
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

@@ -65,6 +65,7 @@ struct Engine {
     Consts K;
     LevConst L[PT_MAXLEV];
     int grids = 0, nsteps = 0, multi[64];
+    int mnsteps = 0, mmulti[64];  // schedule of the mixed-precision solve (PT_CYCLE_*)
     double RKC1_stability = 0, delta_T = 2, delta_C = 2, dts = 0;
     double Tr_base = 0, Trr_base = 0, Trrr_base = 0, Trrrr_base = 0, Trs_base = 0, Trrs_base = 0,
            Trrss_base = 0, Tr_base_so = 0, Trr_base_so = 0;
@@ -99,6 +100,7 @@ struct Engine {
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
     bool coarse_ready = false;  // coarse factorisation valid for coarse_time (mixed precision)
+    bool levels_reused = false; // this solve reuses levels 2..grids (mixed precision)
     double coarse_time = -1.0;
     int ginv_cols = 32;
     int* ipiv = nullptr;

@@ -803,19 +803,19 @@ int mg_setup_solve(Engine& E) {
     CK(cudaMemcpyAsync(E.err[1], E.SF, E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     if ((rc = compute_RHS(E, 1))) return rc;
     if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
-    for (int level = 1; level <= E.grids; level++)
+    // The mixed-precision cycle uses levels 2..grids only as a preconditioner inside FP64 defect
+    // correction on level 1: their viscosity pipeline and the coarse factorisation are refreshed
+    // once per time level (the top-of-step solve) and reused by the RK-stage solves of the step,
+    // whose viscosity differs by O(dt).  Level 1, which defines the residual, is rebuilt every
+    // solve.  The FP64 cycle rebuilds every level every solve, as the reference does.
+    const bool reuse = E.cfg.precision == PT_PREC_MIXED && E.coarse_ready && E.coarse_time == E.time;
+    E.levels_reused = reuse;
+    for (int level = 1; level <= (reuse ? 1 : E.grids); level++)
         if ((rc = compute_viscosity(E, level))) return rc;
-    if (E.time == 0.0 || E.cfg.ivis > 0) {
-        // The mixed-precision cycle uses the coarse solve as a preconditioner inside FP64 defect
-        // correction: its factorisation is refreshed once per time level (the top-of-step solve)
-        // and reused by the RK-stage solves of the step, whose viscosity differs by O(dt).  The
-        // FP64 cycle refactors every solve, as the reference does.
-        const bool reuse = E.cfg.precision == PT_PREC_MIXED && E.coarse_ready && E.coarse_time == E.time;
-        if (!reuse) {
-            if ((rc = coarse_factor(E))) return rc;
-            E.coarse_ready = true;
-            E.coarse_time = E.time;
-        }
+    if (!reuse && (E.time == 0.0 || E.cfg.ivis > 0)) {
+        if ((rc = coarse_factor(E))) return rc;
+        E.coarse_ready = true;
+        E.coarse_time = E.time;
     }
     return 0;
 }

@@ -445,8 +445,8 @@ static int mixed_part(Engine& E, int part) {
         if ((rc = add_correction(E))) return rc;
         return residual64(E, true);
     }
-    const int grids = E.grids, nsteps = E.nsteps;
-    const int* multi = E.multi;
+    const int grids = E.grids, nsteps = E.mnsteps;
+    const int* multi = E.mmulti;
     for (int p = 2; p <= nsteps; p++) {
         const int l = multi[p];
         const Geo& g = E.gl[l];
@@ -519,7 +519,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
     {
         PhaseTimer ts(E, PH_SETUP);
         if ((rc = mg_setup_solve(E))) return rc;
-        for (int l = 1; l < E.grids; l++) {
+        for (int l = 1; l < (E.levels_reused ? 2 : E.grids); l++) {
             size_t n = E.gl[l].elems();
             float* const* f = E.fcoef[l];
             PT_COUNT(), k_coef_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(f[0], f[1], f[2], f[3], f[4], f[5], E.vis[l], E.vx[l],

@@ -210,6 +210,20 @@ static int choose_levels(Engine& E) {
     for (int p = 1; p <= E.nsteps; p++) E.multi[p] = sched[E.grids][p - 1];
     E.multi[0] = E.multi[E.nsteps];
     E.multi[E.nsteps + 1] = E.multi[1];
+    // schedule of the mixed-precision solve: the reference's table or a V-cycle 1..g..2
+    if (E.cfg.mg_cycle != PT_CYCLE_REFERENCE && E.cfg.mg_cycle != PT_CYCLE_V)
+        return fail(PT_ERR_CONFIG, "mg_cycle must be PT_CYCLE_REFERENCE or PT_CYCLE_V");
+    if (E.cfg.mg_cycle == PT_CYCLE_V) {
+        int p = 0;
+        for (int l = 1; l <= E.grids; l++) E.mmulti[++p] = l;
+        for (int l = E.grids - 1; l >= 2; l--) E.mmulti[++p] = l;
+        E.mnsteps = p;
+    } else {
+        E.mnsteps = E.nsteps;
+        for (int p = 1; p <= E.nsteps; p++) E.mmulti[p] = E.multi[p];
+    }
+    E.mmulti[0] = E.mmulti[E.mnsteps];
+    E.mmulti[E.mnsteps + 1] = E.mmulti[1];
     return 0;
 }
 

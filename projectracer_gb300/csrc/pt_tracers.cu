@@ -164,6 +164,59 @@ __global__ void k_cell_partials(const double* __restrict__ r, const double* __re
     }
 }
 
+// Mixed-precision variant of k_cell_partials: the offsets u = (r - ci dr)/dr and v = (s - ck ds)/ds
+// are formed in FP64, the shape weights max(0, 1 - |u - d|), the products and the sums in FP32 with
+// Neumaier compensation (same ascending-ID order, so the result is still deterministic); each
+// partial is stored as the FP64 value of sum + compensation.  Relative error of order 1e-7 on
+// the projected T and C.
+__device__ __forceinline__ void comp_add(float& s, float& c, float x) {
+    float t = s + x;
+    c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+}
+
+__global__ void k_cell_partials_f(const double* __restrict__ r, const double* __restrict__ s,
+                                  const double* __restrict__ Tt, const double* __restrict__ Ct,
+                                  const int32_t* __restrict__ list, const int32_t* __restrict__ start,
+                                  const int32_t* __restrict__ count, int ncell, double* __restrict__ P, int comp) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int nx1 = cK.nx + 1;
+    int ci = c % nx1, ck = c / nx1;
+    float aT[9], cT[9], aC[9], cC[9], aS[9], cS[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) { aT[q] = cT[q] = aC[q] = cC[q] = aS[q] = cS[q] = 0.f; }
+    const double x0 = (double)ci * cK.dr, z0 = (double)ck * cK.ds;
+    int b = start[c], n = count[c];
+    for (int a = 0; a < n; a++) {
+        int32_t t = list[b + a];
+        const float u = (float)((r[t] - x0) * cK.inv_dr), v = (float)((s[t] - z0) * cK.inv_ds);
+        const float tv = (float)Tt[t], cv = comp ? (float)Ct[t] : 0.f;
+        float wx[3], wz[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            wx[d] = fmaxf(0.f, 1.f - fabsf(u - (float)(d - 1)));
+            wz[d] = fmaxf(0.f, 1.f - fabsf(v - (float)(d - 1)));
+        }
+#pragma unroll
+        for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++) {
+                const float S = wx[dx] * wz[dz];
+                const int q = dz * 3 + dx;
+                comp_add(aT[q], cT[q], tv * S);
+                if (comp) comp_add(aC[q], cC[q], cv * S);
+                comp_add(aS[q], cS[q], S);
+            }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        P[(size_t)q * ncell + c] = (double)aT[q] + (double)cT[q];
+        P[(size_t)(9 + q) * ncell + c] = (double)aC[q] + (double)cC[q];
+        P[(size_t)(18 + q) * ncell + c] = (double)aS[q] + (double)cS[q];
+    }
+}
+
 // per node: fixed-order sum of the partials of the 3x3 surrounding cells, then the ratio
 __global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restrict__ count, int ncell,
                             double* Tratio, double* Cnew, int32_t* nempty, Geo g, int comp) {
@@ -209,8 +262,12 @@ int project(Engine& E, const double* r, const double* s, const double* Tt, const
     CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
     PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.cstart, cursor, E.clist);
     PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(E.clist, E.cstart, E.ccount, ncell);
-    PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount, ncell,
-                                                        E.cpart, E.cfg.comp);
+    if (E.cfg.precision == PT_PREC_MIXED)
+        PT_COUNT(), k_cell_partials_f<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount,
+                                                                          ncell, E.cpart, E.cfg.comp);
+    else
+        PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount, ncell,
+                                                            E.cpart, E.cfg.comp);
     dim3 grid(nblk(nx + 1, 128), nz + 1);
     PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(E.cpart, E.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
     CKL("projection");

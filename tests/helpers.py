@@ -39,6 +39,7 @@ def small_case(kind: str = "iso", nx: int = 64, nz: int = 64, tpc: int = 8, seed
         c.CFL = 1
         c.courant = 0.5
         c.mg_scheme = PT_MG_CORRECTION
+        c.mg_cycle = 0  # the reference's schedule in both precisions (parity cases)
     else:
         raise ValueError(kind)
     c.ntr = nx * nz * tpc

@@ -179,6 +179,26 @@ def test_mixed_precision_on_workload_physics():
     e.close()
 
 
+def test_mixed_v_cycle_meets_tolerance():
+    """The V-cycle schedule of the mixed-precision solve reaches the same FP64 residual test."""
+    from projectracer_gb300.config import PT_CYCLE_V, PT_PREC_MIXED
+
+    cfg, st = small_case("c3", nx=128, nz=64)
+    e = eng.Engine(cfg)
+    e.upload(st)
+    e.solve_psi()
+    sf64 = e.get(eng.F_SF)
+    e.close()
+    cfg.precision = PT_PREC_MIXED
+    cfg.mg_cycle = PT_CYCLE_V
+    e = eng.Engine(cfg)
+    e.upload(st)
+    im = e.solve_psi()
+    assert im["resid_ratio"] <= cfg.tolerance
+    assert rel_err(e.get(eng.F_SF), sf64) < 1e-6
+    e.close()
+
+
 def test_mixed_step_close_to_fp64():
     """A full mixed-precision step (FP32 multigrid inside FP64 defect correction, FP32 Taylor
     interpolation, FP64 positions) against the plain FP64 step from the same state: the tracers
