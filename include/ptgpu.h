@@ -199,6 +199,20 @@ int pt_stats(pt_stats_row* out);
  * smoothing on/off (smooth_vis, basics.f90:315). */
 int pt_tracers_to_corners(const double* T0, int smooth_vis);
 
+/* pt_tracers_to_corners without any device allocation, for callers that must not allocate
+ * (no reference counterpart: the reference allocates its projection work arrays on the stack and
+ * heap of tracers_to_corners).  The sort and partial-sum scratch lives in one file-scope device
+ * array of the library (about 12 MB) whose address pt_init resolves once per device, so no
+ * symbol lookup happens inside a stream capture; calls on a thread with no prior pt_init on the
+ * current device resolve it themselves and must not be made during a capture.  Limits: at most
+ * PT_NOALLOC_MAX_TRACERS tracers and PT_NOALLOC_MAX_NODES grid nodes ((nx+1)*(nz+1)); larger
+ * states return PT_ERR_ARG.  The scratch is shared: overlapping calls (other threads or
+ * streams, or another engine on the same device) race on it and must be serialised by the
+ * caller.  Results are identical to pt_tracers_to_corners. */
+#define PT_NOALLOC_MAX_TRACERS 524288
+#define PT_NOALLOC_MAX_NODES 33153
+int pt_tracers_to_corners_noalloc(const double* T0, int smooth_vis);
+
 /* Current simulation time and the RK4 time step of stability_RK4 (energy.f90:756-810). */
 int pt_time(double* time, double* dt);
 

@@ -278,7 +278,7 @@ int pt_init(const pt_config* cfg) {
     g_eng = E;
     TRACE("pt_init: device allocations and constants");
     if ((rc = engine_alloc(*E)) || (rc = upload_consts_fields(*E)) || (rc = upload_consts_tracers(*E)) ||
-        (rc = upload_consts_mg(*E)) || (rc = upload_consts_mixed(*E))) {
+        (rc = upload_consts_mg(*E)) || (rc = upload_consts_mixed(*E)) || (rc = noalloc_scratch_setup())) {
         std::string msg = g_err;
         pt_finalize();
         g_err = msg;
@@ -497,6 +497,18 @@ int pt_tracers_to_corners(const double* T0, int smooth_vis) {
         if ((rc = copy_grid(E, PT_F_TRATIO, const_cast<double*>(T0), true))) return rc;
     }
     rc = project(E, E.rtr, E.str, E.Ttr, E.Tratio, smooth_vis);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(E.st), "projection");
+    return rc;
+}
+
+int pt_tracers_to_corners_noalloc(const double* T0, int smooth_vis) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    Engine& E = *g_eng;
+    int rc;
+    if (T0) {
+        if ((rc = copy_grid(E, PT_F_TRATIO, const_cast<double*>(T0), true))) return rc;
+    }
+    rc = project_noalloc(E, E.Tratio, smooth_vis);
     if (!rc) rc = cuda_check(cudaStreamSynchronize(E.st), "projection");
     return rc;
 }

@@ -192,6 +192,8 @@ int smoother_time_T(Engine& E, const double* Tin);   // smoother.f90:638-672
 int smoother_time_C(Engine& E);                      // smoother.f90:582-636
 int load_conductivity(Engine& E);                    // energy.f90:59-86
 int load_tracer_space(Engine& E);                    // energy.f90:154-179 (+extendT 595-630)
+int noalloc_scratch_setup();  // static scratch address of the current device (before any capture)
+int project_noalloc(Engine& E, const double* T0f, int smooth);
 int tables_to_f32(Engine& E, int which, const double* f);  // FP32 copies for the mixed RK stage
 int compute_derivatives(Engine& E, const double* f, int which);  // composition.f90:1457-1478
 int compute_velocities(Engine& E);                   // momentum.f90:655-710

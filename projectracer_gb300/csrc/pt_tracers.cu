@@ -9,6 +9,7 @@
 // result is deterministic and equals the oracle's canonical order bit for bit (the arithmetic
 // uses explicit round-to-nearest intrinsics, no contraction).
 #include <cstdio>
+#include <string>
 
 #include "pt_consts.cuh"
 
@@ -241,7 +242,16 @@ __global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restr
     }
 }
 
-int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f, int smooth) {
+// scratch of one projection: cell of each tracer, per-cell counts/starts/list, scan blocks,
+// the 27 partial planes and the out-of-domain flag
+struct ProjScratch {
+    int32_t *tcell, *clist, *ccount, *cstart, *scan_tmp;
+    double* cpart;
+    int* derr;
+};
+
+static int project_with(Engine& E, const ProjScratch& W, const double* r, const double* s, const double* Tt,
+                        const double* T0f, int smooth) {
     const int nx = E.K.nx, nz = E.K.nz;
     const int ncell = (nx + 1) * (nz + 1);
     const int64_t n = E.ntr;
@@ -251,28 +261,28 @@ int project(Engine& E, const double* r, const double* s, const double* Tt, const
     if (T0f && T0f != E.Tratio) {
         if ((rc = copy_field(E, E.Tratio, T0f))) return rc;
     }
-    CK(cudaMemsetAsync(E.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
-    CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
-    PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, E.tcell, E.ccount, E.derr);
+    CK(cudaMemsetAsync(W.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+    CK(cudaMemsetAsync(W.derr, 0, sizeof(int), E.st));
+    PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, W.tcell, W.ccount, W.derr);
     int nb = (int)nblk(ncell, 1024);
-    PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(E.ccount, E.cstart, E.scan_tmp, ncell);
-    PT_COUNT(), k_scan_totals<<<1, 32, 0, E.st>>>(E.scan_tmp, nb);
-    PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(E.cstart, E.scan_tmp, ncell);
-    int32_t* cursor = E.scan_tmp + nb + 32;
+    PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(W.ccount, W.cstart, W.scan_tmp, ncell);
+    PT_COUNT(), k_scan_totals<<<1, 32, 0, E.st>>>(W.scan_tmp, nb);
+    PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(W.cstart, W.scan_tmp, ncell);
+    int32_t* cursor = W.scan_tmp + nb + 32;
     CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
-    PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.cstart, cursor, E.clist);
-    PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(E.clist, E.cstart, E.ccount, ncell);
+    PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(W.tcell, n, W.cstart, cursor, W.clist);
+    PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(W.clist, W.cstart, W.ccount, ncell);
     if (E.cfg.precision == PT_PREC_MIXED)
-        PT_COUNT(), k_cell_partials_f<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount,
-                                                                          ncell, E.cpart, E.cfg.comp);
+        PT_COUNT(), k_cell_partials_f<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount,
+                                                                          ncell, W.cpart, E.cfg.comp);
     else
-        PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, E.clist, E.cstart, E.ccount, ncell,
-                                                            E.cpart, E.cfg.comp);
+        PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount, ncell,
+                                                            W.cpart, E.cfg.comp);
     dim3 grid(nblk(nx + 1, 128), nz + 1);
-    PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(E.cpart, E.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
+    PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(W.cpart, W.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
     CKL("projection");
     int herr = 0;
-    CK(cudaMemcpyAsync(&herr, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaMemcpyAsync(&herr, W.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
     if (herr) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
     if (E.cfg.comp) {
@@ -282,6 +292,64 @@ int project(Engine& E, const double* r, const double* s, const double* Tt, const
     if ((rc = enforce_bcs_T(E, E.Tratio))) return rc;
     if (smooth && (rc = smoother_time_T(E, E.Tratio))) return rc;
     return load_conductivity(E);
+}
+
+int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f, int smooth) {
+    ProjScratch W{E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp, E.cpart, E.derr};
+    return project_with(E, W, r, s, Tt, T0f, smooth);
+}
+
+// ---------------------------------------------------------------- projection without allocation
+// Scratch of pt_tracers_to_corners_noalloc: one file-scope device array, carved as
+// [partials 27 x nodes doubles | tcell | clist | ccount | cstart | scan | flag], each part
+// 256-byte aligned.  Sized for PT_NOALLOC_MAX_TRACERS and PT_NOALLOC_MAX_NODES.
+static constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
+static constexpr size_t kNaNodes = PT_NOALLOC_MAX_NODES, kNaTracers = PT_NOALLOC_MAX_TRACERS;
+static constexpr size_t kNaScan = kNaNodes + kNaNodes / 1024 + 64;
+static constexpr size_t kNaOffPart = 0;
+static constexpr size_t kNaOffCell = kNaOffPart + na_round(27 * kNaNodes * sizeof(double));
+static constexpr size_t kNaOffList = kNaOffCell + na_round(kNaTracers * sizeof(int32_t));
+static constexpr size_t kNaOffCount = kNaOffList + na_round(kNaTracers * sizeof(int32_t));
+static constexpr size_t kNaOffStart = kNaOffCount + na_round(kNaNodes * sizeof(int32_t));
+static constexpr size_t kNaOffScan = kNaOffStart + na_round(kNaNodes * sizeof(int32_t));
+static constexpr size_t kNaOffFlag = kNaOffScan + na_round(kNaScan * sizeof(int32_t));
+static constexpr size_t kNaBytes = kNaOffFlag + 256;
+static_assert(kNaBytes <= 16u * 1024u * 1024u, "no-alloc projection scratch stays below 16 MB");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+static unsigned char* s_noalloc_base[64] = {};  // per device, from cudaGetSymbolAddress
+
+// Resolves the scratch address of the current device.  pt_init calls it, so the lookup (which may
+// load the module) never happens inside a stream capture.
+int noalloc_scratch_setup() {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(PT_ERR_CUDA, "device index out of range for the no-alloc scratch table");
+    if (!s_noalloc_base[dev]) {
+        void* p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        s_noalloc_base[dev] = static_cast<unsigned char*>(p);
+    }
+    return 0;
+}
+
+int project_noalloc(Engine& E, const double* T0f, int smooth) {
+    const size_t ncell = (size_t)(E.K.nx + 1) * (size_t)(E.K.nz + 1);
+    if ((size_t)E.ntr > kNaTracers || ncell > kNaNodes)
+        return fail(PT_ERR_ARG, "pt_tracers_to_corners_noalloc: more than " + std::to_string(kNaTracers) +
+                                    " tracers or " + std::to_string(kNaNodes) + " grid nodes");
+    int rc;
+    if ((rc = noalloc_scratch_setup())) return rc;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    unsigned char* b = s_noalloc_base[dev];
+    ProjScratch W{reinterpret_cast<int32_t*>(b + kNaOffCell), reinterpret_cast<int32_t*>(b + kNaOffList),
+                  reinterpret_cast<int32_t*>(b + kNaOffCount), reinterpret_cast<int32_t*>(b + kNaOffStart),
+                  reinterpret_cast<int32_t*>(b + kNaOffScan), reinterpret_cast<double*>(b + kNaOffPart),
+                  reinterpret_cast<int*>(b + kNaOffFlag)};
+    // project_with clears the counts, the scatter cursors and the flag before use; every other
+    // part is fully written before it is read
+    return project_with(E, W, E.rtr, E.str, E.Ttr, T0f, smooth);
 }
 
 // ---------------------------------------------------------------- RK4 stage loops
