@@ -208,6 +208,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--tpc", type=int, default=0,
+                    help="tracers per cell override (profiling captures of a smaller tracer state only)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -223,6 +225,8 @@ def main():
     dist = Dist(world)
     cfg, w = bench_config(args.workload, args.precision)
     apply_bench_solver(cfg, w)
+    if args.tpc > 0:
+        cfg.ntr = cfg.nx * cfg.nz * args.tpc
     st = make_state(cfg, 3 + rank, noise=w.get("noise", 1e-3))
     e = eng.Engine(cfg)
     e.upload(st)
