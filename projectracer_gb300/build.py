@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
           "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
 EXTRA = {"pt_fields.cu": ["--fmad=false"]}
-SOURCES = ["pt_setup.cpp", "pt_fields.cu", "pt_tracers.cu", "pt_mg.cu", "pt_mixed.cu", "pt_api.cu"]
+SOURCES = ["pt_setup.cpp", "pt_fields.cu", "pt_tracers.cu", "pt_mg.cu", "pt_mixed.cu", "pt_api.cu", "pt_unet.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,193 @@
+// pt_tc.cuh -- 5th-generation tensor-core (tcgen05) GEMM tile for sm_103a, hand-written PTX.
+//
+// One CTA of 128 threads computes a 128 x N tile of D = A * B^T (A: M x K, B: N x K, BF16, FP32
+// accumulation in tensor memory):
+//   * the operand tiles of one K chunk (64) are gathered into shared memory by all threads, in
+//     the canonical no-swizzle K-major layout: 8x8 "core matrices" of 128 contiguous bytes (8 rows
+//     of 16 bytes), LBO = 128 B between core matrices adjacent in K, SBO = 1024 B between the
+//     8-row groups (8 core matrices per 64-wide chunk);
+//   * one thread issues the four K=16 MMAs of the chunk (tcgen05.mma.cta_group::1.kind::f16) and
+//     commits them to an mbarrier; the next chunk's gather waits on that barrier (bounded spin);
+//   * the epilogue reads the accumulator with tcgen05.ld.32x32b (warp w owns TMEM lanes
+//     32w..32w+31 = tile rows) and hands each row's values to the problem's store functor.
+// A problem type supplies M, N, K, gather_a / gather_b (element (row, k) of A or B as BF16 bits,
+// zero outside the matrix) and store(row, col, value).  Waits on the mbarrier give up after a
+// fixed number of polls, set an error flag and skip the rest of the tile (TMEM is still freed).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pt {
+namespace tc {
+
+constexpr int kTileM = 128;
+constexpr int kChunkK = 64;
+constexpr int kThreads = 128;
+constexpr int kWaitPolls = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor (tcgen05 format: start, LBO, SBO in 16-byte units, version 1,
+// no swizzle)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M = 128, N
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+// byte offset of element (r, k) of a chunk tile (k < 64) in the core-matrix layout
+__device__ __forceinline__ uint32_t tile_off(int r, int k) {
+    return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// bounded wait for the given phase parity; returns false when the poll budget ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    for (int it = 0; it < kWaitPolls; it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 8 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
+}
+
+__host__ __device__ constexpr uint32_t tmem_cols(int n) {
+    return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : 256u;
+}
+
+// Dynamic shared memory: A tile (128 x 64 BF16 = 16 KB) | B tile (N x 64 BF16) | mbarrier | tmem
+// addr | 16 KB of slack, so that every core-matrix offset a descriptor can form from the tile
+// bases stays inside the allocation.
+__host__ __device__ constexpr size_t smem_bytes(int n) { return 16384 + (size_t)n * 128 + 64 + 16384; }
+
+// The GEMM tile.  Problem P: int M, N, K; uint16_t gather_a(int row, int k) const;
+// uint16_t gather_b(int col, int k) const; void store(int row, int col, float v) const.
+// N must be a multiple of 16 in [16, 256].
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sa = smem;
+    unsigned char* sb = smem + 16384;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 16384 + (size_t)prob.N * 128);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * kTileM;
+    const int n = prob.N;
+    const uint32_t ncols = tmem_cols(n);
+    if (tid == 0) mbar_init(bar, 1);
+    if (warp == 0) tmem_alloc(tslot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tslot;
+    const uint32_t idesc = idesc_bf16(n);
+    const int nchunks = (prob.K + kChunkK - 1) / kChunkK;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int c = 0; c < nchunks && ok; c++) {
+        const int k0 = c * kChunkK;
+        // gather the chunk: A rows m0..m0+127, B rows 0..n-1, k0..k0+63
+        for (int q = tid; q < kTileM * kChunkK; q += kThreads) {
+            const int r = q / kChunkK, k = q % kChunkK;
+            *reinterpret_cast<uint16_t*>(sa + tile_off(r, k)) = prob.gather_a(m0 + r, k0 + k);
+        }
+        for (int q = tid; q < n * kChunkK; q += kThreads) {
+            const int r = q / kChunkK, k = q % kChunkK;
+            *reinterpret_cast<uint16_t*>(sb + tile_off(r, k)) = prob.gather_b(r, k0 + k);
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+#pragma unroll
+            for (int s = 0; s < kChunkK / 16; s++)
+                mma_bf16(taddr, smem_desc(a0 + s * 256, 128, 1024), smem_desc(b0 + s * 256, 128, 1024), idesc,
+                         (c > 0 || s > 0) ? 1u : 0u);
+            mma_commit(bar);
+        }
+        // every thread waits for the chunk's MMAs before the tiles are overwritten; a timeout is
+        // agreed by the whole CTA so every thread leaves the loop together
+        const int timed_out = __syncthreads_or(mbar_wait(bar, phase) ? 0 : 1);
+        if (timed_out) {
+            if (tid == 0) atomicOr(err, 1);
+            ok = false;
+        }
+        phase ^= 1u;
+    }
+    tc_fence_after();
+    if (ok) {
+        const int row = m0 + warp * 32 + (tid & 31);
+        const uint32_t lane_base = taddr + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < n; c0 += 8) {
+            float v[8];
+            tmem_ld8(lane_base + (uint32_t)c0, v);
+            if (row < prob.M)
+#pragma unroll
+                for (int j = 0; j < 8; j++) prob.store(row, c0 + j, v[j]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(taddr, ncols);
+}
+
+}  // namespace tc
+}  // namespace pt
