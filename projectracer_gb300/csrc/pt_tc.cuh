@@ -117,19 +117,21 @@ __host__ __device__ constexpr uint32_t tmem_cols(int n) {
 // bases stays inside the allocation.
 __host__ __device__ constexpr size_t smem_bytes(int n) { return 16384 + (size_t)n * 128 + 64 + 16384; }
 
-// The GEMM tile.  Problem P: int M, N, K; uint16_t gather_a(int row, int k) const;
-// uint16_t gather_b(int col, int k) const; void store(int row, int col, float v) const.
-// N must be a multiple of 16 in [16, 256].
+// The GEMM tile.  Problem P: int M, N, K (matrix sizes), int Ntile (columns per CTA, a multiple
+// of 16 in [16, 256]), int kc_split (K chunks per CTA along grid z; 0 = all);
+// uint16_t gather_a(int row, int k) const; uint16_t gather_b(int col, int k) const (zero outside
+// the matrices); void store(int row, int col, int split, float v) const.
+// Grid: (ceil(M/128), ceil(N/Ntile), number of K splits).
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sa = smem;
     unsigned char* sb = smem + 16384;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 16384 + (size_t)prob.N * 128);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 16384 + (size_t)prob.Ntile * 128);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m0 = blockIdx.x * kTileM;
-    const int n = prob.N;
+    const int n = prob.Ntile, col0 = blockIdx.y * prob.Ntile;
     const uint32_t ncols = tmem_cols(n);
     if (tid == 0) mbar_init(bar, 1);
     if (warp == 0) tmem_alloc(tslot, ncols);
@@ -138,10 +140,12 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
     tc_fence_after();
     const uint32_t taddr = *tslot;
     const uint32_t idesc = idesc_bf16(n);
-    const int nchunks = (prob.K + kChunkK - 1) / kChunkK;
+    const int nall = (prob.K + kChunkK - 1) / kChunkK;
+    const int per = prob.kc_split > 0 ? prob.kc_split : nall;
+    const int cbeg = blockIdx.z * per, cend = min(nall, cbeg + per);
     uint32_t phase = 0;
     bool ok = true;
-    for (int c = 0; c < nchunks && ok; c++) {
+    for (int c = cbeg; c < cend && ok; c++) {
         const int k0 = c * kChunkK;
         // gather the chunk: A rows m0..m0+127, B rows 0..n-1, k0..k0+63
         for (int q = tid; q < kTileM * kChunkK; q += kThreads) {
@@ -150,7 +154,7 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
         }
         for (int q = tid; q < n * kChunkK; q += kThreads) {
             const int r = q / kChunkK, k = q % kChunkK;
-            *reinterpret_cast<uint16_t*>(sb + tile_off(r, k)) = prob.gather_b(r, k0 + k);
+            *reinterpret_cast<uint16_t*>(sb + tile_off(r, k)) = prob.gather_b(col0 + r, k0 + k);
         }
         fence_async_smem();
         __syncthreads();
@@ -160,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
 #pragma unroll
             for (int s = 0; s < kChunkK / 16; s++)
                 mma_bf16(taddr, smem_desc(a0 + s * 256, 128, 1024), smem_desc(b0 + s * 256, 128, 1024), idesc,
-                         (c > 0 || s > 0) ? 1u : 0u);
+                         (c > cbeg || s > 0) ? 1u : 0u);
             mma_commit(bar);
         }
         // every thread waits for the chunk's MMAs before the tiles are overwritten; a timeout is
@@ -176,12 +180,14 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
     if (ok) {
         const int row = m0 + warp * 32 + (tid & 31);
         const uint32_t lane_base = taddr + ((uint32_t)(warp * 32) << 16);
+        const bool empty = cbeg >= cend;  // a K split past the end: the accumulator was never written
         for (int c0 = 0; c0 < n; c0 += 8) {
             float v[8];
             tmem_ld8(lane_base + (uint32_t)c0, v);
             if (row < prob.M)
 #pragma unroll
-                for (int j = 0; j < 8; j++) prob.store(row, c0 + j, v[j]);
+                for (int j = 0; j < 8; j++)
+                    if (col0 + c0 + j < prob.N) prob.store(row, col0 + c0 + j, (int)blockIdx.z, empty ? 0.f : v[j]);
         }
     }
     tc_fence_before();

@@ -1,17 +1,23 @@
 // pt_unet.cu -- learned psi guess (no reference counterpart): BF16 implicit-GEMM convolutions
 // on the tcgen05 tensor cores (pt_tc.cuh), their self-check entry point, and the U-Net built on
 // them.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "pt_internal.h"
+#include "../../include/ptgpu_unet.h"
 #include "pt_tc.cuh"
+#include <cuda_bf16.h>
 
 namespace pt {
 
 // plain GEMM problem: C (M x N, FP32) = A (M x K) * B (N x K)^T, BF16 row-major operands
 struct GemmProb {
-    int M, N, K;
+    int M, N, K, Ntile, kc_split;
     const uint16_t* A;
     const uint16_t* B;
     float* C;
@@ -19,14 +25,522 @@ struct GemmProb {
         return (r < M && k < K) ? A[(size_t)r * K + k] : (uint16_t)0;
     }
     __device__ __forceinline__ uint16_t gather_b(int c, int k) const { return k < K ? B[(size_t)c * K + k] : (uint16_t)0; }
-    __device__ __forceinline__ void store(int r, int c, float v) const { C[(size_t)r * N + c] = v; }
+    __device__ __forceinline__ void store(int r, int c, int, float v) const { C[(size_t)r * N + c] = v; }
 };
 
+
+static inline unsigned nblk(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
+
+// ============================================================================ U-Net kernels
+__device__ __forceinline__ uint16_t f2bf(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+__device__ __forceinline__ float bf2f(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
+
+// The input of a convolution as seen by its im2col gather, at the convolution's resolution
+// (B x H x W): mode 0 one BF16 NHWC tensor; mode 1 a tensor at 2H x 2W averaged over 2x2 (pooling);
+// mode 2 the concatenation of a tensor at H/2 x W/2 read nearest-neighbour (upsampling, channels
+// 0..C0-1) and a skip tensor at H x W (channels C0..C0+C1-1).
+struct InView {
+    const uint16_t* t0;
+    const uint16_t* t1;
+    int B, H, W, C0, C1, mode;
+    __host__ __device__ int C() const { return C0 + C1; }
+    __device__ __forceinline__ float get(int b, int y, int x, int c) const {
+        if (mode == 0) return bf2f(t0[(((size_t)b * H + y) * W + x) * C0 + c]);
+        if (mode == 1) {
+            const size_t W2 = 2 * (size_t)W;
+            const uint16_t* q = t0 + (((size_t)b * 2 * H + 2 * y) * W2 + 2 * x) * C0 + c;
+            const float s = ((bf2f(q[0]) + bf2f(q[C0])) + bf2f(q[W2 * C0])) + bf2f(q[W2 * C0 + C0]);
+            return s * 0.25f;
+        }
+        if (c < C0) return bf2f(t0[(((size_t)b * (H >> 1) + (y >> 1)) * (W >> 1) + (x >> 1)) * C0 + c]);
+        return bf2f(t1[(((size_t)b * H + y) * W + x) * C1 + (c - C0)]);
+    }
+};
+
+// pixel p of a B x H x W grid shifted by tap (3x3, row-major taps); false outside the grid
+__device__ __forceinline__ bool tap_pixel(int p, int tap, int H, int W, int& b, int& y, int& x) {
+    x = p % W;
+    const int r = p / W;
+    y = r % H;
+    b = r / H;
+    y += tap / 3 - 1;
+    x += tap % 3 - 1;
+    return y >= 0 && y < H && x >= 0 && x < W;
+}
+
+// forward: out[p][co] = relu(sum_{tap,ci} in(p+tap)[ci] w[co][tap][ci] + bias[co]) in BF16
+struct ConvFwd {
+    int M, N, K, Ntile, kc_split;
+    InView in;
+    const uint16_t* w;
+    const float* bias;
+    uint16_t* out;
+    int relu;
+    __device__ __forceinline__ uint16_t gather_a(int p, int k) const {
+        if (p >= M || k >= K) return 0;
+        const int cin = in.C(), tap = k / cin, ci = k - tap * cin;
+        int b, y, x;
+        if (!tap_pixel(p, tap, in.H, in.W, b, y, x)) return 0;
+        return f2bf(in.get(b, y, x, ci));
+    }
+    __device__ __forceinline__ uint16_t gather_b(int co, int k) const {
+        return (co < N && k < K) ? w[(size_t)co * K + k] : (uint16_t)0;
+    }
+    __device__ __forceinline__ void store(int p, int co, int, float v) const {
+        v += bias[co];
+        if (relu) v = fmaxf(v, 0.f);
+        out[(size_t)p * N + co] = f2bf(v);
+    }
+};
+
+// gradient w.r.t. the pre-activation of a layer, as a BF16 GEMM operand: dY masked by Y > 0
+__device__ __forceinline__ uint16_t dz_bf(const float* dY, const uint16_t* Y, size_t idx) {
+    const float g = dY[idx];
+    if (Y && !(bf2f(Y[idx]) > 0.f)) return 0;
+    return f2bf(g);
+}
+
+// backward data: dX[q][ci] = sum_{t,co} dZ[q + tap t][co] w[co][8 - t][ci]  (FP32 out)
+struct ConvBwdData {
+    int M, N, K, Ntile, kc_split;  // M pixels, N = Cin, K = 9 Cout
+    int H, W, Cout;
+    const float* dY;
+    const uint16_t* Y;
+    const uint16_t* w;
+    float* dX;
+    __device__ __forceinline__ uint16_t gather_a(int q, int k) const {
+        if (q >= M || k >= K) return 0;
+        const int t = k / Cout, co = k - t * Cout;
+        int b, y, x;
+        if (!tap_pixel(q, t, H, W, b, y, x)) return 0;
+        return dz_bf(dY, Y, (((size_t)b * H + y) * W + x) * Cout + co);
+    }
+    __device__ __forceinline__ uint16_t gather_b(int ci, int k) const {
+        if (ci >= N || k >= K) return 0;
+        const int t = k / Cout, co = k - t * Cout;
+        return w[((size_t)co * 9 + (8 - t)) * N + ci];
+    }
+    __device__ __forceinline__ void store(int q, int ci, int, float v) const { dX[(size_t)q * N + ci] = v; }
+};
+
+// backward weights (split over pixels): part[z][tap*Cin + ci][co] = sum_{p in split z} in(p+tap)[ci] dZ[p][co]
+struct ConvBwdW {
+    int M, N, K, Ntile, kc_split;  // M = 9 Cin, N = Cout, K = pixels
+    InView in;
+    const float* dY;
+    const uint16_t* Y;
+    float* part;
+    __device__ __forceinline__ uint16_t gather_a(int kk, int p) const {
+        if (kk >= M || p >= K) return 0;
+        const int cin = in.C(), tap = kk / cin, ci = kk - tap * cin;
+        int b, y, x;
+        if (!tap_pixel(p, tap, in.H, in.W, b, y, x)) return 0;
+        return f2bf(in.get(b, y, x, ci));
+    }
+    __device__ __forceinline__ uint16_t gather_b(int co, int p) const {
+        return (co < N && p < K) ? dz_bf(dY, Y, (size_t)p * N + co) : (uint16_t)0;
+    }
+    __device__ __forceinline__ void store(int kk, int co, int z, float v) const {
+        part[((size_t)z * M + kk) * N + co] = v;
+    }
+};
+
+// dW[co][kk] = sum_z part[z][kk][co], z ascending
+__global__ void k_wgrad_reduce(float* dW, const float* part, int nsplit, int M, int N) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= M * N) return;
+    const int kk = q / N, co = q % N;
+    float s = 0.f;
+    for (int z = 0; z < nsplit; z++) s += part[((size_t)z * M + kk) * N + co];
+    dW[(size_t)co * M + kk] = s;
+}
+
+// db[co] = sum_p dZ[p][co] (block per channel, fixed-order tree)
+__global__ void k_bias_grad(float* db, const float* dY, const uint16_t* Y, int P, int C) {
+    __shared__ float sh[256];
+    const int co = blockIdx.x;
+    float s = 0.f;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        const size_t idx = (size_t)p * C + co;
+        if (!Y || bf2f(Y[idx]) > 0.f) s += dY[idx];
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[co] = sh[0];
+}
+
+// adjoints of the input views: add dXg (P x C at the view's resolution) into the sources' grads
+__global__ void k_adj_plain(float* g0, const float* dX, size_t n) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) g0[q] += dX[q];
+}
+__global__ void k_adj_pool(float* g0, const float* dX, int B, int H, int W, int C) {  // g0 at 2H x 2W
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)B * 4 * H * W * C;
+    if (q >= n) return;
+    const int c = (int)(q % C);
+    size_t r = q / C;
+    const int x2 = (int)(r % (2 * W));
+    r /= (2 * W);
+    const int y2 = (int)(r % (2 * H));
+    const int b = (int)(r / (2 * H));
+    g0[q] += 0.25f * dX[(((size_t)b * H + (y2 >> 1)) * W + (x2 >> 1)) * C + c];
+}
+__global__ void k_adj_upcat(float* g0, float* g1, const float* dX, int B, int H, int W, int C0, int C1) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n0 = (size_t)B * (H / 2) * (W / 2) * C0, n1 = (size_t)B * H * W * C1;
+    const int C = C0 + C1;
+    if (q < n0) {  // coarse source: sum of its 2x2 fine pixels, fixed order
+        const int c = (int)(q % C0);
+        size_t r = q / C0;
+        const int x = (int)(r % (W / 2));
+        r /= (W / 2);
+        const int y = (int)(r % (H / 2));
+        const int b = (int)(r / (H / 2));
+        const size_t f = (((size_t)b * H + 2 * y) * W + 2 * x) * C + c;
+        g0[q] += ((dX[f] + dX[f + C]) + dX[f + (size_t)W * C]) + dX[f + (size_t)W * C + C];
+    } else if (q < n0 + n1) {
+        const size_t u = q - n0;
+        const int c = (int)(u % C1);
+        const size_t p = u / C1;
+        g1[u] += dX[p * C + C0 + c];
+    }
+}
+
+// 1x1 output convolution (linear, FP32 out) and its backward
+__global__ void k_out_fwd(float* y, const uint16_t* d, const float* w, const float* b, int P, int C) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    float s = b[0];
+    for (int c = 0; c < C; c++) s += bf2f(d[(size_t)p * C + c]) * w[c];
+    y[p] = s;
+}
+// loss = mean (y - t)^2; dy = 2 (y - t) / P; per-block partial sums of (y - t)^2
+__global__ void k_mse(float* dy, float* lpart, const float* y, const float* t, int P) {
+    __shared__ float sh[256];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    float e = 0.f;
+    if (p < P) {
+        const float d = y[p] - t[p];
+        dy[p] = 2.f * d / (float)P;
+        e = d * d;
+    }
+    sh[threadIdx.x] = e;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) lpart[blockIdx.x] = sh[0];
+}
+__global__ void k_out_bwd_data(float* gd, const float* dy, const float* w, int P, int C) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (size_t)P * C) return;
+    gd[q] = dy[q / C] * w[q % C];
+}
+// dw[c] = sum_p dy[p] d[p][c] (block per c), db = sum_p dy[p] (block C)
+__global__ void k_out_bwd_w(float* dw, float* db, const float* dy, const uint16_t* d, int P, int C) {
+    __shared__ float sh[256];
+    const int c = blockIdx.x;
+    float s = 0.f;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) s += c < C ? dy[p] * bf2f(d[(size_t)p * C + c]) : dy[p];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (c < C) dw[c] = sh[0];
+        else db[0] = sh[0];
+    }
+}
+
+// Adam on FP32 master weights, with the BF16 copy used by the convolution GEMMs
+__global__ void k_adam(float* w, float* m, float* v, uint16_t* wbf, const float* g, size_t n, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const float gg = g[q];
+    const float mm = b1 * m[q] + (1.f - b1) * gg;
+    const float vv = b2 * v[q] + (1.f - b2) * gg * gg;
+    m[q] = mm;
+    v[q] = vv;
+    const float wn = w[q] - lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    w[q] = wn;
+    wbf[q] = f2bf(wn);
+}
+__global__ void k_to_bf16(uint16_t* o, const float* i, size_t n) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) o[q] = f2bf(i[q]);
+}
+// NCHW FP32 -> NHWC BF16
+__global__ void k_input_nhwc(uint16_t* o, const float* i, int B, int C, int H, int W) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)B * C * H * W;
+    if (q >= n) return;
+    const int c = (int)(q % C);
+    size_t r = q / C;
+    const int x = (int)(r % W);
+    r /= W;
+    const int y = (int)(r % H);
+    const int b = (int)(r / H);
+    o[q] = f2bf(i[(((size_t)b * C + c) * H + y) * W + x]);
+}
+
+// ============================================================================ U-Net host side
+// 4 levels, base width 32, 3x3 convolutions with ReLU, 2x2 average pooling, nearest upsampling
+// with skip concatenation, 1x1 linear output.  Activations BF16 NHWC; FP32 master weights with
+// BF16 copies for the tensor-core GEMMs; FP32 gradients; Adam.
+struct UConv {
+    int src0, src1, mode, cin, cout, level, out;  // src -1 = network input
+    size_t woff, boff;                             // in the flat parameter vector
+};
+
+struct UNet {
+    int H = 0, W = 0, maxB = 0;
+    std::vector<UConv> L;
+    int tch[14] = {}, tlev[14] = {};
+    size_t nparams = 0, out_w = 0, out_b = 0;
+    float *w32 = nullptr, *m = nullptr, *v = nullptr, *g = nullptr;
+    uint16_t* wbf = nullptr;
+    int step = 0;
+    uint16_t* act[14] = {};
+    float* grad[14] = {};
+    uint16_t* x0 = nullptr;
+    float *xin = nullptr, *y = nullptr, *dy = nullptr, *tgt = nullptr, *lpart = nullptr, *dXg = nullptr,
+          *part = nullptr;
+    size_t part_cap = 0, dxg_cap = 0;
+    int* derr = nullptr;
+    cudaStream_t st = nullptr;
+    std::vector<void*> owned;
+};
+
+static uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double unit_open(uint64_t& s) { return ((double)(splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+static double normal01(uint64_t& s) {  // Box-Muller
+    const double u1 = unit_open(s), u2 = unit_open(s);
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+}
+
+template <class T>
+static int ualloc(UNet& U, T** p, size_t n) {
+    CK(cudaMalloc(p, sizeof(T) * (n ? n : 1)));
+    U.owned.push_back(*p);
+    CK(cudaMemsetAsync(*p, 0, sizeof(T) * (n ? n : 1), U.st));
+    return 0;
+}
+
+// split of a weight-gradient GEMM over pixels: about two CTAs per SM in total
+static void wsplit(int Mw, int P, int* per, int* ns) {
+    const int gx = (Mw + 127) / 128, chunks = (P + 63) / 64;
+    const int n0 = std::max(1, std::min(chunks, 304 / gx));
+    *per = (chunks + n0 - 1) / n0;
+    *ns = (chunks + *per - 1) / *per;
+}
+
+static int unet_build(UNet& U, int H, int W, int maxB, uint64_t seed) {
+    U.H = H;
+    U.W = W;
+    U.maxB = maxB;
+    // tensor ids: 0 e1a 1 e1 2 e2a 3 e2 4 e3a 5 e3 6 b1 7 b2 8 d3a 9 d3 10 d2a 11 d2 12 d1a 13 d1
+    const int spec[14][7] = {{-1, -1, 0, 4, 32, 0, 0},   {0, -1, 0, 32, 32, 0, 1},   {1, -1, 1, 32, 64, 1, 2},
+                             {2, -1, 0, 64, 64, 1, 3},   {3, -1, 1, 64, 128, 2, 4},  {4, -1, 0, 128, 128, 2, 5},
+                             {5, -1, 1, 128, 256, 3, 6}, {6, -1, 0, 256, 256, 3, 7}, {7, 5, 2, 384, 128, 2, 8},
+                             {8, -1, 0, 128, 128, 2, 9}, {9, 3, 2, 192, 64, 1, 10},  {10, -1, 0, 64, 64, 1, 11},
+                             {11, 1, 2, 96, 32, 0, 12},  {12, -1, 0, 32, 32, 0, 13}};
+    size_t off = 0;
+    for (auto& r : spec) {
+        UConv c{r[0], r[1], r[2], r[3], r[4], r[5], r[6], 0, 0};
+        c.woff = off;
+        off += (size_t)c.cout * 9 * c.cin;
+        c.boff = off;
+        off += c.cout;
+        U.L.push_back(c);
+        U.tch[c.out] = c.cout;
+        U.tlev[c.out] = c.level;
+    }
+    U.out_w = off;
+    off += 32;
+    U.out_b = off;
+    off += 1;
+    U.nparams = off;
+    int rc;
+    if ((rc = ualloc(U, &U.w32, off)) || (rc = ualloc(U, &U.m, off)) || (rc = ualloc(U, &U.v, off)) ||
+        (rc = ualloc(U, &U.g, off)) || (rc = ualloc(U, &U.wbf, off)) || (rc = ualloc(U, &U.derr, 1)))
+        return rc;
+    // He-normal initialisation from a portable generator; biases zero
+    std::vector<float> h(off, 0.f);
+    uint64_t sd = seed;
+    for (auto& c : U.L) {
+        const double sdev = std::sqrt(2.0 / (9.0 * c.cin));
+        for (size_t q = 0; q < (size_t)c.cout * 9 * c.cin; q++) h[c.woff + q] = (float)(sdev * normal01(sd));
+    }
+    for (int q = 0; q < 32; q++) h[U.out_w + q] = (float)(std::sqrt(1.0 / 32.0) * normal01(sd));
+    CK(cudaMemcpyAsync(U.w32, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice, U.st));
+    k_to_bf16<<<nblk(off, 256), 256, 0, U.st>>>(U.wbf, U.w32, off);
+    CK(cudaGetLastError());
+    // activations and gradients for maxB samples
+    const size_t P0 = (size_t)maxB * H * W;
+    for (int t = 0; t < 14; t++) {
+        const size_t n = (P0 >> (2 * U.tlev[t])) * U.tch[t];
+        if ((rc = ualloc(U, &U.act[t], n)) || (rc = ualloc(U, &U.grad[t], n))) return rc;
+    }
+    if ((rc = ualloc(U, &U.x0, P0 * 4)) || (rc = ualloc(U, &U.xin, P0 * 4)) || (rc = ualloc(U, &U.y, P0)) ||
+        (rc = ualloc(U, &U.dy, P0)) || (rc = ualloc(U, &U.tgt, P0)) || (rc = ualloc(U, &U.lpart, P0 / 256 + 1)))
+        return rc;
+    // workspaces: the largest view gradient, and the largest split-K partial buffer
+    size_t dxg = 0, part = 0;
+    for (auto& c : U.L) {
+        const size_t P = P0 >> (2 * c.level);
+        dxg = std::max(dxg, P * (size_t)c.cin);
+        int per, ns;
+        wsplit(9 * c.cin, (int)P, &per, &ns);
+        part = std::max(part, (size_t)ns * 9 * c.cin * c.cout);
+    }
+    U.dxg_cap = dxg;
+    U.part_cap = part;
+    if ((rc = ualloc(U, &U.dXg, dxg)) || (rc = ualloc(U, &U.part, part))) return rc;
+    const int smax = (int)tc::smem_bytes(256);
+    CK(cudaFuncSetAttribute(tc::k_tc_gemm<ConvFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    CK(cudaFuncSetAttribute(tc::k_tc_gemm<ConvBwdData>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    CK(cudaFuncSetAttribute(tc::k_tc_gemm<ConvBwdW>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    return 0;
+}
+
+static int ntile_for(int n) {
+    const int tiles = (n + 255) / 256;
+    const int t = (n + tiles - 1) / tiles;
+    return (t + 15) / 16 * 16;
+}
+
+template <class Prob>
+static int run_gemm(UNet& U, Prob p, int nsplit) {
+    dim3 grid((p.M + tc::kTileM - 1) / tc::kTileM, (p.N + p.Ntile - 1) / p.Ntile, nsplit);
+    tc::k_tc_gemm<Prob><<<grid, tc::kThreads, tc::smem_bytes(p.Ntile), U.st>>>(p, U.derr);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static InView view_of(const UNet& U, const UConv& c, int B) {
+    InView v{};
+    v.B = B;
+    v.H = U.H >> c.level;
+    v.W = U.W >> c.level;
+    v.mode = c.mode;
+    if (c.src0 < 0) {
+        v.t0 = U.x0;
+        v.C0 = 4;
+    } else {
+        v.t0 = U.act[c.src0];
+        v.C0 = U.tch[c.src0];
+    }
+    if (c.mode == 2) {
+        v.t1 = U.act[c.src1];
+        v.C1 = U.tch[c.src1];
+    }
+    return v;
+}
+
+// network input already in U.xin (device, NCHW FP32); output in U.y ([B][H][W] FP32)
+static int unet_forward(UNet& U, int B) {
+    const size_t P0 = (size_t)B * U.H * U.W;
+    k_input_nhwc<<<nblk(P0 * 4, 256), 256, 0, U.st>>>(U.x0, U.xin, B, 4, U.H, U.W);
+    CK(cudaGetLastError());
+    for (auto& c : U.L) {
+        const InView v = view_of(U, c, B);
+        const int P = B * v.H * v.W;
+        ConvFwd f{P, c.cout, 9 * c.cin, ntile_for(c.cout), 0, v, U.wbf + c.woff, U.w32 + c.boff, U.act[c.out], 1};
+        if (int rc = run_gemm(U, f, 1)) return rc;
+    }
+    k_out_fwd<<<nblk(P0, 256), 256, 0, U.st>>>(U.y, U.act[13], U.w32 + U.out_w, U.w32 + U.out_b, (int)P0, 32);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int gemm_error(UNet& U) {
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, U.derr, sizeof(int), cudaMemcpyDeviceToHost, U.st));
+    CK(cudaStreamSynchronize(U.st));
+    if (herr) return fail(PT_ERR_ITER_CAP, "U-Net tensor-core GEMM: mbarrier wait gave up");
+    return 0;
+}
+
+// gradients of the MSE loss against U.tgt into U.g; loss on the host
+static int unet_backward(UNet& U, int B, float* loss) {
+    const int P0 = B * U.H * U.W;
+    const int nb = (int)nblk(P0, 256);
+    k_mse<<<nb, 256, 0, U.st>>>(U.dy, U.lpart, U.y, U.tgt, P0);
+    for (int t = 0; t < 14; t++)
+        CK(cudaMemsetAsync(U.grad[t], 0, sizeof(float) * ((size_t)P0 >> (2 * U.tlev[t])) * U.tch[t], U.st));
+    k_out_bwd_data<<<nblk((size_t)P0 * 32, 256), 256, 0, U.st>>>(U.grad[13], U.dy, U.w32 + U.out_w, P0, 32);
+    k_out_bwd_w<<<33, 256, 0, U.st>>>(U.g + U.out_w, U.g + U.out_b, U.dy, U.act[13], P0, 32);
+    CK(cudaGetLastError());
+    for (int li = (int)U.L.size() - 1; li >= 0; li--) {
+        const UConv& c = U.L[li];
+        const InView v = view_of(U, c, B);
+        const int P = B * v.H * v.W;
+        const float* dY = U.grad[c.out];
+        const uint16_t* Y = U.act[c.out];
+        // weights: split over pixels, then a fixed-order reduction of the splits
+        const int Mw = 9 * c.cin;
+        int per, ns;
+        wsplit(Mw, P, &per, &ns);
+        if ((size_t)ns * Mw * c.cout > U.part_cap) return fail(PT_ERR_STATE, "U-Net: split workspace too small");
+        ConvBwdW bw{Mw, c.cout, P, ntile_for(c.cout), per, v, dY, Y, U.part};
+        if (int rc = run_gemm(U, bw, ns)) return rc;
+        k_wgrad_reduce<<<nblk((size_t)Mw * c.cout, 256), 256, 0, U.st>>>(U.g + c.woff, U.part, ns, Mw, c.cout);
+        k_bias_grad<<<c.cout, 256, 0, U.st>>>(U.g + c.boff, dY, Y, P, c.cout);
+        CK(cudaGetLastError());
+        if (c.src0 < 0) continue;  // the network input needs no gradient
+        if ((size_t)P * c.cin > U.dxg_cap) return fail(PT_ERR_STATE, "U-Net: view-gradient workspace too small");
+        ConvBwdData bd{P, c.cin, 9 * c.cout, ntile_for(c.cin), 0, v.H, v.W, c.cout, dY, Y, U.wbf + c.woff, U.dXg};
+        if (int rc = run_gemm(U, bd, 1)) return rc;
+        if (c.mode == 0) {
+            const size_t n = (size_t)P * c.cin;
+            k_adj_plain<<<nblk(n, 256), 256, 0, U.st>>>(U.grad[c.src0], U.dXg, n);
+        } else if (c.mode == 1) {
+            const size_t n = (size_t)B * 4 * v.H * v.W * c.cin;
+            k_adj_pool<<<nblk(n, 256), 256, 0, U.st>>>(U.grad[c.src0], U.dXg, B, v.H, v.W, c.cin);
+        } else {
+            const size_t n = (size_t)B * (v.H / 2) * (v.W / 2) * v.C0 + (size_t)P * v.C1;
+            k_adj_upcat<<<nblk(n, 256), 256, 0, U.st>>>(U.grad[c.src0], U.grad[c.src1], U.dXg, B, v.H, v.W, v.C0, v.C1);
+        }
+        CK(cudaGetLastError());
+    }
+    std::vector<float> lp(nb);
+    CK(cudaMemcpyAsync(lp.data(), U.lpart, sizeof(float) * nb, cudaMemcpyDeviceToHost, U.st));
+    if (int rc = gemm_error(U)) return rc;
+    double sum = 0.0;
+    for (float a : lp) sum += a;
+    if (loss) *loss = (float)(sum / P0);
+    return 0;
+}
+
+static int unet_adam(UNet& U, float lr) {
+    U.step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)U.step), c2 = 1.f - std::pow(b2, (float)U.step);
+    k_adam<<<nblk(U.nparams, 256), 256, 0, U.st>>>(U.w32, U.m, U.v, U.wbf, U.g, U.nparams, lr, b1, b2, 1e-8f, c1, c2);
+    CK(cudaGetLastError());
+    return 0;
+}
 }  // namespace pt
 
 using namespace pt;
 
-extern "C" int pt_tc_gemm_check(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K) {
+extern "C" {
+
+int pt_tc_gemm_check(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K) {
     if (!A || !B || !C) return fail(PT_ERR_ARG, "null pointer");
     if (M <= 0 || K <= 0 || N < 16 || N > 256 || N % 16) return fail(PT_ERR_ARG, "pt_tc_gemm_check: N must be 16..256, a multiple of 16");
     uint16_t *dA = nullptr, *dB = nullptr;
@@ -52,8 +566,8 @@ extern "C" int pt_tc_gemm_check(const uint16_t* A, const uint16_t* B, float* C, 
         cleanup();
         return rc;
     }
-    GemmProb p{M, N, K, dA, dB, dC};
-    tc::k_tc_gemm<GemmProb><<<(M + tc::kTileM - 1) / tc::kTileM, tc::kThreads, smem>>>(p, derr);
+    GemmProb p{M, N, K, N, 0, dA, dB, dC};
+    tc::k_tc_gemm<GemmProb><<<dim3((M + tc::kTileM - 1) / tc::kTileM, 1, 1), tc::kThreads, smem>>>(p, derr);
     rc = cuda_check(cudaGetLastError(), "k_tc_gemm launch");
     if (!rc) rc = cuda_check(cudaDeviceSynchronize(), "k_tc_gemm");
     if (!rc) rc = cuda_check(cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost), "gemm check");
@@ -62,3 +576,140 @@ extern "C" int pt_tc_gemm_check(const uint16_t* A, const uint16_t* B, float* C, 
     if (!rc && herr) rc = fail(PT_ERR_ITER_CAP, "tensor-core GEMM: mbarrier wait gave up");
     return rc;
 }
+
+struct pt_unet {
+    UNet u;
+};
+
+static void unet_release(pt_unet* n) {
+    for (void* p : n->u.owned) cudaFree(p);
+    if (n->u.st) cudaStreamDestroy(n->u.st);
+    delete n;
+}
+
+int pt_unet_create(int nz, int nx, int max_batch, uint64_t seed, pt_unet** out) {
+    if (!out) return fail(PT_ERR_ARG, "null pointer");
+    *out = nullptr;
+    if (nz < 8 || nx < 8 || nz % 8 || nx % 8 || max_batch < 1)
+        return fail(PT_ERR_ARG, "pt_unet_create: nz and nx must be positive multiples of 8, max_batch >= 1");
+    pt_unet* n = new pt_unet();
+    int rc = cuda_check(cudaStreamCreateWithFlags(&n->u.st, cudaStreamNonBlocking), "U-Net stream");
+    if (!rc) rc = unet_build(n->u, nz, nx, max_batch, seed);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(n->u.st), "U-Net init");
+    if (rc) {
+        std::string msg = g_err;
+        unet_release(n);
+        g_err = msg;
+        return rc;
+    }
+    *out = n;
+    return 0;
+}
+
+int pt_unet_destroy(pt_unet* net) {
+    if (net) unet_release(net);
+    return 0;
+}
+
+int pt_unet_num_params(pt_unet* net, int64_t* n) {
+    if (!net || !n) return fail(PT_ERR_ARG, "null pointer");
+    *n = (int64_t)net->u.nparams;
+    return 0;
+}
+
+int pt_unet_get_params(pt_unet* net, float* host) {
+    if (!net || !host) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    CK(cudaMemcpyAsync(host, U.w32, sizeof(float) * U.nparams, cudaMemcpyDeviceToHost, U.st));
+    CK(cudaStreamSynchronize(U.st));
+    return 0;
+}
+
+int pt_unet_set_params(pt_unet* net, const float* host) {
+    if (!net || !host) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    CK(cudaMemcpyAsync(U.w32, host, sizeof(float) * U.nparams, cudaMemcpyHostToDevice, U.st));
+    k_to_bf16<<<nblk(U.nparams, 256), 256, 0, U.st>>>(U.wbf, U.w32, U.nparams);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(U.st));
+    return 0;
+}
+
+static int unet_input(UNet& U, const float* x, int batch) {
+    if (batch < 1 || batch > U.maxB) return fail(PT_ERR_ARG, "U-Net: batch outside 1..max_batch");
+    CK(cudaMemcpyAsync(U.xin, x, sizeof(float) * (size_t)batch * 4 * U.H * U.W, cudaMemcpyHostToDevice, U.st));
+    return 0;
+}
+
+int pt_unet_forward(pt_unet* net, const float* x, int batch, float* y) {
+    if (!net || !x || !y) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    int rc;
+    if ((rc = unet_input(U, x, batch)) || (rc = unet_forward(U, batch))) return rc;
+    CK(cudaMemcpyAsync(y, U.y, sizeof(float) * (size_t)batch * U.H * U.W, cudaMemcpyDeviceToHost, U.st));
+    return gemm_error(U);
+}
+
+int pt_unet_gradients(pt_unet* net, const float* x, const float* target, int batch, float* grads, float* loss) {
+    if (!net || !x || !target || !grads) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    int rc;
+    if ((rc = unet_input(U, x, batch)) || (rc = unet_forward(U, batch))) return rc;
+    CK(cudaMemcpyAsync(U.tgt, target, sizeof(float) * (size_t)batch * U.H * U.W, cudaMemcpyHostToDevice, U.st));
+    if ((rc = unet_backward(U, batch, loss))) return rc;
+    CK(cudaMemcpyAsync(grads, U.g, sizeof(float) * U.nparams, cudaMemcpyDeviceToHost, U.st));
+    CK(cudaStreamSynchronize(U.st));
+    return 0;
+}
+
+int pt_unet_train_step(pt_unet* net, const float* x, const float* target, int batch, float lr, float* loss) {
+    if (!net || !x || !target) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    int rc;
+    if ((rc = unet_input(U, x, batch)) || (rc = unet_forward(U, batch))) return rc;
+    CK(cudaMemcpyAsync(U.tgt, target, sizeof(float) * (size_t)batch * U.H * U.W, cudaMemcpyHostToDevice, U.st));
+    if ((rc = unet_backward(U, batch, loss)) || (rc = unet_adam(U, lr))) return rc;
+    CK(cudaStreamSynchronize(U.st));
+    return 0;
+}
+
+int pt_unet_save(pt_unet* net, const char* path) {
+    if (!net || !path) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    std::vector<float> h(U.nparams);
+    if (int rc = pt_unet_get_params(net, h.data())) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(PT_ERR_ARG, std::string("cannot write ") + path);
+    const int32_t dims[2] = {U.H, U.W};
+    const int64_t n = (int64_t)U.nparams;
+    bool ok = std::fwrite("PTUNET01", 1, 8, f) == 8 && std::fwrite(dims, 4, 2, f) == 2 && std::fwrite(&n, 8, 1, f) == 1 &&
+              std::fwrite(h.data(), 4, h.size(), f) == h.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? 0 : fail(PT_ERR_ARG, std::string("short write to ") + path);
+}
+
+int pt_unet_load(const char* path, int nz, int nx, int max_batch, pt_unet** out) {
+    if (!path || !out) return fail(PT_ERR_ARG, "null pointer");
+    *out = nullptr;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(PT_ERR_ARG, std::string("cannot read ") + path);
+    char magic[8];
+    int32_t dims[2];
+    int64_t n = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "PTUNET01", 8) == 0 && std::fread(dims, 4, 2, f) == 2 &&
+              std::fread(&n, 8, 1, f) == 1 && n > 0 && n < ((int64_t)1 << 30);
+    std::vector<float> h(ok ? (size_t)n : 0);
+    ok = ok && std::fread(h.data(), 4, h.size(), f) == h.size();
+    std::fclose(f);
+    if (!ok) return fail(PT_ERR_ARG, std::string("not a U-Net weight file: ") + path);
+    int rc = pt_unet_create(nz, nx, max_batch, 0, out);
+    if (rc) return rc;
+    if ((int64_t)(*out)->u.nparams != n) {
+        pt_unet_destroy(*out);
+        *out = nullptr;
+        return fail(PT_ERR_ARG, "U-Net weight file has a different parameter count");
+    }
+    return pt_unet_set_params(*out, h.data());
+}
+
+}  // extern "C"

@@ -34,3 +34,122 @@ def test_tc_gemm_matches_fp64_reference(M, N, K):
     ref = bf16_to_f32(A).astype(np.float64) @ bf16_to_f32(B).astype(np.float64).T
     # products of BF16 values are exact in FP32; the FP32 accumulation over K terms bounds the error
     assert np.max(np.abs(C - ref)) <= 1e-6 * K * np.max(np.abs(ref))
+
+
+class _Net:
+    """ctypes handle of a pt_unet."""
+
+    def __init__(self, nz, nx, batch, seed):
+        self.L = eng.load_library()
+        L = self.L
+        L.pt_unet_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                     ctypes.POINTER(ctypes.c_void_p)]
+        for f in ("pt_unet_destroy",):
+            getattr(L, f).argtypes = [ctypes.c_void_p]
+        L.pt_unet_num_params.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+        L.pt_unet_get_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.pt_unet_set_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.pt_unet_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.pt_unet_gradients.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]
+        L.pt_unet_train_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                         ctypes.POINTER(ctypes.c_float)]
+        L.pt_unet_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.pt_unet_load.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_void_p)]
+        self.h = ctypes.c_void_p()
+        self.nz, self.nx = nz, nx
+        self._ok(L.pt_unet_create(nz, nx, batch, seed, ctypes.byref(self.h)))
+
+    def _ok(self, rc):
+        assert rc == 0, self.L.pt_last_error()
+
+    def params(self):
+        n = ctypes.c_int64()
+        self._ok(self.L.pt_unet_num_params(self.h, ctypes.byref(n)))
+        p = np.zeros(n.value, dtype=np.float32)
+        self._ok(self.L.pt_unet_get_params(self.h, p.ctypes.data))
+        return p
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros((x.shape[0], self.nz, self.nx), dtype=np.float32)
+        self._ok(self.L.pt_unet_forward(self.h, x.ctypes.data, x.shape[0], y.ctypes.data))
+        return y
+
+    def gradients(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.zeros(self.params().size, dtype=np.float32)
+        loss = ctypes.c_float()
+        self._ok(self.L.pt_unet_gradients(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], g.ctypes.data,
+                                          ctypes.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, x, t, lr):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = ctypes.c_float()
+        self._ok(self.L.pt_unet_train_step(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], lr, ctypes.byref(loss)))
+        return loss.value
+
+    def close(self):
+        self.L.pt_unet_destroy(self.h)
+
+
+def _smooth_batch(rng, B, nz, nx):
+    z, x = np.meshgrid(np.linspace(0, 1, nz), np.linspace(0, 2, nx), indexing="ij")
+    xs = np.zeros((B, 4, nz, nx), dtype=np.float32)
+    for b in range(B):
+        for c in range(4):
+            a, kx, kz = rng.uniform(0.5, 1.5), rng.integers(1, 4), rng.integers(1, 4)
+            xs[b, c] = a * np.sin(kx * np.pi * x / 2 + rng.uniform(0, 6)) * np.sin(kz * np.pi * z + rng.uniform(0, 6))
+    t = (0.5 * xs[:, 0] - 0.3 * xs[:, 3]).astype(np.float32)
+    return xs, t
+
+
+def test_unet_forward_and_gradients_match_cpu_oracle():
+    """GPU U-Net (tcgen05 implicit-GEMM convolutions) against the numpy oracle with the same BF16
+    rounding points: output, loss and every parameter gradient."""
+    import oracle.unet_ref as ur
+
+    nz, nx, B = 16, 32, 2
+    net = _Net(nz, nx, B, 11)
+    rng = np.random.default_rng(3)
+    x, t = _smooth_batch(rng, B, nz, nx)
+    p = net.params().astype(np.float64)
+    y_gpu = net.forward(x)
+    y_ref, _ = ur.forward(p, x)
+    assert np.max(np.abs(y_gpu - y_ref)) <= 1e-2 * np.max(np.abs(y_ref))
+    loss_gpu, g_gpu = net.gradients(x, t)
+    loss_ref, g_ref = ur.gradients(p, x, t)
+    assert abs(loss_gpu - loss_ref) <= 1e-2 * loss_ref
+    offs, out_w, out_b, total = ur.layout()
+    cos = float(g_gpu @ g_ref / (np.linalg.norm(g_gpu) * np.linalg.norm(g_ref)))
+    assert cos > 0.999
+    for li, (wo, bo) in enumerate(offs):
+        for a, b in ((wo, bo), (bo, bo + ur.SPEC[li][4])):
+            err = np.linalg.norm(g_gpu[a:b] - g_ref[a:b]) / max(np.linalg.norm(g_ref[a:b]), 1e-30)
+            assert err < 3e-2, (li, a == wo, err)
+    net.close()
+
+
+def test_unet_adam_reduces_loss_and_weights_round_trip(tmp_path):
+    nz, nx, B = 32, 64, 4
+    net = _Net(nz, nx, B, 7)
+    rng = np.random.default_rng(9)
+    x, t = _smooth_batch(rng, B, nz, nx)
+    first = net.train_step(x, t, 1e-3)
+    for _ in range(80):
+        last = net.train_step(x, t, 1e-3)
+    assert last < 0.3 * first
+    path = str(tmp_path / "w.bin")
+    assert net.L.pt_unet_save(net.h, path.encode()) == 0
+    h2 = ctypes.c_void_p()
+    assert net.L.pt_unet_load(path.encode(), nz, nx, B, ctypes.byref(h2)) == 0
+    y1 = net.forward(x)
+    y2 = np.zeros_like(y1)
+    assert net.L.pt_unet_forward(h2, np.ascontiguousarray(x).ctypes.data, B, y2.ctypes.data) == 0
+    assert np.array_equal(y1, y2)
+    net.L.pt_unet_destroy(h2)
+    net.close()
