@@ -41,6 +41,18 @@ int pt_unet_train_step(pt_unet* net, const float* x, const float* target, int ba
 int pt_unet_save(pt_unet* net, const char* path);
 int pt_unet_load(const char* path, int nz, int nx, int max_batch, pt_unet** out);
 
+/* Training pair of the current engine state (after pt_solve_psi): the network's input planes
+ * x4 [4][nz][nx] (T, C, log10(eta)/5, RHS/max|RHS|) and the target psi/max|psi| [nz][nx], on
+ * nodes i < nx, k < nz.  The FP64 solver's own output, written out for training. */
+int pt_training_pair(float* x4, float* psi);
+
+/* Outcome of the last solve's learned guess (pt_set_guess_mode(PT_GUESS_UNET, path)).  The
+ * network's psi shape is scaled by the least-squares factor fitted on the coarsest multigrid level;
+ * the previous psi and the scaled guess each get the level-1 smoothing of a cycle and the one with
+ * the lower residual starts the solve.  used = 1 when the network's guess won; resid_prev and
+ * resid_net are the two mean|r| / mean|RHS| after that smoothing. */
+int pt_unet_guess_info(int* used, double* resid_prev, double* resid_net);
+
 /* Tensor-core GEMM self-check: C (M x N, FP32) = A (M x K) * B (N x K)^T with BF16 operands
  * (uint16 bit patterns); N a multiple of 16 in [16, 256]. */
 int pt_tc_gemm_check(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K);

@@ -128,6 +128,7 @@ static int engine_alloc(Engine& E) {
 }
 
 static void engine_free(Engine& E) {
+    unet_engine_release(E);
     double** fine[] = {&E.T, &E.Tratio, &E.Tvis, &E.Tbuoy, &E.Cnew, &E.Cvis, &E.Cbuoy, &E.SF, &E.u, &E.w,
                        &E.cond, &E.cond_r, &E.cond_s, &E.tsa, &E.Text, &E.T0, &E.C0, &E.scratch, &E.psi_keep,
                        &E.red, &E.dscal, &E.cpart, &E.rtr, &E.str, &E.Ttr, &E.Ctr, &E.rtr0, &E.str0,
@@ -529,8 +530,7 @@ int pt_set_guess_mode(int mode, const char* weights_path) {
     if (mode != PT_GUESS_PREVIOUS && mode != PT_GUESS_ZERO && mode != PT_GUESS_UNET)
         return fail(PT_ERR_ARG, "unknown guess mode");
     if (mode == PT_GUESS_UNET) {
-        (void)weights_path;
-        return fail(PT_ERR_CONFIG, "U-Net guess is not available in this build");
+        if (int rc = unet_engine_load(*g_eng, weights_path)) return rc;
     }
     g_eng->cfg.guess_mode = mode;
     return 0;

@@ -99,6 +99,11 @@ struct Engine {
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
+    void* unet = nullptr;        // pt_unet* of the learned guess (PT_GUESS_UNET)
+    void* unet_core = nullptr;   // its network (pt::UNet*)
+    float* pair_buf = nullptr;   // staging of pt_training_pair (5 planes of nz x nx)
+    int unet_used = 0;           // last solve started from the network's guess
+    double unet_r_prev = 0.0, unet_r_net = 0.0;
     bool coarse_ready = false;  // coarse factorisation valid for coarse_time (mixed precision)
     bool levels_reused = false; // this solve reuses levels 2..grids (mixed precision)
     double coarse_time = -1.0;
@@ -194,6 +199,12 @@ int load_conductivity(Engine& E);                    // energy.f90:59-86
 int load_tracer_space(Engine& E);                    // energy.f90:154-179 (+extendT 595-630)
 int noalloc_scratch_setup();  // static scratch address of the current device (before any capture)
 int project_noalloc(Engine& E, const double* T0f, int smooth);
+// learned initial psi (pt_unet.cu): after mg_setup_solve; fallback check after the first cycle
+int unet_guess(Engine& E);
+int unet_check_fallback(Engine& E, double ratio);
+int coarse_scale_fit(Engine& E, double* alpha);   // pt_mg.cu
+int unet_engine_release(Engine& E);
+int unet_engine_load(Engine& E, const char* path);  // PT_GUESS_UNET weights
 int tables_to_f32(Engine& E, int which, const double* f);  // FP32 copies for the mixed RK stage
 int compute_derivatives(Engine& E, const double* f, int which);  // composition.f90:1457-1478
 int compute_velocities(Engine& E);                   // momentum.f90:655-710

@@ -882,6 +882,7 @@ int multigrid(Engine& E, pt_solve_info* info) {
     {
         PhaseTimer ts(E, PH_SETUP);
         if ((rc = mg_setup_solve(E))) return rc;
+        if (E.cfg.guess_mode == PT_GUESS_UNET && (rc = unet_guess(E))) return rc;
     }
     const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int q = 1;
@@ -899,6 +900,14 @@ int multigrid(Engine& E, pt_solve_info* info) {
         if (mag1 > 1.0e10 * E.res_ref[1])
             return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
         if (trace_on()) fprintf(stderr, "[ptgpu] cycle %d residual ratio %.4e\n", q, mag1 / E.res_ref[1]);
+        if (q == 2) {  // one full cycle from a learned guess: keep it or restart from the previous psi
+            const int fb = unet_check_fallback(E, mag1 / E.res_ref[1]);
+            if (fb < 0) return fail(PT_ERR_CUDA, "learned-guess fallback copy");
+            if (fb) {
+                q++;  // the cycle spent on the dropped guess counts
+                continue;
+            }
+        }
         if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
         {
             PhaseTimer tp(E, PH_CYCLE_COARSE);
@@ -958,6 +967,72 @@ int mg_alloc(Engine& E) {
         CK(cudaFuncSetAttribute(k_band_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(double) * (size_t)E.ngc * C)));
     }
+    return 0;
+}
+
+// ------------------------------------------------------------------ learned-guess support
+// level-1 values at the nodes of level L (every s-th node), boundary included
+__global__ void k_inject(double* c, const double* f, Geo gc, Geo gf, int nxc, int nzc, int s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    if (i > nxc || k > nzc) return;
+    c[gc.at(i, k)] = f[gf.at(i * s, k * s)];
+}
+// per interior row of a level: sum RHS*(RHS - r) and (RHS - r)^2  (r = RHS - A g, so RHS - r = A g)
+__global__ void k_fit_rows(const double* rhs, const double* r, Geo g, int nx, double* part) {
+    __shared__ double s1[128], s2[128];
+    const int k = blockIdx.x + 1;
+    double a = 0.0, b = 0.0;
+    for (int i = 1 + threadIdx.x; i <= nx - 1; i += blockDim.x) {
+        const size_t o = g.at(i, k);
+        const double ag = rhs[o] - r[o];
+        a += rhs[o] * ag;
+        b += ag * ag;
+    }
+    s1[threadIdx.x] = a;
+    s2[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s1[threadIdx.x] += s1[threadIdx.x + o];
+            s2[threadIdx.x] += s2[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = s1[0];
+        part[2 * blockIdx.x + 1] = s2[0];
+    }
+}
+
+// Scale of a psi shape held in err[1], fitted on the coarsest level where the shape's
+// grid-scale noise is averaged away: RHS restricted by full weighting (as at a descent), the shape
+// injected, alpha = <RHS_L, A_L g> / <A_L g, A_L g> with the level-L operator.  Uses the level
+// arrays of levels 2..L, which the cycles overwrite anyway.
+int coarse_scale_fit(Engine& E, double* alpha) {
+    const int L = E.grids;
+    for (int l = 2; l <= L; l++) {
+        const Geo& g = E.gl[l];
+        PT_COUNT(), k_restrict<<<dim3(nblk(g.nx - 1, 128), g.nz - 1), 128, 0, E.st>>>(E.RHS[l], E.RHS[l - 1], g,
+                                                                                       E.gl[l - 1], g.nx, g.nz);
+    }
+    const Geo& gc = E.gl[L];
+    PT_COUNT(), k_inject<<<dim3(nblk(gc.nx + 1, 128), gc.nz + 1), 128, 0, E.st>>>(E.err[L], E.err[1], gc, E.gl[1], gc.nx,
+                                                                                   gc.nz, 1 << (L - 1));
+    CKL("k_inject");
+    if (int rc = enforce_bcs_stream(E, L, E.err[L])) return rc;
+    PT_COUNT(), k_residual<<<dim3(nblk(gc.nx - 1, 128), gc.nz - 1), 128, 0, E.st>>>(E.res[L], E.err[L], stream_op(E, L),
+                                                                                     gc, L, E.cfg.ivis);
+    PT_COUNT(), k_fit_rows<<<gc.nz - 1, 128, 0, E.st>>>(E.RHS[L], E.res[L], gc, gc.nx, E.red);
+    CKL("coarse_scale_fit");
+    std::vector<double> part(2 * (size_t)(gc.nz - 1));
+    CK(cudaMemcpyAsync(part.data(), E.red, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    double a = 0.0, b = 0.0;
+    for (size_t k = 0; k + 1 < part.size(); k += 2) {
+        a += part[k];
+        b += part[k + 1];
+    }
+    *alpha = b > 0.0 ? a / b : 0.0;
     return 0;
 }
 

@@ -519,6 +519,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
     {
         PhaseTimer ts(E, PH_SETUP);
         if ((rc = mg_setup_solve(E))) return rc;
+        if (E.cfg.guess_mode == PT_GUESS_UNET && (rc = unet_guess(E))) return rc;
         for (int l = 1; l < (E.levels_reused ? 2 : E.grids); l++) {
             size_t n = E.gl[l].elems();
             float* const* f = E.fcoef[l];
@@ -542,6 +543,14 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
         if (mag1 > 1.0e10 * E.res_ref[1])
             return fail(PT_ERR_MG_DIVERGED, "mixed-precision solve: abnormally high residual");
         if (trace_on()) fprintf(stderr, "[ptgpu] mixed cycle %d residual ratio %.4e\n", cycles, mag1 / E.res_ref[1]);
+        if (cycles == 1) {  // one full cycle from a learned guess: keep it or restart from the previous psi
+            const int fb = unet_check_fallback(E, mag1 / E.res_ref[1]);
+            if (fb < 0) return fail(PT_ERR_CUDA, "learned-guess fallback copy");
+            if (fb) {
+                cycles++;
+                continue;
+            }
+        }
         if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
         if (cycles >= E.cfg.max_cycles)
             return fail(PT_ERR_MG_MAX_CYCLES, "mixed-precision solve: too many cycles");

@@ -534,6 +534,107 @@ static int unet_adam(UNet& U, float lr) {
     CK(cudaGetLastError());
     return 0;
 }
+
+// ============================================================================ engine side
+// features of node (i, k), i < nx, k < nz, as the network's input planes [4][nz][nx]:
+// T, C, log10(eta)/5, RHS/max|RHS| (0 on the boundary rows), and psi/max|psi| (training target)
+__global__ void k_absmax_grid(const double* f, Geo g, int nx, int nz, unsigned long long* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    double a = 0.0;
+    if (i <= nx && k <= nz) a = fabs(f[g.at(i, k)]);
+    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if ((threadIdx.x & 31) == 0 && a > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(a));
+}
+__global__ void k_features(float* x4, float* psi, const double* Tb, const double* Cb, const double* vis,
+                           const double* rhs, const double* sf, Geo g, int nx, int nz, const unsigned long long* scal,
+                           int comp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    if (i >= nx || k >= nz) return;
+    const size_t o = g.at(i, k), plane = (size_t)nx * nz, q = (size_t)k * nx + i;
+    const double rmax = __longlong_as_double((long long)scal[0]), smax = __longlong_as_double((long long)scal[1]);
+    x4[q] = (float)Tb[o];
+    x4[plane + q] = comp ? (float)Cb[o] : 0.f;
+    x4[2 * plane + q] = (float)(log10(vis[o]) * 0.2);
+    x4[3 * plane + q] = (i > 0 && k > 0 && rmax > 0.0) ? (float)(rhs[o] / rmax) : 0.f;
+    if (psi) psi[q] = smax > 0.0 ? (float)(sf[o] / smax) : 0.f;
+}
+// network output (psi shape, [nz][nx]) into the level-1 iterate: interior nodes, boundary 0
+__global__ void k_guess_scatter(double* x, const float* y, Geo g, int nx, int nz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    if (i > nx || k > nz) return;
+    x[g.at(i, k)] = (i > 0 && k > 0 && i < nx && k < nz) ? (double)y[(size_t)k * nx + i] : 0.0;
+}
+__global__ void k_scale_all(double* x, double a, size_t n) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) x[q] *= a;
+}
+
+static int engine_features(Engine& E, float* x4, float* psi) {
+    const Geo& g = E.g1;
+    const int nx = E.cfg.nx, nz = E.cfg.nz;
+    unsigned long long* scal = reinterpret_cast<unsigned long long*>(E.dscal);
+    CK(cudaMemsetAsync(scal, 0, 16, E.st));
+    dim3 gm(nblk(nx + 1, 128), nz + 1);
+    k_absmax_grid<<<gm, 128, 0, E.st>>>(E.RHS[1], g, nx, nz, scal);
+    if (psi) k_absmax_grid<<<gm, 128, 0, E.st>>>(E.SF, g, nx, nz, scal + 1);
+    k_features<<<dim3(nblk(nx, 128), nz), 128, 0, E.st>>>(x4, psi, E.Tbuoy, E.Cbuoy, E.vis[1], E.RHS[1], E.SF, g, nx, nz,
+                                                           scal, E.cfg.comp);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int mean_resid(Engine& E, double* ratio) {
+    if (int rc = residual_level1(E)) return rc;
+    CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    *ratio = E.hscal[0] / (double)(E.gl[1].nx - 2) / (double)(E.gl[1].nz - 2) / E.res_ref[1];
+    return 0;
+}
+
+// Learned initial guess.  The network's psi shape g (BF16 output, grid-scale noise of order 1e-3)
+// is scaled by the least-squares factor fitted on the coarsest level (coarse_scale_fit) and
+// starts the solve.  The residual of the previous psi (the reference's warm start) is kept: if the
+// residual after the first full cycle is not below it, the solver falls back to the previous psi
+// (unet_check_fallback), so a poor guess costs one cycle.
+int unet_guess(Engine& E) {
+    E.unet_used = 0;
+    if (!E.unet) return 0;
+    UNet& U = *static_cast<UNet*>(E.unet_core);
+    const Geo& g = E.g1;
+    const int nx = E.cfg.nx, nz = E.cfg.nz;
+    int rc;
+    double r_prev = 0.0, alpha = 0.0;
+    if ((rc = mean_resid(E, &r_prev))) return rc;  // err[1] holds the previous psi
+    if ((rc = engine_features(E, U.xin, nullptr))) return rc;
+    CK(cudaStreamSynchronize(E.st));
+    if ((rc = unet_forward(U, 1)) || (rc = gemm_error(U))) return rc;
+    k_guess_scatter<<<dim3(nblk(nx + 1, 128), nz + 1), 128, 0, E.st>>>(E.err[1], U.y, g, nx, nz);
+    CK(cudaGetLastError());
+    if ((rc = enforce_bcs_stream(E, 1, E.err[1])) || (rc = coarse_scale_fit(E, &alpha))) return rc;
+    k_scale_all<<<nblk(g.elems(), 256), 256, 0, E.st>>>(E.err[1], alpha, g.elems());
+    CK(cudaGetLastError());
+    E.unet_r_prev = r_prev;
+    E.unet_r_net = 0.0;
+    E.unet_used = 1;
+    return 0;
+}
+
+// Called with the residual ratio measured after the first full cycle from the network's guess:
+// falls back to the previous psi when the guess did not lower the residual.  Returns 1 when the
+// solve restarts from the previous psi.
+int unet_check_fallback(Engine& E, double ratio) {
+    if (E.unet_used != 1) return 0;
+    E.unet_r_net = ratio;
+    if (ratio < E.unet_r_prev) {
+        E.unet_used = 2;  // kept; checked
+        return 0;
+    }
+    E.unet_used = 0;
+    if (cudaMemcpyAsync(E.err[1], E.SF, E.g1.elems() * sizeof(double), cudaMemcpyDeviceToDevice, E.st) != cudaSuccess)
+        return -1;
+    return 1;
+}
+
 }  // namespace pt
 
 using namespace pt;
@@ -712,4 +813,47 @@ int pt_unet_load(const char* path, int nz, int nx, int max_batch, pt_unet** out)
     return pt_unet_set_params(*out, h.data());
 }
 
+int pt_training_pair(float* x4, float* psi) {
+    if (!x4 || !psi) return fail(PT_ERR_ARG, "null pointer");
+    if (!g_eng) return fail(PT_ERR_STATE, "call pt_init, pt_upload_state and pt_solve_psi first");
+    Engine& E = *g_eng;
+    if (!E.uploaded) return fail(PT_ERR_STATE, "call pt_upload_state and pt_solve_psi first");
+    const size_t plane = (size_t)E.cfg.nx * E.cfg.nz;
+    if (!E.pair_buf) CK(cudaMalloc(&E.pair_buf, sizeof(float) * 5 * plane));
+    if (int rc = engine_features(E, E.pair_buf, E.pair_buf + 4 * plane)) return rc;
+    CK(cudaMemcpyAsync(x4, E.pair_buf, sizeof(float) * 4 * plane, cudaMemcpyDeviceToHost, E.st));
+    CK(cudaMemcpyAsync(psi, E.pair_buf + 4 * plane, sizeof(float) * plane, cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    return 0;
+}
+
+int pt_unet_guess_info(int* used, double* resid_prev, double* resid_net) {
+    if (!g_eng) return fail(PT_ERR_STATE, "call pt_init first");
+    Engine& E = *g_eng;
+    if (used) *used = E.unet_used;
+    if (resid_prev) *resid_prev = E.unet_r_prev;
+    if (resid_net) *resid_net = E.unet_r_net;
+    return 0;
+}
+
 }  // extern "C"
+
+namespace pt {
+int unet_engine_load(Engine& E, const char* path) {
+    if (!path) return fail(PT_ERR_ARG, "PT_GUESS_UNET needs a weight file");
+    pt_unet* net = nullptr;
+    if (int rc = pt_unet_load(path, E.cfg.nz, E.cfg.nx, 1, &net)) return rc;
+    unet_engine_release(E);
+    E.unet = net;
+    E.unet_core = &net->u;
+    return 0;
+}
+int unet_engine_release(Engine& E) {
+    if (E.unet) pt_unet_destroy(static_cast<pt_unet*>(E.unet));
+    E.unet = nullptr;
+    E.unet_core = nullptr;
+    if (E.pair_buf) cudaFree(E.pair_buf);
+    E.pair_buf = nullptr;
+    return 0;
+}
+}  // namespace pt

@@ -36,65 +36,10 @@ def test_tc_gemm_matches_fp64_reference(M, N, K):
     assert np.max(np.abs(C - ref)) <= 1e-6 * K * np.max(np.abs(ref))
 
 
-class _Net:
-    """ctypes handle of a pt_unet."""
+def _Net(nz, nx, batch, seed):
+    from projectracer_gb300.learned import UNet
 
-    def __init__(self, nz, nx, batch, seed):
-        self.L = eng.load_library()
-        L = self.L
-        L.pt_unet_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
-                                     ctypes.POINTER(ctypes.c_void_p)]
-        for f in ("pt_unet_destroy",):
-            getattr(L, f).argtypes = [ctypes.c_void_p]
-        L.pt_unet_num_params.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
-        L.pt_unet_get_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-        L.pt_unet_set_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-        L.pt_unet_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-        L.pt_unet_gradients.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
-                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]
-        L.pt_unet_train_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
-                                         ctypes.POINTER(ctypes.c_float)]
-        L.pt_unet_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
-        L.pt_unet_load.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                   ctypes.POINTER(ctypes.c_void_p)]
-        self.h = ctypes.c_void_p()
-        self.nz, self.nx = nz, nx
-        self._ok(L.pt_unet_create(nz, nx, batch, seed, ctypes.byref(self.h)))
-
-    def _ok(self, rc):
-        assert rc == 0, self.L.pt_last_error()
-
-    def params(self):
-        n = ctypes.c_int64()
-        self._ok(self.L.pt_unet_num_params(self.h, ctypes.byref(n)))
-        p = np.zeros(n.value, dtype=np.float32)
-        self._ok(self.L.pt_unet_get_params(self.h, p.ctypes.data))
-        return p
-
-    def forward(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float32)
-        y = np.zeros((x.shape[0], self.nz, self.nx), dtype=np.float32)
-        self._ok(self.L.pt_unet_forward(self.h, x.ctypes.data, x.shape[0], y.ctypes.data))
-        return y
-
-    def gradients(self, x, t):
-        x = np.ascontiguousarray(x, dtype=np.float32)
-        t = np.ascontiguousarray(t, dtype=np.float32)
-        g = np.zeros(self.params().size, dtype=np.float32)
-        loss = ctypes.c_float()
-        self._ok(self.L.pt_unet_gradients(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], g.ctypes.data,
-                                          ctypes.byref(loss)))
-        return loss.value, g
-
-    def train_step(self, x, t, lr):
-        x = np.ascontiguousarray(x, dtype=np.float32)
-        t = np.ascontiguousarray(t, dtype=np.float32)
-        loss = ctypes.c_float()
-        self._ok(self.L.pt_unet_train_step(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], lr, ctypes.byref(loss)))
-        return loss.value
-
-    def close(self):
-        self.L.pt_unet_destroy(self.h)
+    return UNet(nz, nx, batch, seed)
 
 
 def _smooth_batch(rng, B, nz, nx):
@@ -144,12 +89,10 @@ def test_unet_adam_reduces_loss_and_weights_round_trip(tmp_path):
         last = net.train_step(x, t, 1e-3)
     assert last < 0.3 * first
     path = str(tmp_path / "w.bin")
-    assert net.L.pt_unet_save(net.h, path.encode()) == 0
-    h2 = ctypes.c_void_p()
-    assert net.L.pt_unet_load(path.encode(), nz, nx, B, ctypes.byref(h2)) == 0
-    y1 = net.forward(x)
-    y2 = np.zeros_like(y1)
-    assert net.L.pt_unet_forward(h2, np.ascontiguousarray(x).ctypes.data, B, y2.ctypes.data) == 0
-    assert np.array_equal(y1, y2)
-    net.L.pt_unet_destroy(h2)
+    net.save(path)
+    from projectracer_gb300.learned import UNet
+
+    net2 = UNet.load(path, nz, nx, B)
+    assert np.array_equal(net.forward(x), net2.forward(x))
+    net2.close()
     net.close()
