@@ -199,9 +199,11 @@ int pt_stats(pt_stats_row* out);
  * smoothing on/off (smooth_vis, basics.f90:315). */
 int pt_tracers_to_corners(const double* T0, int smooth_vis);
 
-/* pt_tracers_to_corners without any device allocation, for callers that must not allocate
- * (no reference counterpart: the reference allocates its projection work arrays on the stack and
- * heap of tracers_to_corners).  The sort and partial-sum scratch lives in one file-scope device
+/* pt_tracers_to_corners without any device allocation (no counterpart in the reference).  It is
+ * for callers that cannot call cudaMalloc: a host program that hands all free device memory to its
+ * own pool allocator at start-up, where any further allocation fails or fragments the pool, or one
+ * that projects while other streams are busy, where cudaMalloc/cudaFree can synchronise the device
+ * and stall them.  The sort and partial-sum scratch lives in one file-scope device
  * array of the library (about 12 MB) whose address pt_init resolves once per device, so no
  * symbol lookup happens inside a stream capture; calls on a thread with no prior pt_init on the
  * current device resolve it themselves and must not be made during a capture.  Limits: at most

@@ -1,7 +1,8 @@
-"""pt_tracers_to_corners_noalloc against pt_tracers_to_corners (same engine, same tracer state):
-two consecutive calls of each give bit-identical T, C and tracer counts; states above the static
-scratch limits are rejected.  Collected last (file name) so that it also runs after the rest of
-the suite has used the device."""
+"""pt_tracers_to_corners_noalloc, the projection for drivers that cannot allocate device memory
+(their pool owns the GPU, or cudaMalloc would stall other streams), against pt_tracers_to_corners
+on the same engine and tracer state: two consecutive calls of each give bit-identical T, C and
+tracer counts; states above the static scratch limits are rejected.  Collected last (file name)
+so that it also runs after the rest of the suite has used the device."""
 import ctypes
 
 import numpy as np
