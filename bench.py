@@ -317,8 +317,12 @@ def fp64_comparison(eng, cfg, snap, steps: int = 2) -> dict:
     state: one untimed step, then `steps` timed steps."""
     from projectracer_gb300.config import PT_PREC_FP64
 
+    from projectracer_gb300.config import PtConfig
+
     c = cfg.copy()
     c.precision = PT_PREC_FP64
+    ref = PtConfig.defaults()  # the reference's smoother (35 stages, damping 1000)
+    c.nstageS, c.dampingS = ref.nstageS, ref.dampingS
     e = eng.Engine(c)
     e.upload(snap)
     e.solve_psi()

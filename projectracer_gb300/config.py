@@ -182,10 +182,13 @@ WORKLOADS = {
     # plain FP64 solve levels off at 2.0e-8 (first solve) and 1.6e-7 (the RK-stage solves of
     # the first step), a floor set by rounding psi itself to FP64.  Timings therefore use
     # bench_tolerance = 1e-6 for every arm.  The mixed-precision solve runs a V-cycle (mg_cycle):
-    # more cycles than the reference's W-type schedule but far less coarse-level work per cycle.
+    # more cycles than the reference's W-type schedule but far less coarse-level work per cycle,
+    # and an 8-stage RKC1 smoother (damping 50) instead of 35 stages (damping 1000): 9.0 instead of
+    # 7.4 cycles per solve, 27% less time per step (measured on GB300).  The FP64 comparison keeps
+    # the reference's smoother.
     "C3": dict(nx=1024, nz=512, aspect=2.0, RaT=1e7, RaC=2e6, comp=1, ivis=1, visT=1e5, visP=10.0,
                tpc=32, courant=0.5, tolerance=1e-8, steps=200, CFL=1, mg_scheme=1, bench_tolerance=1e-6,
-               mg_cycle=PT_CYCLE_V),
+               mg_cycle=PT_CYCLE_V, mixed_nstageS=8, mixed_dampingS=50.0),
     # 512x256 learned-guess configuration (Ra_T and contrast sampled per run)
     "C4": dict(nx=512, nz=256, aspect=2.0, RaT=1e6, RaC=2e5, comp=1, ivis=1, visT=1e2, visP=1.0,
                tpc=16, courant=0.5, tolerance=1e-8, steps=1),
@@ -218,6 +221,9 @@ def workload(name: str, scale: float = 1.0, precision: int = PT_PREC_FP64) -> tu
     c.CFL = w.get("CFL", 0)
     c.mg_scheme = w.get("mg_scheme", PT_MG_REFERENCE)
     c.mg_cycle = w.get("mg_cycle", PT_CYCLE_REFERENCE)
+    if precision == PT_PREC_MIXED and "mixed_nstageS" in w:
+        c.nstageS = w["mixed_nstageS"]
+        c.dampingS = w["mixed_dampingS"]
     c.precision = precision
     c.ntr = c.nx * c.nz * w["tpc"]
     return c, w

@@ -107,7 +107,6 @@ struct Engine {
     bool coarse_ready = false;  // coarse factorisation valid for coarse_time (mixed precision)
     bool levels_reused = false; // this solve reuses levels 2..grids (mixed precision)
     double coarse_time = -1.0;
-    int ginv_cols = 32;
     int* ipiv = nullptr;
     // reductions
     double* red = nullptr;       // partial sums scratch

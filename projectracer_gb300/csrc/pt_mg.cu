@@ -651,42 +651,81 @@ __global__ void k_band_solve(const double* ab, const int* ipiv, double* bg, int 
     for (int q = lane; q < n; q += 32) bg[q] = b[q];
 }
 
-// Explicit inverse of the factored coarse matrix, G = (P L U)^{-1}: thread t of a block carries
-// column c = blockIdx.x * blockDim.x + t through the same forward/back substitution as
-// k_band_solve (DGBTRS restated) on the unit vector e_c.  The band entries are shared by all
-// threads of the block (broadcast loads), each column lives in shared memory, y[q * C + t].
-// G is stored row-major so the per-cycle coarse solve is a coalesced GEMV (k_coarse_apply).
-__global__ void k_band_inverse(const double* ab, const int* ipiv, double* G, int n, int kl, int ku) {
-    extern __shared__ double y[];
-    const int C = blockDim.x, t = threadIdx.x, c = blockIdx.x * C + t;
-    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1;
-    if (c >= n) return;  // no block-level synchronisation below: every thread owns its column
+// Explicit inverse of the factored coarse matrix, G = (P L U)^{-1}.  Warp w of a block carries
+// column c = 4 blockIdx.x + w through the forward/back substitution of k_band_solve (DGBTRS
+// restated) on the unit vector e_c, its lanes splitting each step's band update.  The four warps
+// share the band columns, staged through shared memory kInvChunk at a time; each column vector
+// lives in shared memory.  G is row-major, so the per-cycle coarse solve is a coalesced GEMV.
+constexpr int kInvWarps = 4, kInvChunk = 16;
+__host__ __device__ constexpr size_t inv_smem(int n, int kl, int ku) {
+    return sizeof(double) * ((size_t)kInvChunk * (kl + ku + 1) + (size_t)kInvWarps * n) + sizeof(int) * kInvChunk;
+}
+__global__ void __launch_bounds__(32 * kInvWarps) k_band_inverse(const double* ab, const int* ipiv, double* G, int n,
+                                                                 int kl, int ku) {
+    extern __shared__ double sm[];
+    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1, k = kl + ku, kp1 = k + 1;
+    double* band = sm;                                           // kInvChunk x kp1
+    double* y = band + (size_t)kInvChunk * kp1 + (size_t)(threadIdx.x >> 5) * n;
+    int* piv = reinterpret_cast<int*>(sm + (size_t)kInvChunk * kp1 + (size_t)kInvWarps * n);
+    const int lane = threadIdx.x & 31, c = blockIdx.x * kInvWarps + (threadIdx.x >> 5);
+    const bool active = c < n;  // inactive warps still join every __syncthreads
 #define AB(r, cc) ab[(size_t)((r) - 1) + (size_t)((cc) - 1) * (size_t)ldab]
-#define Y(q) y[(size_t)(q) * C + t]
-    for (int q = 0; q < n; q++) Y(q) = (q == c) ? 1.0 : 0.0;
-    for (int j = 1; j <= n - 1; j++) {
-        int lm = kl < n - j ? kl : n - j;
-        int l = ipiv[j - 1];
-        if (l != j) { double tt = Y(l - 1); Y(l - 1) = Y(j - 1); Y(j - 1) = tt; }
-        double bj = Y(j - 1);
-        if (bj != 0.0) {
-            double temp = -1.0 * bj;
-            for (int i = 1; i <= lm; i++) Y(j + i - 1) = Y(j + i - 1) + AB(kd + i, j) * temp;
+    if (active)
+        for (int q = lane; q < n; q += 32) y[q] = (q == c) ? 1.0 : 0.0;
+    // forward: L with the row interchanges
+    for (int j0 = 1; j0 <= n - 1; j0 += kInvChunk) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < kInvChunk * kl; t += blockDim.x) {
+            const int jj = j0 + t / kl, i = t % kl + 1;
+            band[(size_t)(t / kl) * kl + (i - 1)] = (jj <= n - 1 && i <= n - jj) ? AB(kd + i, jj) : 0.0;
+        }
+        for (int t = threadIdx.x; t < kInvChunk; t += blockDim.x) piv[t] = (j0 + t <= n - 1) ? ipiv[j0 + t - 1] : 0;
+        __syncthreads();
+        if (!active) continue;
+        const int jend = min(n - 1, j0 + kInvChunk - 1);
+        for (int j = j0; j <= jend; j++) {
+            const int lm = kl < n - j ? kl : n - j, l = piv[j - j0];
+            if (l != j && lane == 0) {
+                const double tt = y[l - 1];
+                y[l - 1] = y[j - 1];
+                y[j - 1] = tt;
+            }
+            __syncwarp();
+            const double bj = y[j - 1];
+            if (bj != 0.0) {
+                const double temp = -1.0 * bj;
+                const double* bc = band + (size_t)(j - j0) * kl;
+                for (int i = 1 + lane; i <= lm; i += 32) y[j + i - 1] = y[j + i - 1] + bc[i - 1] * temp;
+            }
+            __syncwarp();
         }
     }
-    const int k = kl + ku, kp1 = k + 1;
-    for (int j = n; j >= 1; j--) {
-        double bj = Y(j - 1);
-        if (bj != 0.0) {
-            double x = bj / AB(kp1, j);
-            Y(j - 1) = x;
-            int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
-            for (int i = j - 1; i >= i0; i--) Y(i - 1) = Y(i - 1) - x * AB(l + i, j);
+    // backward: U (band rows 1..kp1 of each column), columns n..1
+    for (int j1 = n; j1 >= 1; j1 -= kInvChunk) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < kInvChunk * kp1; t += blockDim.x) {
+            const int jj = j1 - t / kp1, r = t % kp1 + 1;
+            band[(size_t)(t / kp1) * kp1 + (r - 1)] = (jj >= 1) ? AB(r, jj) : 0.0;
+        }
+        __syncthreads();
+        if (!active) continue;
+        const int jend = max(1, j1 - kInvChunk + 1);
+        for (int j = j1; j >= jend; j--) {
+            const double* bc = band + (size_t)(j1 - j) * kp1;  // bc[r - 1] = AB(r, j)
+            const double bj = y[j - 1];
+            if (bj != 0.0) {
+                const double x = bj / bc[kp1 - 1];
+                __syncwarp();
+                if (lane == 0) y[j - 1] = x;
+                const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+                for (int i = j - 1 - lane; i >= i0; i -= 32) y[i - 1] = y[i - 1] - x * bc[l + i - 1];
+            }
+            __syncwarp();
         }
     }
-    for (int q = 0; q < n; q++) G[(size_t)q * n + c] = Y(q);
-#undef Y
 #undef AB
+    if (active)
+        for (int q = lane; q < n; q += 32) G[(size_t)q * n + c] = y[q];
 }
 
 // coarse solve through the explicit inverse: b = RowB * RHS on interior nodes (0 on the
@@ -739,9 +778,8 @@ static int coarse_factor(Engine& E) {
     CK(cudaStreamSynchronize(E.st));
     if (h) return fail(PT_ERR_SINGULAR_COARSE, "coarse banded LU: zero row or pivot");
     if (E.Ginv) {
-        const int C = E.ginv_cols;
-        PT_COUNT(), k_band_inverse<<<nblk(n, C), C, sizeof(double) * (size_t)n * C, E.st>>>(E.Mc, E.ipiv, E.Ginv, n,
-                                                                                           E.kl, E.ku);
+        PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st>>>(
+            E.Mc, E.ipiv, E.Ginv, n, E.kl, E.ku);
         CKL("k_band_inverse");
     }
     return 0;
@@ -958,14 +996,11 @@ int mg_alloc(Engine& E) {
     CK(cudaFuncSetAttribute(k_coarse_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // explicit coarse inverse for the mixed-precision cycle: n^2 doubles, kept while it is small
     // next to the level arrays (n <= 4096: <= 134 MB)
-    if (E.cfg.precision == PT_PREC_MIXED && E.ngc <= 4096) {
-        int C = 32;
-        while (C > 1 && sizeof(double) * (size_t)E.ngc * C > 200 * 1024) C /= 2;
-        E.ginv_cols = C;
+    if (E.cfg.precision == PT_PREC_MIXED && E.ngc <= 4096 && inv_smem(E.ngc, E.kl, E.ku) <= 200 * 1024) {
         CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
         E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
         CK(cudaFuncSetAttribute(k_band_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(double) * (size_t)E.ngc * C)));
+                                (int)inv_smem(E.ngc, E.kl, E.ku)));
     }
     return 0;
 }
