@@ -33,21 +33,27 @@ __device__ __forceinline__ int cell_index(double x, double inv, double h, int ex
 }
 
 // ---------------------------------------------------------------- projection
+// Cell of each tracer and the per-cell counts.  Tracer IDs are spatially grouped (seeding order),
+// so the lanes of a warp mostly share a cell: one atomic per distinct cell of the warp
+// (__match_any_sync) instead of one per tracer.  Integer counts: the result does not depend on
+// the grouping.  The grid is a whole number of warps; lanes past n carry cell -1.
 __global__ void k_cells(const double* __restrict__ r, const double* __restrict__ s, int64_t n,
                         int32_t* __restrict__ cell, int32_t* __restrict__ count, int* err) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    double rr = r[t], ss = s[t];
-    if (!(rr >= 0.0 && rr <= cK.aspect && ss >= 0.0 && ss <= 1.0)) {
-        atomicOr(err, 1);  // composition.f90:1007-1010
-        cell[t] = -1;
-        return;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1;
+    if (t < n) {
+        const double rr = r[t], ss = s[t];
+        if (!(rr >= 0.0 && rr <= cK.aspect && ss >= 0.0 && ss <= 1.0)) {
+            atomicOr(err, 1);  // composition.f90:1007-1010
+        } else {
+            const int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div);
+            const int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div);
+            c = i + (cK.nx + 1) * k;
+        }
+        cell[t] = c;
     }
-    int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div);
-    int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div);
-    int c = i + (cK.nx + 1) * k;
-    cell[t] = c;
-    atomicAdd(&count[c], 1);
+    const unsigned group = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && (int)(threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(&count[c], __popc(group));
 }
 
 // exclusive scan of int32 counts: block scan, scan of block totals, add offsets
@@ -90,14 +96,19 @@ __global__ void k_scan_add(int32_t* out, const int32_t* totals, int n) {
     if (gid < n) out[gid] += totals[blockIdx.x];
 }
 
+// Tracer IDs into their cell's segment: one atomic per distinct cell of a warp, lanes placed by
+// rank, so IDs of one warp keep ascending order inside a cell and the per-cell sort that follows
+// mostly sees sorted input.
 __global__ void k_scatter(const int32_t* __restrict__ cell, int64_t n, const int32_t* __restrict__ start,
                           int32_t* cursor, int32_t* __restrict__ list) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    int c = cell[t];
-    if (c < 0) return;
-    int slot = start[c] + atomicAdd(&cursor[c], 1);
-    list[slot] = (int32_t)t;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t < n ? cell[t] : -1;
+    const unsigned group = __match_any_sync(0xffffffffu, c);
+    const int lane = (int)(threadIdx.x & 31), leader = __ffs(group) - 1;
+    int base = 0;
+    if (c >= 0 && lane == leader) base = atomicAdd(&cursor[c], __popc(group));
+    base = __shfl_sync(group, base, leader);
+    if (c >= 0) list[start[c] + base + __popc(group & ((1u << lane) - 1u))] = (int32_t)t;
 }
 
 // ascending tracer IDs inside each cell (insertion sort: cells hold a few dozen tracers)
@@ -165,56 +176,59 @@ __global__ void k_cell_partials(const double* __restrict__ r, const double* __re
     }
 }
 
-// Mixed-precision variant of k_cell_partials: the offsets u = (r - ci dr)/dr and v = (s - ck ds)/ds
-// are formed in FP64, the shape weights max(0, 1 - |u - d|), the products and the sums in FP32 with
-// Neumaier compensation (same ascending-ID order, so the result is still deterministic); each
-// partial is stored as the FP64 value of sum + compensation.  Relative error of order 1e-7 on
-// the projected T and C.
-__device__ __forceinline__ void comp_add(float& s, float& c, float x) {
-    float t = s + x;
-    c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
-    s = t;
-}
-
-__global__ void k_cell_partials_f(const double* __restrict__ r, const double* __restrict__ s,
-                                  const double* __restrict__ Tt, const double* __restrict__ Ct,
-                                  const int32_t* __restrict__ list, const int32_t* __restrict__ start,
-                                  const int32_t* __restrict__ count, int ncell, double* __restrict__ P, int comp) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    const int nx1 = cK.nx + 1;
-    int ci = c % nx1, ck = c / nx1;
-    float aT[9], cT[9], aC[9], cC[9], aS[9], cS[9];
+// Mixed-precision variant of k_cell_partials, one warp per cell, with no per-cell ID sort: each
+// tracer's 27 contributions (T*S, C*S, S for the 3x3 target nodes; offsets formed in FP64, shape
+// weights and products in FP32) are rounded to fixed point (int32, scale 2^28) before any
+// addition, and the sums are integer sums, exactly associative, so the result does not depend on
+// the order of the cell's list and is bit-deterministic.  Lane sums meet through a shared-memory
+// transpose.  Valid while |T| and |C| stay below 8; relative error of order 1e-7 (FP32 products).
+constexpr int kPartWarps = 4;
+constexpr float kFix = 268435456.0f;  // 2^28
+__global__ void __launch_bounds__(32 * kPartWarps) k_cell_partials_fx(
+    const double* __restrict__ r, const double* __restrict__ s, const double* __restrict__ Tt,
+    const double* __restrict__ Ct, const int32_t* __restrict__ list, const int32_t* __restrict__ start,
+    const int32_t* __restrict__ count, int ncell, double* __restrict__ P, int comp) {
+    __shared__ long long red[kPartWarps][27][33];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kPartWarps + w;
+    long long acc[27];
 #pragma unroll
-    for (int q = 0; q < 9; q++) { aT[q] = cT[q] = aC[q] = cC[q] = aS[q] = cS[q] = 0.f; }
-    const double x0 = (double)ci * cK.dr, z0 = (double)ck * cK.ds;
-    int b = start[c], n = count[c];
-    for (int a = 0; a < n; a++) {
-        int32_t t = list[b + a];
-        const float u = (float)((r[t] - x0) * cK.inv_dr), v = (float)((s[t] - z0) * cK.inv_ds);
-        const float tv = (float)Tt[t], cv = comp ? (float)Ct[t] : 0.f;
-        float wx[3], wz[3];
+    for (int q = 0; q < 27; q++) acc[q] = 0;
+    if (c < ncell) {
+        const int nx1 = cK.nx + 1;
+        const int ci = c % nx1, ck = c / nx1;
+        const double x0 = (double)ci * cK.dr, z0 = (double)ck * cK.ds;
+        const float idr = (float)cK.inv_dr, ids = (float)cK.inv_ds;
+        const int b = start[c], n = count[c];
+        for (int a = lane; a < n; a += 32) {
+            const int32_t t = list[b + a];
+            const float u = (float)(r[t] - x0) * idr, v = (float)(s[t] - z0) * ids;
+            const float tv = (float)Tt[t], cv = comp ? (float)Ct[t] : 0.f;
+            float wx[3], wz[3];
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-            wx[d] = fmaxf(0.f, 1.f - fabsf(u - (float)(d - 1)));
-            wz[d] = fmaxf(0.f, 1.f - fabsf(v - (float)(d - 1)));
-        }
-#pragma unroll
-        for (int dz = 0; dz < 3; dz++)
-#pragma unroll
-            for (int dx = 0; dx < 3; dx++) {
-                const float S = wx[dx] * wz[dz];
-                const int q = dz * 3 + dx;
-                comp_add(aT[q], cT[q], tv * S);
-                if (comp) comp_add(aC[q], cC[q], cv * S);
-                comp_add(aS[q], cS[q], S);
+            for (int d = 0; d < 3; d++) {
+                wx[d] = fmaxf(0.f, 1.f - fabsf(u - (float)(d - 1)));
+                wz[d] = fmaxf(0.f, 1.f - fabsf(v - (float)(d - 1)));
             }
+#pragma unroll
+            for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++) {
+                    const float S = wx[dx] * wz[dz];
+                    const int q = dz * 3 + dx;
+                    acc[q] += __float2int_rn(tv * S * kFix);
+                    acc[9 + q] += __float2int_rn(cv * S * kFix);
+                    acc[18 + q] += __float2int_rn(S * kFix);
+                }
+        }
     }
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-        P[(size_t)q * ncell + c] = (double)aT[q] + (double)cT[q];
-        P[(size_t)(9 + q) * ncell + c] = (double)aC[q] + (double)cC[q];
-        P[(size_t)(18 + q) * ncell + c] = (double)aS[q] + (double)cS[q];
+    for (int q = 0; q < 27; q++) red[w][q][lane] = acc[q];
+    __syncwarp();
+    if (c < ncell && lane < 27) {
+        long long sum = 0;
+        for (int l = 0; l < 32; l++) sum += red[w][lane][l];
+        P[(size_t)lane * ncell + c] = (double)sum * (1.0 / 268435456.0);
     }
 }
 
@@ -271,13 +285,14 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
     int32_t* cursor = W.scan_tmp + nb + 32;
     CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
     PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(W.tcell, n, W.cstart, cursor, W.clist);
-    PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(W.clist, W.cstart, W.ccount, ncell);
-    if (E.cfg.precision == PT_PREC_MIXED)
-        PT_COUNT(), k_cell_partials_f<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount,
-                                                                          ncell, W.cpart, E.cfg.comp);
-    else
+    if (E.cfg.precision == PT_PREC_MIXED) {  // order-independent fixed-point sums: no ID sort
+        PT_COUNT(), k_cell_partials_fx<<<nblk(ncell, kPartWarps), 32 * kPartWarps, 0, E.st>>>(
+            r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount, ncell, W.cpart, E.cfg.comp);
+    } else {  // the reference's association: ascending tracer ID per cell, FP64
+        PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(W.clist, W.cstart, W.ccount, ncell);
         PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount, ncell,
                                                             W.cpart, E.cfg.comp);
+    }
     dim3 grid(nblk(nx + 1, 128), nz + 1);
     PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(W.cpart, W.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
     CKL("projection");
