@@ -323,6 +323,7 @@ def fp64_comparison(eng, cfg, snap, steps: int = 2) -> dict:
     c.precision = PT_PREC_FP64
     ref = PtConfig.defaults()  # the reference's smoother (35 stages, damping 1000)
     c.nstageS, c.dampingS = ref.nstageS, ref.dampingS
+    c.guess_mode = ref.guess_mode  # the reference's warm start (previous psi)
     e = eng.Engine(c)
     e.upload(snap)
     e.solve_psi()

@@ -58,6 +58,11 @@ extern "C" {
 #define PT_GUESS_PREVIOUS 0 /* previous psi (the reference's warm start, iterative_solver.f90:134) */
 #define PT_GUESS_ZERO 1
 #define PT_GUESS_UNET 2
+/* Linear extrapolation in time from the last two converged psi at distinct solve times (no
+ * reference counterpart): inside an RK4 step the stage solves at t+dt/2 and t+dt start from
+ * 2 psi(latest) - psi(earlier) scaled to the stage time; solves at the time of the latest psi
+ * start from it, as PT_GUESS_PREVIOUS does. */
+#define PT_GUESS_EXTRAPOLATE 3
 
 /*
  * Run configuration: the &inputs, &Rayleigh_numbers, &heating_conductivity and &viscosity namelist

@@ -1,6 +1,7 @@
 // pt_api.cu -- the C ABI of include/ptgpu.h: context set-up, field exchange, the restart upload
 // and the time-step orchestration (energy_time, energy.f90:181-556) on one CUDA stream.
 #include <nvtx3/nvToolsExt.h>
+#include <utility>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -129,6 +130,8 @@ static int engine_alloc(Engine& E) {
 
 static void engine_free(Engine& E) {
     unet_engine_release(E);
+    if (E.psi_a) cudaFree(E.psi_a);
+    if (E.psi_b) cudaFree(E.psi_b);
     double** fine[] = {&E.T, &E.Tratio, &E.Tvis, &E.Tbuoy, &E.Cnew, &E.Cvis, &E.Cbuoy, &E.SF, &E.u, &E.w,
                        &E.cond, &E.cond_r, &E.cond_s, &E.tsa, &E.Text, &E.T0, &E.C0, &E.scratch, &E.psi_keep,
                        &E.red, &E.dscal, &E.cpart, &E.rtr, &E.str, &E.Ttr, &E.Ctr, &E.rtr0, &E.str0,
@@ -318,7 +321,10 @@ int pt_field_extent(int field, int32_t* lo_x, int32_t* hi_x, int32_t* lo_z, int3
 }
 
 int pt_set_field(int field, const void* host) {
-    if (g_eng) g_eng->coarse_ready = false;  // new inputs: refactor the coarse operator
+    if (g_eng) {  // new inputs: refactor the coarse operator; a new psi restarts the psi history
+        g_eng->coarse_ready = false;
+        if (field == PT_F_SF) g_eng->hist_n = 0;
+    }
     if (int rc = need(g_eng != nullptr)) return rc;
     if (!host) return fail(PT_ERR_ARG, "null pointer");
     Engine& E = *g_eng;
@@ -385,6 +391,7 @@ int pt_upload_state(const double* xg, const double* zg, const double* T, const d
     E.have_mass = 0;
     E.uploaded = 1;
     E.coarse_ready = false;
+    E.hist_n = 0;
     CK(cudaStreamSynchronize(E.st));
     return 0;
 }
@@ -402,6 +409,38 @@ int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* 
     return 0;
 }
 
+// x = a + c (a - b) over the whole padded array (boundary-consistent inputs stay consistent)
+__global__ void k_extrapolate(double* x, const double* pa, const double* pb, double c, size_t n) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) x[q] = pa[q] + c * (pa[q] - pb[q]);
+}
+
+static int extrapolated_guess(Engine& E) {
+    if (E.hist_n < 2 || !(E.tau_a > E.tau_b) || E.solve_tau == E.tau_a) return 0;  // previous psi
+    const double c = (E.solve_tau - E.tau_a) / (E.tau_a - E.tau_b);
+    const size_t n = E.g1.elems();
+    k_extrapolate<<<(unsigned)((n + 255) / 256), 256, 0, E.st>>>(E.SF, E.psi_a, E.psi_b, c, n);
+    return cuda_check(cudaGetLastError(), "k_extrapolate");
+}
+
+static int record_psi(Engine& E) {
+    const size_t bytes = E.g1.elems() * sizeof(double);
+    if (!E.psi_a) {
+        CK(cudaMalloc(&E.psi_a, bytes));
+        CK(cudaMalloc(&E.psi_b, bytes));
+    }
+    if (E.hist_n > 0 && E.solve_tau == E.tau_a) {  // same solve time: the newer psi replaces a
+        CK(cudaMemcpyAsync(E.psi_a, E.SF, bytes, cudaMemcpyDeviceToDevice, E.st));
+        return 0;
+    }
+    std::swap(E.psi_a, E.psi_b);
+    E.tau_b = E.tau_a;
+    CK(cudaMemcpyAsync(E.psi_a, E.SF, bytes, cudaMemcpyDeviceToDevice, E.st));
+    E.tau_a = E.solve_tau;
+    E.hist_n = E.hist_n < 2 ? E.hist_n + 1 : 2;
+    return 0;
+}
+
 static int solve_psi(Engine& E, pt_solve_info* info) {
     int rc;
     cudaEvent_t a, b;
@@ -409,7 +448,9 @@ static int solve_psi(Engine& E, pt_solve_info* info) {
     cudaEventCreate(&b);
     cudaEventRecord(a, E.st);
     if (E.cfg.guess_mode == PT_GUESS_ZERO) CK(cudaMemsetAsync(E.SF, 0, E.g1.elems() * 8, E.st));
+    if (E.cfg.guess_mode == PT_GUESS_EXTRAPOLATE && (rc = extrapolated_guess(E))) return rc;
     rc = (E.cfg.precision == PT_PREC_MIXED) ? multigrid_mixed(E, info) : multigrid(E, info);
+    if (!rc && E.cfg.guess_mode == PT_GUESS_EXTRAPOLATE) rc = record_psi(E);
     if (!rc) rc = compute_velocities(E);
     cudaEventRecord(b, E.st);
     cudaEventSynchronize(b);
@@ -428,6 +469,7 @@ static int solve_psi(Engine& E, pt_solve_info* info) {
 int pt_solve_psi(pt_solve_info* info) {
     if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
     if (info) std::memset(info, 0, sizeof *info);
+    g_eng->solve_tau = g_eng->time;
     return solve_psi(*g_eng, info);
 }
 
@@ -470,6 +512,7 @@ int pt_step(double* dt_out, pt_solve_info* info) {
         if (comp && st > 2 && (rc = copy_field(E, E.Cnew, E.C0))) return rc;
         if ((rc = project(E, sr[st - 2], ss[st - 2], sT[st - 2], E.T0, 1))) return rc;
         if ((rc = stage_tables(E))) return rc;
+        E.solve_tau = E.time + (st == 4 ? E.dt : 0.5 * E.dt);  // stage time of this solve
         if ((rc = solve_psi(E, info))) return rc;
         if ((rc = velocity_tables(E)) || (rc = rk_stage(E, st))) return rc;
     }
@@ -527,7 +570,7 @@ int pt_time(double* time, double* dt) {
 
 int pt_set_guess_mode(int mode, const char* weights_path) {
     if (int rc = need(g_eng != nullptr)) return rc;
-    if (mode != PT_GUESS_PREVIOUS && mode != PT_GUESS_ZERO && mode != PT_GUESS_UNET)
+    if (mode != PT_GUESS_PREVIOUS && mode != PT_GUESS_ZERO && mode != PT_GUESS_UNET && mode != PT_GUESS_EXTRAPOLATE)
         return fail(PT_ERR_ARG, "unknown guess mode");
     if (mode == PT_GUESS_UNET) {
         if (int rc = unet_engine_load(*g_eng, weights_path)) return rc;

@@ -99,6 +99,11 @@ struct Engine {
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
+    // PT_GUESS_EXTRAPOLATE: the last converged psi (a) and the last one at an earlier solve time
+    // (b), with their solve times; solve_tau is the time of the solve being set up
+    double *psi_a = nullptr, *psi_b = nullptr;
+    double tau_a = 0.0, tau_b = 0.0, solve_tau = 0.0;
+    int hist_n = 0;
     void* unet = nullptr;        // pt_unet* of the learned guess (PT_GUESS_UNET)
     void* unet_core = nullptr;   // its network (pt::UNet*)
     float* pair_buf = nullptr;   // staging of pt_training_pair (5 planes of nz x nx)

@@ -223,3 +223,29 @@ def test_mixed_step_close_to_fp64():
         assert rel_err(b[f], a[f]) < 1e-7, f
     assert rel_err(b[eng.F_TRACER_T], a[eng.F_TRACER_T]) < 1e-6
     assert rel_err(b[eng.F_T], a[eng.F_T]) < 1e-6
+
+
+def test_extrapolated_guess_steps_close_to_previous_guess():
+    """PT_GUESS_EXTRAPOLATE (psi extrapolated in time between the solves of a step) only changes
+    where each solve starts: after two full steps the tracers agree with the previous-psi run to
+    the solve tolerance, and the extrapolated run needs no more cycles."""
+    from projectracer_gb300.config import PT_GUESS_EXTRAPOLATE, PT_GUESS_PREVIOUS, PT_PREC_MIXED
+
+    cfg, st = small_case("c3", nx=128, nz=64)
+    cfg.precision = PT_PREC_MIXED
+    out, cycles = {}, {}
+    for mode in (PT_GUESS_PREVIOUS, PT_GUESS_EXTRAPOLATE):
+        c = cfg.copy()
+        c.guess_mode = mode
+        e = eng.Engine(c)
+        e.upload(st)
+        n = 0
+        for _ in range(3):
+            n += e.solve_psi()["cycles"]
+            n += e.step()[1]["cycles"]
+        out[mode] = (e.get(eng.F_TRACER_R), e.get(eng.F_TRACER_S), e.get(eng.F_T))
+        cycles[mode] = n
+        e.close()
+    for a, b in zip(out[PT_GUESS_PREVIOUS], out[PT_GUESS_EXTRAPOLATE]):
+        assert rel_err(b, a) < 1e-6
+    assert cycles[PT_GUESS_EXTRAPOLATE] <= cycles[PT_GUESS_PREVIOUS]
