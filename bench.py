@@ -275,6 +275,7 @@ def main():
         e.close()
         e = None
         fp64 = fp64_comparison(eng, cfg, snap)
+        fp64_same = fp64_comparison(eng, cfg, snap, same_schedule=True)
     line = {"metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": args.steps,
             "warmup": W, "ms_per_step": elapsed / args.steps * 1e3, "host_ms_per_step": host_s / args.steps * 1e3,
             "higher_is_better": True,
@@ -289,6 +290,8 @@ def main():
     if fp64 is not None:
         line["fp64_path"] = fp64
         line["psi_solve_speedup_vs_fp64"] = fp64["psi_solve_ms"] / max(1e-9, line["psi_solve_ms"])
+        line["fp64_same_schedule"] = fp64_same
+        line["psi_solve_speedup_vs_fp64_same_schedule"] = fp64_same["psi_solve_ms"] / max(1e-9, line["psi_solve_ms"])
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args.workload).items()
@@ -312,18 +315,20 @@ def snapshot(e, eng, st) -> dict:
     return snap
 
 
-def fp64_comparison(eng, cfg, snap, steps: int = 2) -> dict:
-    """The plain FP64 GPU path (PT_PREC_FP64, same schedule and tolerance) from the mixed run's
-    state: one untimed step, then `steps` timed steps."""
-    from projectracer_gb300.config import PT_PREC_FP64
-
-    from projectracer_gb300.config import PtConfig
+def fp64_comparison(eng, cfg, snap, steps: int = 2, same_schedule: bool = False) -> dict:
+    """The plain FP64 GPU path from the mixed run's state at the same tolerance: one untimed step,
+    then `steps` timed steps.  Default: the reference's algorithm (its W-type schedule, 35-stage
+    RKC1 smoother, previous-psi start).  same_schedule: FP64 with the mixed run's schedule,
+    smoother and initial guess, so that only the precision differs."""
+    from projectracer_gb300.config import PT_CYCLE_REFERENCE, PT_PREC_FP64, PtConfig
 
     c = cfg.copy()
     c.precision = PT_PREC_FP64
-    ref = PtConfig.defaults()  # the reference's smoother (35 stages, damping 1000)
-    c.nstageS, c.dampingS = ref.nstageS, ref.dampingS
-    c.guess_mode = ref.guess_mode  # the reference's warm start (previous psi)
+    if not same_schedule:
+        ref = PtConfig.defaults()  # the reference's smoother (35 stages, damping 1000), warm start
+        c.nstageS, c.dampingS = ref.nstageS, ref.dampingS
+        c.guess_mode = ref.guess_mode
+        c.mg_cycle = PT_CYCLE_REFERENCE
     e = eng.Engine(c)
     e.upload(snap)
     e.solve_psi()
@@ -339,7 +344,9 @@ def fp64_comparison(eng, cfg, snap, steps: int = 2) -> dict:
     el = time.perf_counter() - t0
     e.close()
     return {"timesteps_per_s": steps / el, "ms_per_step": el / steps * 1e3, "psi_solve_ms": solve_ms / nsolve,
-            "mg_cycles_per_solve": cycles / nsolve, "steps": steps, "tolerance": c.tolerance}
+            "mg_cycles_per_solve": cycles / nsolve, "steps": steps, "tolerance": c.tolerance,
+            "schedule": "V-cycle" if c.mg_cycle else "reference W-type", "rkc_stages": c.nstageS,
+            "guess": {0: "previous psi", 1: "zero", 2: "learned", 3: "time-extrapolated"}[c.guess_mode]}
 
 
 def end_to_end(e, eng, cfg, st, steps, dist, world):

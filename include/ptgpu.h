@@ -48,9 +48,9 @@ extern "C" {
 #define PT_MG_REFERENCE 0
 #define PT_MG_CORRECTION 1
 
-/* Level schedule of the mixed-precision solve (the FP64 solve always runs the reference's
- * schedule, multigrid_setup in iterative_solver.f90:1-122): PT_CYCLE_REFERENCE the reference's
- * table for the level count (a W-type cycle), PT_CYCLE_V one descent and one ascent. */
+/* Level schedule of the solve: PT_CYCLE_REFERENCE the reference's table for the level count (a
+ * W-type cycle, multigrid_setup in multigrid_cycle.f90:1-99), PT_CYCLE_V one descent and one
+ * ascent (no reference counterpart). */
 #define PT_CYCLE_REFERENCE 0
 #define PT_CYCLE_V 1
 

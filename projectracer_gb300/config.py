@@ -221,7 +221,8 @@ def workload(name: str, scale: float = 1.0, precision: int = PT_PREC_FP64) -> tu
     c.H = w.get("H", 0.0)
     c.CFL = w.get("CFL", 0)
     c.mg_scheme = w.get("mg_scheme", PT_MG_REFERENCE)
-    c.mg_cycle = w.get("mg_cycle", PT_CYCLE_REFERENCE)
+    # schedule, smoother and guess of the mixed-precision method; FP64 keeps the reference's
+    c.mg_cycle = w.get("mg_cycle", PT_CYCLE_REFERENCE) if precision == PT_PREC_MIXED else PT_CYCLE_REFERENCE
     if precision == PT_PREC_MIXED and "mixed_nstageS" in w:
         c.nstageS = w["mixed_nstageS"]
         c.dampingS = w["mixed_dampingS"]

@@ -864,8 +864,11 @@ int mg_setup_solve(Engine& E) {
 // prolong back to level 1).  Neither part synchronises, so both are captured as CUDA graphs.
 static int cycle_part(Engine& E, int part) {
     int rc;
-    const int grids = E.grids, nsteps = E.nsteps;
-    const int* multi = E.multi;
+    // the reference's schedule, or a V-cycle when asked for (mg_cycle); the parity path keeps the
+    // reference's
+    const bool v = E.cfg.mg_cycle == PT_CYCLE_V;
+    const int grids = E.grids, nsteps = v ? E.mnsteps : E.nsteps;
+    const int* multi = v ? E.mmulti : E.multi;
     if (part == 0) return iterate_stream(E, 1, 1);
     for (int p = 2; p <= nsteps; p++) {
         const int level = multi[p];
