@@ -234,6 +234,19 @@ __global__ void __launch_bounds__(128) k_residual64(double* __restrict__ res, co
     res[o] = op.rhs[o] - apply_A<double, double, DOp>(x, g, 1, op, i, k, ivis);
 }
 
+// Residual after the level-1 pre-smoothing, updated instead of recomputed: r -= A e with the
+// FP32 stencil on the FP32 correction.  e was built from r, so its rounding error is a fraction
+// ~1e-5 of |r| (not of |x|, which is what forces FP64 when A is applied to the iterate itself);
+// the solve's final convergence test recomputes the FP64 residual from x.
+__global__ void __launch_bounds__(128) k_residual_update(double* __restrict__ res, const float* __restrict__ e, FOp op,
+                                                         Geo g, int nx, int nz, int ivis) {
+    pdl_begin();
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    const size_t o = g.at(i, k);
+    res[o] -= (double)apply_A<float>(e, g, 1, op, i, k, ivis);
+}
+
 // full weighting (restrict, iterative_solver.f90:398-418) into FP32; R = double restricts the
 // FP64 level-1 residual directly
 template <typename R>
@@ -443,7 +456,11 @@ static int mixed_part(Engine& E, int part) {
             return rc;
         if ((rc = smooth_f(E, 1, true, false))) return rc;
         if ((rc = add_correction(E))) return rc;
-        return residual64(E, true);
+        dim3 blk(32, 4), grd(nblk(g1.nx - 1, 32), nblk(g1.nz - 1, 4));
+        if ((rc = launch_pdl("k_residual_update", k_residual_update, grd, blk, 0, E.st, E.res[1], (const float*)E.ferr[1],
+                             fop(E, 1), g1, g1.nx, g1.nz, E.cfg.ivis)))
+            return rc;
+        return reduce_sum_abs_interior(E, E.res[1], g1.nx, g1.nz, g1.pitch, E.dscal + 8);
     }
     const int grids = E.grids, nsteps = E.mnsteps;
     const int* multi = E.mmulti;
@@ -551,7 +568,14 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
                 continue;
             }
         }
-        if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
+        if (mag1 / E.res_ref[1] <= E.cfg.tolerance) {
+            // the updated residual says converged: confirm with the FP64 residual of x
+            if ((rc = residual64(E, true))) return rc;
+            CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+            CK(cudaStreamSynchronize(E.st));
+            mag1 = E.hscal[0] / norm;
+            if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
+        }
         if (cycles >= E.cfg.max_cycles)
             return fail(PT_ERR_MG_MAX_CYCLES, "mixed-precision solve: too many cycles");
         {
