@@ -212,16 +212,19 @@ __global__ void __launch_bounds__(256) k_rkc_stage_f(float* out, const float* __
     else store_ghosts_f(out, g, i, k, nx, nz, d, sz);
 }
 
-// Residual of the correction equation with FP64 arithmetic on the FP32 correction: for smooth
-// modes the biharmonic stencil cancels by orders of magnitude, which FP32 cannot resolve on the
-// fine levels; this residual is what the coarser levels see.
+// Residual of the correction equation, the RHS the next coarser level sees.  T = double when the
+// correction holds a prolongated coarse correction: for smooth modes the biharmonic stencil
+// cancels by orders of magnitude, which FP32 cannot resolve on the fine levels.  T = float after a
+// smoothing pass that started from zero: the correction was built from this RHS, so FP32 rounding
+// stays a small fraction of |RHS|.
+template <typename T>
 __global__ void __launch_bounds__(256) k_residual_f(float* __restrict__ res, const float* __restrict__ S, FOp op, Geo g,
                                                     int l, int nx, int nz, int ivis) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
     size_t o = g.at(i, k);
-    res[o] = (float)((double)op.rhs[o] - apply_A<double>(S, g, l, op, i, k, ivis));
+    res[o] = (float)((T)op.rhs[o] - apply_A<T>(S, g, l, op, i, k, ivis));
 }
 
 // FP64 residual of the level-1 iterate, r = RHS - A x, with the folded FP64 stencil
@@ -418,8 +421,9 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
         CKL("k_rkc_stage_f");
     }
     if (want_res) {
-        if (int rc = launch_pdl("k_residual_f", k_residual_f, grd64, blk64, 0, E.st, E.fres[l], (const float*)e, op, g, l,
-                                g.nx, g.nz, ivis))
+        auto kres = zero ? k_residual_f<float> : k_residual_f<double>;
+        if (int rc = launch_pdl("k_residual_f", kres, zero ? grd : grd64, zero ? blk : blk64, 0, E.st, E.fres[l],
+                                (const float*)e, op, g, l, g.nx, g.nz, ivis))
             return rc;
     }
     return 0;
