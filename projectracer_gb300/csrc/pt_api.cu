@@ -142,8 +142,7 @@ static void engine_free(Engine& E) {
         for (int j = 0; j < 3; j++)
             if (E.der[f][j]) cudaFree(E.der[f][j]);
     for (int f = 0; f < 3; f++)
-        for (int j = 0; j < 4; j++)
-            if (E.fder[f][j]) cudaFree(E.fder[f][j]);
+        if (E.ftab[f]) cudaFree(E.ftab[f]);
     for (int l = 0; l < PT_MAXLEV; l++) {
         double* arrs[] = {E.err[l], E.S0[l], E.S1[l], E.S2[l], E.RHS[l], E.res[l], E.dtst[l], E.ratio[l],
                           E.vis[l], E.visst[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l],

@@ -54,6 +54,7 @@ struct Consts {
     double dr_pow[4], ds_pow[4], fact[4];
     double inv_ds_pow[4], inv_fact[4];
     int exact_div;  // dr and ds are powers of two: x/dr == x*inv_dr exactly
+    int p_inv_dr, p_inv_ds;  // inv_dr = 2^p_inv_dr, inv_ds = 2^p_inv_ds when exact_div
     double two_over_D20;
     double Tbot_iso, Ttop_iso, H, Htype, conduct_factor;
     double RaT, RaC, lvisT, lvisP, lvisC;
@@ -79,7 +80,7 @@ struct Engine {
            *cond = nullptr, *cond_r = nullptr, *cond_s = nullptr, *tsa = nullptr, *Text = nullptr,
            *T0 = nullptr, *C0 = nullptr, *scratch = nullptr;
     double* der[3][3] = {};  // derivative tables: [field u,w,tsa][order 1..3]
-    float* fder[3][4] = {};  // mixed precision: FP32 [field][value, orders 1..3] for the RK stages
+    float4* ftab[3] = {};    // mixed precision: per node (value, x-derivatives 1..3) in FP32, fields u, w, dT/dt
     double* coef[3] = {};    // 16 Taylor coefficients per node per field (advection)
     int32_t* nempty = nullptr;
     // multigrid

@@ -602,13 +602,12 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
 }
 
 int mixed_alloc(Engine& E) {
-    for (int f = 0; f < 3; f++)
-        for (int j = 0; j < 4; j++) {
-            const size_t n = E.g1.elems();
-            CK(cudaMalloc(&E.fder[f][j], n * sizeof(float)));
-            CK(cudaMemsetAsync(E.fder[f][j], 0, n * sizeof(float), E.st));
-            E.bytes_allocated += n * sizeof(float);
-        }
+    for (int f = 0; f < 3; f++) {
+        const size_t n = E.g1.elems();
+        CK(cudaMalloc(&E.ftab[f], n * sizeof(float4)));
+        CK(cudaMemsetAsync(E.ftab[f], 0, n * sizeof(float4), E.st));
+        E.bytes_allocated += n * sizeof(float4);
+    }
     for (int l = 1; l <= E.grids; l++) {
         const size_t n = E.gl[l].elems();
         float** arrs[] = {&E.ferr[l], &E.fS0[l], &E.fS1[l], &E.fS2[l], &E.fRHS[l], &E.fres[l], &E.fcoef[l][0],

@@ -262,6 +262,13 @@ int setup_constants(Engine& E) {
     K.inv_ds = 1.0 / K.ds;
     int ex;
     K.exact_div = (std::frexp(K.dr, &ex) == 0.5 && std::frexp(K.ds, &ex) == 0.5) ? 1 : 0;
+    K.p_inv_dr = K.p_inv_ds = 0;
+    if (K.exact_div) {
+        std::frexp(K.inv_dr, &ex);
+        K.p_inv_dr = ex - 1;
+        std::frexp(K.inv_ds, &ex);
+        K.p_inv_ds = ex - 1;
+    }
     K.fact[0] = 1.0; K.dr_pow[0] = 1.0; K.ds_pow[0] = 1.0;
     for (int j = 1; j <= 3; j++) {
         K.fact[j] = (double)j * K.fact[j - 1];

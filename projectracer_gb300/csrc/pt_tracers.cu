@@ -27,9 +27,33 @@ int upload_consts_tracers(const Engine& E) {
     return 0;
 }
 
-__device__ __forceinline__ int cell_index(double x, double inv, double h, int exact) {
-    double q = exact ? x * inv : x / h;
-    return (int)llround(q);
+// nint(x * 2^p) (round half away from zero, as llround), exactly, from the bit pattern with
+// integer operations (this part's FP64 pipe is its scarcest resource).  |x * 2^p| >= 2^30
+// (and NaN) saturate to +-2^30; zero and subnormal x give 0.
+__device__ __forceinline__ int nint_pow2(double x, int p) {
+    const unsigned long long raw = (unsigned long long)__double_as_longlong(x);
+    const bool neg = (raw >> 63) != 0;
+    const unsigned long long b = raw & 0x7FFFFFFFFFFFFFFFull;
+    const int be = (int)(b >> 52);
+    const int e = be - 1023 + p;  // exponent of |x| * 2^p
+    if (be == 0 || e < -1) return 0;
+    if (e >= 30) return neg ? -(1 << 30) : (1 << 30);
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;  // m * 2^(e-52)
+    const int sh = 52 - e;  // 23..53
+    const int v = (int)((m + (1ull << (sh - 1))) >> sh);
+    return neg ? -v : v;
+}
+
+__device__ __forceinline__ int cell_index(double x, double inv, double h, int exact, int p) {
+    if (exact) return nint_pow2(x, p);
+    return (int)llround(x / h);
+}
+
+// 0 <= x <= hi (hi > 0) by comparing bit patterns: non-negative doubles order like their bits,
+// negative values and NaN compare above hi, -0 counts as 0
+__device__ __forceinline__ bool in_range(double x, double hi) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return b <= (unsigned long long)__double_as_longlong(hi) || b == 0x8000000000000000ull;
 }
 
 // ---------------------------------------------------------------- projection
@@ -43,11 +67,11 @@ __global__ void k_cells(const double* __restrict__ r, const double* __restrict__
     int c = -1;
     if (t < n) {
         const double rr = r[t], ss = s[t];
-        if (!(rr >= 0.0 && rr <= cK.aspect && ss >= 0.0 && ss <= 1.0)) {
+        if (!(in_range(rr, cK.aspect) && in_range(ss, 1.0))) {
             atomicOr(err, 1);  // composition.f90:1007-1010
         } else {
-            const int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div);
-            const int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div);
+            const int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
+            const int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
             c = i + (cK.nx + 1) * k;
         }
         cell[t] = c;
@@ -420,8 +444,8 @@ __global__ void __launch_bounds__(256) k_rk_stage(StageArgs A, Geo g) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.n) return;
     double r = A.xr[t], s = A.xs[t];
-    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div);
-    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div);
+    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
+    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
     i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
     k = min(max(k, 0), cK.nz);
     double hr = r - (double)i * cK.dr, hs = s - (double)k * cK.ds;
@@ -454,17 +478,14 @@ __global__ void __launch_bounds__(256) k_rk_stage(StageArgs A, Geo g) {
 // dT/dt tables: positions, step-start values and the RK accumulators stay FP64.  Interpolated
 // velocities carry a relative error of order 1e-7, below the psi solve's tolerance; the FP64
 // stage (k_rk_stage) is the reference-order path.
-struct FTables {
-    const float *f, *d1, *d2, *d3;
-};
-
-__device__ __forceinline__ float interp_f(const FTables& tb, Geo g, int i, int k, float a1, float a2, float a3,
-                                          float b1, float b2, float b3) {
+// one 16-byte load per table row: (value, x-derivatives of order 1..3) interleaved per node
+__device__ __forceinline__ float interp_f(const float4* __restrict__ tb, Geo g, int i, int k, float a1, float a2,
+                                          float a3, float b1, float b2, float b3) {
     float fR[7];
 #pragma unroll
     for (int jj = 0; jj < 7; jj++) {
-        size_t o = g.at(i, k + jj - 3);
-        fR[jj] = tb.f[o] + tb.d1[o] * a1 + tb.d2[o] * a2 + tb.d3[o] * a3;
+        const float4 q = __ldg(tb + g.at(i, k + jj - 3));
+        fR[jj] = q.x + q.y * a1 + q.z * a2 + q.w * a3;
     }
     float s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll
@@ -477,7 +498,7 @@ __device__ __forceinline__ float interp_f(const FTables& tb, Geo g, int i, int k
 }
 
 struct StageArgsF {
-    FTables u, w, t;
+    const float4 *u, *w, *t;
     const double *xr, *xs;
     double *rtr, *str, *Ttr;
     const double *r0, *s0, *T0;
@@ -491,8 +512,8 @@ __global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.n) return;
     double r = A.xr[t], s = A.xs[t];
-    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div);
-    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div);
+    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
+    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
     i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
     k = min(max(k, 0), cK.nz);
     const float hr = (float)(r - (double)i * cK.dr), hs = (float)(s - (double)k * cK.ds);
@@ -520,19 +541,18 @@ __global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
     }
 }
 
-// FP32 copies of one interpolation table set (value and its three x-derivatives)
-__global__ void k_tables_to_f32(float* f, float* d1, float* d2, float* d3, const double* F, const double* D1,
-                                const double* D2, const double* D3, size_t n) {
+// FP32 copy of one interpolation table set, interleaved per node (value, x-derivatives 1..3)
+__global__ void k_tables_to_f32(float4* out, const double* F, const double* D1, const double* D2, const double* D3,
+                                size_t n) {
     size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    f[q] = (float)F[q]; d1[q] = (float)D1[q]; d2[q] = (float)D2[q]; d3[q] = (float)D3[q];
+    out[q] = make_float4((float)F[q], (float)D1[q], (float)D2[q], (float)D3[q]);
 }
 
 int tables_to_f32(Engine& E, int which, const double* f) {
-    if (!E.fder[which][0]) return 0;
+    if (!E.ftab[which]) return 0;
     const size_t n = E.g1.elems();
-    PT_COUNT(), k_tables_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(E.fder[which][0], E.fder[which][1], E.fder[which][2],
-                                                                E.fder[which][3], f, E.der[which][0], E.der[which][1],
+    PT_COUNT(), k_tables_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(E.ftab[which], f, E.der[which][0], E.der[which][1],
                                                                 E.der[which][2], n);
     CKL("k_tables_to_f32");
     return 0;
@@ -554,9 +574,8 @@ int rk_stage(Engine& E, int stage) {
         case 3: A.xr = E.rtr2; A.xs = E.str2; A.rn = E.rtr1; A.sn = E.str1; A.Tn = E.Ttr1; A.dtstage = E.dt; break;
         default: A.xr = E.rtr1; A.xs = E.str1; A.rn = nullptr; A.sn = nullptr; A.Tn = nullptr; A.dtstage = E.dt / 6.0; break;
     }
-    if (E.fder[0][0]) {  // mixed precision: FP32 interpolation
-        auto ft = [&](int w) { return FTables{E.fder[w][0], E.fder[w][1], E.fder[w][2], E.fder[w][3]}; };
-        StageArgsF F{ft(0), ft(1), ft(2), A.xr, A.xs, A.rtr, A.str, A.Ttr, A.r0, A.s0, A.T0, A.rn, A.sn, A.Tn,
+    if (E.ftab[0]) {  // mixed precision: FP32 interpolation
+        StageArgsF F{E.ftab[0], E.ftab[1], E.ftab[2], A.xr, A.xs, A.rtr, A.str, A.Ttr, A.r0, A.s0, A.T0, A.rn, A.sn, A.Tn,
                      A.dtstage, A.stage, A.n};
         KernelTimer kt(E, KT_RK_STAGE, 1);
         PT_COUNT(), k_rk_stage_f<<<nblk(E.ntr, 256), 256, 0, E.st>>>(F, E.g1);
