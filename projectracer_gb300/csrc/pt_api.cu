@@ -160,7 +160,16 @@ static void engine_free(Engine& E) {
     for (auto a : ia)
         if (a) cudaFree(a);
     if (E.ipiv) cudaFree(E.ipiv);
+    if (E.st2) cudaStreamSynchronize(E.st2);  // a factorisation may still be in flight
     if (E.Ginv) cudaFree(E.Ginv);
+    for (double* p : {E.Ginv2, E.Mc2, E.RowB2})
+        if (p) cudaFree(p);
+    if (E.ipiv2) cudaFree(E.ipiv2);
+    if (E.derr2) cudaFree(E.derr2);
+    if (E.hflag2) cudaFreeHost(E.hflag2);
+    if (E.ev_in) cudaEventDestroy(E.ev_in);
+    if (E.ev_fact) cudaEventDestroy(E.ev_fact);
+    if (E.st2) cudaStreamDestroy(E.st2);
     if (E.derr) cudaFree(E.derr);
     if (E.hscal) cudaFreeHost(E.hscal);
     for (int q = 0; q < PT_NPHASE; q++)

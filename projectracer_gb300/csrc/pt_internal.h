@@ -100,6 +100,13 @@ struct Engine {
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
+    // mixed precision: the next time level's coarse factorisation, built on st2 while the
+    // top-of-step solve runs with the previous one, then copied into Mc/RowB/ipiv/Ginv
+    double *Mc2 = nullptr, *RowB2 = nullptr, *Ginv2 = nullptr;
+    int *ipiv2 = nullptr, *derr2 = nullptr, *hflag2 = nullptr;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_fact = nullptr;
+    bool fact_pending = false;
     // PT_GUESS_EXTRAPOLATE: the last converged psi (a) and the last one at an earlier solve time
     // (b), with their solve times; solve_tau is the time of the solve being set up
     double *psi_a = nullptr, *psi_b = nullptr;

@@ -785,6 +785,40 @@ static int coarse_factor(Engine& E) {
     return 0;
 }
 
+// Mixed precision: build the coarse matrix, its LU and inverse for the viscosity just computed
+// on st into the second buffer set on st2, overlapped with the solve that follows on st (the LU
+// runs on one SM).  coarse_resolve copies the result into the live buffers.
+static int coarse_factor_async(Engine& E) {
+    const int L = E.grids, n = E.ngc;
+    CK(cudaEventRecord(E.ev_in, E.st));
+    CK(cudaStreamWaitEvent(E.st2, E.ev_in, 0));
+    CK(cudaMemsetAsync(E.derr2, 0, sizeof(int), E.st2));
+    PT_COUNT(), k_coarse_matrix<<<nblk(n, 128), 128, 0, E.st2>>>(E.Mc2, E.gl[L], L, E.kl, E.ku, n, E.RowB2, E.cfg.Vbc,
+                                                     E.cfg.ivis, E.vis[L], E.vx[L], E.vz[L], E.vxz[L], E.vxxmzz[L],
+                                                     E.derr2);
+    PT_COUNT(), k_band_lu<<<1, 1024, 0, E.st2>>>(E.Mc2, E.ipiv2, n, E.kl, E.ku, E.derr2);
+    PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st2>>>(
+        E.Mc2, E.ipiv2, E.Ginv2, n, E.kl, E.ku);
+    CKL("async coarse factorisation");
+    CK(cudaMemcpyAsync(E.hflag2, E.derr2, sizeof(int), cudaMemcpyDeviceToHost, E.st2));
+    CK(cudaEventRecord(E.ev_fact, E.st2));
+    E.fact_pending = true;
+    return 0;
+}
+
+int coarse_resolve(Engine& E) {
+    if (!E.fact_pending) return 0;
+    E.fact_pending = false;
+    CK(cudaEventSynchronize(E.ev_fact));
+    if (*E.hflag2) return fail(PT_ERR_SINGULAR_COARSE, "coarse banded LU: zero row or pivot");
+    const int n = E.ngc, ldab = 2 * E.kl + E.ku + 1;
+    CK(cudaMemcpyAsync(E.Mc, E.Mc2, sizeof(double) * (size_t)ldab * n, cudaMemcpyDeviceToDevice, E.st));
+    CK(cudaMemcpyAsync(E.RowB, E.RowB2, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, E.st));
+    CK(cudaMemcpyAsync(E.ipiv, E.ipiv2, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, E.st));
+    CK(cudaMemcpyAsync(E.Ginv, E.Ginv2, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
+    return 0;
+}
+
 // x = G b into err[L] (FP64) or ferr[L] (FP32); needs E.Ginv
 int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, const float* rhs32) {
     const int L = E.grids, n = E.ngc;
@@ -838,6 +872,7 @@ int residual_level1(Engine& E) {
 // ------------------------------------------------------------------ driver
 int mg_setup_solve(Engine& E) {
     int rc;
+    if ((rc = coarse_resolve(E))) return rc;  // a factorisation built during the previous solve
     CK(cudaMemcpyAsync(E.err[1], E.SF, E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     if ((rc = compute_RHS(E, 1))) return rc;
     if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
@@ -851,7 +886,10 @@ int mg_setup_solve(Engine& E) {
     for (int level = 1; level <= (reuse ? 1 : E.grids); level++)
         if ((rc = compute_viscosity(E, level))) return rc;
     if (!reuse && (E.time == 0.0 || E.cfg.ivis > 0)) {
-        if ((rc = coarse_factor(E))) return rc;
+        // mixed precision with a factorisation in place: refresh it off the critical path; this
+        // solve keeps the previous time level's (a preconditioner, O(dt) older)
+        const bool async = E.cfg.precision == PT_PREC_MIXED && E.coarse_ready && E.Ginv2;
+        if ((rc = async ? coarse_factor_async(E) : coarse_factor(E))) return rc;
         E.coarse_ready = true;
         E.coarse_time = E.time;
     }
@@ -1002,6 +1040,17 @@ int mg_alloc(Engine& E) {
     if (E.cfg.precision == PT_PREC_MIXED && E.ngc <= 4096 && inv_smem(E.ngc, E.kl, E.ku) <= 200 * 1024) {
         CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
         E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
+        CK(cudaMalloc(&E.Ginv2, sizeof(double) * (size_t)E.ngc * E.ngc));
+        CK(cudaMalloc(&E.Mc2, sizeof(double) * (size_t)ldab * E.ngc));
+        CK(cudaMalloc(&E.RowB2, sizeof(double) * (size_t)E.ngc));
+        CK(cudaMalloc(&E.ipiv2, sizeof(int) * (size_t)E.ngc));
+        CK(cudaMalloc(&E.derr2, sizeof(int)));
+        CK(cudaMallocHost(&E.hflag2, sizeof(int)));
+        *E.hflag2 = 0;
+        CK(cudaStreamCreateWithFlags(&E.st2, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&E.ev_in, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&E.ev_fact, cudaEventDisableTiming));
+        E.bytes_allocated += sizeof(double) * ((size_t)E.ngc * E.ngc + (size_t)ldab * E.ngc + E.ngc);
         CK(cudaFuncSetAttribute(k_band_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)inv_smem(E.ngc, E.kl, E.ku)));
     }
