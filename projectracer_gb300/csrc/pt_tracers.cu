@@ -2,12 +2,16 @@
 // with the Taylor interpolation of interpolate (composition.f90:1359-1393), and the tracer->grid
 // projection tracers_to_corners_iC_continuous (composition.f90:942-1087).
 //
-// Projection, GB300 form: a counting sort of tracer IDs by cell (cell = nint of the position),
-// a per-cell sort of the IDs, per-cell partial sums of T*S, C*S and S for the 3x3 target nodes
-// in ascending ID order, then per node a fixed-order sum of the 9 partials.  Counts and cell
-// indices are integers (bit-exact); every floating-point sum has a fixed association, so the
-// result is deterministic and equals the oracle's canonical order bit for bit (the arithmetic
-// uses explicit round-to-nearest intrinsics, no contraction).
+// Projection, GB300 form.  FP64 precision: a counting sort of tracer IDs by cell (cell = nint of
+// the position), a per-cell sort of the IDs, per-cell partial sums of T*S, C*S and S for the 3x3
+// target nodes in ascending ID order, then per node a fixed-order sum of the 9 partials.  Counts
+// and cell indices are integers (bit-exact); every floating-point sum has a fixed association, so
+// the result is deterministic and equals the oracle's canonical order bit for bit (the arithmetic
+// uses explicit round-to-nearest intrinsics, no contraction).  Mixed precision: one pass with
+// per-tracer fixed-point contributions and integer sums (k_project_fx), deterministic without a
+// sort and independent of the tracer order; counts bit-exact, sums to 2^-28.
+#include <climits>
+#include <cstdint>
 #include <cstdio>
 #include <string>
 
@@ -200,62 +204,6 @@ __global__ void k_cell_partials(const double* __restrict__ r, const double* __re
     }
 }
 
-// Mixed-precision variant of k_cell_partials, one warp per cell, with no per-cell ID sort: each
-// tracer's 27 contributions (T*S, C*S, S for the 3x3 target nodes; offsets formed in FP64, shape
-// weights and products in FP32) are rounded to fixed point (int32, scale 2^28) before any
-// addition, and the sums are integer sums, exactly associative, so the result does not depend on
-// the order of the cell's list and is bit-deterministic.  Lane sums meet through a shared-memory
-// transpose.  Valid while |T| and |C| stay below 8; relative error of order 1e-7 (FP32 products).
-constexpr int kPartWarps = 4;
-constexpr float kFix = 268435456.0f;  // 2^28
-__global__ void __launch_bounds__(32 * kPartWarps) k_cell_partials_fx(
-    const double* __restrict__ r, const double* __restrict__ s, const double* __restrict__ Tt,
-    const double* __restrict__ Ct, const int32_t* __restrict__ list, const int32_t* __restrict__ start,
-    const int32_t* __restrict__ count, int ncell, double* __restrict__ P, int comp) {
-    __shared__ long long red[kPartWarps][27][33];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * kPartWarps + w;
-    long long acc[27];
-#pragma unroll
-    for (int q = 0; q < 27; q++) acc[q] = 0;
-    if (c < ncell) {
-        const int nx1 = cK.nx + 1;
-        const int ci = c % nx1, ck = c / nx1;
-        const double x0 = (double)ci * cK.dr, z0 = (double)ck * cK.ds;
-        const float idr = (float)cK.inv_dr, ids = (float)cK.inv_ds;
-        const int b = start[c], n = count[c];
-        for (int a = lane; a < n; a += 32) {
-            const int32_t t = list[b + a];
-            const float u = (float)(r[t] - x0) * idr, v = (float)(s[t] - z0) * ids;
-            const float tv = (float)Tt[t], cv = comp ? (float)Ct[t] : 0.f;
-            float wx[3], wz[3];
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                wx[d] = fmaxf(0.f, 1.f - fabsf(u - (float)(d - 1)));
-                wz[d] = fmaxf(0.f, 1.f - fabsf(v - (float)(d - 1)));
-            }
-#pragma unroll
-            for (int dz = 0; dz < 3; dz++)
-#pragma unroll
-                for (int dx = 0; dx < 3; dx++) {
-                    const float S = wx[dx] * wz[dz];
-                    const int q = dz * 3 + dx;
-                    acc[q] += __float2int_rn(tv * S * kFix);
-                    acc[9 + q] += __float2int_rn(cv * S * kFix);
-                    acc[18 + q] += __float2int_rn(S * kFix);
-                }
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 27; q++) red[w][q][lane] = acc[q];
-    __syncwarp();
-    if (c < ncell && lane < 27) {
-        long long sum = 0;
-        for (int l = 0; l < 32; l++) sum += red[w][lane][l];
-        P[(size_t)lane * ncell + c] = (double)sum * (1.0 / 268435456.0);
-    }
-}
-
 // per node: fixed-order sum of the partials of the 3x3 surrounding cells, then the ratio
 __global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restrict__ count, int ncell,
                             double* Tratio, double* Cnew, int32_t* nempty, Geo g, int comp) {
@@ -280,6 +228,215 @@ __global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restr
     }
 }
 
+// ---------------------------------------------------------------- projection, mixed precision
+// The same sums as k_cell_partials, in fixed point (scale 2^28) with integer arithmetic only, so
+// that each node's totals are exact integer sums: the result does not depend on the tracer order
+// or on the scheduling, it is bit-deterministic, and oracle/project_fx.py restates it exactly.
+//   position  u = x / dr (x * 2^p for dr = 2^-p, from the bit pattern); cell i0 = floor(u),
+//             fraction fx = floor((u - i0) * 2^28); a tracer on the right (top) wall goes to the
+//             last cell with fx = 2^28;
+//   counts    per nearest node (the reference's nint cell): i0 + (fx >= 2^27);
+//   weights   wx = (2^28 - fx, fx) for the nodes i0, i0+1 (the reference's hat functions: the
+//             third node of its 3x3 neighbourhood has weight 0), wz likewise,
+//             S = (wx_a wz_b + 2^27) >> 28;
+//   values    T28 = round(T 2^28) (half away from zero, |T| < 4), TS = (T28 S + 2^27) >> 28, CS.
+constexpr int kFixOne = 1 << 28;
+
+// floor(x * 2^p) and the first 28 bits of its fraction for x >= 0 (domain-checked), from the bit
+// pattern with 32-bit operations: x * 2^(p+28) = m * 2^-sh with m the 53-bit significand (high
+// word mh, low word lo).  Zero and subnormal x give sh >= 64, hence 0; x * 2^p >= 2^24 saturates.
+__device__ __forceinline__ int floor_fix_pow2(double x, int p, uint32_t& frac) {
+    const uint32_t hw = (uint32_t)__double2hiint(x) & 0x7FFFFFFFu, lo = (uint32_t)__double2loint(x);
+    const int sh = 1047 - p - (int)(hw >> 20);
+    if (sh <= 4) {
+        frac = 0;
+        return 1 << 24;
+    }
+    const uint32_t mh = (hw & 0xFFFFFu) | 0x100000u;
+    const uint32_t xl = sh < 32 ? __funnelshift_r(lo, mh, sh) : (sh < 64 ? mh >> (sh - 32) : 0u);
+    frac = xl & (uint32_t)(kFixOne - 1);
+    return sh - 4 < 32 ? (int)(mh >> (sh - 4)) : 0;  // m >> (sh + 28)
+}
+
+template <bool EXACT>
+__device__ __forceinline__ int floor_fix(double x, double h, int p, uint32_t& frac) {
+    if (EXACT) return floor_fix_pow2(x, p, frac);
+    const double u = x / h;
+    const double fl = floor(u);
+    frac = (uint32_t)((u - fl) * 268435456.0);
+    return (int)fl;
+}
+
+// round(v * 2^28), half away from zero, from the bit pattern: |v| * 2^28 = m * 2^-sh, and with
+// q = floor(2 |v| 2^28) = m >> (sh - 1) (below 2^31 for |v| < 4) the result is (q + 1) >> 1.
+// |v| >= 4 (and NaN/Inf) set bad.
+__device__ __forceinline__ int fix28(double v, int& bad) {
+    const uint32_t hw = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
+    const int k = 1046 - (int)((hw >> 20) & 0x7FFu);  // sh - 1
+    if (k < 22) {
+        bad |= 2;
+        return 0;
+    }
+    const uint32_t mh = (hw & 0xFFFFFu) | 0x100000u;
+    const uint32_t q = k < 32 ? __funnelshift_r(lo, mh, k) : (k < 64 ? mh >> (k - 32) : 0u);
+    const int a = (int)((q + 1u) >> 1);
+    return (hw >> 31) ? -a : a;
+}
+
+// cell and fractions of a tracer; false outside the domain (composition.f90:1007-1010).  EXACT:
+// dr and ds are powers of two (integer decoding only, no FP64 arithmetic)
+struct TracerCell {
+    int i0, k0, near;  // cell, nearest corner (a + 2 b)
+    uint32_t fx, fz;
+};
+template <bool EXACT>
+__device__ __forceinline__ bool locate(double rr, double ss, TracerCell& c) {
+    if (!(in_range(rr, cK.aspect) && in_range(ss, 1.0))) return false;
+    c.i0 = floor_fix<EXACT>(rr, cK.dr, cK.p_inv_dr, c.fx);
+    c.k0 = floor_fix<EXACT>(ss, cK.ds, cK.p_inv_ds, c.fz);
+    int ni = c.i0 + (int)(c.fx >> 27), nk = c.k0 + (int)(c.fz >> 27);
+    if (c.i0 >= cK.nx) { c.i0 = cK.nx - 1; c.fx = kFixOne; }  // on the right wall
+    if (c.k0 >= cK.nz) { c.k0 = cK.nz - 1; c.fz = kFixOne; }  // on the top wall
+    c.near = (ni - c.i0) + 2 * (nk - c.k0);
+    return true;
+}
+
+// One CTA per chunk of kPjChunk consecutive tracers, kPjPer consecutive tracers per thread.
+// Tracer IDs are spatially grouped (seeding order), so a thread's tracers mostly share a cell: it
+// keeps the running sums of the current cell in registers and adds them, when the cell changes,
+// to a shared-memory window of the grid (64-bit integer shared atomics); at the end the window is
+// added to the global sums with one integer atomic per non-zero value.  The window is the box of
+// the cells of every thread's first and last tracer plus one cell of margin; runs outside it (and
+// every run when the box is too large for the window) go to the global sums directly.
+// acc: [node][TS, CS, S, count] int64.
+constexpr int kPjThreads = 256, kPjPer = 16, kPjChunk = kPjThreads * kPjPer, kPjWin = 1280;
+template <bool EXACT>
+__global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __restrict__ r, const double* __restrict__ s,
+                                                              const double* __restrict__ Tt,
+                                                              const double* __restrict__ Ct, int64_t n,
+                                                              unsigned long long* __restrict__ acc, int comp, int* err) {
+    __shared__ unsigned long long win[4 * kPjWin];  // planes [TS | CS | S | count] of the window
+    __shared__ int box[4];
+    const int nx1 = cK.nx + 1;
+    const int64_t t0 = (int64_t)blockIdx.x * kPjChunk + (int64_t)threadIdx.x * kPjPer;
+    const int64_t t1 = t0 + kPjPer < n ? t0 + kPjPer : n;
+    int bad = 0;
+    if (threadIdx.x == 0) { box[0] = INT_MAX; box[1] = -1; box[2] = INT_MAX; box[3] = -1; }
+    __syncthreads();
+    for (int q = 0; q < 2 && t0 < t1; q++) {
+        const int64_t t = q ? t1 - 1 : t0;
+        TracerCell c;
+        if (locate<EXACT>(r[t], s[t], c)) {
+            atomicMin(&box[0], c.i0); atomicMax(&box[1], c.i0);
+            atomicMin(&box[2], c.k0); atomicMax(&box[3], c.k0);
+        }
+    }
+    __syncthreads();
+    // window: cells box +- 1, i.e. nodes [imin-1, imax+2] x [kmin-1, kmax+2], odd row pitch; its
+    // geometry is re-derived from box[] where needed (fewer live registers in the tracer loop)
+    auto geometry = [&](int& wi, int& wk, int& W, int& H, int& P) {
+        wi = box[0] - 1; wk = box[2] - 1;
+        W = box[1] - box[0] + 4; H = box[3] - box[2] + 4; P = W | 1;
+        return box[1] >= 0 && P * H <= kPjWin;
+    };
+    {
+        int wi, wk, W, H, P;
+        if (geometry(wi, wk, W, H, P)) {
+            for (int q = threadIdx.x; q < 4 * kPjWin; q += kPjThreads) win[q] = 0ull;
+            __syncthreads();
+        }
+    }
+    long long aT[4], aC[4], aS[4];
+    uint32_t cnt = 0;  // four 8-bit counters, one per corner (a run holds at most kPjPer tracers)
+    int ri = -1, rk = -1;
+    auto flush = [&]() {
+        if (ri < 0) return;
+        int wi, wk, W, H, P;
+        const bool use_win = geometry(wi, wk, W, H, P);
+        const int li = ri - wi, lk = rk - wk;
+        const bool inside = use_win && li >= 0 && lk >= 0 && li + 1 < W && lk + 1 < H;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int a = j & 1, b = j >> 1;
+            const long long v[4] = {aT[j], aC[j], aS[j], (long long)((cnt >> (8 * j)) & 255u)};
+            if (inside) {
+                const int o = (li + a) + P * (lk + b);
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+                    if (v[p]) atomicAdd(&win[p * kPjWin + o], (unsigned long long)v[p]);
+            } else {
+                const size_t node = (size_t)(ri + a) + (size_t)nx1 * (size_t)(rk + b);
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+                    if (v[p]) atomicAdd(&acc[4 * node + p], (unsigned long long)v[p]);
+            }
+        }
+    };
+    auto add = [&](double rr, double ss, double tv, double cv) {
+        TracerCell c;
+        if (!locate<EXACT>(rr, ss, c)) {
+            bad |= 1;
+            return;
+        }
+        if (c.i0 != ri || c.k0 != rk) {
+            flush();
+            ri = c.i0;
+            rk = c.k0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) aT[j] = aC[j] = aS[j] = 0;
+            cnt = 0;
+        }
+        const int T28 = fix28(tv, bad), C28 = comp ? fix28(cv, bad) : 0;
+        const uint32_t wx[2] = {(uint32_t)kFixOne - c.fx, c.fx}, wz[2] = {(uint32_t)kFixOne - c.fz, c.fz};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int S = (int)(((unsigned long long)wx[j & 1] * wz[j >> 1] + (1ull << 27)) >> 28);
+            aS[j] += S;
+            aT[j] += (int)(((long long)T28 * S + (1ll << 27)) >> 28);  // |.| <= |T28|: fits
+            if (comp) aC[j] += (int)(((long long)C28 * S + (1ll << 27)) >> 28);
+        }
+        cnt += 1u << (8 * c.near);
+    };
+    // consecutive pairs with 16-byte loads (t0 is even; the arrays are 16-byte aligned)
+    auto ld2 = [](const double* a, int64_t i) { return __ldg(reinterpret_cast<const double2*>(a + i)); };
+    int64_t t = t0;
+    for (; t + 1 < t1; t += 2) {
+        const double2 r2 = ld2(r, t), s2 = ld2(s, t), T2 = ld2(Tt, t);
+        const double2 C2 = comp ? ld2(Ct, t) : make_double2(0.0, 0.0);
+        add(r2.x, s2.x, T2.x, C2.x);
+        add(r2.y, s2.y, T2.y, C2.y);
+    }
+    if (t < t1) add(r[t], s[t], Tt[t], comp ? Ct[t] : 0.0);
+    flush();
+    if (bad) atomicOr(err, bad);
+    int wi, wk, W, H, P;
+    if (!geometry(wi, wk, W, H, P)) return;
+    __syncthreads();
+    const int nw = W * H;
+    for (int q = threadIdx.x; q < 4 * nw; q += kPjThreads) {
+        const int p = q & 3, cell = q >> 2;
+        const int row = cell / W, col = cell - row * W;
+        const unsigned long long v = win[p * kPjWin + row * P + col];
+        if (v) atomicAdd(&acc[4 * ((size_t)(wi + col) + (size_t)nx1 * (size_t)(wk + row)) + p], v);
+    }
+}
+
+// per node: the ratios of the fixed-point sums (the 2^28 scale cancels exactly) and the count
+__global__ void k_node_fx(const unsigned long long* __restrict__ acc, double* Tratio, double* Cnew, int32_t* nempty,
+                          Geo g, int comp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    const int nx = cK.nx;
+    if (i > nx) return;
+    const size_t c = (size_t)i + (size_t)(nx + 1) * (size_t)k;
+    nempty[c] = (int32_t)acc[4 * c + 3];
+    const long long sS = (long long)acc[4 * c + 2];
+    if (sS > 0) {
+        const double dS = (double)sS;
+        Tratio[g.at(i, k)] = __ddiv_rn((double)(long long)acc[4 * c], dS);
+        if (comp) Cnew[g.at(i, k)] = __ddiv_rn((double)(long long)acc[4 * c + 1], dS);
+    }
+}
+
 // scratch of one projection: cell of each tracer, per-cell counts/starts/list, scan blocks,
 // the 27 partial planes and the out-of-domain flag
 struct ProjScratch {
@@ -295,35 +452,47 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
     const int64_t n = E.ntr;
     int rc;
     PhaseTimer tm(E, PH_PROJECT);
-    KernelTimer kt(E, KT_PROJECT, 1);
     if (T0f && T0f != E.Tratio) {
         if ((rc = copy_field(E, E.Tratio, T0f))) return rc;
     }
-    CK(cudaMemsetAsync(W.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
-    CK(cudaMemsetAsync(W.derr, 0, sizeof(int), E.st));
-    PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, W.tcell, W.ccount, W.derr);
-    int nb = (int)nblk(ncell, 1024);
-    PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(W.ccount, W.cstart, W.scan_tmp, ncell);
-    PT_COUNT(), k_scan_totals<<<1, 32, 0, E.st>>>(W.scan_tmp, nb);
-    PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(W.cstart, W.scan_tmp, ncell);
-    int32_t* cursor = W.scan_tmp + nb + 32;
-    CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
-    PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(W.tcell, n, W.cstart, cursor, W.clist);
-    if (E.cfg.precision == PT_PREC_MIXED) {  // order-independent fixed-point sums: no ID sort
-        PT_COUNT(), k_cell_partials_fx<<<nblk(ncell, kPartWarps), 32 * kPartWarps, 0, E.st>>>(
-            r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount, ncell, W.cpart, E.cfg.comp);
-    } else {  // the reference's association: ascending tracer ID per cell, FP64
-        PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(W.clist, W.cstart, W.ccount, ncell);
-        PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount, ncell,
-                                                            W.cpart, E.cfg.comp);
+    {
+        KernelTimer kt(E, KT_PROJECT, 1);
+        CK(cudaMemsetAsync(W.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+        CK(cudaMemsetAsync(W.derr, 0, sizeof(int), E.st));
+        dim3 grid(nblk(nx + 1, 128), nz + 1);
+        if (E.cfg.precision == PT_PREC_MIXED) {  // one pass, order-independent fixed-point sums
+            for (const void* p : {(const void*)r, (const void*)s, (const void*)Tt, (const void*)E.Ctr})
+                if (reinterpret_cast<uintptr_t>(p) % 16)
+                    return fail(PT_ERR_ARG, "mixed-precision projection: tracer arrays must be 16-byte aligned");
+            unsigned long long* acc = reinterpret_cast<unsigned long long*>(W.cpart);
+            CK(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 4 * (size_t)ncell, E.st));
+            auto kern = E.K.exact_div ? k_project_fx<true> : k_project_fx<false>;
+            PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, E.cfg.comp, W.derr);
+            PT_COUNT(), k_node_fx<<<grid, 128, 0, E.st>>>(acc, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
+        } else {  // the reference's association: ascending tracer ID per cell, FP64
+            PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, W.tcell, W.ccount, W.derr);
+            int nb = (int)nblk(ncell, 1024);
+            PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(W.ccount, W.cstart, W.scan_tmp, ncell);
+            PT_COUNT(), k_scan_totals<<<1, 32, 0, E.st>>>(W.scan_tmp, nb);
+            PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(W.cstart, W.scan_tmp, ncell);
+            int32_t* cursor = W.scan_tmp + nb + 32;
+            CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+            PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(W.tcell, n, W.cstart, cursor, W.clist);
+            PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(W.clist, W.cstart, W.ccount, ncell);
+            PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount,
+                                                                            ncell, W.cpart, E.cfg.comp);
+            PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(W.cpart, W.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1,
+                                                            E.cfg.comp);
+        }
+        CKL("projection");
     }
-    dim3 grid(nblk(nx + 1, 128), nz + 1);
-    PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(W.cpart, W.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
-    CKL("projection");
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, W.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
-    if (herr) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
+    if (herr & 1) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
+    if (herr & 2)
+        return fail(PT_ERR_CONFIG, "mixed-precision projection: a tracer's T or C is outside (-4, 4) (FP64 precision "
+                                   "has no such limit)");
     if (E.cfg.comp) {
         if ((rc = enforce_bcs_C(E, E.Cnew))) return rc;
         if (smooth && (rc = smoother_time_C(E))) return rc;

@@ -52,3 +52,13 @@ def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     b = np.asarray(b, dtype=np.float64)
     scale = max(float(np.max(np.abs(b))), 1e-300)
     return float(np.max(np.abs(a - b))) / scale
+
+
+def walls(cfg, st):
+    """A copy of st with a few tracers on the walls and corners (x = 0 or aspect, z = 0 or 1)."""
+    st = dict(st)
+    r, s = st["rtr"].copy(), st["str"].copy()
+    r[:4], s[:4] = [0.0, cfg.aspect, 0.0, cfg.aspect], [0.0, 1.0, 1.0, 0.0]
+    r[-3:], s[-2:] = cfg.aspect, 1.0
+    st["rtr"], st["str"] = r, s
+    return st

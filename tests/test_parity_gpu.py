@@ -11,7 +11,7 @@ import pytest
 
 from oracle.ptref import Oracle
 from projectracer_gb300 import engine as eng
-from tests.helpers import rel_err, small_case
+from tests.helpers import rel_err, small_case, walls
 
 pytestmark = pytest.mark.gpu
 
@@ -37,6 +37,52 @@ def test_upload_projection_bit_exact(kind):
     if cfg.comp:
         assert np.array_equal(e.get(eng.F_CNEW), o.get(4))
     e.close()
+
+
+@pytest.mark.parametrize("kind", ["iso", "chem", "c3"])
+def test_mixed_projection_bit_exact(kind):
+    """The one-pass fixed-point projection of the mixed-precision path equals its integer
+    restatement bit for bit (counts, Tratio and Cnew on every node with tracers), tracers on the
+    walls and corners included."""
+    from oracle.project_fx import project_fx, ratios
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    cfg, st = small_case(kind)
+    st = walls(cfg, st)
+    cfg.precision = PT_PREC_MIXED
+    e = eng.Engine(cfg)
+    e.upload(st)
+    TS, CS, S, cnt = project_fx(cfg.nx, cfg.nz, cfg.aspect, st["rtr"], st["str"], st["Ttr"],
+                                st["Ctr"] if cfg.comp else None)
+    assert np.array_equal(e.get(eng.F_NEMPTY), cnt)
+    Tg = e.get(eng.F_TRATIO)[3:-3, 3:-3]
+    Cg = e.get(eng.F_CNEW)[5:-5, 5:-5] if cfg.comp else None
+    Tr, Cr = ratios(TS, CS, S, Tg, Cg)
+    # interior nodes (the wall nodes take boundary values afterwards)
+    assert np.array_equal(Tg[1:-1, 1:-1], Tr[1:-1, 1:-1])
+    if cfg.comp:
+        assert np.array_equal(Cg[1:-1, 1:-1], Cr[1:-1, 1:-1])
+    e.close()
+
+
+def test_mixed_projection_independent_of_tracer_order():
+    """Integer sums: permuting the tracers leaves the mixed-precision projection bit-identical."""
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    cfg, st = small_case("chem")
+    cfg.precision = PT_PREC_MIXED
+    perm = np.random.default_rng(7).permutation(len(st["rtr"]))
+    st2 = dict(st)
+    for f in ("rtr", "str", "Ctr", "Ttr"):
+        st2[f] = st[f][perm]
+    out = []
+    for state in (st, st2):
+        e = eng.Engine(cfg)
+        e.upload(state)
+        out.append([e.get(f) for f in (eng.F_NEMPTY, eng.F_TRATIO, eng.F_CNEW, eng.F_T)])
+        e.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
