@@ -61,6 +61,12 @@ struct Consts {
     int nx, nz, comp, Tbot, Vbc, ivis;
 };
 
+// weights of the exact-sum level-1 residual (pt_mixed.cu, k_residual_fx)
+struct ResFxK {
+    double k[10];  // per derivative group: the weight that turns its integer sum into the term
+    int square;    // dr == ds: the derivatives are combined in integer arithmetic into 5 groups
+};
+
 struct Engine {
     pt_config cfg;
     Consts K;
@@ -100,6 +106,8 @@ struct Engine {
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
+    bool res_int = false;     // mixed precision: level-1 residual with exact integer stencil sums
+    ResFxK resfx{};
     // mixed precision: the next time level's coarse factorisation, built on st2 while the
     // top-of-step solve runs with the previous one, then copied into Mc/RowB/ipiv/Ginv
     double *Mc2 = nullptr, *RowB2 = nullptr, *Ginv2 = nullptr;
