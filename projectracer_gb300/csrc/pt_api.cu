@@ -164,6 +164,8 @@ static void engine_free(Engine& E) {
     if (E.Ginv) cudaFree(E.Ginv);
     for (double* p : {E.Ginv2, E.Mc2, E.RowB2})
         if (p) cudaFree(p);
+    for (float* p : {E.Gf, E.Gf2})
+        if (p) cudaFree(p);
     if (E.ipiv2) cudaFree(E.ipiv2);
     if (E.derr2) cudaFree(E.derr2);
     if (E.hflag2) cudaFreeHost(E.hflag2);

@@ -111,6 +111,7 @@ struct Engine {
     // mixed precision: the next time level's coarse factorisation, built on st2 while the
     // top-of-step solve runs with the previous one, then copied into Mc/RowB/ipiv/Ginv
     double *Mc2 = nullptr, *RowB2 = nullptr, *Ginv2 = nullptr;
+    float *Gf = nullptr, *Gf2 = nullptr;  // FP32 copies of the inverse (the mixed V-cycle's coarse solve)
     int *ipiv2 = nullptr, *derr2 = nullptr, *hflag2 = nullptr;
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_in = nullptr, ev_fact = nullptr;

@@ -751,6 +751,34 @@ __global__ void __launch_bounds__(256) k_coarse_apply(R* Eout, const R* RHS, con
     if (lane == 0) Eout[g.at(p / N, p % N)] = (R)a;
 }
 
+// The mixed-precision V-cycle's coarse solve: x = G b in FP32 with the FP32 copy of the inverse.
+// The result is a coarse correction inside an FP32 preconditioner of the FP64 defect correction;
+// FP32 rounding of G and of the sum (relative 1e-5 or so for this small, smooth inverse) leaves
+// the cycle count unchanged (measured), and the GEMV no longer runs on the FP64 pipe.
+__global__ void __launch_bounds__(256) k_coarse_apply32(float* Eout, const float* RHS, const float* G,
+                                                        const double* RowB, Geo g, int nxc, int nzc) {
+    extern __shared__ float bsf[];
+    const int N = nzc + 1, n = (nxc + 1) * N;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        int ip = q / N, kp = q % N;
+        bsf[q] = (ip > 0 && ip < nxc && kp > 0 && kp < nzc) ? (float)((double)RHS[g.at(ip, kp)] * RowB[q]) : 0.0f;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int p = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (p >= n) return;
+    const float* row = G + (size_t)p * n;
+    float a = 0.0f;
+    for (int q = lane; q < n; q += 32) a = fmaf(row[q], bsf[q], a);
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) Eout[g.at(p / N, p % N)] = a;
+}
+
+__global__ void k_g_to_f32(float* out, const double* in, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
 __global__ void k_coarse_rhs(double* B, const double* RHS, const double* RowB, Geo g, int nxc, int nzc) {
     int p = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int N = nzc + 1, n = (nxc + 1) * N;
@@ -780,6 +808,8 @@ static int coarse_factor(Engine& E) {
     if (E.Ginv) {
         PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st>>>(
             E.Mc, E.ipiv, E.Ginv, n, E.kl, E.ku);
+        const size_t nn = (size_t)n * n;
+        PT_COUNT(), k_g_to_f32<<<nblk(nn, 256), 256, 0, E.st>>>(E.Gf, E.Ginv, nn);
         CKL("k_band_inverse");
     }
     return 0;
@@ -799,6 +829,7 @@ static int coarse_factor_async(Engine& E) {
     PT_COUNT(), k_band_lu<<<1, 1024, 0, E.st2>>>(E.Mc2, E.ipiv2, n, E.kl, E.ku, E.derr2);
     PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st2>>>(
         E.Mc2, E.ipiv2, E.Ginv2, n, E.kl, E.ku);
+    PT_COUNT(), k_g_to_f32<<<nblk((size_t)n * n, 256), 256, 0, E.st2>>>(E.Gf2, E.Ginv2, (size_t)n * n);
     CKL("async coarse factorisation");
     CK(cudaMemcpyAsync(E.hflag2, E.derr2, sizeof(int), cudaMemcpyDeviceToHost, E.st2));
     CK(cudaEventRecord(E.ev_fact, E.st2));
@@ -816,6 +847,7 @@ int coarse_resolve(Engine& E) {
     CK(cudaMemcpyAsync(E.RowB, E.RowB2, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, E.st));
     CK(cudaMemcpyAsync(E.ipiv, E.ipiv2, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, E.st));
     CK(cudaMemcpyAsync(E.Ginv, E.Ginv2, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
+    CK(cudaMemcpyAsync(E.Gf, E.Gf2, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
     return 0;
 }
 
@@ -826,7 +858,7 @@ int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, co
     const unsigned blocks = nblk(n, 8);
     const size_t smem = sizeof(double) * (size_t)n;
     if (out64) PT_COUNT(), k_coarse_apply<double><<<blocks, 256, smem, E.st>>>(out64, rhs64, E.Ginv, E.RowB, g, g.nx, g.nz);
-    else PT_COUNT(), k_coarse_apply<float><<<blocks, 256, smem, E.st>>>(out32, rhs32, E.Ginv, E.RowB, g, g.nx, g.nz);
+    else PT_COUNT(), k_coarse_apply32<<<blocks, 256, smem / 2, E.st>>>(out32, rhs32, E.Gf, E.RowB, g, g.nx, g.nz);
     CKL("k_coarse_apply");
     return 0;
 }
@@ -1041,6 +1073,9 @@ int mg_alloc(Engine& E) {
         CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
         E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
         CK(cudaMalloc(&E.Ginv2, sizeof(double) * (size_t)E.ngc * E.ngc));
+        CK(cudaMalloc(&E.Gf, sizeof(float) * (size_t)E.ngc * E.ngc));
+        CK(cudaMalloc(&E.Gf2, sizeof(float) * (size_t)E.ngc * E.ngc));
+        CK(cudaFuncSetAttribute(k_coarse_apply32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2)));
         CK(cudaMalloc(&E.Mc2, sizeof(double) * (size_t)ldab * E.ngc));
         CK(cudaMalloc(&E.RowB2, sizeof(double) * (size_t)E.ngc));
         CK(cudaMalloc(&E.ipiv2, sizeof(int) * (size_t)E.ngc));
