@@ -146,8 +146,8 @@ __global__ void k_smooth_T(double* out, const double* in, Geo g, double dts) {
     for (int j = -2; j <= 2; j++) trr = trr + cK.D2[3 + j] * in[g.at(i + j, k)];
 #pragma unroll
     for (int j = -2; j <= 2; j++) tss = tss + cK.D2[3 + j] * in[g.at(i, k + j)];
-    trr = trr / cK.dr2;
-    tss = tss / cK.ds2;
+    trr = qdiv(trr, cK.dr2, cK.inv_dr2);
+    tss = qdiv(tss, cK.ds2, cK.inv_ds2);
     out[g.at(i, k)] = in[g.at(i, k)] + dts * (trr + tss);
 }
 
@@ -208,8 +208,8 @@ __global__ void k_cond_grad(double* cr, double* cs, const double* cd, Geo g) {
     for (int j = -2; j <= 2; j++) a = a + cK.D1[3 + j] * cd[g.at(i + j, k)];
 #pragma unroll
     for (int j = -2; j <= 2; j++) b = b + cK.D1[3 + j] * cd[g.at(i, k + j)];
-    cr[g.at(i, k)] = a / cK.dr;
-    cs[g.at(i, k)] = b / cK.ds;
+    cr[g.at(i, k)] = qdiv(a, cK.dr, cK.inv_dr);
+    cs[g.at(i, k)] = qdiv(b, cK.ds, cK.inv_ds);
 }
 
 int load_conductivity(Engine& E) {
@@ -232,16 +232,16 @@ __global__ void k_tracer_space(double* tsa, const double* X, const double* cd, c
     double Tx = 0, Tz = 0, Txx = 0, Tzz = 0;
 #pragma unroll
     for (int j = -2; j <= 2; j++) Tx = Tx + cK.D1[3 + j] * X[g.at(i + j, k)];
-    Tx = Tx / cK.dr;
+    Tx = qdiv(Tx, cK.dr, cK.inv_dr);
 #pragma unroll
     for (int j = -2; j <= 2; j++) Tz = Tz + cK.D1[3 + j] * X[g.at(i, k + j)];
-    Tz = Tz / cK.ds;
+    Tz = qdiv(Tz, cK.ds, cK.inv_ds);
 #pragma unroll
     for (int j = -2; j <= 2; j++) Txx = Txx + cK.D2[3 + j] * X[g.at(i + j, k)];
-    Txx = Txx / cK.dr2;
+    Txx = qdiv(Txx, cK.dr2, cK.inv_dr2);
 #pragma unroll
     for (int j = -2; j <= 2; j++) Tzz = Tzz + cK.D2[3 + j] * X[g.at(i, k + j)];
-    Tzz = Tzz / cK.ds2;
+    Tzz = qdiv(Tzz, cK.ds2, cK.inv_ds2);
     double h = heating_at(Cvis, g, i, k);
     size_t a = g.at(i, k);
     tsa[a] = cd[a] * (Txx + Tzz) + (cr[a] * Tx + cs[a] * Tz) + h;
@@ -272,9 +272,9 @@ __global__ void k_derivs(double* d1, double* d2, double* d3, const double* f, Ge
         c = c + cK.Dm[3][j] * v[j];
     }
     size_t o = g.at(i, k);
-    d1[o] = a / cK.dr_pow[1];
-    d2[o] = b / cK.dr_pow[2];
-    d3[o] = c / cK.dr_pow[3];
+    d1[o] = qdiv(a, cK.dr_pow[1], cK.inv_dr_pow[1]);
+    d2[o] = qdiv(b, cK.dr_pow[2], cK.inv_dr_pow[2]);
+    d3[o] = qdiv(c, cK.dr_pow[3], cK.inv_dr_pow[3]);
 }
 
 int compute_derivatives(Engine& E, const double* f, int which) {
@@ -293,8 +293,8 @@ __global__ void k_vel_interior(double* u, double* w, const double* SF, Geo g) {
     for (int j = -2; j <= 2; j++) a = a + cK.D1[3 + j] * SF[g.at(i + j, k)];
 #pragma unroll
     for (int j = -2; j <= 2; j++) b = b + cK.D1[3 + j] * SF[g.at(i, k + j)];
-    w[g.at(i, k)] = -a / cK.dr;
-    u[g.at(i, k)] = b / cK.ds;
+    w[g.at(i, k)] = qdiv(-a, cK.dr, cK.inv_dr);
+    u[g.at(i, k)] = qdiv(b, cK.ds, cK.inv_ds);
 }
 __global__ void k_vel_bc(double* u, double* w, Geo g) {
     const int nx = cK.nx, nz = cK.nz;
@@ -424,7 +424,7 @@ __global__ void k_stats_tail(const double* rows, const double* T, const double* 
         double t1 = 0.0, t2 = 0.0;
         for (int j = -2; j <= 2; j++) t1 = t1 + cK.D1[3 + j] * T[g.at(i, nz + j)];
         for (int j = -2; j <= 2; j++) t2 = t2 + cK.D1[3 + j] * T[g.at(i, j)];
-        double tzs = t1 / cK.ds / 1.0, tzb = t2 / cK.ds / 1.0;
+        double tzs = qdiv(t1, cK.ds, cK.inv_ds), tzb = qdiv(t2, cK.ds, cK.inv_ds);  // (the reference's / 1.0 is exact)
         double st = -(cd[g.at(i, nz)] * tzs), sb = -(cd[g.at(i, 0)] * tzb), t0 = T[g.at(i, 0)];
         double uu = u[g.at(i, nz)], ww = w[g.at(i, nz)];
         double m = uu * uu + ww * ww;
@@ -442,9 +442,9 @@ __global__ void k_stats_tail(const double* rows, const double* T, const double* 
         int k = nz;
         double Sxx = 0, Szz = 0, Sxz = 0;
         for (int j = -2; j <= 2; j++) Sxx = Sxx + cK.D2[3 + j] * E1[g.at(i + j, k)];
-        Sxx = Sxx / cK.dr2;
+        Sxx = qdiv(Sxx, cK.dr2, cK.inv_dr2);
         for (int j = -2; j <= 2; j++) Szz = Szz + cK.D2[3 + j] * E1[g.at(i, k + j)];
-        Szz = Szz / cK.ds2;
+        Szz = qdiv(Szz, cK.ds2, cK.inv_ds2);
         for (int k2 = -2; k2 <= 2; k2++)
             for (int i2 = -2; i2 <= 2; i2++) Sxz = Sxz + cK.Drs[i2 + 2][k2 + 2] * E1[g.at(i + i2, k + k2)];
         Sxz = Sxz / (cK.dr * cK.ds);
@@ -460,13 +460,13 @@ __global__ void k_stats_tail(const double* rows, const double* T, const double* 
     }
     double q1, q2, q3, q4, d;
     d = 0; for (int j = -2; j <= 2; j++) d = d + cK.D1[3 + j] * T[g.at(0, nz + j)];
-    q1 = -(cd[g.at(0, nz)] * d / cK.ds / 1.0);
+    q1 = -qdiv(cd[g.at(0, nz)] * d, cK.ds, cK.inv_ds);
     d = 0; for (int j = -2; j <= 2; j++) d = d + cK.D1[3 + j] * T[g.at(nx, nz + j)];
-    q2 = -(cd[g.at(nx, nz)] * d / cK.ds / 1.0);
+    q2 = -qdiv(cd[g.at(nx, nz)] * d, cK.ds, cK.inv_ds);
     d = 0; for (int j = -2; j <= 2; j++) d = d + cK.D1[3 + j] * T[g.at(nx, j)];
-    q3 = -(cd[g.at(nx, 0)] * d / cK.ds / 1.0);
+    q3 = -qdiv(cd[g.at(nx, 0)] * d, cK.ds, cK.inv_ds);
     d = 0; for (int j = -2; j <= 2; j++) d = d + cK.D1[3 + j] * T[g.at(0, j)];
-    q4 = -(cd[g.at(0, 0)] * d / cK.ds / 1.0);
+    q4 = -qdiv(cd[g.at(0, 0)] * d, cK.ds, cK.inv_ds);
     out[0] = I[0];   // integral of T
     out[1] = I[1];   // integral of C
     out[2] = I[2];   // integral of u^2+w^2

@@ -37,7 +37,7 @@ struct LevConst {
     int nx, nz;
     double dr, ds, dr2, ds2, dr3, ds3, dr4, ds4, drds, drds2, dr2ds, dr2ds2;
     // reciprocals of the above (exact for the power-of-two spacings of a multigrid hierarchy)
-    double idr2, ids2, idr3, ids3, idr4, ids4, idrds, idrds2, idr2ds, idr2ds2;
+    double idr, ids, idr2, ids2, idr3, ids3, idr4, ids4, idrds, idrds2, idr2ds, idr2ds2;
     double SR1, SR2, SR4, SR5, SR6, SI1, SI2, SI4, SI5, SI6;
     double dt_vis;
 };
@@ -52,7 +52,7 @@ struct Consts {
     double mewt[64], mew[64], vv[64], cc[64];
     double dr, ds, dr2, ds2, inv_dr, inv_ds, aspect;
     double dr_pow[4], ds_pow[4], fact[4];
-    double inv_ds_pow[4], inv_fact[4];
+    double inv_ds_pow[4], inv_dr_pow[4], inv_fact[4], inv_dr2, inv_ds2;
     int exact_div;  // dr and ds are powers of two: x/dr == x*inv_dr exactly
     int p_inv_dr, p_inv_ds;  // inv_dr = 2^p_inv_dr, inv_ds = 2^p_inv_ds when exact_div
     double two_over_D20;
@@ -61,7 +61,7 @@ struct Consts {
     int nx, nz, comp, Tbot, Vbc, ivis;
 };
 
-// weights of the exact-sum level-1 residual (pt_mixed.cu, k_residual_fx)
+// weights of the exact-sum stream operator of one level (pt_exact.cuh)
 struct ResFxK {
     double k[10];  // per derivative group: the weight that turns its integer sum into the term
     int square;    // dr == ds: the derivatives are combined in integer arithmetic into 5 groups
@@ -106,8 +106,8 @@ struct Engine {
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;
     double* Ginv = nullptr;  // explicit coarse inverse (row-major n x n), mixed precision
-    bool res_int = false;     // mixed precision: level-1 residual with exact integer stencil sums
-    ResFxK resfx{};
+    bool res_int = false;     // stream operator with exact integer stencil sums (pt_exact.cuh)
+    ResFxK resfx[PT_MAXLEV]{};  // per level (both precisions: the FP64 path's stages use them too)
     // mixed precision: the next time level's coarse factorisation, built on st2 while the
     // top-of-step solve runs with the previous one, then copied into Mc/RowB/ipiv/Ginv
     double *Mc2 = nullptr, *RowB2 = nullptr, *Ginv2 = nullptr;

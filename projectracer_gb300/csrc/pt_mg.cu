@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "pt_consts.cuh"
+#include "pt_exact.cuh"
 
 namespace pt {
 
@@ -85,18 +86,18 @@ __global__ void k_vis_grad(VisSet S, Geo g, int l, int full, int ivis) {
     const double* v = S.vis;
     double xx = 0.0, zz = 0.0;
     for (int j = -1; j <= 1; j++) xx = xx + cK.D2so[j + 1] * v[g.at(i + j, k)];
-    xx = xx / L.dr2;
+    xx = qdiv(xx, L.dr2, L.idr2);
     for (int j = -1; j <= 1; j++) zz = zz + cK.D2so[j + 1] * v[g.at(i, k + j)];
-    zz = zz / L.ds2;
+    zz = qdiv(zz, L.ds2, L.ids2);
     if (full) {
         double xz = 0.0, x = 0.0, z = 0.0;
         for (int k2 = -1; k2 <= 1; k2++)
             for (int i2 = -1; i2 <= 1; i2++) xz = xz + cK.Drsso[i2 + 1][k2 + 1] * v[g.at(i + i2, k + k2)];
         for (int j = -1; j <= 1; j++) x = x + cK.D1so[j + 1] * v[g.at(i + j, k)];
         for (int j = -1; j <= 1; j++) z = z + cK.D1so[j + 1] * v[g.at(i, k + j)];
-        S.vxz[o] = xz / L.drds;
-        S.vx[o] = x / L.dr;
-        S.vz[o] = z / L.ds;
+        S.vxz[o] = qdiv(xz, L.drds, L.idrds);
+        S.vx[o] = qdiv(x, L.dr, L.idr);
+        S.vz[o] = qdiv(z, L.ds, L.ids);
         S.vxxmzz[o] = xx - zz;
     }
     S.vxx[o] = xx;
@@ -126,11 +127,27 @@ __global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double 
     if ((threadIdx.x & 31) == 0) atomicMin(rmin, (unsigned long long)__double_as_longlong(m));
 }
 
-__global__ void k_vis_update(double* v, const double* vsm, Geo g, int nx, int nz, double c) {
+// The smoothing update v += c vsm (smoother_vis) followed by viscosityBCs, in one pass.  Every node writes its own mirror images:
+// the column and row ghosts take the updated value; a corner ghost is what viscosityBCs' column
+// phase copies from the row ghost of the mirrored column, which still holds what the previous
+// call wrote there: the mirrored node's value before this update.  (The first call of a smoothing
+// pass is a plain vis_bcs, so that previous call always exists.)
+__global__ void k_vis_update_bc(double* v, const double* vsm, Geo g, int nx, int nz, double c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
     if (i > nx) return;
-    size_t o = g.at(i, k);
-    v[o] = v[o] + c * vsm[o];
+    const size_t o = g.at(i, k);
+    const double old = v[o];
+    const double nv = old + c * vsm[o];
+    v[o] = nv;
+    int xs[2], zs[2], nxm = 0, nzm = 0;
+    if (i >= 1 && i <= 3) xs[nxm++] = -i;
+    if (i >= nx - 3 && i <= nx - 1) xs[nxm++] = 2 * nx - i;
+    if (k >= 1 && k <= 3) zs[nzm++] = -k;
+    if (k >= nz - 3 && k <= nz - 1) zs[nzm++] = 2 * nz - k;
+    for (int a = 0; a < nxm; a++) v[g.at(xs[a], k)] = nv;
+    for (int b = 0; b < nzm; b++) v[g.at(i, zs[b])] = nv;
+    for (int a = 0; a < nxm; a++)
+        for (int b = 0; b < nzm; b++) v[g.at(xs[a], zs[b])] = old;
 }
 
 static const double kPi = 3.1415926535897932;
@@ -180,9 +197,8 @@ static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record)
             int ntemp = Niter - nn + 1;
             double c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
             c = 0.99 * c;
-            PT_COUNT(), k_vis_update<<<gg, 128, 0, E.st>>>(S.vis, S.vsm, g, nx, nz, c);
-            CKL("k_vis_update");
-            if ((rc = vis_bcs(E, S.vis, l))) return rc;
+            PT_COUNT(), k_vis_update_bc<<<gg, 128, 0, E.st>>>(S.vis, S.vsm, g, nx, nz, c);
+            CKL("k_vis_update_bc");
         }
         if (trigger) return 0;
         Nvis_store++;
@@ -258,12 +274,12 @@ __global__ void k_rhs1(double* RHS, const double* Tb, const double* Cb, Geo g, i
     if (cK.RaT != 0.0) {
         double tr = 0.0;
         for (int j = -2; j <= 2; j++) tr = tr + cK.D1[3 + j] * Tb[g.at(i + j, k)];
-        v = cK.RaT * (tr / cK.dr / 1.0);
+        v = cK.RaT * qdiv(tr, cK.dr, cK.inv_dr);  // (the reference's / 1.0 is exact)
     }
     if (comp) {
         double cr = 0.0;
         for (int j = -2; j <= 2; j++) cr = cr + cK.D1[3 + j] * Cb[g.at(i + j, k)];
-        v = v - cK.RaC * (cr / cK.dr / 1.0);
+        v = v - cK.RaC * qdiv(cr, cK.dr, cK.inv_dr);
     }
     RHS[g.at(i, k)] = v;
 }
@@ -386,6 +402,53 @@ __global__ void __launch_bounds__(128) k_rkc_stage(double* __restrict__ out, con
     store_with_ghosts(out, g, i, k, L.nx, L.nz, v, sz);
 }
 
+// k_rkc_stage with the stream operator's stencil sums formed exactly (pt_exact.cuh); a CTA owns a
+// 32 x 16 tile of nodes.
+template <bool SQUARE>
+__global__ void __launch_bounds__(256) k_rkc_stage_fx(double* __restrict__ out, const double* __restrict__ S1,
+                                                      const double* __restrict__ S2, const double* __restrict__ S0,
+                                                      StreamOp op, Geo g, int l, double cS0, double mew, double vv,
+                                                      double mewtc, int first, int ivis, double sz, ResFxK K) {
+    __shared__ int2 X[kRfHt][kRfW];
+    __shared__ int emax_s;
+    const LevConst& L = cL[l];
+    const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
+    const int emax = load_tile_fx(X, &emax_s, S1, g, i0, k0, L.nx, L.nz);
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+        const int lx = threadIdx.x, lz = threadIdx.y + 8 * r;
+        const int i = i0 + lx, k = k0 + lz;
+        if (i > L.nx - 1 || k > L.nz - 1) continue;
+        const size_t o = g.at(i, k);
+        const double F = op.rhs[o] - tile_apply_A<SQUARE>(X, lx + kRfH, lz + kRfH, emax, op.vis, op.vx, op.vz, op.vxz,
+                                                          op.vxxmzz, o, ivis, K);
+        double v;
+        if (first) v = S1[o] + mewtc * op.dtst[o] * F;
+        else v = cS0 * S0[o] + mew * S1[o] + vv * S2[o] + mewtc * op.dtst[o] * F;
+        store_with_ghosts(out, g, i, k, L.nx, L.nz, v, sz);
+    }
+}
+
+// k_residual with exact stencil sums
+template <bool SQUARE>
+__global__ void __launch_bounds__(256) k_residual_fx64(double* __restrict__ res, const double* __restrict__ S,
+                                                       StreamOp op, Geo g, int l, int ivis, ResFxK K) {
+    __shared__ int2 X[kRfHt][kRfW];
+    __shared__ int emax_s;
+    const LevConst& L = cL[l];
+    const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
+    const int emax = load_tile_fx(X, &emax_s, S, g, i0, k0, L.nx, L.nz);
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+        const int lx = threadIdx.x, lz = threadIdx.y + 8 * r;
+        const int i = i0 + lx, k = k0 + lz;
+        if (i > L.nx - 1 || k > L.nz - 1) continue;
+        const size_t o = g.at(i, k);
+        res[o] = op.rhs[o] - tile_apply_A<SQUARE>(X, lx + kRfH, lz + kRfH, emax, op.vis, op.vx, op.vz, op.vxz, op.vxxmzz,
+                                                  o, ivis, K);
+    }
+}
+
 // residual = -(L S - RHS) on the interior (compute_residual)
 __global__ void k_residual(double* __restrict__ res, const double* __restrict__ S, StreamOp op, Geo g, int l, int ivis) {
     const LevConst& L = cL[l];
@@ -426,6 +489,32 @@ static StreamOp stream_op(Engine& E, int l) {
     return StreamOp{E.vis[l], E.vx[l], E.vz[l], E.vxz[l], E.vxxmzz[l], E.RHS[l], E.dtst[l]};
 }
 
+// one RKC1 stage / one residual on level l: the exact-sum kernels when the stencils allow them
+static void launch_stage(Engine& E, int l, double* out, const double* S1, const double* S2, const double* S0,
+                         const StreamOp& op, double cS0, double mew, double vv, double mewtc, int first, double sz) {
+    const Geo& g = E.gl[l];
+    const int ivis = E.cfg.ivis;
+    if (E.res_int) {
+        dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
+        auto kern = E.resfx[l].square ? k_rkc_stage_fx<true> : k_rkc_stage_fx<false>;
+        PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(out, S1, S2, S0, op, g, l, cS0, mew, vv, mewtc, first, ivis, sz,
+                                                E.resfx[l]);
+    } else {
+        dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
+        PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(out, S1, S2, S0, op, g, l, cS0, mew, vv, mewtc, first, ivis, sz);
+    }
+}
+static void launch_residual(Engine& E, int l, double* res, const double* S, const StreamOp& op) {
+    const Geo& g = E.gl[l];
+    if (E.res_int) {
+        dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
+        auto kern = E.resfx[l].square ? k_residual_fx64<true> : k_residual_fx64<false>;
+        PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(res, S, op, g, l, E.cfg.ivis, E.resfx[l]);
+    } else {
+        PT_COUNT(), k_residual<<<dim3(nblk(g.nx - 1, 128), g.nz - 1), 128, 0, E.st>>>(res, S, op, g, l, E.cfg.ivis);
+    }
+}
+
 // iterate_stream (RKC1 = 1, splitting = 0) + compute_residual.  The last stage writes straight
 // into error(:,:,level): a stage reads S0 only at its own node, so the update is safe in place.
 // With want_sum the sum of |residual| is left in dscal[8] (no host synchronisation, so the
@@ -433,10 +522,9 @@ static StreamOp stream_op(Engine& E, int l) {
 // from allocation and are never written by the stage kernel.
 static int iterate_stream(Engine& E, int l, int want_sum) {
     const Geo& g = E.gl[l];
-    const int N = E.cfg.nstageS, Niter = E.cfg.Nmulti, ivis = E.cfg.ivis;
+    const int N = E.cfg.nstageS, Niter = E.cfg.Nmulti;
     const double sz = E.cfg.Vbc == 0 ? -1.0 : 1.0;
     StreamOp op = stream_op(E, l);
-    dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
     double* buf[3] = {E.S0[l], E.S1[l], E.S2[l]};
     for (int n = 1; n <= Niter; n++) {
         int ntemp = Niter - n + 1;
@@ -445,22 +533,21 @@ static int iterate_stream(Engine& E, int l, int want_sum) {
         const double* S0 = E.err[l];
         GraphTimer gt(E, 0, (l == 1 && want_sum) ? N : 0);
         int cur = 0;
-        PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(buf[cur], S0, nullptr, nullptr, op, g, l, 0, 0, 0, E.K.mewt[1] * c, 1, ivis, sz);
+        launch_stage(E, l, buf[cur], S0, nullptr, nullptr, op, 0, 0, 0, E.K.mewt[1] * c, 1, sz);
         const double* Sm1 = buf[cur];
         const double* Sm2 = S0;
         for (int j = 2; j <= N; j++) {
             int nxt = (cur + 1) % 3;
             if (buf[nxt] == Sm2) nxt = (nxt + 1) % 3;
             double* out = (j == N) ? E.err[l] : buf[nxt];
-            PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(out, Sm1, Sm2, S0, op, g, l, E.K.cc[j], E.K.mew[j], E.K.vv[j],
-                                               E.K.mewt[j] * c, 0, ivis, sz);
+            launch_stage(E, l, out, Sm1, Sm2, S0, op, E.K.cc[j], E.K.mew[j], E.K.vv[j], E.K.mewt[j] * c, 0, sz);
             Sm2 = Sm1;
             Sm1 = out;
             cur = nxt;
         }
         CKL("k_rkc_stage");
     }
-    PT_COUNT(), k_residual<<<gs, 128, 0, E.st>>>(E.res[l], E.err[l], op, g, l, ivis);
+    launch_residual(E, l, E.res[l], E.err[l], op);
     CKL("k_residual");
     if (want_sum) return reduce_sum_abs_interior(E, E.res[l], g.nx, g.nz, g.pitch, E.dscal + 8);
     return 0;
@@ -616,39 +703,73 @@ __global__ void __launch_bounds__(1024) k_band_lu(double* ab, int* ipiv, int n, 
 #undef AB
 }
 
-// DGBTRS (no transpose) + DTBSV upper, one warp; b is staged in shared memory
-__global__ void k_band_solve(const double* ab, const int* ipiv, double* bg, int n, int kl, int ku) {
+// DGBTRS (forward substitution with the row interchanges and L, back substitution with U) on one
+// right-hand side.  The substitutions are sequential over the n columns, so one warp carries
+// them, its lanes splitting each column's band update; the band columns (and pivots) a chunk of
+// steps needs are staged in shared memory by the whole CTA beforehand, so each step works from
+// shared memory instead of waiting on a global load.  Same operations in the same order as the
+// column-by-column DGBTRS.
+constexpr int kBsChunk = 32, kBsThreads = 128;
+__host__ __device__ constexpr size_t band_solve_smem(int n, int kl, int ku) {
+    return sizeof(double) * ((size_t)n + (size_t)kBsChunk * (kl + ku + 1)) + sizeof(int) * kBsChunk;
+}
+__global__ void __launch_bounds__(kBsThreads) k_band_solve(const double* ab, const int* ipiv, double* bg, int n, int kl,
+                                                         int ku) {
     extern __shared__ double b[];
-    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1, lane = threadIdx.x;
-    for (int q = lane; q < n; q += 32) b[q] = bg[q];
-    __syncwarp();
+    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1, kp1 = kl + ku + 1, k = kl + ku;
+    double* cb = b + n;
+    int* cp = reinterpret_cast<int*>(cb + (size_t)kBsChunk * kp1);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int q = tid; q < n; q += kBsThreads) b[q] = bg[q];
 #define AB(r, c) ab[(size_t)((r) - 1) + (size_t)((c) - 1) * (size_t)ldab]
-    for (int j = 1; j <= n - 1; j++) {
-        int lm = kl < n - j ? kl : n - j;
-        int l = ipiv[j - 1];
-        if (l != j && lane == 0) { double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
-        __syncwarp();
-        double bj = b[j - 1];
-        if (bj != 0.0) {
-            double temp = -1.0 * bj;
-            for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + AB(kd + i, j) * temp;
+    // forward: columns 1..n-1, rows kd+1..kd+kl of each (the multipliers of L)
+    for (int c0 = 1; c0 <= n - 1; c0 += kBsChunk) {
+        const int cn = min(kBsChunk, n - c0);
+        __syncthreads();
+        for (int q = tid; q < cn * kl; q += kBsThreads) cb[q] = AB(kd + 1 + q % kl, c0 + q / kl);
+        for (int q = tid; q < cn; q += kBsThreads) cp[q] = ipiv[c0 + q - 1];
+        __syncthreads();
+        if (warp == 0) {
+            for (int jj = 0; jj < cn; jj++) {
+                const int j = c0 + jj;
+                const int lm = kl < n - j ? kl : n - j;
+                const int l = cp[jj];
+                if (l != j && lane == 0) { double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
+                __syncwarp();
+                const double bj = b[j - 1];
+                if (bj != 0.0) {
+                    const double temp = -1.0 * bj;
+                    for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + cb[jj * kl + i - 1] * temp;
+                }
+                __syncwarp();
+            }
         }
-        __syncwarp();
     }
-    const int k = kl + ku, kp1 = k + 1;
-    for (int j = n; j >= 1; j--) {
-        double bj = b[j - 1];
-        if (bj != 0.0) {
-            double x = bj / AB(kp1, j);
-            __syncwarp();
-            if (lane == 0) b[j - 1] = x;
-            int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
-            for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * AB(l + i, j);
+    // back substitution: columns n..1, rows 1..kp1 of each (U, diagonal in row kp1)
+    for (int c1 = n; c1 >= 1; c1 -= kBsChunk) {
+        const int cn = min(kBsChunk, c1);
+        __syncthreads();
+        for (int q = tid; q < cn * kp1; q += kBsThreads) cb[q] = AB(1 + q % kp1, c1 - q / kp1);
+        __syncthreads();
+        if (warp == 0) {
+            for (int jj = 0; jj < cn; jj++) {
+                const int j = c1 - jj;
+                const double* col = cb + (size_t)jj * kp1;  // col[r - 1] = AB(r, j)
+                const double bj = b[j - 1];
+                if (bj != 0.0) {
+                    const double x = bj / col[kp1 - 1];
+                    __syncwarp();
+                    if (lane == 0) b[j - 1] = x;
+                    const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+                    for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * col[l + i - 1];
+                }
+                __syncwarp();
+            }
         }
-        __syncwarp();
     }
 #undef AB
-    for (int q = lane; q < n; q += 32) bg[q] = b[q];
+    __syncthreads();
+    for (int q = tid; q < n; q += kBsThreads) bg[q] = b[q];
 }
 
 // Explicit inverse of the factored coarse matrix, G = (P L U)^{-1}.  Warp w of a block carries
@@ -866,12 +987,12 @@ int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, co
 static int coarse_solve(Engine& E) {
     const int L = E.grids, n = E.ngc;
     const Geo& g = E.gl[L];
-    if (E.Ginv && E.cfg.precision == PT_PREC_MIXED) {
+    if (E.Ginv) {
         if (int rc = coarse_apply(E, E.err[L], nullptr, E.RHS[L], nullptr)) return rc;
         return enforce_bcs_stream(E, L, E.err[L]);
     }
     PT_COUNT(), k_coarse_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.RHS[L], E.RowB, g, g.nx, g.nz);
-    PT_COUNT(), k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
+    PT_COUNT(), k_band_solve<<<1, kBsThreads, band_solve_smem(n, E.kl, E.ku), E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
     PT_COUNT(), k_coarse_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.err[L], E.Bc, g, g.nx, g.nz);
     CKL("coarse solve");
     return enforce_bcs_stream(E, L, E.err[L]);
@@ -880,23 +1001,20 @@ static int coarse_solve(Engine& E) {
 // helpers shared with the mixed-precision solver (pt_mixed.cu)
 int coarse_band_solve(Engine& E) {
     const int n = E.ngc;
-    PT_COUNT(), k_band_solve<<<1, 32, sizeof(double) * n, E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
+    PT_COUNT(), k_band_solve<<<1, kBsThreads, band_solve_smem(n, E.kl, E.ku), E.st>>>(E.Mc, E.ipiv, E.Bc, n, E.kl, E.ku);
     CKL("k_band_solve");
     return 0;
 }
 
 int residual_level1_nosum(Engine& E) {
-    const Geo& g = E.gl[1];
-    dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
-    PT_COUNT(), k_residual<<<gs, 128, 0, E.st>>>(E.res[1], E.err[1], stream_op(E, 1), g, 1, E.cfg.ivis);
+    launch_residual(E, 1, E.res[1], E.err[1], stream_op(E, 1));
     CKL("k_residual");
     return 0;
 }
 
 int residual_level1(Engine& E) {
     const Geo& g = E.gl[1];
-    dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
-    PT_COUNT(), k_residual<<<gs, 128, 0, E.st>>>(E.res[1], E.err[1], stream_op(E, 1), g, 1, E.cfg.ivis);
+    launch_residual(E, 1, E.res[1], E.err[1], stream_op(E, 1));
     CKL("k_residual");
     return reduce_sum_abs_interior(E, E.res[1], g.nx, g.nz, g.pitch, E.dscal + 8);
 }
@@ -1057,6 +1175,7 @@ int mg_alloc(Engine& E) {
     }
     for (int q = 0; q < 11; q++)
         if (int rc = alloc(&E.visw[q], E.gl[1].elems())) return rc;
+    E.res_int = exact_stencils_setup(E);
     int ldab = 2 * E.kl + E.ku + 1;
     if (int rc = alloc(&E.Mc, (size_t)ldab * E.ngc)) return rc;
     if (int rc = alloc(&E.Bc, E.ngc)) return rc;
@@ -1064,12 +1183,16 @@ int mg_alloc(Engine& E) {
     CK(cudaMalloc(&E.ipiv, sizeof(int) * E.ngc));
     const size_t smem = sizeof(double) * (size_t)E.ngc;
     if (smem > 220 * 1024) return fail(PT_ERR_CONFIG, "coarsest grid too large for the banded solve");
-    CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (band_solve_smem(E.ngc, E.kl, E.ku) > 220 * 1024)
+        return fail(PT_ERR_CONFIG, "coarsest grid too large for the banded solve");
+    CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)band_solve_smem(E.ngc, E.kl, E.ku)));
     CK(cudaFuncSetAttribute(k_coarse_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_coarse_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    // explicit coarse inverse for the mixed-precision cycle: n^2 doubles, kept while it is small
-    // next to the level arrays (n <= 4096: <= 134 MB)
-    if (E.cfg.precision == PT_PREC_MIXED && E.ngc <= 4096 && inv_smem(E.ngc, E.kl, E.ku) <= 200 * 1024) {
+    // explicit coarse inverse (both precisions): the coarse solve becomes a GEMV spread over the
+    // SMs instead of two sequential banded substitutions on one warp of this part's narrow FP64
+    // pipe; n^2 doubles, kept while it is small next to the level arrays (n <= 4096: <= 134 MB)
+    if (E.ngc <= 4096 && inv_smem(E.ngc, E.kl, E.ku) <= 200 * 1024) {
         CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
         E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
         CK(cudaMalloc(&E.Ginv2, sizeof(double) * (size_t)E.ngc * E.ngc));
@@ -1142,8 +1265,7 @@ int coarse_scale_fit(Engine& E, double* alpha) {
                                                                                    gc.nz, 1 << (L - 1));
     CKL("k_inject");
     if (int rc = enforce_bcs_stream(E, L, E.err[L])) return rc;
-    PT_COUNT(), k_residual<<<dim3(nblk(gc.nx - 1, 128), gc.nz - 1), 128, 0, E.st>>>(E.res[L], E.err[L], stream_op(E, L),
-                                                                                     gc, L, E.cfg.ivis);
+    launch_residual(E, L, E.res[L], E.err[L], stream_op(E, L));
     PT_COUNT(), k_fit_rows<<<gc.nz - 1, 128, 0, E.st>>>(E.RHS[L], E.res[L], gc, gc.nx, E.red);
     CKL("coarse_scale_fit");
     std::vector<double> part(2 * (size_t)(gc.nz - 1));

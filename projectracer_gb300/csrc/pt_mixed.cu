@@ -18,6 +18,7 @@
 #include <utility>
 
 #include "pt_consts.cuh"
+#include "pt_exact.cuh"
 
 namespace pt {
 
@@ -241,198 +242,25 @@ __global__ void __launch_bounds__(128) k_residual64(double* __restrict__ res, co
 }
 
 // ---------------------------------------------------------------- level-1 residual, exact sums
-// r = RHS - A x with the stencil sums of A formed exactly in integer arithmetic.  The reference's
-// finite-difference weights are small rationals (D1 = [1,-8,0,8,-1]/12, D2 = [-1,16,-30,16,-1]/12,
-// D3 = [1,-8,13,0,-13,8,-1]/8, D4 = [-1,12,-39,56,-39,12,-1]/6, checked against the FP64 weights
-// at setup), so with x in fixed point every derivative sum is an integer.  A CTA stages its tile
-// of x (plus the 3-node halo) in shared memory as X = round(x 2^s), s chosen from the tile's
-// largest exponent so that |X| < 2^62, split as X = Xh 2^31 + Xl (Xl in [0, 2^31)); each sum is
-// accumulated exactly on both halves in 64-bit integers.  Only the final combination with the
-// viscosity fields is FP64 arithmetic (about 16 operations per node instead of about 120), and the
-// result is at least as accurate as the FP64 stencil: the sums are exact and the fixed-point
-// rounding of x is 2^-62 of the tile's largest value.
-static __constant__ int cD1i[5], cD2i[5], cD3i[7], cD4i[7];
-
-constexpr int kRfTX = 32, kRfTZ = 16, kRfH = 3;
-constexpr int kRfW = kRfTX + 2 * kRfH, kRfHt = kRfTZ + 2 * kRfH;
-
-// v * 2^e2 as a double, exactly (|v| < 2^53, result normal), from integer operations only
-__device__ __forceinline__ double i64_to_double_scaled(long long v, int e2) {
-    if (v == 0) return 0.0;
-    const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
-    const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-    const int lz = __clzll(a);                      // a < 2^53: lz >= 11
-    const unsigned long long mant = a << (lz - 11);  // leading one at bit 52
-    const unsigned long long ex = (unsigned long long)(1023 + 63 - lz + e2);
-    if ((long long)ex <= 0) return 0.0;  // below the normal range (x itself near underflow)
-    return __longlong_as_double((long long)(sgn | (ex << 52) | (mant & 0xFFFFFFFFFFFFFull)));
-}
-
-struct HL {
-    long long h, l;
-};
-__device__ __forceinline__ void mac(HL& a, int c, int2 v) {
-    a.h += (long long)c * v.x;
-    a.l += (long long)c * v.y;
-}
-__device__ __forceinline__ void mac64(HL& a, int c, const HL& v) {
-    a.h += (long long)c * v.h;
-    a.l += (long long)c * v.l;
-}
-// (h 2^31 + l) 2^-s, rounded once
-__device__ __forceinline__ double hl_value(const HL& a, int s) {
-    return i64_to_double_scaled(a.h, 31 - s) + i64_to_double_scaled(a.l, -s);
-}
-
+// r = RHS - A x with the stencil sums of A formed exactly in integer arithmetic (pt_exact.cuh):
+// about 16 FP64 operations per node instead of about 120, at least as accurate as the FP64 stencil.
 template <bool SQUARE>
 __global__ void __launch_bounds__(256) k_residual_fx(double* __restrict__ res, const double* __restrict__ x, DOp op,
                                                      Geo g, int nx, int nz, int ivis, ResFxK K) {
-    __shared__ int2 X[kRfHt][kRfW];  // (Xh, Xl)
+    __shared__ int2 X[kRfHt][kRfW];
     __shared__ int emax_s;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kRfTX + tx;
-    const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;  // first interior node of the tile
-    if (tid == 0) emax_s = 0;
-    __syncthreads();
-    // stage the tile's raw bit patterns (nodes i0-3 .. i0+TX+2; beyond nx+3 / nz+3: zero)
-    unsigned long long raw[(kRfW * kRfHt + 255) / 256];
-    int em = 0;
-#pragma unroll
-    for (int q = 0; q < (kRfW * kRfHt + 255) / 256; q++) {
-        const int idx = tid + 256 * q;
-        unsigned long long b = 0;
-        if (idx < kRfW * kRfHt) {
-            const int i = i0 - kRfH + idx % kRfW, k = k0 - kRfH + idx / kRfW;
-            if (i <= nx + kRfH && k <= nz + kRfH) b = (unsigned long long)__double_as_longlong(x[g.at(i, k)]);
-        }
-        raw[q] = b;
-        em = max(em, (int)((b >> 52) & 0x7FF));
-    }
-    atomicMax(&emax_s, em);
-    __syncthreads();
-    const int emax = emax_s;
-    const int s = 1084 - emax;  // |x| < 2^(emax-1022): |x| 2^s < 2^62
-#pragma unroll
-    for (int q = 0; q < (kRfW * kRfHt + 255) / 256; q++) {
-        const int idx = tid + 256 * q;
-        if (idx >= kRfW * kRfHt) break;
-        const unsigned long long b = raw[q];
-        const int e = (int)((b >> 52) & 0x7FF);
-        long long v = 0;
-        if (e != 0) {
-            const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-            const int sh = emax - 9 - e;  // X = m 2^-sh
-            unsigned long long a;
-            if (sh <= 0) a = m << (-sh);
-            else if (sh < 64) a = (m + (1ull << (sh - 1))) >> sh;
-            else a = 0;
-            v = (b >> 63) ? -(long long)a : (long long)a;
-        }
-        const long long h = v >> 31;  // floor
-        X[idx / kRfW][idx % kRfW] = make_int2((int)h, (int)(v - (h << 31)));
-    }
-    __syncthreads();
+    const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
+    const int emax = load_tile_fx(X, &emax_s, x, g, i0, k0, nx, nz);
 #pragma unroll 1
     for (int r = 0; r < 2; r++) {
-        const int lz = ty + 8 * r, lx = tx;  // tile-local node
+        const int lz = threadIdx.y + 8 * r, lx = threadIdx.x;
         const int i = i0 + lx, k = k0 + lz;
         if (i > nx - 1 || k > nz - 1) continue;
-        const int cx = lx + kRfH, cz = lz + kRfH;
-        HL I2x{0, 0}, I3x{0, 0}, I4x{0, 0}, I2z{0, 0}, I3z{0, 0}, I4z{0, 0};
-#pragma unroll
-        for (int j = 0; j < 7; j++) {
-            const int2 vx = X[cz][cx + j - 3], vz = X[cz + j - 3][cx];
-            if (j >= 1 && j <= 5) { mac(I2x, cD2i[j - 1], vx); mac(I2z, cD2i[j - 1], vz); }
-            if (j != 3) { mac(I3x, cD3i[j], vx); mac(I3z, cD3i[j], vz); }
-            mac(I4x, cD4i[j], vx);
-            mac(I4z, cD4i[j], vz);
-        }
-        HL I11{0, 0}, I12{0, 0}, I21{0, 0}, I22{0, 0};  // I<x order><z order>
-#pragma unroll
-        for (int kk = 0; kk < 5; kk++) {
-            HL d1{0, 0}, d2{0, 0};
-#pragma unroll
-            for (int ii = 0; ii < 5; ii++) {
-                const int2 v = X[cz + kk - 2][cx + ii - 2];
-                if (ii != 2) mac(d1, cD1i[ii], v);
-                mac(d2, cD2i[ii], v);
-            }
-            if (kk != 2) { mac64(I11, cD1i[kk], d1); mac64(I21, cD1i[kk], d2); }
-            mac64(I12, cD2i[kk], d1);
-            mac64(I22, cD2i[kk], d2);
-        }
         const size_t o = g.at(i, k);
-        if (emax == 0x7FF) {  // Inf/NaN in the tile: propagate, the solve's finiteness test stops it
-            res[o] = __longlong_as_double(0x7FF8000000000000ll);
-            continue;
-        }
-        double acc;
-        if (SQUARE) {
-            // vis (Sxxxx + Szzzz + 2 Sxxzz) = vis (24 I4x + 24 I4z + 2 I22) / (144 h^4), etc.
-            HL ga{24 * (I4x.h + I4z.h) + 2 * I22.h, 24 * (I4x.l + I4z.l) + 2 * I22.l};
-            acc = K.k[0] * op.vis[o] * hl_value(ga, s);
-            if (ivis != 0) {
-                HL gb{I2x.h - I2z.h, I2x.l - I2z.l};
-                HL gd{18 * I3x.h + I12.h, 18 * I3x.l + I12.l};
-                HL ge{18 * I3z.h + I21.h, 18 * I3z.l + I21.l};
-                acc = fma(K.k[1] * op.vxxmzz[o], hl_value(gb, s), acc);
-                acc = fma(K.k[2] * op.vxz[o], hl_value(I11, s), acc);
-                acc = fma(K.k[3] * op.vx[o], hl_value(gd, s), acc);
-                acc = fma(K.k[4] * op.vz[o], hl_value(ge, s), acc);
-            }
-        } else {
-            // k: [Sxxxx, Szzzz, Sxxzz, Sxx, Szz, Sxz, Sxxx, Sxzz, Szzz, Sxxz] weights
-            const double Sxxxx = K.k[0] * hl_value(I4x, s), Szzzz = K.k[1] * hl_value(I4z, s);
-            const double Sxxzz = K.k[2] * hl_value(I22, s);
-            acc = op.vis[o] * (Sxxxx + Szzzz + 2.0 * Sxxzz);
-            if (ivis != 0) {
-                const double Sxx = K.k[3] * hl_value(I2x, s), Szz = K.k[4] * hl_value(I2z, s);
-                const double Sxz = K.k[5] * hl_value(I11, s);
-                const double Sxxx = K.k[6] * hl_value(I3x, s), Sxzz = K.k[7] * hl_value(I12, s);
-                const double Szzz = K.k[8] * hl_value(I3z, s), Sxxz = K.k[9] * hl_value(I21, s);
-                acc += op.vxxmzz[o] * (Sxx - Szz) + 4.0 * op.vxz[o] * Sxz + 2.0 * op.vx[o] * (Sxxx + Sxzz) +
-                       2.0 * op.vz[o] * (Szzz + Sxxz);
-            }
-        }
+        const double acc = tile_apply_A<SQUARE>(X, lx + kRfH, lz + kRfH, emax, op.vis, op.vx, op.vz, op.vxz, op.vxxmzz,
+                                                o, ivis, K);
         res[o] = op.rhs[o] - acc;
     }
-}
-
-// Integer forms of the stencils and the per-group weights of level 1; false (and the FP64
-// residual is used) when the weights are not the rationals above.
-bool residual_fx_setup(Engine& E) {
-    const Consts& K = E.K;
-    const int d1[5] = {1, -8, 0, 8, -1}, d2[5] = {-1, 16, -30, 16, -1};
-    const int d3[7] = {1, -8, 13, 0, -13, 8, -1}, d4[7] = {-1, 12, -39, 56, -39, 12, -1};
-    for (int j = 0; j < 5; j++)
-        if (std::fabs(12.0 * K.D1[j + 1] - d1[j]) > 1e-9 || std::fabs(12.0 * K.D2[j + 1] - d2[j]) > 1e-9) return false;
-    for (int j = 0; j < 7; j++)
-        if (std::fabs(8.0 * K.D3[j] - d3[j]) > 1e-9 || std::fabs(6.0 * K.D4[j] - d4[j]) > 1e-9) return false;
-    if (cudaMemcpyToSymbol(cD1i, d1, sizeof d1) != cudaSuccess || cudaMemcpyToSymbol(cD2i, d2, sizeof d2) != cudaSuccess ||
-        cudaMemcpyToSymbol(cD3i, d3, sizeof d3) != cudaSuccess || cudaMemcpyToSymbol(cD4i, d4, sizeof d4) != cudaSuccess)
-        return false;
-    const LevConst& L = E.L[1];
-    ResFxK& R = E.resfx;
-    R.square = L.dr == L.ds ? 1 : 0;
-    if (R.square) {
-        const double h = L.dr;
-        R.k[0] = 1.0 / (144.0 * h * h * h * h);
-        R.k[1] = 1.0 / (12.0 * h * h);
-        R.k[2] = 4.0 / (144.0 * h * h);
-        R.k[3] = 2.0 / (144.0 * h * h * h);
-        R.k[4] = 2.0 / (144.0 * h * h * h);
-    } else {
-        R.k[0] = 1.0 / (6.0 * L.dr4);
-        R.k[1] = 1.0 / (6.0 * L.ds4);
-        R.k[2] = 1.0 / (144.0 * L.dr2ds2);
-        R.k[3] = 1.0 / (12.0 * L.dr2);
-        R.k[4] = 1.0 / (12.0 * L.ds2);
-        R.k[5] = 1.0 / (144.0 * L.drds);
-        R.k[6] = 1.0 / (8.0 * L.dr3);
-        R.k[7] = 1.0 / (144.0 * L.drds2);
-        R.k[8] = 1.0 / (8.0 * L.ds3);
-        R.k[9] = 1.0 / (144.0 * L.dr2ds);
-    }
-    return true;
 }
 
 // Residual after the level-1 pre-smoothing, updated instead of recomputed: r -= A e with the
@@ -555,9 +383,9 @@ static int residual64(Engine& E, bool want_sum) {
     DOp op{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.RHS[1]};
     if (E.res_int) {
         dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
-        auto kern = E.resfx.square ? k_residual_fx<true> : k_residual_fx<false>;
+        auto kern = E.resfx[1].square ? k_residual_fx<true> : k_residual_fx<false>;
         if (int rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.res[1], (const double*)E.err[1], op, g, g.nx,
-                                g.nz, E.cfg.ivis, E.resfx))
+                                g.nz, E.cfg.ivis, E.resfx[1]))
             return rc;
     } else {
         dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
@@ -807,7 +635,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
 }
 
 int mixed_alloc(Engine& E) {
-    E.res_int = residual_fx_setup(E);
+    if (E.res_int && !exact_stencils_setup(E)) return fail(PT_ERR_CUDA, "exact-stencil constants (mixed kernels)");
     for (int f = 0; f < 3; f++) {
         const size_t n = E.g1.elems();
         CK(cudaMalloc(&E.ftab[f], n * sizeof(float4)));

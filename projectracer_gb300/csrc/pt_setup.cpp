@@ -260,6 +260,8 @@ int setup_constants(Engine& E) {
     K.ds2 = K.ds * K.ds;
     K.inv_dr = 1.0 / K.dr;
     K.inv_ds = 1.0 / K.ds;
+    K.inv_dr2 = 1.0 / K.dr2;
+    K.inv_ds2 = 1.0 / K.ds2;
     int ex;
     K.exact_div = (std::frexp(K.dr, &ex) == 0.5 && std::frexp(K.ds, &ex) == 0.5) ? 1 : 0;
     K.p_inv_dr = K.p_inv_ds = 0;
@@ -277,6 +279,7 @@ int setup_constants(Engine& E) {
     }
     for (int j = 0; j <= 3; j++) {
         K.inv_ds_pow[j] = 1.0 / K.ds_pow[j];
+        K.inv_dr_pow[j] = 1.0 / K.dr_pow[j];
         K.inv_fact[j] = 1.0 / K.fact[j];
     }
     K.two_over_D20 = 2.0 / K.D2[3];
@@ -301,6 +304,7 @@ int setup_constants(Engine& E) {
         L.dr3 = std::pow(L.dr, 3.0); L.ds3 = std::pow(L.ds, 3.0);
         L.dr4 = std::pow(L.dr, 4.0); L.ds4 = std::pow(L.ds, 4.0);
         L.drds = L.dr * L.ds; L.drds2 = L.dr * L.ds2; L.dr2ds = L.dr2 * L.ds; L.dr2ds2 = L.dr2 * L.ds2;
+        L.idr = 1.0 / L.dr; L.ids = 1.0 / L.ds;
         L.idr2 = 1.0 / L.dr2; L.ids2 = 1.0 / L.ds2; L.idr3 = 1.0 / L.dr3; L.ids3 = 1.0 / L.ds3;
         L.idr4 = 1.0 / L.dr4; L.ids4 = 1.0 / L.ds4; L.idrds = 1.0 / L.drds; L.idrds2 = 1.0 / L.drds2;
         L.idr2ds = 1.0 / L.dr2ds; L.idr2ds2 = 1.0 / L.dr2ds2;
