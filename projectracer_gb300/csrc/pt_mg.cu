@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(256) k_coarse_apply(R* Eout, const R* RHS, con
 // FP32 rounding of G and of the sum (relative 1e-5 or so for this small, smooth inverse) leaves
 // the cycle count unchanged (measured), and the GEMV no longer runs on the FP64 pipe.
 __global__ void __launch_bounds__(256) k_coarse_apply32(float* Eout, const float* RHS, const float* G,
-                                                        const double* RowB, Geo g, int nxc, int nzc) {
+                                                        const double* RowB, Geo g, int nxc, int nzc, float sz) {
     extern __shared__ float bsf[];
     const int N = nzc + 1, n = (nxc + 1) * N;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
@@ -892,7 +892,25 @@ __global__ void __launch_bounds__(256) k_coarse_apply32(float* Eout, const float
     float a = 0.0f;
     for (int q = lane; q < n; q += 32) a = fmaf(row[q], bsf[q], a);
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if (lane == 0) Eout[g.at(p / N, p % N)] = a;
+    if (lane != 0) return;
+    // the correction with its boundary values: wall nodes zero, interior nodes with their free-slip
+    // images (antisymmetric across the side walls, sign sz across top and bottom)
+    const int ip = p / N, kp = p % N;
+    if (ip == 0 || ip == nxc || kp == 0 || kp == nzc) {
+        Eout[g.at(ip, kp)] = 0.0f;
+        return;
+    }
+    int xs[3], zs[3];
+    float xf[3], zf[3];
+    int nxp = 0, nzp = 0;
+    xs[nxp] = ip; xf[nxp++] = 1.0f;
+    if (ip <= 3) { xs[nxp] = -ip; xf[nxp++] = -1.0f; }
+    if (ip >= nxc - 3) { xs[nxp] = 2 * nxc - ip; xf[nxp++] = -1.0f; }
+    zs[nzp] = kp; zf[nzp++] = 1.0f;
+    if (kp <= 3) { zs[nzp] = -kp; zf[nzp++] = sz; }
+    if (kp >= nzc - 3) { zs[nzp] = 2 * nzc - kp; zf[nzp++] = sz; }
+    for (int u = 0; u < nxp; u++)
+        for (int v = 0; v < nzp; v++) Eout[g.at(xs[u], zs[v])] = (xf[u] * zf[v]) * a;
 }
 
 __global__ void k_g_to_f32(float* out, const double* in, size_t n) {
@@ -979,7 +997,8 @@ int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, co
     const unsigned blocks = nblk(n, 8);
     const size_t smem = sizeof(double) * (size_t)n;
     if (out64) PT_COUNT(), k_coarse_apply<double><<<blocks, 256, smem, E.st>>>(out64, rhs64, E.Ginv, E.RowB, g, g.nx, g.nz);
-    else PT_COUNT(), k_coarse_apply32<<<blocks, 256, smem / 2, E.st>>>(out32, rhs32, E.Gf, E.RowB, g, g.nx, g.nz);
+    else PT_COUNT(), k_coarse_apply32<<<blocks, 256, smem / 2, E.st>>>(out32, rhs32, E.Gf, E.RowB, g, g.nx, g.nz,
+                                                                       E.cfg.Vbc == 0 ? -1.f : 1.f);
     CKL("k_coarse_apply");
     return 0;
 }

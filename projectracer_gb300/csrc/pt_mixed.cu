@@ -181,13 +181,9 @@ __device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, co
 // right-hand side itself (the ZERO variant also clears Y_0's interior node, so no separate
 // clearing pass is needed).
 template <bool ZERO>
-__global__ void __launch_bounds__(256) k_rkc_first_f(float* __restrict__ D1, float* __restrict__ F0,
-                                                     float* __restrict__ Y0, FOp op, Geo g, int l, int nx,
-                                                     int nz, float mewtc, int ivis, float sz) {
-    pdl_begin();
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i > nx - 1 || k > nz - 1) return;
-    size_t o = g.at(i, k);
+__device__ __forceinline__ void rkc_first_node(float* D1, float* F0, float* Y0, const FOp& op, Geo g, int l, int nx,
+                                               int nz, float mewtc, int ivis, float sz, int i, int k) {
+    const size_t o = g.at(i, k);
     float F;
     if (ZERO) {
         F = op.rhs[o];
@@ -197,6 +193,33 @@ __global__ void __launch_bounds__(256) k_rkc_first_f(float* __restrict__ D1, flo
     }
     F0[o] = F;
     store_ghosts_f(D1, g, i, k, nx, nz, mewtc * op.dtst[o] * F, sz);
+}
+
+template <bool ZERO>
+__global__ void __launch_bounds__(256) k_rkc_first_f(float* __restrict__ D1, float* __restrict__ F0,
+                                                     float* __restrict__ Y0, FOp op, Geo g, int l, int nx,
+                                                     int nz, float mewtc, int ivis, float sz) {
+    pdl_begin();
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    rkc_first_node<ZERO>(D1, F0, Y0, op, g, l, nx, nz, mewtc, ivis, sz, i, k);
+}
+
+template <typename R>
+__device__ __forceinline__ float restrict_node(const R* in, Geo gf, int i, int k);
+
+// the restriction of the finer level's residual (full weighting) fused into the zero-start first
+// stage of the level it lands on: writes that level's RHS and runs rkc_first_node<true>
+template <typename R>
+__global__ void __launch_bounds__(256) k_restrict_first_f(float* __restrict__ D1, float* __restrict__ F0,
+                                                          float* __restrict__ Y0, float* __restrict__ rhs, const R* fine,
+                                                          Geo gf, FOp op, Geo g, int l, int nx, int nz, float mewtc,
+                                                          int ivis, float sz) {
+    pdl_begin();
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    rhs[g.at(i, k)] = restrict_node(fine, gf, i, k);
+    rkc_first_node<true>(D1, F0, Y0, op, g, l, nx, nz, mewtc, ivis, sz, i, k);
 }
 
 // stage j >= 2: out may alias Dm2 (each thread reads Dm2 only at its own interior node).
@@ -245,8 +268,9 @@ __global__ void __launch_bounds__(128) k_residual64(double* __restrict__ res, co
 // r = RHS - A x with the stencil sums of A formed exactly in integer arithmetic (pt_exact.cuh):
 // about 16 FP64 operations per node instead of about 120, at least as accurate as the FP64 stencil.
 template <bool SQUARE>
-__global__ void __launch_bounds__(256) k_residual_fx(double* __restrict__ res, const double* __restrict__ x, DOp op,
-                                                     Geo g, int nx, int nz, int ivis, ResFxK K) {
+__global__ void __launch_bounds__(256) k_residual_fx(double* __restrict__ res, float* __restrict__ res32,
+                                                     const double* __restrict__ x, DOp op, Geo g, int nx, int nz,
+                                                     int ivis, ResFxK K) {
     __shared__ int2 X[kRfHt][kRfW];
     __shared__ int emax_s;
     const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
@@ -259,7 +283,9 @@ __global__ void __launch_bounds__(256) k_residual_fx(double* __restrict__ res, c
         const size_t o = g.at(i, k);
         const double acc = tile_apply_A<SQUARE>(X, lx + kRfH, lz + kRfH, emax, op.vis, op.vx, op.vz, op.vxz, op.vxxmzz,
                                                 o, ivis, K);
-        res[o] = op.rhs[o] - acc;
+        const double rv = op.rhs[o] - acc;
+        res[o] = rv;
+        if (res32) res32[o] = (float)rv;  // the FP32 right-hand side of the level-1 correction
     }
 }
 
@@ -279,28 +305,38 @@ __global__ void __launch_bounds__(128) k_residual_update(double* __restrict__ re
 // full weighting (restrict, iterative_solver.f90:398-418) into FP32; R = double restricts the
 // FP64 level-1 residual directly
 template <typename R>
+__device__ __forceinline__ float restrict_node(const R* in, Geo gf, int i, int k) {
+    const int ii = 2 * i, kk = 2 * k;
+    R corners = (in[gf.at(ii - 1, kk - 1)] + in[gf.at(ii - 1, kk + 1)] + in[gf.at(ii + 1, kk + 1)] + in[gf.at(ii + 1, kk - 1)]) * (R)0.0625;
+    R sides = (in[gf.at(ii - 1, kk)] + in[gf.at(ii, kk - 1)] + in[gf.at(ii + 1, kk)] + in[gf.at(ii, kk + 1)]) * (R)0.125;
+    return (float)(corners + sides + in[gf.at(ii, kk)] * (R)0.25);
+}
+
+template <typename R>
 __global__ void k_restrict_f(float* out, const R* in, Geo gc, Geo gf, int nxc, int nzc) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxc - 1) return;
-    int ii = 2 * i, kk = 2 * k;
-    R corners = (in[gf.at(ii - 1, kk - 1)] + in[gf.at(ii - 1, kk + 1)] + in[gf.at(ii + 1, kk + 1)] + in[gf.at(ii + 1, kk - 1)]) * (R)0.0625;
-    R sides = (in[gf.at(ii - 1, kk)] + in[gf.at(ii, kk - 1)] + in[gf.at(ii + 1, kk)] + in[gf.at(ii, kk + 1)]) * (R)0.125;
-    out[gc.at(i, k)] = (float)(corners + sides + in[gf.at(ii, kk)] * (R)0.25);
+    out[gc.at(i, k)] = restrict_node(in, gf, i, k);
 }
 
-__global__ void k_prolong_f(float* F, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
+// bilinear prolongation of the coarse correction C at fine node (i,k)
+__device__ __forceinline__ float prolong_value(const float* C, Geo gc, int i, int k) {
+    if (!(i & 1) && !(k & 1)) return C[gc.at(i / 2, k / 2)];
+    if (!(i & 1)) return (C[gc.at(i / 2, (k - 1) / 2)] + C[gc.at(i / 2, (k + 1) / 2)]) * 0.5f;
+    if (!(k & 1)) return (C[gc.at((i - 1) / 2, k / 2)] + C[gc.at((i + 1) / 2, k / 2)]) * 0.5f;
+    return (C[gc.at((i - 1) / 2, (k - 1) / 2)] + C[gc.at((i + 1) / 2, (k - 1) / 2)] + C[gc.at((i + 1) / 2, (k + 1) / 2)] +
+            C[gc.at((i - 1) / 2, (k + 1) / 2)]) * 0.25f;
+}
+
+// the prolongation added to F followed by F's boundary values (k_stream_bcs_f), in one pass: each
+// interior node writes its mirror images; the wall nodes and the images of wall nodes are zero
+// (nothing else writes them), which is what the boundary pass would set
+__global__ void k_prolong_bc_f(float* F, const float* C, Geo gf, Geo gc, int nxf, int nzf, float sz) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxf - 1) return;
-    float add;
-    if (!(i & 1) && !(k & 1)) add = C[gc.at(i / 2, k / 2)];
-    else if (!(i & 1)) add = (C[gc.at(i / 2, (k - 1) / 2)] + C[gc.at(i / 2, (k + 1) / 2)]) * 0.5f;
-    else if (!(k & 1)) add = (C[gc.at((i - 1) / 2, k / 2)] + C[gc.at((i + 1) / 2, k / 2)]) * 0.5f;
-    else
-        add = (C[gc.at((i - 1) / 2, (k - 1) / 2)] + C[gc.at((i + 1) / 2, (k - 1) / 2)] + C[gc.at((i + 1) / 2, (k + 1) / 2)] +
-               C[gc.at((i - 1) / 2, (k + 1) / 2)]) * 0.25f;
-    F[gf.at(i, k)] += add;
+    store_ghosts_f(F, gf, i, k, nxf, nzf, F[gf.at(i, k)] + prolong_value(C, gc, i, k), sz);
 }
 
 __global__ void k_stream_bcs_f(float* S, Geo g, int nx, int nz, float sz) {
@@ -337,9 +373,26 @@ __global__ void k_res_to_f32(float* out, const double* in, size_t n) {
     if (q < n) out[q] = (float)in[q];
 }
 
+// writes value v of interior node (i,k) of the FP64 iterate and its free-slip ghost images (the
+// per-node form of enforceBCs_stream: antisymmetric across the side walls, sign sz across top and
+// bottom; wall nodes and their images are zero and are not written)
+__device__ __forceinline__ void store_ghosts_d(double* out, Geo g, int i, int k, int nx, int nz, double v, double sz) {
+    int xs[3], zs[3];
+    double xf[3], zf[3];
+    int nxp = 0, nzp = 0;
+    xs[nxp] = i; xf[nxp++] = 1.0;
+    if (i <= 3) { xs[nxp] = -i; xf[nxp++] = -1.0; }
+    if (i >= nx - 3) { xs[nxp] = 2 * nx - i; xf[nxp++] = -1.0; }
+    zs[nzp] = k; zf[nzp++] = 1.0;
+    if (k <= 3) { zs[nzp] = -k; zf[nzp++] = sz; }
+    if (k >= nz - 3) { zs[nzp] = 2 * nz - k; zf[nzp++] = sz; }
+    for (int a = 0; a < nxp; a++)
+        for (int b = 0; b < nzp; b++) out[g.at(xs[a], zs[b])] = (xf[a] * zf[b]) * v;
+}
+
 // x += P e2 on the interior in FP64: the closing prolongation of a cycle (level 2 -> 1) fused
 // with the update, so the level-1 correction is never rounded to FP32
-__global__ void k_prolong_add(double* x, const float* C, Geo gf, Geo gc, int nxf, int nzf) {
+__global__ void k_prolong_add(double* x, const float* C, Geo gf, Geo gc, int nxf, int nzf, double sz) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nxf - 1) return;
@@ -351,16 +404,16 @@ __global__ void k_prolong_add(double* x, const float* C, Geo gf, Geo gc, int nxf
         add = ((double)C[gc.at((i - 1) / 2, (k - 1) / 2)] + (double)C[gc.at((i + 1) / 2, (k - 1) / 2)] +
                (double)C[gc.at((i + 1) / 2, (k + 1) / 2)] + (double)C[gc.at((i - 1) / 2, (k + 1) / 2)]) * 0.25;
     size_t o = gf.at(i, k);
-    x[o] += add;
+    store_ghosts_d(x, gf, i, k, nxf, nzf, x[o] + add, sz);
 }
 
-// x += e on the interior (FP64 accumulate of the FP32 correction)
-__global__ void k_add_correction(double* x, const float* e, Geo g, int nx, int nz) {
+// x += e on the interior (FP64 accumulate of the FP32 correction), with the ghost images
+__global__ void k_add_correction(double* x, const float* e, Geo g, int nx, int nz, double sz) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     if (i > nx - 1) return;
     size_t o = g.at(i, k);
-    x[o] += (double)e[o];
+    store_ghosts_d(x, g, i, k, nx, nz, x[o] + (double)e[o], sz);
 }
 
 __global__ void k_coarse_rhs_f(double* B, const float* R, const double* RowB, Geo g, int nxc, int nzc) {
@@ -378,20 +431,26 @@ __global__ void k_coarse_scatter_f(float* e, const double* B, Geo g, int nxc, in
 }
 
 // FP64 level-1 residual (and optionally the sum of |r| into dscal[8])
-static int residual64(Engine& E, bool want_sum) {
+static int residual64(Engine& E, bool want_sum, float* res32 = nullptr) {
     const Geo& g = E.gl[1];
     DOp op{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.RHS[1]};
     if (E.res_int) {
         dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
         auto kern = E.resfx[1].square ? k_residual_fx<true> : k_residual_fx<false>;
-        if (int rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.res[1], (const double*)E.err[1], op, g, g.nx,
-                                g.nz, E.cfg.ivis, E.resfx[1]))
+        if (int rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.res[1], res32, (const double*)E.err[1], op, g,
+                                g.nx, g.nz, E.cfg.ivis, E.resfx[1]))
             return rc;
     } else {
         dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
         if (int rc = launch_pdl("k_residual64", k_residual64, grd, blk, 0, E.st, E.res[1], (const double*)E.err[1], op, g,
                                 g.nx, g.nz, E.cfg.ivis))
             return rc;
+        if (res32) {
+            const size_t n1 = g.elems();
+            if (int rc = launch_pdl("k_res_to_f32", k_res_to_f32, dim3(nblk(n1, 256)), dim3(256), 0, E.st, res32,
+                                    (const double*)E.res[1], n1))
+                return rc;
+        }
     }
     if (want_sum) return reduce_sum_abs_interior(E, E.res[1], g.nx, g.nz, g.pitch, E.dscal + 8);
     return 0;
@@ -399,10 +458,8 @@ static int residual64(Engine& E, bool want_sum) {
 
 static int add_correction(Engine& E) {
     const Geo& g1 = E.gl[1];
-    if (int rc = launch_pdl("k_add_correction", k_add_correction, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0,
-                            E.st, E.err[1], (const float*)E.ferr[1], g1, g1.nx, g1.nz))
-        return rc;
-    return enforce_bcs_stream(E, 1, E.err[1]);
+    return launch_pdl("k_add_correction", k_add_correction, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0, E.st,
+                      E.err[1], (const float*)E.ferr[1], g1, g1.nx, g1.nz, E.cfg.Vbc == 0 ? -1.0 : 1.0);
 }
 
 static FOp fop(Engine& E, int l) {
@@ -419,7 +476,7 @@ static int bcs_f(Engine& E, int l, float* f) {
 // FP32 iterate_stream on the correction of level l, RKC1 in increment form (k_rkc_first_f).
 // zero: the correction is zero on entry (first visit after a descent); want_res: the residual is
 // needed (the next step descends).
-static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
+static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in = false) {
     const Geo& g = E.gl[l];
     const int N = E.cfg.nstageS, ivis = E.cfg.ivis;
     const float sz = E.cfg.Vbc == 0 ? -1.f : 1.f;
@@ -435,10 +492,23 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
         GraphTimer gt(E, 1, (l == 1 && zero) ? N : 0);
         float* Dm1 = E.fS1[l];
         float* Dm2 = E.fS2[l];
-        auto first = (zero && n == 1) ? k_rkc_first_f<true> : k_rkc_first_f<false>;
-        if (int rc = launch_pdl("k_rkc_first_f", first, grd, blk, 0, E.st, Dm1, F0, e, op, g, l,
-                                g.nx, g.nz, (float)(E.K.mewt[1] * c), ivis, sz))
-            return rc;
+        const float mewtc1 = (float)(E.K.mewt[1] * c);
+        if (restrict_in && zero && n == 1) {  // restriction of the finer residual fused in
+            const Geo& gf = E.gl[l - 1];
+            int rc;
+            if (l == 2)
+                rc = launch_pdl("k_restrict_first_f", k_restrict_first_f<double>, grd, blk, 0, E.st, Dm1, F0, e,
+                                E.fRHS[l], (const double*)E.res[1], gf, op, g, l, g.nx, g.nz, mewtc1, ivis, sz);
+            else
+                rc = launch_pdl("k_restrict_first_f", k_restrict_first_f<float>, grd, blk, 0, E.st, Dm1, F0, e,
+                                E.fRHS[l], (const float*)E.fres[l - 1], gf, op, g, l, g.nx, g.nz, mewtc1, ivis, sz);
+            if (rc) return rc;
+        } else {
+            auto first = (zero && n == 1) ? k_rkc_first_f<true> : k_rkc_first_f<false>;
+            if (int rc = launch_pdl("k_rkc_first_f", first, grd, blk, 0, E.st, Dm1, F0, e, op, g, l, g.nx, g.nz, mewtc1,
+                                    ivis, sz))
+                return rc;
+        }
         for (int j = 2; j <= N; j++) {
             const bool last = (j == N);
             // D_{j-2} = D_0 = 0 at j = 2; the output overwrites D_{j-2}
@@ -465,10 +535,7 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res) {
 static int coarse_solve_f(Engine& E) {
     const int L = E.grids, n = E.ngc;
     const Geo& g = E.gl[L];
-    if (E.Ginv) {
-        if (int rc = coarse_apply(E, nullptr, E.ferr[L], nullptr, E.fRHS[L])) return rc;
-        return bcs_f(E, L, E.ferr[L]);
-    }
+    if (E.Ginv) return coarse_apply(E, nullptr, E.ferr[L], nullptr, E.fRHS[L]);  // with the boundary values
     PT_COUNT(), k_coarse_rhs_f<<<nblk(n, 128), 128, 0, E.st>>>(E.Bc, E.fRHS[L], E.RowB, g, g.nx, g.nz);
     int rc = coarse_band_solve(E);
     if (rc) return rc;
@@ -485,12 +552,8 @@ static int coarse_solve_f(Engine& E) {
 static int mixed_part(Engine& E, int part) {
     int rc;
     const Geo& g1 = E.gl[1];
-    const size_t n1 = g1.elems();
     if (part == 0) {
-        if ((rc = residual64(E, false))) return rc;
-        if ((rc = launch_pdl("k_res_to_f32", k_res_to_f32, dim3(nblk(n1, 256)), dim3(256), 0, E.st, E.fRHS[1],
-                             (const double*)E.res[1], n1)))
-            return rc;
+        if ((rc = residual64(E, false, E.fRHS[1]))) return rc;
         if ((rc = smooth_f(E, 1, true, false))) return rc;
         if ((rc = add_correction(E))) return rc;
         dim3 blk(32, 4), grd(nblk(g1.nx - 1, 32), nblk(g1.nz - 1, 4));
@@ -508,7 +571,7 @@ static int mixed_part(Engine& E, int part) {
         // part 0 is already in x, so the cycle's level-1 correction is the closing prolongation
         if (l == 1) return fail(PT_ERR_CONFIG, "mixed-precision cycle: schedule revisits level 1");
         const bool descend = multi[p - 1] < multi[p];
-        if (descend) {
+        if (descend && l == grids) {  // (above the coarsest level the restriction is fused into smooth_f)
             const Geo& gf = E.gl[l - 1];
             dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
             // the correction of level l restarts from zero: cleared by the first smoothing stage
@@ -522,22 +585,21 @@ static int mixed_part(Engine& E, int part) {
             if (rc) return rc;
         }
         if (l < grids) {
-            if ((rc = smooth_f(E, l, descend, multi[p + 1] > multi[p]))) return rc;
+            if ((rc = smooth_f(E, l, descend, multi[p + 1] > multi[p], descend))) return rc;
         } else if ((rc = coarse_solve_f(E))) {
             return rc;
         }
         if (multi[p + 1] < multi[p]) {
             if (l == 2) {  // closing prolongation, added to x in FP64
-                if ((rc = launch_pdl("k_prolong_add", k_prolong_add, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0,
-                                     E.st, E.err[1], (const float*)E.ferr[2], g1, g, g1.nx, g1.nz)))
-                    return rc;
-                return enforce_bcs_stream(E, 1, E.err[1]);
+                return launch_pdl("k_prolong_add", k_prolong_add, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0,
+                                  E.st, E.err[1], (const float*)E.ferr[2], g1, g, g1.nx, g1.nz,
+                                  E.cfg.Vbc == 0 ? -1.0 : 1.0);
             }
             const Geo& gf = E.gl[l - 1];
-            if ((rc = launch_pdl("k_prolong_f", k_prolong_f, dim3(nblk(gf.nx - 1, 128), gf.nz - 1), dim3(128), 0, E.st,
-                                 E.ferr[l - 1], (const float*)E.ferr[l], gf, g, gf.nx, gf.nz)))
+            if ((rc = launch_pdl("k_prolong_bc_f", k_prolong_bc_f, dim3(nblk(gf.nx - 1, 128), gf.nz - 1), dim3(128), 0,
+                                 E.st, E.ferr[l - 1], (const float*)E.ferr[l], gf, g, gf.nx, gf.nz,
+                                 E.cfg.Vbc == 0 ? -1.f : 1.f)))
                 return rc;
-            if ((rc = bcs_f(E, l - 1, E.ferr[l - 1]))) return rc;
         }
     }
     return fail(PT_ERR_CONFIG, "mixed-precision cycle: schedule does not return to level 1");
@@ -582,6 +644,9 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
         }
         CKL("k_coef_to_f32");
     }
+    // the level-1 updates write each node's ghost images and never the wall nodes: start from an
+    // iterate whose walls and images are consistent (a restart's psi may not be)
+    if ((rc = enforce_bcs_stream(E, 1, E.err[1]))) return rc;
     const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int cycles = 0;
     double mag1 = 0.0;
