@@ -14,7 +14,7 @@
 namespace pt {
 
 Engine* g_eng = nullptr;
-int64_t g_launches = 0;
+std::atomic<int64_t> g_launches{0};
 thread_local std::string g_err;
 
 int upload_consts_fields(const Engine& E);
@@ -160,7 +160,21 @@ static void engine_free(Engine& E) {
     for (auto a : ia)
         if (a) cudaFree(a);
     if (E.ipiv) cudaFree(E.ipiv);
+    if (E.job_active) {  // a coarse-level build may still be running on the worker thread
+        E.coarse_job.join();
+        E.job_active = false;
+    }
     if (E.st2) cudaStreamSynchronize(E.st2);  // a factorisation may still be in flight
+    for (int l = 1; l < PT_MAXLEV; l++) {
+        double** sets[kVisArrays] = {E.vl2.vis, E.vl2.visst, E.vl2.vx, E.vl2.vz, E.vl2.vxx, E.vl2.vzz, E.vl2.vxz,
+                                     E.vl2.vxxpzz, E.vl2.vxxmzz, E.vl2.vsm, E.vl2.ratio, E.vl2.dtst};
+        for (double** s : sets)
+            if (s[l]) cudaFree(s[l]);
+    }
+    for (double* p : E.visw2)
+        if (p) cudaFree(p);
+    if (E.dscal2) cudaFree(E.dscal2);
+    if (E.hscal2) cudaFreeHost(E.hscal2);
     if (E.Ginv) cudaFree(E.Ginv);
     for (double* p : {E.Ginv2, E.Mc2, E.RowB2})
         if (p) cudaFree(p);
@@ -610,7 +624,7 @@ int pt_prof_kernel(int id, int64_t* launches, double* total_ms) {
     return 0;
 }
 
-int64_t pt_prof_launches(void) { return g_launches; }
+int64_t pt_prof_launches(void) { return g_launches.load(); }
 
 int pt_prof_region(int end, double* ms) {
     if (int rc = need(g_eng != nullptr)) return rc;

@@ -12,7 +12,9 @@
 #include <cstdio>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/ptgpu.h"
@@ -60,6 +62,14 @@ struct Consts {
     double RaT, RaC, lvisT, lvisP, lvisC;
     int nx, nz, comp, Tbot, Vbc, ivis;
 };
+
+// the per-level arrays a viscosity pass writes (compute_viscosity): the cycle's own, or the set
+// the next time level's coarse levels are built into on the side stream (mixed precision)
+struct VisLevels {
+    double *vis[PT_MAXLEV], *visst[PT_MAXLEV], *vx[PT_MAXLEV], *vz[PT_MAXLEV], *vxx[PT_MAXLEV], *vzz[PT_MAXLEV],
+        *vxz[PT_MAXLEV], *vxxpzz[PT_MAXLEV], *vxxmzz[PT_MAXLEV], *vsm[PT_MAXLEV], *ratio[PT_MAXLEV], *dtst[PT_MAXLEV];
+};
+constexpr int kVisArrays = 12;  // the members of VisLevels
 
 // weights of the exact-sum stream operator of one level (pt_exact.cuh)
 struct ResFxK {
@@ -116,6 +126,18 @@ struct Engine {
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_in = nullptr, ev_fact = nullptr;
     bool fact_pending = false;
+    // mixed precision: levels 2..grids of the next time level (viscosity pipeline + coarse
+    // factorisation) built by a host worker thread on st2 into vl2 while the top-of-step solve runs
+    // with the previous ones; the first RK-stage solve joins it and copies them in
+    VisLevels vl2{};
+    double* visw2[11] = {};
+    double *dscal2 = nullptr, *hscal2 = nullptr;
+    std::thread coarse_job;
+    bool job_active = false, coarse_fresh = false;
+    std::atomic<bool> job_done{false};
+    int job_rc = 0;
+    std::string job_msg;
+    int device = 0;
     // PT_GUESS_EXTRAPOLATE: the last converged psi (a) and the last one at an earlier solve time
     // (b), with their solve times; solve_tau is the time of the solve being set up
     double *psi_a = nullptr, *psi_b = nullptr;
@@ -169,7 +191,7 @@ struct Engine {
 };
 
 extern Engine* g_eng;
-extern int64_t g_launches;
+extern std::atomic<int64_t> g_launches;
 #define PT_COUNT() (++pt::g_launches)
 
 // brackets a batch of n launches of kernel class `id` with events when profiling is on

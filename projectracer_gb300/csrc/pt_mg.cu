@@ -25,9 +25,30 @@ struct VisSet {
     double *vis, *vx, *vz, *vxx, *vzz, *vxz, *vxxpzz, *vxxmzz, *vsm, *ratio, *dtst;
 };
 
-static VisSet level_set(Engine& E, int l) {
-    return VisSet{E.vis[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l], E.vxxmzz[l],
-                  E.vsm[l], E.ratio[l], E.dtst[l]};
+// where a viscosity pass runs and writes: the stream, the test_eig scalars, the work arrays and
+// the level arrays (the cycle's own, or the side set of the next time level)
+struct VisCtx {
+    cudaStream_t st;
+    double *dscal, *hscal;
+    double* const* visw;
+    VisLevels V;
+};
+
+static VisLevels primary_levels(Engine& E) {
+    VisLevels V{};
+    for (int l = 0; l < PT_MAXLEV; l++) {
+        V.vis[l] = E.vis[l]; V.visst[l] = E.visst[l]; V.vx[l] = E.vx[l]; V.vz[l] = E.vz[l]; V.vxx[l] = E.vxx[l];
+        V.vzz[l] = E.vzz[l]; V.vxz[l] = E.vxz[l]; V.vxxpzz[l] = E.vxxpzz[l]; V.vxxmzz[l] = E.vxxmzz[l];
+        V.vsm[l] = E.vsm[l]; V.ratio[l] = E.ratio[l]; V.dtst[l] = E.dtst[l];
+    }
+    return V;
+}
+static VisCtx primary_ctx(Engine& E) { return VisCtx{E.st, E.dscal, E.hscal, E.visw, primary_levels(E)}; }
+static VisCtx side_ctx(Engine& E) { return VisCtx{E.st2, E.dscal2, E.hscal2, E.visw2, E.vl2}; }
+
+static VisSet level_set(const VisLevels& V, int l) {
+    return VisSet{V.vis[l], V.vx[l], V.vz[l], V.vxx[l], V.vzz[l], V.vxz[l], V.vxxpzz[l], V.vxxmzz[l],
+                  V.vsm[l], V.ratio[l], V.dtst[l]};
 }
 
 // ------------------------------------------------------------------ viscosity pipeline
@@ -65,10 +86,10 @@ __global__ void k_visbc_rows(double* v, Geo g, int nx, int nz) {
     if (q < 3) v[g.at(i, -j)] = v[g.at(i, j)];
     else v[g.at(i, nz + j)] = v[g.at(i, nz - j)];
 }
-static int vis_bcs(Engine& E, double* v, int l) {
+static int vis_bcs(Engine& E, double* v, int l, cudaStream_t st) {
     const Geo& g = E.gl[l];
-    PT_COUNT(), k_visbc_cols<<<nblk(6 * (g.nz + 7), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
-    PT_COUNT(), k_visbc_rows<<<nblk(6 * (g.nx + 1), 128), 128, 0, E.st>>>(v, g, g.nx, g.nz);
+    PT_COUNT(), k_visbc_cols<<<nblk(6 * (g.nz + 7), 128), 128, 0, st>>>(v, g, g.nx, g.nz);
+    PT_COUNT(), k_visbc_rows<<<nblk(6 * (g.nx + 1), 128), 128, 0, st>>>(v, g, g.nx, g.nz);
     CKL("vis_bcs");
     return 0;
 }
@@ -153,11 +174,11 @@ __global__ void k_vis_update_bc(double* v, const double* vsm, Geo g, int nx, int
 static const double kPi = 3.1415926535897932;
 
 // smoother_vis (smoother.f90:454-580) on the arrays of set S at level l
-static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record) {
+static int smoother_vis(Engine& E, const VisCtx& C, int l, int interpolate, VisSet S, int record) {
     const Geo& g = E.gl[l];
     const int nx = g.nx, nz = g.nz, ivis = E.cfg.ivis;
     int rc;
-    if ((rc = vis_bcs(E, S.vis, l))) return rc;
+    if ((rc = vis_bcs(E, S.vis, l, C.st))) return rc;
     int option, Niter;
     double lb, la;
     if (interpolate == 0) { option = 1; Niter = 3; lb = -3.0; la = -2.0; }
@@ -169,18 +190,18 @@ static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record)
     dim3 gg(nblk(nx + 1, 128), nz + 1);
     for (int guard = 0; guard < 100000; guard++) {
         for (int nn = nn_store; nn <= Niter; nn++) {
-            PT_COUNT(), k_vis_grad<<<gg, 128, 0, E.st>>>(S, g, l, Nvis_store != 0, ivis);
+            PT_COUNT(), k_vis_grad<<<gg, 128, 0, C.st>>>(S, g, l, Nvis_store != 0, ivis);
             CKL("k_vis_grad");
             if (interpolate == 0 && (Nvis_store >= 1 || ivis == 0)) {
-                unsigned long long* d = (unsigned long long*)E.dscal;
+                unsigned long long* d = (unsigned long long*)C.dscal;
                 unsigned long long init = (unsigned long long)__builtin_bit_cast(long long, 1.0e100);
-                CK(cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, E.st));
+                CK(cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, C.st));
                 dim3 ge(nblk(nx - 1, 128), nz - 1);
-                PT_COUNT(), k_test_eig<<<ge, 128, 0, E.st>>>(S, g, l, ae, be, ctemp, d);
+                PT_COUNT(), k_test_eig<<<ge, 128, 0, C.st>>>(S, g, l, ae, be, ctemp, d);
                 CKL("k_test_eig");
-                CK(cudaMemcpyAsync(E.hscal, d, 8, cudaMemcpyDeviceToHost, E.st));
-                CK(cudaStreamSynchronize(E.st));
-                ratio_min = E.hscal[0];
+                CK(cudaMemcpyAsync(C.hscal, d, 8, cudaMemcpyDeviceToHost, C.st));
+                CK(cudaStreamSynchronize(C.st));
+                ratio_min = C.hscal[0];
             }
             if (option == 1) {
                 if ((Nvis_store >= 1 && ratio_min > E.cfg.eig_ratio_min) || ivis == 0 || n > 20) {
@@ -197,7 +218,7 @@ static int smoother_vis(Engine& E, int l, int interpolate, VisSet S, int record)
             int ntemp = Niter - nn + 1;
             double c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
             c = 0.99 * c;
-            PT_COUNT(), k_vis_update_bc<<<gg, 128, 0, E.st>>>(S.vis, S.vsm, g, nx, nz, c);
+            PT_COUNT(), k_vis_update_bc<<<gg, 128, 0, C.st>>>(S.vis, S.vsm, g, nx, nz, c);
             CKL("k_vis_update_bc");
         }
         if (trigger) return 0;
@@ -239,31 +260,32 @@ __global__ void k_visbc_init(double* v, const double* vf, Geo g, Geo gf, int nx,
     v[g.at(i, k)] = val;
 }
 
-static int compute_viscosity(Engine& E, int level) {
+static int compute_viscosity(Engine& E, const VisCtx& C, int level) {
     int rc;
     const Geo& g = E.gl[level];
+    const VisLevels& V = C.V;
     if (level == 1) {
         dim3 gg(nblk(g.nx + 1, 128), g.nz + 1);
-        PT_COUNT(), k_visf<<<gg, 128, 0, E.st>>>(E.visst[1], E.Tvis, E.Cvis, g);
+        PT_COUNT(), k_visf<<<gg, 128, 0, C.st>>>(V.visst[1], E.Tvis, E.Cvis, g);
         CKL("k_visf");
-        CK(cudaMemcpyAsync(E.vis[1], E.visst[1], g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
-        return smoother_vis(E, 1, 0, level_set(E, 1), 1);
+        CK(cudaMemcpyAsync(V.vis[1], V.visst[1], g.elems() * 8, cudaMemcpyDeviceToDevice, C.st));
+        return smoother_vis(E, C, 1, 0, level_set(V, 1), 1);
     }
     const int lf = level - 1;
     const Geo& gf = E.gl[lf];
     // smooth a work copy of the finer static viscosity (the reference smooths in place and
     // restores the finer level's arrays afterwards)
-    VisSet W{E.visw[0], E.visw[1], E.visw[2], E.visw[3], E.visw[4], E.visw[5], E.visw[6], E.visw[7],
-             E.visw[8], E.visw[9], E.visw[10]};
-    CK(cudaMemcpyAsync(W.vis, E.visst[lf], gf.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
-    if ((rc = smoother_vis(E, lf, 1, W, 0))) return rc;
+    VisSet W{C.visw[0], C.visw[1], C.visw[2], C.visw[3], C.visw[4], C.visw[5], C.visw[6], C.visw[7],
+             C.visw[8], C.visw[9], C.visw[10]};
+    CK(cudaMemcpyAsync(W.vis, V.visst[lf], gf.elems() * 8, cudaMemcpyDeviceToDevice, C.st));
+    if ((rc = smoother_vis(E, C, lf, 1, W, 0))) return rc;
     dim3 gr(nblk(g.nx - 1, 128), g.nz - 1);
-    PT_COUNT(), k_restrict<<<gr, 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz);
+    PT_COUNT(), k_restrict<<<gr, 128, 0, C.st>>>(V.vis[level], W.vis, g, gf, g.nx, g.nz);
     int tot = (g.nx + 7) * (g.nz + 7);
-    PT_COUNT(), k_visbc_init<<<nblk(tot, 128), 128, 0, E.st>>>(E.vis[level], W.vis, g, gf, g.nx, g.nz, gf.nx, gf.nz);
+    PT_COUNT(), k_visbc_init<<<nblk(tot, 128), 128, 0, C.st>>>(V.vis[level], W.vis, g, gf, g.nx, g.nz, gf.nx, gf.nz);
     CKL("restrict_coefficients");
-    CK(cudaMemcpyAsync(E.visst[level], E.vis[level], g.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
-    return smoother_vis(E, level, 0, level_set(E, level), 0);
+    CK(cudaMemcpyAsync(V.visst[level], V.vis[level], g.elems() * 8, cudaMemcpyDeviceToDevice, C.st));
+    return smoother_vis(E, C, level, 0, level_set(V, level), 0);
 }
 
 // ------------------------------------------------------------------ RHS and residual norms
@@ -957,13 +979,11 @@ static int coarse_factor(Engine& E) {
 // Mixed precision: build the coarse matrix, its LU and inverse for the viscosity just computed
 // on st into the second buffer set on st2, overlapped with the solve that follows on st (the LU
 // runs on one SM).  coarse_resolve copies the result into the live buffers.
-static int coarse_factor_async(Engine& E) {
+static int coarse_factor_async(Engine& E, const VisLevels& V) {
     const int L = E.grids, n = E.ngc;
-    CK(cudaEventRecord(E.ev_in, E.st));
-    CK(cudaStreamWaitEvent(E.st2, E.ev_in, 0));
     CK(cudaMemsetAsync(E.derr2, 0, sizeof(int), E.st2));
     PT_COUNT(), k_coarse_matrix<<<nblk(n, 128), 128, 0, E.st2>>>(E.Mc2, E.gl[L], L, E.kl, E.ku, n, E.RowB2, E.cfg.Vbc,
-                                                     E.cfg.ivis, E.vis[L], E.vx[L], E.vz[L], E.vxz[L], E.vxxmzz[L],
+                                                     E.cfg.ivis, V.vis[L], V.vx[L], V.vz[L], V.vxz[L], V.vxxmzz[L],
                                                      E.derr2);
     PT_COUNT(), k_band_lu<<<1, 1024, 0, E.st2>>>(E.Mc2, E.ipiv2, n, E.kl, E.ku, E.derr2);
     PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st2>>>(
@@ -971,8 +991,50 @@ static int coarse_factor_async(Engine& E) {
     PT_COUNT(), k_g_to_f32<<<nblk((size_t)n * n, 256), 256, 0, E.st2>>>(E.Gf2, E.Ginv2, (size_t)n * n);
     CKL("async coarse factorisation");
     CK(cudaMemcpyAsync(E.hflag2, E.derr2, sizeof(int), cudaMemcpyDeviceToHost, E.st2));
-    CK(cudaEventRecord(E.ev_fact, E.st2));
     E.fact_pending = true;
+    return 0;
+}
+
+// The worker thread of a new time level (mixed precision): the viscosity pipeline of levels
+// 2..grids into the side set vl2 (from the snapshot of level 1's static viscosity in
+// vl2.visst[1]) and the coarse factorisation from it, all on st2; ev_fact marks the end.  Reads
+// only its own arrays and the engine's constant configuration; its status goes to job_rc.
+static void coarse_levels_worker(Engine* Ep) {
+    Engine& E = *Ep;
+    int rc = 0;
+    if (cudaSetDevice(E.device) != cudaSuccess || cudaStreamWaitEvent(E.st2, E.ev_in, 0) != cudaSuccess)
+        rc = fail(PT_ERR_CUDA, "coarse-level worker: device or event");
+    const VisCtx C = side_ctx(E);
+    for (int level = 2; level <= E.grids && !rc; level++) rc = compute_viscosity(E, C, level);
+    if (!rc && E.cfg.ivis > 0) rc = coarse_factor_async(E, E.vl2);
+    if (!rc && cudaEventRecord(E.ev_fact, E.st2) != cudaSuccess) rc = fail(PT_ERR_CUDA, "coarse-level worker: event");
+    E.job_rc = rc;
+    if (rc) E.job_msg = g_err;
+    E.job_done = true;
+}
+
+// Joins the worker and moves its levels into the cycle's arrays (after st2's work, in stream
+// order); the factorisation follows in coarse_resolve.  Unless `wait`, only a worker whose work
+// has completed on the device is joined: the solves of this time level keep the previous coarse
+// levels until then (a preconditioner, O(dt) older), so the worker never delays a solve.
+static int coarse_join(Engine& E, bool wait) {
+    if (!E.job_active) return 0;
+    if (!wait && !(E.job_done.load() && cudaEventQuery(E.ev_fact) == cudaSuccess)) {
+        cudaGetLastError();  // a not-ready query is not an error
+        return 0;
+    }
+    E.coarse_job.join();
+    E.job_active = false;
+    if (E.job_rc) return fail(E.job_rc, E.job_msg);
+    CK(cudaStreamWaitEvent(E.st, E.ev_fact, 0));
+    const VisLevels P = primary_levels(E);
+    double* const* dst[kVisArrays] = {P.vis, P.visst, P.vx, P.vz, P.vxx, P.vzz, P.vxz, P.vxxpzz, P.vxxmzz, P.vsm, P.ratio, P.dtst};
+    double* const* src[kVisArrays] = {E.vl2.vis, E.vl2.visst, E.vl2.vx, E.vl2.vz, E.vl2.vxx, E.vl2.vzz, E.vl2.vxz,
+                                      E.vl2.vxxpzz, E.vl2.vxxmzz, E.vl2.vsm, E.vl2.ratio, E.vl2.dtst};
+    for (int l = 2; l <= E.grids; l++)
+        for (int a = 0; a < kVisArrays; a++)
+            CK(cudaMemcpyAsync(dst[a][l], src[a][l], E.gl[l].elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    E.coarse_fresh = true;
     return 0;
 }
 
@@ -1041,7 +1103,11 @@ int residual_level1(Engine& E) {
 // ------------------------------------------------------------------ driver
 int mg_setup_solve(Engine& E) {
     int rc;
-    if ((rc = coarse_resolve(E))) return rc;  // a factorisation built during the previous solve
+    // coarse levels and factorisation built by the worker of this time level, once they are done
+    // (at a new time level: always, before the next worker starts)
+    const bool new_level = !(E.coarse_ready && E.coarse_time == E.time);
+    if ((rc = coarse_join(E, new_level))) return rc;
+    if (!E.job_active && (rc = coarse_resolve(E))) return rc;
     CK(cudaMemcpyAsync(E.err[1], E.SF, E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
     if ((rc = compute_RHS(E, 1))) return rc;
     if ((rc = mean_abs(E, E.RHS[1], 1, &E.res_ref[1]))) return rc;
@@ -1050,15 +1116,26 @@ int mg_setup_solve(Engine& E) {
     // once per time level (the top-of-step solve) and reused by the RK-stage solves of the step,
     // whose viscosity differs by O(dt).  Level 1, which defines the residual, is rebuilt every
     // solve.  The FP64 cycle rebuilds every level every solve, as the reference does.
-    const bool reuse = E.cfg.precision == PT_PREC_MIXED && E.coarse_ready && E.coarse_time == E.time;
-    E.levels_reused = reuse;
-    for (int level = 1; level <= (reuse ? 1 : E.grids); level++)
-        if ((rc = compute_viscosity(E, level))) return rc;
-    if (!reuse && (E.time == 0.0 || E.cfg.ivis > 0)) {
-        // mixed precision with a factorisation in place: refresh it off the critical path; this
-        // solve keeps the previous time level's (a preconditioner, O(dt) older)
-        const bool async = E.cfg.precision == PT_PREC_MIXED && E.coarse_ready && E.Ginv2;
-        if ((rc = async ? coarse_factor_async(E) : coarse_factor(E))) return rc;
+    const bool mixed = E.cfg.precision == PT_PREC_MIXED;
+    const bool reuse = mixed && E.coarse_ready && E.coarse_time == E.time;
+    // a new time level with coarse levels in place (mixed precision): build the new ones on the
+    // worker thread, off the critical path; this solve keeps the previous time level's (a
+    // preconditioner, O(dt) older)
+    const bool async = mixed && E.coarse_ready && !reuse && E.Ginv2 && E.vl2.vis[2];
+    E.levels_reused = reuse || async;
+    const VisCtx C = primary_ctx(E);
+    for (int level = 1; level <= (E.levels_reused ? 1 : E.grids); level++)
+        if ((rc = compute_viscosity(E, C, level))) return rc;
+    if (async) {
+        CK(cudaMemcpyAsync(E.vl2.visst[1], E.visst[1], E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+        CK(cudaEventRecord(E.ev_in, E.st));
+        E.job_rc = 0;
+        E.job_done = false;
+        E.coarse_job = std::thread(coarse_levels_worker, &E);
+        E.job_active = true;
+        E.coarse_time = E.time;
+    } else if (!reuse && (E.time == 0.0 || E.cfg.ivis > 0)) {
+        if ((rc = coarse_factor(E))) return rc;
         E.coarse_ready = true;
         E.coarse_time = E.time;
     }
@@ -1096,7 +1173,7 @@ static int cycle_part(Engine& E, int part) {
 
 static int capture_part(Engine& E, int part, cudaGraphExec_t* exec, int64_t* nlaunch) {
     cudaGraph_t graph = nullptr;
-    int64_t before = g_launches;
+    int64_t before = g_launches.load();
     CK(cudaStreamBeginCapture(E.st, cudaStreamCaptureModeThreadLocal));
     int rc = cycle_part(E, part);
     cudaError_t e = cudaStreamEndCapture(E.st, &graph);
@@ -1225,6 +1302,21 @@ int mg_alloc(Engine& E) {
         CK(cudaMallocHost(&E.hflag2, sizeof(int)));
         *E.hflag2 = 0;
         CK(cudaStreamCreateWithFlags(&E.st2, cudaStreamNonBlocking));
+        CK(cudaGetDevice(&E.device));
+        // the side set of the coarse levels (and level 1's static viscosity snapshot), its work
+        // arrays and scalars
+        for (int l = 1; l <= E.grids; l++) {
+            double** sets[kVisArrays] = {E.vl2.vis, E.vl2.visst, E.vl2.vx, E.vl2.vz, E.vl2.vxx, E.vl2.vzz, E.vl2.vxz,
+                                         E.vl2.vxxpzz, E.vl2.vxxmzz, E.vl2.vsm, E.vl2.ratio, E.vl2.dtst};
+            for (int a = 0; a < kVisArrays; a++) {
+                if (l == 1 && a != 1) continue;  // level 1: only visst (the snapshot)
+                if (int rc = alloc(&sets[a][l], E.gl[l].elems())) return rc;
+            }
+        }
+        for (int q = 0; q < 11; q++)
+            if (int rc = alloc(&E.visw2[q], E.gl[1].elems())) return rc;
+        CK(cudaMalloc(&E.dscal2, 32 * sizeof(double)));
+        CK(cudaMallocHost(&E.hscal2, 64 * sizeof(double)));
         CK(cudaEventCreateWithFlags(&E.ev_in, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&E.ev_fact, cudaEventDisableTiming));
         E.bytes_allocated += sizeof(double) * ((size_t)E.ngc * E.ngc + (size_t)ldab * E.ngc + E.ngc);

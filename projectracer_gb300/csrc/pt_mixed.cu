@@ -610,7 +610,7 @@ static int run_mixed(Engine& E, int part) {
     int64_t& n = part == 0 ? E.nM1 : E.nM2;
     if (!ex) {
         cudaGraph_t graph = nullptr;
-        int64_t before = g_launches;
+        int64_t before = g_launches.load();
         CK(cudaStreamBeginCapture(E.st, cudaStreamCaptureModeThreadLocal));
         int rc = mixed_part(E, part);
         cudaError_t e = cudaStreamEndCapture(E.st, &graph);
@@ -636,7 +636,11 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
         PhaseTimer ts(E, PH_SETUP);
         if ((rc = mg_setup_solve(E))) return rc;
         if (E.cfg.guess_mode == PT_GUESS_UNET && (rc = unet_guess(E))) return rc;
-        for (int l = 1; l < (E.levels_reused ? 2 : E.grids); l++) {
+        // FP32 coefficients: level 1 every solve, the coarse levels when they were rebuilt (here, or
+        // by the worker thread of this time level, joined in mg_setup_solve)
+        const int lmax = (E.levels_reused && !E.coarse_fresh) ? 2 : E.grids;
+        E.coarse_fresh = false;
+        for (int l = 1; l < lmax; l++) {
             size_t n = E.gl[l].elems();
             float* const* f = E.fcoef[l];
             PT_COUNT(), k_coef_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(f[0], f[1], f[2], f[3], f[4], f[5], E.vis[l], E.vx[l],
