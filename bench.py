@@ -399,16 +399,22 @@ def algorithmic_bytes(kid: int, cfg) -> float:
     FP64 stage: S_j-1 stencil, S_j-2, S_0, dtst, rhs, 5 coefficient fields, out = 11 x 8 B per node;
     FP32 stage (increment form): D_j-1 stencil, D_j-2, F0, dtst, 5 coefficient fields, out = 10 x 4 B
     per node (+4 B for Y0 on the last stage, not counted);
-    RK tracer stage: 2 stage positions, 3 step-start values, 3 accumulators read + written, 3 next
-    positions written = 14 x 8 B per tracer (the derivative tables, 12 x 8 B per node, are counted);
-    projection: position pair + T (+C) per tracer read twice (count, scatter), cell ids, the sorted
-    list and per-node sums: 32 B per tracer + 28 B per node."""
+    RK tracer stage, FP64 path: 2 stage positions, 3 step-start values, 3 accumulators read +
+    written, 3 next positions written = 14 x 8 B per tracer, + the derivative tables, 12 x 8 B per
+    node; mixed path: the positions, step-start values and results in FP64, the 3 slope sums in
+    FP32 (read + written in stages 2-3, one way in stages 1 and 4): 82 B per tracer averaged over
+    the four stages, + the FP32 tables, 3 x 16 B per node;
+    projection: position pair + T (+C) per tracer, and the per-node sums: 32 B per tracer + 28 B
+    per node."""
     nx, nz = cfg.nx, cfg.nz
     interior = (nx - 1) * (nz - 1)
     nodes = (nx + 1) * (nz + 1)
     n = float(cfg.ntr)
-    return {0: 88.0 * interior, 1: 40.0 * interior, 2: 112.0 * n + 96.0 * nodes,
-            3: 32.0 * n + 28.0 * nodes}[kid]
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    mixed = cfg.precision == PT_PREC_MIXED
+    rk = 82.0 * n + 48.0 * nodes if mixed else 112.0 * n + 96.0 * nodes
+    return {0: 88.0 * interior, 1: 40.0 * interior, 2: rk, 3: 32.0 * n + 28.0 * nodes}[kid]
 
 
 def roofline(kinds: dict, cfg) -> dict | None:

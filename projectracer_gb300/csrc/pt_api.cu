@@ -141,8 +141,10 @@ static void engine_free(Engine& E) {
     for (int f = 0; f < 3; f++)
         for (int j = 0; j < 3; j++)
             if (E.der[f][j]) cudaFree(E.der[f][j]);
-    for (int f = 0; f < 3; f++)
+    for (int f = 0; f < 3; f++) {
         if (E.ftab[f]) cudaFree(E.ftab[f]);
+        if (E.facc[f]) cudaFree(E.facc[f]);
+    }
     for (int l = 0; l < PT_MAXLEV; l++) {
         double* arrs[] = {E.err[l], E.S0[l], E.S1[l], E.S2[l], E.RHS[l], E.res[l], E.dtst[l], E.ratio[l],
                           E.vis[l], E.visst[l], E.vx[l], E.vz[l], E.vxx[l], E.vzz[l], E.vxz[l], E.vxxpzz[l],

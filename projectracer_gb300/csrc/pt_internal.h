@@ -97,6 +97,7 @@ struct Engine {
            *T0 = nullptr, *C0 = nullptr, *scratch = nullptr;
     double* der[3][3] = {};  // derivative tables: [field u,w,tsa][order 1..3]
     float4* ftab[3] = {};    // mixed precision: per node (value, x-derivatives 1..3) in FP32, fields u, w, dT/dt
+    float* facc[3] = {};     // mixed precision: per tracer FP32 sums of the RK slopes of r, s, T
     double* coef[3] = {};    // 16 Taylor coefficients per node per field (advection)
     int32_t* nempty = nullptr;
     // multigrid

@@ -709,6 +709,8 @@ int mixed_alloc(Engine& E) {
         const size_t n = E.g1.elems();
         CK(cudaMalloc(&E.ftab[f], n * sizeof(float4)));
         CK(cudaMemsetAsync(E.ftab[f], 0, n * sizeof(float4), E.st));
+        CK(cudaMalloc(&E.facc[f], (size_t)E.ntr * sizeof(float)));
+        E.bytes_allocated += (size_t)E.ntr * sizeof(float);
         E.bytes_allocated += n * sizeof(float4);
     }
     for (int l = 1; l <= E.grids; l++) {

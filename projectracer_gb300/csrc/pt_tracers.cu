@@ -21,6 +21,9 @@ namespace pt {
 
 // z-direction interpolation stencils with 1/ds^j folded in, FP32 (mixed-precision stage)
 static __constant__ float cDmf[4][7];
+// dr / 2^28 and ds / 2^28 in FP32 (exact for power-of-two spacings): 28-bit fixed-point offsets
+// to lengths
+static __constant__ float cH28[2];
 
 int upload_consts_tracers(const Engine& E) {
     if (int rc = upload_tu_consts(E)) return rc;
@@ -28,6 +31,8 @@ int upload_consts_tracers(const Engine& E) {
     for (int m = 1; m <= 3; m++)
         for (int j = 0; j < 7; j++) d[m][j] = (float)(E.K.Dm[m][j] * E.K.inv_ds_pow[m]);
     CK(cudaMemcpyToSymbol(cDmf, d, sizeof d));
+    const float h28[2] = {(float)(E.K.dr / 268435456.0), (float)(E.K.ds / 268435456.0)};
+    CK(cudaMemcpyToSymbol(cH28, h28, sizeof h28));
     return 0;
 }
 
@@ -669,43 +674,76 @@ __device__ __forceinline__ float interp_f(const float4* __restrict__ tb, Geo g, 
 struct StageArgsF {
     const float4 *u, *w, *t;
     const double *xr, *xs;
-    double *rtr, *str, *Ttr;
+    double *rtr, *str, *Ttr;  // the step's result (stage 4)
+    float *ar, *as, *aT;      // FP32 sums of the RK slopes, k1 + 2 k2 + 2 k3 (stages 1-3)
     const double *r0, *s0, *T0;
     double *rn, *sn, *Tn;
     double dtstage;
+    float dtf;  // dtstage in FP32
     int stage;
     int64_t n;
 };
 
+// nearest node of x (spacing 2^-p, x >= 0) and the offset x - i h as a multiple of h 2^-28, from
+// the bit pattern (floor_fix_pow2): no FP64 arithmetic
+__device__ __forceinline__ int nearest_off_pow2(double x, int p, int& off28) {
+    uint32_t f;
+    const int fl = floor_fix_pow2(x, p, f);
+    if (f >= (1u << 27)) {
+        off28 = (int)f - (1 << 28);
+        return fl + 1;
+    }
+    off28 = (int)f;
+    return fl;
+}
+
+// One RK4 stage (energy.f90:258-536) with FP32 interpolation: the cell and the offsets come from
+// the positions' bit patterns, the slopes are summed in FP32, and only the position/value updates
+// (FP64 state + an FP32 increment) use the FP64 pipe.
 __global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.n) return;
-    double r = A.xr[t], s = A.xs[t];
-    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
-    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
-    i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
-    k = min(max(k, 0), cK.nz);
-    const float hr = (float)(r - (double)i * cK.dr), hs = (float)(s - (double)k * cK.ds);
+    const double r = A.xr[t], s = A.xs[t];
+    int i, k;
+    float hr, hs;
+    if (cK.exact_div) {
+        int qr, qs;
+        i = nearest_off_pow2(r, cK.p_inv_dr, qr);
+        k = nearest_off_pow2(s, cK.p_inv_ds, qs);
+        hr = (float)qr * cH28[0];
+        hs = (float)qs * cH28[1];
+    } else {
+        i = cell_index(r, cK.inv_dr, cK.dr, 0, 0);
+        k = cell_index(s, cK.inv_ds, cK.ds, 0, 0);
+        hr = (float)(r - (double)i * cK.dr);
+        hs = (float)(s - (double)k * cK.ds);
+    }
+    if (i < 0 || i > cK.nx || k < 0 || k > cK.nz) {  // validated by the projection; keep reads in bounds
+        i = min(max(i, 0), cK.nx);
+        k = min(max(k, 0), cK.nz);
+        hr = (float)(r - (double)i * cK.dr);
+        hs = (float)(s - (double)k * cK.ds);
+    }
     const float a1 = hr, a2 = 0.5f * hr * hr, a3 = hr * hr * hr * (1.0f / 6.0f);
     const float b1 = hs, b2 = 0.5f * hs * hs, b3 = hs * hs * hs * (1.0f / 6.0f);
-    const double tr = interp_f(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
-    const double ts = interp_f(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
-    const double tT = interp_f(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
+    const float tr = interp_f(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
+    const float ts = interp_f(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
+    const float tT = interp_f(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
     const double r0 = A.r0[t], s0 = A.s0[t], T0 = A.T0[t];
     switch (A.stage) {
         case 1:
-            A.rtr[t] = tr; A.str[t] = ts; A.Ttr[t] = tT;
-            A.rn[t] = r0 + A.dtstage * tr; A.sn[t] = s0 + A.dtstage * ts; A.Tn[t] = T0 + A.dtstage * tT;
+            A.ar[t] = tr; A.as[t] = ts; A.aT[t] = tT;
+            A.rn[t] = r0 + (double)(A.dtf * tr); A.sn[t] = s0 + (double)(A.dtf * ts); A.Tn[t] = T0 + (double)(A.dtf * tT);
             break;
         case 2:
         case 3:
-            A.rtr[t] = A.rtr[t] + 2.0 * tr; A.str[t] = A.str[t] + 2.0 * ts; A.Ttr[t] = A.Ttr[t] + 2.0 * tT;
-            A.rn[t] = r0 + A.dtstage * tr; A.sn[t] = s0 + A.dtstage * ts; A.Tn[t] = T0 + A.dtstage * tT;
+            A.ar[t] += 2.0f * tr; A.as[t] += 2.0f * ts; A.aT[t] += 2.0f * tT;
+            A.rn[t] = r0 + (double)(A.dtf * tr); A.sn[t] = s0 + (double)(A.dtf * ts); A.Tn[t] = T0 + (double)(A.dtf * tT);
             break;
         default:
-            A.rtr[t] = r0 + A.dtstage * (A.rtr[t] + tr);
-            A.str[t] = s0 + A.dtstage * (A.str[t] + ts);
-            A.Ttr[t] = T0 + A.dtstage * (A.Ttr[t] + tT);
+            A.rtr[t] = r0 + (double)(A.dtf * (A.ar[t] + tr));
+            A.str[t] = s0 + (double)(A.dtf * (A.as[t] + ts));
+            A.Ttr[t] = T0 + (double)(A.dtf * (A.aT[t] + tT));
             break;
     }
 }
@@ -744,8 +782,8 @@ int rk_stage(Engine& E, int stage) {
         default: A.xr = E.rtr1; A.xs = E.str1; A.rn = nullptr; A.sn = nullptr; A.Tn = nullptr; A.dtstage = E.dt / 6.0; break;
     }
     if (E.ftab[0]) {  // mixed precision: FP32 interpolation
-        StageArgsF F{E.ftab[0], E.ftab[1], E.ftab[2], A.xr, A.xs, A.rtr, A.str, A.Ttr, A.r0, A.s0, A.T0, A.rn, A.sn, A.Tn,
-                     A.dtstage, A.stage, A.n};
+        StageArgsF F{E.ftab[0], E.ftab[1], E.ftab[2], A.xr, A.xs, A.rtr, A.str, A.Ttr, E.facc[0], E.facc[1], E.facc[2],
+                     A.r0, A.s0, A.T0, A.rn, A.sn, A.Tn, A.dtstage, (float)A.dtstage, A.stage, A.n};
         KernelTimer kt(E, KT_RK_STAGE, 1);
         PT_COUNT(), k_rk_stage_f<<<nblk(E.ntr, 256), 256, 0, E.st>>>(F, E.g1);
     } else {
