@@ -347,8 +347,13 @@ int pt_field_extent(int field, int32_t* lo_x, int32_t* hi_x, int32_t* lo_z, int3
 }
 
 int pt_set_field(int field, const void* host) {
-    if (g_eng) {  // new inputs: refactor the coarse operator; a new psi restarts the psi history
-        g_eng->coarse_ready = false;
+    if (g_eng) {
+        // new temperature or composition fields change the viscosity, hence the operator: the
+        // coarse levels and factorisation are rebuilt at the next solve.  Tracer arrays do not enter
+        // the operator before the next projection (which the time level's own rebuild follows);
+        // a new psi restarts the psi history.
+        const bool tracers = field >= PT_F_TRACER_R && field <= PT_F_TRACER_C;
+        if (!tracers && field != PT_F_SF && field != PT_F_U && field != PT_F_W) g_eng->coarse_ready = false;
         if (field == PT_F_SF) g_eng->hist_n = 0;
     }
     if (int rc = need(g_eng != nullptr)) return rc;
