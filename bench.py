@@ -417,6 +417,26 @@ def algorithmic_bytes(kid: int, cfg) -> float:
     return {0: 88.0 * interior, 1: 40.0 * interior, 2: rk, 3: 32.0 * n + 28.0 * nodes}[kid]
 
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
+# each kernel class on the 1024x512 grid with 4 tracers per cell (the commands and figures are in
+# the profiles/ summaries named here).  Grid kernels are captured at full size; the tracer
+# kernels' traffic grows with the tracer count and is scaled by it.  Cold-cache figures: ncu
+# flushes the caches before each pass, so for the L2-resident stage kernel this is an upper bound.
+NCU_TRAFFIC = {
+    1: ("per launch", 17.05e6, "profiles/k_rkc_stage_f_C3_1024x512.md"),
+    2: ("per tracer", 109.9e6 / 2097152, "profiles/k_rk_stage_f_C3_1024x512.md"),
+    3: ("per tracer", 91.3e6 / 2097152, "profiles/k_project_fx_C3_1024x512.md"),
+}
+
+
+def ncu_traffic(kid: int, cfg):
+    """(bytes per launch, source) for kernel class kid at this workload, or (None, None)."""
+    if kid not in NCU_TRAFFIC or cfg.nx != 1024 or cfg.nz != 512:
+        return None, None
+    kind, v, src = NCU_TRAFFIC[kid]
+    return (v if kind == "per launch" else v * float(cfg.ntr)), src
+
+
 def roofline(kinds: dict, cfg) -> dict | None:
     """Roofline of the kernel class with the largest share of the timed region, from the live
     event timings (launch-averaged)."""
@@ -428,10 +448,13 @@ def roofline(kinds: dict, cfg) -> dict | None:
     avg_s = ms / cnt * 1e-3
     per = algorithmic_bytes(kid, cfg)
     achieved = per / avg_s / 1e9
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    traffic, src = ncu_traffic(kid, cfg) if cfg.precision == PT_PREC_MIXED else (None, None)  # mixed-path kernels
     return {"bound": "hbm", "kernel": KERNEL_NAMES[kid], "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)",
-            "traffic": None, "algorithmic_bytes_per_launch": per, "avg_launch_ms": avg_s * 1e3,
-            "timed_kernels": timed}
+            "traffic": traffic, "traffic_source": src, "algorithmic_bytes_per_launch": per,
+            "avg_launch_ms": avg_s * 1e3, "timed_kernels": timed}
 
 
 if __name__ == "__main__":
