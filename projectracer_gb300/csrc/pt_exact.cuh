@@ -22,8 +22,23 @@ namespace pt {
 
 static __constant__ int cD1i[5], cD2i[5], cD3i[7], cD4i[7];
 
-constexpr int kRfTX = 32, kRfTZ = 16, kRfH = 3;  // tile of 32 x 16 nodes, 256 threads (2 nodes each)
-constexpr int kRfW = kRfTX + 2 * kRfH, kRfHt = kRfTZ + 2 * kRfH;
+// Tile geometry: TX x TZ nodes, a CTA of TX x TY threads (TZ / TY rows of nodes per thread), halo 3.
+// Large tiles amortise the halo on the fine levels; small ones keep enough CTAs in flight on the
+// coarse levels, where a kernel's time is its CTAs' critical path.
+template <int TX_, int TZ_, int TY_>
+struct TileGeo {
+    static constexpr int TX = TX_, TZ = TZ_, TY = TY_, H = 3;
+    static constexpr int W = TX + 2 * H, HT = TZ + 2 * H, NT = TX * TY, RPT = TZ / TY;
+};
+using TileBig = TileGeo<32, 16, 8>;   // 256 threads, 2 nodes each
+using TileSmall = TileGeo<16, 8, 8>;  // 128 threads, 1 node each
+constexpr int kRfTX = TileBig::TX, kRfTZ = TileBig::TZ, kRfH = TileBig::H;
+constexpr int kRfW = TileBig::W, kRfHt = TileBig::HT;
+// the tiling for a level of (nx-1) x (nz-1) interior nodes: large tiles while they give at least
+// two CTAs per SM of this part (152 SMs)
+__host__ __forceinline__ bool use_big_tiles(int nx, int nz) {
+    return (size_t)((nx - 2) / TileBig::TX + 1) * (size_t)((nz - 2) / TileBig::TZ + 1) >= 304;
+}
 
 // v * 2^e2 as a double, exactly (|v| < 2^53, result normal), from integer operations only
 __device__ __forceinline__ double i64_to_double_scaled(long long v, int e2) {
@@ -54,20 +69,22 @@ __device__ __forceinline__ double hl_value(const HL& a, int emax) {
     return i64_to_double_scaled(a.h, 31 - s) + i64_to_double_scaled(a.l, -s);
 }
 
-// Stages the tile of S with first interior node (i0, k0) (nodes i0-3 .. i0+34, k0-3 .. k0+18;
+// Stages the tile of S with first interior node (i0, k0) (nodes i0-3 .. i0+TX+2, k0-3 .. k0+TZ+2;
 // zero beyond nx+3 / nz+3) as fixed point in X; returns the tile's largest biased exponent (0x7FF
-// when the tile holds Inf/NaN).  Called by all 256 threads of the CTA (blockDim 32 x 8).
-__device__ __forceinline__ int load_tile_fx(int2 (*X)[kRfW], int* emax_s, const double* __restrict__ S, Geo g, int i0,
+// when the tile holds Inf/NaN).  Called by all TG::NT threads of the CTA (blockDim TX x TY).
+template <class TG>
+__device__ __forceinline__ int load_tile_fx(int2 (*X)[TG::W], int* emax_s, const double* __restrict__ S, Geo g, int i0,
                                             int k0, int nx, int nz) {
-    constexpr int NT = kRfW * kRfHt, PER = (NT + 255) / 256;
-    const int tid = threadIdx.y * kRfTX + threadIdx.x;
+    constexpr int kRfW = TG::W, kRfH = TG::H;
+    constexpr int NT = TG::W * TG::HT, PER = (NT + TG::NT - 1) / TG::NT;
+    const int tid = threadIdx.y * TG::TX + threadIdx.x;
     if (tid == 0) *emax_s = 0;
     __syncthreads();
     unsigned long long raw[PER];
     int em = 0;
 #pragma unroll
     for (int q = 0; q < PER; q++) {
-        const int idx = tid + 256 * q;
+        const int idx = tid + TG::NT * q;
         unsigned long long b = 0;
         if (idx < NT) {
             const int i = i0 - kRfH + idx % kRfW, k = k0 - kRfH + idx / kRfW;
@@ -81,7 +98,7 @@ __device__ __forceinline__ int load_tile_fx(int2 (*X)[kRfW], int* emax_s, const 
     const int emax = *emax_s;
 #pragma unroll
     for (int q = 0; q < PER; q++) {
-        const int idx = tid + 256 * q;
+        const int idx = tid + TG::NT * q;
         if (idx >= NT) break;
         const unsigned long long b = raw[q];
         const int e = (int)((b >> 52) & 0x7FF);
@@ -104,8 +121,8 @@ __device__ __forceinline__ int load_tile_fx(int2 (*X)[kRfW], int* emax_s, const 
 
 // A S at the node at tile position (cx, cz) (stream_derivatives + the viscosity terms of
 // stream_space, without the right-hand side); NaN when the tile holds Inf/NaN.
-template <bool SQUARE>
-__device__ __forceinline__ double tile_apply_A(const int2 (*X)[kRfW], int cx, int cz, int emax,
+template <bool SQUARE, int W>
+__device__ __forceinline__ double tile_apply_A(const int2 (*X)[W], int cx, int cz, int emax,
                                                const double* __restrict__ vis, const double* __restrict__ vx,
                                                const double* __restrict__ vz, const double* __restrict__ vxz,
                                                const double* __restrict__ vxxmzz, size_t o, int ivis,

@@ -425,24 +425,24 @@ __global__ void __launch_bounds__(128) k_rkc_stage(double* __restrict__ out, con
 }
 
 // k_rkc_stage with the stream operator's stencil sums formed exactly (pt_exact.cuh); a CTA owns a
-// 32 x 16 tile of nodes.
-template <bool SQUARE>
-__global__ void __launch_bounds__(256) k_rkc_stage_fx(double* __restrict__ out, const double* __restrict__ S1,
-                                                      const double* __restrict__ S2, const double* __restrict__ S0,
-                                                      StreamOp op, Geo g, int l, double cS0, double mew, double vv,
-                                                      double mewtc, int first, int ivis, double sz, ResFxK K) {
-    __shared__ int2 X[kRfHt][kRfW];
+// TG::TX x TG::TZ tile of nodes.
+template <bool SQUARE, class TG>
+__global__ void __launch_bounds__(TG::NT) k_rkc_stage_fx(double* __restrict__ out, const double* __restrict__ S1,
+                                                         const double* __restrict__ S2, const double* __restrict__ S0,
+                                                         StreamOp op, Geo g, int l, double cS0, double mew, double vv,
+                                                         double mewtc, int first, int ivis, double sz, ResFxK K) {
+    __shared__ int2 X[TG::HT][TG::W];
     __shared__ int emax_s;
     const LevConst& L = cL[l];
-    const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
-    const int emax = load_tile_fx(X, &emax_s, S1, g, i0, k0, L.nx, L.nz);
+    const int i0 = blockIdx.x * TG::TX + 1, k0 = blockIdx.y * TG::TZ + 1;
+    const int emax = load_tile_fx<TG>(X, &emax_s, S1, g, i0, k0, L.nx, L.nz);
 #pragma unroll 1
-    for (int r = 0; r < 2; r++) {
-        const int lx = threadIdx.x, lz = threadIdx.y + 8 * r;
+    for (int r = 0; r < TG::RPT; r++) {
+        const int lx = threadIdx.x, lz = threadIdx.y + TG::TY * r;
         const int i = i0 + lx, k = k0 + lz;
         if (i > L.nx - 1 || k > L.nz - 1) continue;
         const size_t o = g.at(i, k);
-        const double F = op.rhs[o] - tile_apply_A<SQUARE>(X, lx + kRfH, lz + kRfH, emax, op.vis, op.vx, op.vz, op.vxz,
+        const double F = op.rhs[o] - tile_apply_A<SQUARE>(X, lx + TG::H, lz + TG::H, emax, op.vis, op.vx, op.vz, op.vxz,
                                                           op.vxxmzz, o, ivis, K);
         double v;
         if (first) v = S1[o] + mewtc * op.dtst[o] * F;
@@ -452,22 +452,22 @@ __global__ void __launch_bounds__(256) k_rkc_stage_fx(double* __restrict__ out, 
 }
 
 // k_residual with exact stencil sums
-template <bool SQUARE>
-__global__ void __launch_bounds__(256) k_residual_fx64(double* __restrict__ res, const double* __restrict__ S,
-                                                       StreamOp op, Geo g, int l, int ivis, ResFxK K) {
-    __shared__ int2 X[kRfHt][kRfW];
+template <bool SQUARE, class TG>
+__global__ void __launch_bounds__(TG::NT) k_residual_fx64(double* __restrict__ res, const double* __restrict__ S,
+                                                          StreamOp op, Geo g, int l, int ivis, ResFxK K) {
+    __shared__ int2 X[TG::HT][TG::W];
     __shared__ int emax_s;
     const LevConst& L = cL[l];
-    const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
-    const int emax = load_tile_fx(X, &emax_s, S, g, i0, k0, L.nx, L.nz);
+    const int i0 = blockIdx.x * TG::TX + 1, k0 = blockIdx.y * TG::TZ + 1;
+    const int emax = load_tile_fx<TG>(X, &emax_s, S, g, i0, k0, L.nx, L.nz);
 #pragma unroll 1
-    for (int r = 0; r < 2; r++) {
-        const int lx = threadIdx.x, lz = threadIdx.y + 8 * r;
+    for (int r = 0; r < TG::RPT; r++) {
+        const int lx = threadIdx.x, lz = threadIdx.y + TG::TY * r;
         const int i = i0 + lx, k = k0 + lz;
         if (i > L.nx - 1 || k > L.nz - 1) continue;
         const size_t o = g.at(i, k);
-        res[o] = op.rhs[o] - tile_apply_A<SQUARE>(X, lx + kRfH, lz + kRfH, emax, op.vis, op.vx, op.vz, op.vxz, op.vxxmzz,
-                                                  o, ivis, K);
+        res[o] = op.rhs[o] - tile_apply_A<SQUARE>(X, lx + TG::H, lz + TG::H, emax, op.vis, op.vx, op.vz, op.vxz,
+                                                  op.vxxmzz, o, ivis, K);
     }
 }
 
@@ -517,10 +517,18 @@ static void launch_stage(Engine& E, int l, double* out, const double* S1, const 
     const Geo& g = E.gl[l];
     const int ivis = E.cfg.ivis;
     if (E.res_int) {
-        dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
-        auto kern = E.resfx[l].square ? k_rkc_stage_fx<true> : k_rkc_stage_fx<false>;
-        PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(out, S1, S2, S0, op, g, l, cS0, mew, vv, mewtc, first, ivis, sz,
-                                                E.resfx[l]);
+        const bool sq = E.resfx[l].square;
+        if (use_big_tiles(g.nx, g.nz)) {
+            dim3 blk(TileBig::TX, TileBig::TY), grd(nblk(g.nx - 1, TileBig::TX), nblk(g.nz - 1, TileBig::TZ));
+            auto kern = sq ? k_rkc_stage_fx<true, TileBig> : k_rkc_stage_fx<false, TileBig>;
+            PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(out, S1, S2, S0, op, g, l, cS0, mew, vv, mewtc, first, ivis, sz,
+                                                    E.resfx[l]);
+        } else {
+            dim3 blk(TileSmall::TX, TileSmall::TY), grd(nblk(g.nx - 1, TileSmall::TX), nblk(g.nz - 1, TileSmall::TZ));
+            auto kern = sq ? k_rkc_stage_fx<true, TileSmall> : k_rkc_stage_fx<false, TileSmall>;
+            PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(out, S1, S2, S0, op, g, l, cS0, mew, vv, mewtc, first, ivis, sz,
+                                                    E.resfx[l]);
+        }
     } else {
         dim3 gs(nblk(g.nx - 1, 128), g.nz - 1);
         PT_COUNT(), k_rkc_stage<<<gs, 128, 0, E.st>>>(out, S1, S2, S0, op, g, l, cS0, mew, vv, mewtc, first, ivis, sz);
@@ -529,9 +537,16 @@ static void launch_stage(Engine& E, int l, double* out, const double* S1, const 
 static void launch_residual(Engine& E, int l, double* res, const double* S, const StreamOp& op) {
     const Geo& g = E.gl[l];
     if (E.res_int) {
-        dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
-        auto kern = E.resfx[l].square ? k_residual_fx64<true> : k_residual_fx64<false>;
-        PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(res, S, op, g, l, E.cfg.ivis, E.resfx[l]);
+        const bool sq = E.resfx[l].square;
+        if (use_big_tiles(g.nx, g.nz)) {
+            dim3 blk(TileBig::TX, TileBig::TY), grd(nblk(g.nx - 1, TileBig::TX), nblk(g.nz - 1, TileBig::TZ));
+            auto kern = sq ? k_residual_fx64<true, TileBig> : k_residual_fx64<false, TileBig>;
+            PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(res, S, op, g, l, E.cfg.ivis, E.resfx[l]);
+        } else {
+            dim3 blk(TileSmall::TX, TileSmall::TY), grd(nblk(g.nx - 1, TileSmall::TX), nblk(g.nz - 1, TileSmall::TZ));
+            auto kern = sq ? k_residual_fx64<true, TileSmall> : k_residual_fx64<false, TileSmall>;
+            PT_COUNT(), kern<<<grd, blk, 0, E.st>>>(res, S, op, g, l, E.cfg.ivis, E.resfx[l]);
+        }
     } else {
         PT_COUNT(), k_residual<<<dim3(nblk(g.nx - 1, 128), g.nz - 1), 128, 0, E.st>>>(res, S, op, g, l, E.cfg.ivis);
     }

@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(256) k_residual_fx(double* __restrict__ res, f
     __shared__ int2 X[kRfHt][kRfW];
     __shared__ int emax_s;
     const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
-    const int emax = load_tile_fx(X, &emax_s, x, g, i0, k0, nx, nz);
+    const int emax = load_tile_fx<TileBig>(X, &emax_s, x, g, i0, k0, nx, nz);
 #pragma unroll 1
     for (int r = 0; r < 2; r++) {
         const int lz = threadIdx.y + 8 * r, lx = threadIdx.x;
