@@ -106,7 +106,8 @@ typedef struct pt_config {
     int32_t CFL;           /* &inputs CFL: 1 = velocity terms in the advective eigenvalue and
                               dt <= 2/eigD_max (energy.f90:809, 859-866) */
     int32_t mg_cycle;      /* PT_CYCLE_*: level schedule of the mixed-precision solve (&gpu group) */
-    int32_t reserved;
+    int32_t nstageC;       /* RKC1 stages on levels 2..grids of the mixed-precision V-cycle; 0 = nstageS
+                              (&gpu group; the FP64 path always uses nstageS) */
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

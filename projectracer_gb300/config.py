@@ -71,7 +71,7 @@ class PtConfig(ctypes.Structure):
         ("mg_scheme", ctypes.c_int32),
         ("CFL", ctypes.c_int32),
         ("mg_cycle", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("nstageC", ctypes.c_int32),
     ]
 
     @staticmethod
@@ -189,7 +189,8 @@ WORKLOADS = {
     # the reference's smoother.
     "C3": dict(nx=1024, nz=512, aspect=2.0, RaT=1e7, RaC=2e6, comp=1, ivis=1, visT=1e5, visP=10.0,
                tpc=32, courant=0.5, tolerance=1e-8, steps=200, CFL=1, mg_scheme=1, bench_tolerance=1e-6,
-               mg_cycle=PT_CYCLE_V, mixed_nstageS=10, mixed_dampingS=30.0, mixed_guess=PT_GUESS_EXTRAPOLATE),
+               mg_cycle=PT_CYCLE_V, mixed_nstageS=10, mixed_nstageC=8, mixed_dampingS=30.0,
+               mixed_guess=PT_GUESS_EXTRAPOLATE),
     # 512x256 learned-guess configuration (Ra_T and contrast sampled per run)
     "C4": dict(nx=512, nz=256, aspect=2.0, RaT=1e6, RaC=2e5, comp=1, ivis=1, visT=1e2, visP=1.0,
                tpc=16, courant=0.5, tolerance=1e-8, steps=1),
@@ -225,6 +226,7 @@ def workload(name: str, scale: float = 1.0, precision: int = PT_PREC_FP64) -> tu
     c.mg_cycle = w.get("mg_cycle", PT_CYCLE_REFERENCE) if precision == PT_PREC_MIXED else PT_CYCLE_REFERENCE
     if precision == PT_PREC_MIXED and "mixed_nstageS" in w:
         c.nstageS = w["mixed_nstageS"]
+        c.nstageC = w.get("mixed_nstageC", 0)
         c.dampingS = w["mixed_dampingS"]
     if precision == PT_PREC_MIXED and "mixed_guess" in w:
         c.guess_mode = w["mixed_guess"]

@@ -84,6 +84,9 @@ struct Engine {
     int grids = 0, nsteps = 0, multi[64];
     int mnsteps = 0, mmulti[64];  // schedule of the mixed-precision solve (PT_CYCLE_*)
     double RKC1_stability = 0, delta_T = 2, delta_C = 2, dts = 0;
+    // the coarse-level RKC1 smoother of the mixed V-cycle (nstageC stages, same damping)
+    int nstageC = 0;
+    double RKC1_stability_c = 0, mew_c[64] = {}, vv_c[64] = {}, mewt_c[64] = {};
     double Tr_base = 0, Trr_base = 0, Trrr_base = 0, Trrrr_base = 0, Trs_base = 0, Trrs_base = 0,
            Trrss_base = 0, Tr_base_so = 0, Trr_base_so = 0;
     int kl = 0, ku = 0, ngc = 0, kent = 0;

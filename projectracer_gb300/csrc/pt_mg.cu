@@ -185,8 +185,12 @@ static int smoother_vis(Engine& E, const VisCtx& C, int l, int interpolate, VisS
     else { option = 0; Niter = E.cfg.vis_iter; lb = -2.0; la = -1.0; }
     int Nvis_store = 0, nn_store = 1, n = 0, trigger = 0;
     double ratio_min = 1.0e100;
-    const double ae = -E.RKC1_stability / 2.0, be = (double)E.cfg.nstageS;
-    const double ctemp = E.cfg.courant_stream * (E.RKC1_stability / (ae * ae));
+    // the pseudo-time step (test_eigenvalues) matches the smoother that will run on level l: the
+    // mixed V-cycle's coarse-level smoother has its own stage count
+    const bool coarse_smoother = E.cfg.precision == PT_PREC_MIXED && l >= 2;
+    const double stab = coarse_smoother ? E.RKC1_stability_c : E.RKC1_stability;
+    const double ae = -stab / 2.0, be = (double)(coarse_smoother ? E.nstageC : E.cfg.nstageS);
+    const double ctemp = E.cfg.courant_stream * (stab / (ae * ae));
     dim3 gg(nblk(nx + 1, 128), nz + 1);
     for (int guard = 0; guard < 100000; guard++) {
         for (int nn = nn_store; nn <= Niter; nn++) {

@@ -478,7 +478,12 @@ static int bcs_f(Engine& E, int l, float* f) {
 // needed (the next step descends).
 static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in = false) {
     const Geo& g = E.gl[l];
-    const int N = E.cfg.nstageS, ivis = E.cfg.ivis;
+    // level 1: the nstageS-stage smoother; levels 2..grids: the nstageC-stage one
+    const bool coarse = l >= 2;
+    const int N = coarse ? E.nstageC : E.cfg.nstageS, ivis = E.cfg.ivis;
+    const double* kmew = coarse ? E.mew_c : E.K.mew;
+    const double* kvv = coarse ? E.vv_c : E.K.vv;
+    const double* kmewt = coarse ? E.mewt_c : E.K.mewt;
     const float sz = E.cfg.Vbc == 0 ? -1.f : 1.f;
     FOp op = fop(E, l);
     dim3 blk(32, 8), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 8));
@@ -492,7 +497,7 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in
         GraphTimer gt(E, 1, (l == 1 && zero) ? N : 0);
         float* Dm1 = E.fS1[l];
         float* Dm2 = E.fS2[l];
-        const float mewtc1 = (float)(E.K.mewt[1] * c);
+        const float mewtc1 = (float)(kmewt[1] * c);
         if (restrict_in && zero && n == 1) {  // restriction of the finer residual fused in
             const Geo& gf = E.gl[l - 1];
             int rc;
@@ -514,7 +519,7 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in
             // D_{j-2} = D_0 = 0 at j = 2; the output overwrites D_{j-2}
             if (int rc = launch_pdl("k_rkc_stage_f", k_rkc_stage_f, grd, blk, 0, E.st, Dm2, (const float*)Dm1,
                                     (const float*)(j == 2 ? nullptr : Dm2), (const float*)F0, last ? e : nullptr, op, g,
-                                    l, g.nx, g.nz, (float)E.K.mew[j], (float)E.K.vv[j], (float)(E.K.mewt[j] * c), ivis,
+                                    l, g.nx, g.nz, (float)kmew[j], (float)kvv[j], (float)(kmewt[j] * c), ivis,
                                     sz))
                 return rc;
             float* t = Dm1;

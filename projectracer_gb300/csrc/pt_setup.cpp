@@ -155,7 +155,36 @@ static void fourier_bases(Engine& E) {
     E.Tr_base_so = m1so; E.Trr_base_so = m2so;
 }
 
+// RKC1 coefficients of an N-stage smoother with the configured damping (Chebyshev_prep_stream);
+// returns the stability bound
+static double rkc1_table(const Engine& E, int N, double* mew, double* vv, double* cc, double* mewt) {
+    double T[64], Tx[64], b[64];
+    const double w0 = 1.0 + E.cfg.dampingS / (double)(N * N);
+    T[0] = 1.0; T[1] = w0; Tx[0] = 0.0; Tx[1] = 1.0;
+    for (int j = 2; j <= N; j++) {
+        T[j] = 2.0 * w0 * T[j - 1] - T[j - 2];
+        Tx[j] = 2.0 * T[j - 1] + 2.0 * w0 * Tx[j - 1] - Tx[j - 2];
+    }
+    const double w1 = T[N] / Tx[N];
+    for (int j = 0; j <= N; j++) b[j] = 1.0 / T[j];
+    mewt[1] = b[1] * w1;
+    for (int j = 2; j <= N; j++) {
+        mew[j] = 2.0 * b[j] * w0 / b[j - 1];
+        vv[j] = -b[j] / b[j - 2];
+        if (cc) cc[j] = 1.0 - mew[j] - vv[j];
+        mewt[j] = 2.0 * b[j] * w1 / b[j - 1];
+    }
+    return -2.0 * w0 / w1;
+}
+
+static void rkc1_coefficients_c(Engine& E) {
+    const int N = E.cfg.nstageC > 0 ? E.cfg.nstageC : E.cfg.nstageS;
+    E.nstageC = N;
+    E.RKC1_stability_c = rkc1_table(E, N, E.mew_c, E.vv_c, nullptr, E.mewt_c);
+}
+
 static void rkc1_coefficients(Engine& E) {
+    rkc1_coefficients_c(E);
     Consts& K = E.K;
     const int N = E.cfg.nstageS;
     double T[64], Tx[64], b[64];
@@ -235,6 +264,7 @@ int setup_constants(Engine& E) {
     if (c.iheattype != 0) return fail(PT_ERR_CONFIG, "iheattype must be 0 (constant heating)");
     if (c.nx < 8 || c.nz < 8) return fail(PT_ERR_CONFIG, "grid too small");
     if (c.nstageS < 2 || c.nstageS > 60) return fail(PT_ERR_CONFIG, "nstageS must be 2..60");
+    if (c.nstageC != 0 && (c.nstageC < 2 || c.nstageC > 60)) return fail(PT_ERR_CONFIG, "nstageC must be 0 or 2..60");
     if (c.comp != 0 && c.comp != 1) return fail(PT_ERR_CONFIG, "comp must be 0 or 1");
     if (c.RaT == 0.0) return fail(PT_ERR_CONFIG, "RaT=0 (manual dt) is not supported");
     if (c.ntr <= 0) return fail(PT_ERR_CONFIG, "ntr must be positive");
