@@ -126,16 +126,18 @@ __device__ __forceinline__ const Stencil<float>& stencil<float>(int l) { return 
 template <>
 __device__ __forceinline__ const Stencil<double>& stencil<double>(int l) { return cSD[l]; }
 
-// A S (no right-hand side) at node (i,k) of the FP32 array S, in arithmetic T with the folded
-// stencils of level l (FP32: the smoother stages; FP64: residuals and F0)
-template <typename T, typename SIn = float, typename Op = FOp>
-__device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, const Op& op, int i, int k, int ivis) {
+// A S (no right-hand side) at a node, in arithmetic T with the folded stencils of level l
+// (FP32: the smoother stages; FP64: residuals); ld(dx, dz) returns S at offset (dx, dz) from the
+// node (global memory or values held in registers: the same operations in the same order either
+// way), o is the node's index into the coefficient fields
+template <typename T, typename Ld, typename Op>
+__device__ __forceinline__ T apply_A_ld(const Ld& ld, int l, const Op& op, size_t o, int ivis) {
     const Stencil<T>& C = stencil<T>(l);
     T sx[7], sz[7];
 #pragma unroll
     for (int j = 0; j < 7; j++) {
-        sx[j] = (T)S[g.at(i + j - 3, k)];
-        sz[j] = (T)S[g.at(i, k + j - 3)];
+        sx[j] = (T)ld(j - 3, 0);
+        sz[j] = (T)ld(0, j - 3);
     }
     T Sxx = 0, Sxxx = 0, Sxxxx = 0, Szz = 0, Szzz = 0, Szzzz = 0;
 #pragma unroll
@@ -151,7 +153,7 @@ __device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, co
         T d1 = 0, d2 = 0;
 #pragma unroll
         for (int ii = 0; ii < 5; ii++) {
-            T v = (kk == 2) ? sx[ii + 1] : (T)S[g.at(i + ii - 2, k + kk - 2)];
+            T v = (kk == 2) ? sx[ii + 1] : (T)ld(ii - 2, kk - 2);
             d1 += C.i1[ii] * v;
             d2 += C.i2[ii] * v;
         }
@@ -160,12 +162,17 @@ __device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, co
         Sxxz += C.o_xxz[kk] * d2;
         Sxxzz += C.o_xxzz[kk] * d2;
     }
-    size_t o = g.at(i, k);
     T r = (T)op.vis[o] * (Sxxxx + Szzzz + (T)2 * Sxxzz);
     if (ivis != 0)
         r += (T)op.vxxmzz[o] * (Sxx - Szz) + (T)4 * (T)op.vxz[o] * Sxz + (T)2 * (T)op.vx[o] * (Sxxx + Sxzz) +
              (T)2 * (T)op.vz[o] * (Szzz + Sxxz);
     return r;
+}
+
+// A S at node (i,k) of the array S in global memory
+template <typename T, typename SIn = float, typename Op = FOp>
+__device__ __forceinline__ T apply_A(const SIn* __restrict__ S, Geo g, int l, const Op& op, int i, int k, int ivis) {
+    return apply_A_ld<T>([&](int dx, int dz) { return S[g.at(i + dx, k + dz)]; }, l, op, g.at(i, k), ivis);
 }
 
 // RKC1 in increment form.  With Y_0 = e and D_j = Y_j - Y_0 the reference's recurrence
@@ -237,6 +244,40 @@ __global__ void __launch_bounds__(256) k_rkc_stage_f(float* out, const float* __
     if (Dm2) d += vv * Dm2[o];
     if (Y0out) store_ghosts_f(Y0out, g, i, k, nx, nz, Y0out[o] + d, sz);
     else store_ghosts_f(out, g, i, k, nx, nz, d, sz);
+}
+
+// k_rkc_stage_f for two vertically adjacent nodes per thread: the union of their stencils (36
+// values of D_{j-1}: rows k-3..k+4 of column i, rows k-2..k+3 of columns i-2..i+2, rows k and k+1
+// of columns i-3 and i+3) is loaded once into registers, about half the loads per node of the
+// one-node kernel.  Same arithmetic per node.
+__global__ void __launch_bounds__(128) k_rkc_stage_f2(float* out, const float* __restrict__ Dm1, const float* Dm2,
+                                                      const float* __restrict__ F0, float* Y0out, FOp op, Geo g,
+                                                      int l, int nx, int nz, float mew, float vv, float mewtc,
+                                                      int ivis, float sz) {
+    pdl_begin();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    // w[r + 3][c + 3] = D_{j-1}(i + c, k + r), r = -3..4 (the rows of both nodes' stencils)
+    float w[8][7];
+#pragma unroll
+    for (int r = -3; r <= 4; r++)
+#pragma unroll
+        for (int c = -3; c <= 3; c++) {
+            const bool need = c == 0 || ((r >= -2 && r <= 3) && (c >= -2 && c <= 2)) || r == 0 || r == 1;
+            w[r + 3][c + 3] = need ? Dm1[g.at(i + c, k + r)] : 0.0f;
+        }
+#pragma unroll
+    for (int n = 0; n < 2; n++) {
+        const int kn = k + n;
+        if (kn > nz - 1) break;
+        const size_t o = g.at(i, kn);
+        const float A = apply_A_ld<float>([&](int dx, int dz) { return w[n + dz + 3][dx + 3]; }, l, op, o, ivis);
+        const float F = F0[o] - A;
+        float d = mew * w[n + 3][3] + mewtc * op.dtst[o] * F;
+        if (Dm2) d += vv * Dm2[o];
+        if (Y0out) store_ghosts_f(Y0out, g, i, kn, nx, nz, Y0out[o] + d, sz);
+        else store_ghosts_f(out, g, i, kn, nx, nz, d, sz);
+    }
 }
 
 // Residual of the correction equation, the RHS the next coarser level sees.  T = double when the
@@ -487,6 +528,8 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in
     const float sz = E.cfg.Vbc == 0 ? -1.f : 1.f;
     FOp op = fop(E, l);
     dim3 blk(32, 8), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 8));
+    const dim3 blk2(32, 4), grd2(nblk(g.nx - 1, 32), nblk(g.nz - 1, 8));  // two nodes per thread in z
+    const bool two = (size_t)(g.nx - 1) * (size_t)(g.nz - 1) >= 262144;
     // FP64-arithmetic residual in 64-thread blocks: this part issues about two FP64 FMAs per
     // clock per SM, so the coarse levels need every SM they can get
     dim3 blk64(32, 2), grd64(nblk(g.nx - 1, 32), nblk(g.nz - 1, 2));
@@ -517,10 +560,12 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in
         for (int j = 2; j <= N; j++) {
             const bool last = (j == N);
             // D_{j-2} = D_0 = 0 at j = 2; the output overwrites D_{j-2}
-            if (int rc = launch_pdl("k_rkc_stage_f", k_rkc_stage_f, grd, blk, 0, E.st, Dm2, (const float*)Dm1,
-                                    (const float*)(j == 2 ? nullptr : Dm2), (const float*)F0, last ? e : nullptr, op, g,
-                                    l, g.nx, g.nz, (float)kmew[j], (float)kvv[j], (float)(kmewt[j] * c), ivis,
-                                    sz))
+            // large levels: two nodes per thread (half the loads); small ones: one (twice the threads)
+            auto kst = two ? k_rkc_stage_f2 : k_rkc_stage_f;
+            if (int rc = launch_pdl(two ? "k_rkc_stage_f2" : "k_rkc_stage_f", kst, two ? grd2 : grd, two ? blk2 : blk, 0,
+                                    E.st, Dm2, (const float*)Dm1, (const float*)(j == 2 ? nullptr : Dm2),
+                                    (const float*)F0, last ? e : nullptr, op, g, l, g.nx, g.nz, (float)kmew[j],
+                                    (float)kvv[j], (float)(kmewt[j] * c), ivis, sz))
                 return rc;
             float* t = Dm1;
             Dm1 = Dm2;
