@@ -32,6 +32,10 @@ int64_t pt_prof_launches(void);
  * range "pt_timed"; end=1 records the stop event, waits for it, closes the range and returns the
  * elapsed milliseconds in *ms. */
 int pt_prof_region(int end, double* ms);
+/* Mixed precision tracer order (internal: tracer fields are always exchanged in the caller's
+ * order): re-sorts by cell since the last pt_upload_state, and the average number of cell runs per
+ * projection thread (of 16 consecutive tracers) in the last projection. */
+int pt_prof_tracer_order(int64_t* resorts, double* runs_per_thread);
 
 #ifdef __cplusplus
 }

@@ -123,6 +123,15 @@ static int engine_alloc(Engine& E) {
     if ((rc = ialloc(E, &E.cstart, (size_t)ncell))) return rc;
     if ((rc = ialloc(E, &E.scan_tmp, (size_t)ncell + (size_t)ncell / 1024 + 64))) return rc;
     if ((rc = dalloc(E, &E.cpart, (size_t)27 * ncell))) return rc;
+    if (E.cfg.precision == PT_PREC_MIXED) {  // tracer order (re-sorted by cell when locality is lost)
+        if ((rc = ialloc(E, &E.perm, nt)) || (rc = ialloc(E, &E.perm2, nt))) return rc;
+        const size_t nkey = resort_nkey(E.K.nx, E.K.nz);
+        if ((rc = ialloc(E, &E.rs_count, nkey)) || (rc = ialloc(E, &E.rs_start, nkey)) ||
+            (rc = ialloc(E, &E.rs_tot, nkey / 1024 + 64)))
+            return rc;
+        CK(cudaMalloc(&E.proj_runs, sizeof(unsigned long long)));
+        if ((rc = tracer_order_reset(E))) return rc;
+    }
     if ((rc = mg_alloc(E))) return rc;
     if (E.cfg.precision == PT_PREC_MIXED && (rc = mixed_alloc(E))) return rc;
     return 0;
@@ -158,7 +167,8 @@ static void engine_free(Engine& E) {
     }
     for (int q = 0; q < 11; q++)
         if (E.visw[q]) cudaFree(E.visw[q]);
-    int32_t* ia[] = {E.nempty, E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp};
+    if (E.proj_runs) cudaFree(E.proj_runs);
+    int32_t* ia[] = {E.nempty, E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp, E.perm, E.perm2, E.rs_count, E.rs_start, E.rs_tot};
     for (auto a : ia)
         if (a) cudaFree(a);
     if (E.ipiv) cudaFree(E.ipiv);
@@ -361,7 +371,15 @@ int pt_set_field(int field, const void* host) {
     Engine& E = *g_eng;
     if (field == PT_F_NEMPTY || field == PT_F_VIS || field == PT_F_RHS) return fail(PT_ERR_ARG, "field is read-only");
     if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) {
-        CK(cudaMemcpy(field_ptr(E, field), host, sizeof(double) * (size_t)E.ntr, cudaMemcpyHostToDevice));
+        const size_t nb = sizeof(double) * (size_t)E.ntr;
+        if (!E.perm_active) {
+            CK(cudaMemcpy(field_ptr(E, field), host, nb, cudaMemcpyHostToDevice));
+            return 0;
+        }
+        // re-sorted tracers: the host array is in the user's order (staged in an RK stage buffer)
+        CK(cudaMemcpyAsync(E.str2, host, nb, cudaMemcpyHostToDevice, E.st));
+        if (int rc = tracer_user_order(E, field_ptr(E, field), E.str2, false)) return rc;
+        CK(cudaStreamSynchronize(E.st));
         return 0;
     }
     return copy_grid(E, field, const_cast<void*>(host), true);
@@ -377,7 +395,14 @@ int pt_get_field(int field, void* host) {
         return 0;
     }
     if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) {
-        CK(cudaMemcpy(host, field_ptr(E, field), sizeof(double) * (size_t)E.ntr, cudaMemcpyDeviceToHost));
+        const size_t nb = sizeof(double) * (size_t)E.ntr;
+        const double* src = field_ptr(E, field);
+        if (E.perm_active) {  // back to the user's order
+            if (int rc = tracer_user_order(E, const_cast<double*>(src), E.str2, true)) return rc;
+            src = E.str2;
+        }
+        CK(cudaMemcpyAsync(host, src, nb, cudaMemcpyDeviceToHost, E.st));
+        CK(cudaStreamSynchronize(E.st));
         return 0;
     }
     return copy_grid(E, field, host, false);
@@ -407,6 +432,7 @@ int pt_upload_state(const double* xg, const double* zg, const double* T, const d
     CK(cudaMemcpyAsync(E.str, str, nb, cudaMemcpyHostToDevice, E.st));
     CK(cudaMemcpyAsync(E.Ttr, Ttr, nb, cudaMemcpyHostToDevice, E.st));
     if (E.cfg.comp) CK(cudaMemcpyAsync(E.Ctr, Ctr, nb, cudaMemcpyHostToDevice, E.st));
+    if ((rc = tracer_order_reset(E))) return rc;
     TRACE("upload: boundary conditions");
     // grid.f90:67-73: boundary conditions on the restart fields
     if ((rc = enforce_bcs_T(E, E.T))) return rc;
@@ -525,6 +551,7 @@ int pt_step(double* dt_out, pt_solve_info* info) {
     Engine& E = *g_eng;
     if (info) std::memset(info, 0, sizeof *info);
     int rc;
+    if (E.want_resort && (rc = resort_tracers(E))) return rc;
     if ((rc = stability_dt(E, &E.dt))) return rc;
     const int comp = E.cfg.comp;
     const size_t nb = sizeof(double) * (size_t)E.ntr;
@@ -632,6 +659,13 @@ int pt_prof_kernel(int id, int64_t* launches, double* total_ms) {
 }
 
 int64_t pt_prof_launches(void) { return g_launches.load(); }
+
+int pt_prof_tracer_order(int64_t* resorts, double* runs_per_thread) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    if (resorts) *resorts = g_eng->resorts;
+    if (runs_per_thread) *runs_per_thread = g_eng->last_runs;
+    return 0;
+}
 
 int pt_prof_region(int end, double* ms) {
     if (int rc = need(g_eng != nullptr)) return rc;

@@ -167,6 +167,14 @@ struct Engine {
            *str0 = nullptr, *Ttr0 = nullptr, *rtr1 = nullptr, *str1 = nullptr, *Ttr1 = nullptr,
            *rtr2 = nullptr, *str2 = nullptr, *Ttr2 = nullptr;
     int32_t *tcell = nullptr, *cstart = nullptr, *ccount = nullptr, *clist = nullptr;
+    // mixed precision: tracer order (perm[p] = user index of the tracer at position p; perm2 the
+    // re-sort's target), the projection's runs counter, and the re-sort state
+    int32_t *perm = nullptr, *perm2 = nullptr;
+    unsigned long long* proj_runs = nullptr;
+    int32_t *rs_count = nullptr, *rs_start = nullptr, *rs_tot = nullptr;  // re-sort: per-key counts, starts
+    bool perm_active = false, want_resort = false;
+    int64_t resorts = 0;
+    double last_runs = 0.0;  // average runs per thread of the last mixed projection
     double* cpart = nullptr;  // 27 partial sums per cell
     int32_t* scan_tmp = nullptr;
     // state
@@ -260,6 +268,13 @@ int stats(Engine& E, pt_stats_row* out);             // basics.f90:363-462
 int copy_field(Engine& E, double* dst, const double* src);
 
 // tracers (pt_tracers.cu)
+// mixed precision tracer order: identity after an upload; re-sort by cell; exchange of one tracer
+// array with a host-order staging buffer (to_user: staging = user order of internal)
+int tracer_order_reset(Engine& E);
+// sort keys of the re-sort: cells x 4x4 sub-cells
+inline size_t resort_nkey(int nx, int nz) { return (size_t)(nx + 1) * (size_t)(nz + 1) * 16; }
+int resort_tracers(Engine& E);
+int tracer_user_order(Engine& E, double* internal, double* staging, bool to_user);
 int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f,
             int smooth);                              // composition.f90:923-1087
 int rk_stage(Engine& E, int stage);                   // energy.f90:258-536 tracer loops

@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 
 #include "pt_consts.cuh"
 
@@ -115,13 +116,37 @@ __global__ void k_scan_block(const int32_t* in, int32_t* out, int32_t* totals, i
     if (gid < n) out[gid] = base + x - v;
     if (threadIdx.x == blockDim.x - 1) totals[blockIdx.x] = base + x;
 }
-__global__ void k_scan_totals(int32_t* totals, int nb) {
-    if (threadIdx.x != 0) return;
-    int acc = 0;
-    for (int b = 0; b < nb; b++) {
-        int v = totals[b];
+// exclusive scan of the nb block totals in place: one CTA of 1024 threads, a contiguous chunk per
+// thread (chunk sums scanned across the CTA, then each chunk written serially)
+constexpr int kScanTotThreads = 1024;
+__global__ void __launch_bounds__(kScanTotThreads) k_scan_totals(int32_t* totals, int nb) {
+    __shared__ int32_t ws[32];
+    const int per = (nb + kScanTotThreads - 1) / kScanTotThreads;
+    const int b0 = (int)threadIdx.x * per, b1 = min(b0 + per, nb);
+    int v = 0;
+    for (int b = b0; b < b1; b++) v += totals[b];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int y = ws[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += z;
+        }
+        ws[lane] = y;
+    }
+    __syncthreads();
+    int acc = (wid > 0 ? ws[wid - 1] : 0) + x - v;
+    for (int b = b0; b < b1; b++) {
+        const int t = totals[b];
         totals[b] = acc;
-        acc += v;
+        acc += t;
     }
 }
 __global__ void k_scan_add(int32_t* out, const int32_t* totals, int n) {
@@ -288,6 +313,13 @@ __device__ __forceinline__ int fix28(double v, int& bad) {
     return (hw >> 31) ? -a : a;
 }
 
+// average runs per projection thread above which the mixed path re-sorts its tracers by cell.
+// Measured at 1024x512 with 32 tracers per cell: one step of advection takes a sorted order to
+// about 4 runs of 16, the seeding order reaches 7 within ten steps, a random order has 16; the
+// projection costs about the same from 1 to 7 runs (0.47-0.53 ms), the RK stage rises from 0.42 to
+// 1.25 ms and the projection to 0.93 ms in a random order, and a re-sort costs about 0.35 ms.
+constexpr double kResortRuns = 8.0;
+
 // cell and fractions of a tracer; false outside the domain (composition.f90:1007-1010).  EXACT:
 // dr and ds are powers of two (integer decoding only, no FP64 arithmetic)
 struct TracerCell {
@@ -319,7 +351,8 @@ template <bool EXACT>
 __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __restrict__ r, const double* __restrict__ s,
                                                               const double* __restrict__ Tt,
                                                               const double* __restrict__ Ct, int64_t n,
-                                                              unsigned long long* __restrict__ acc, int comp, int* err) {
+                                                              unsigned long long* __restrict__ acc, int comp, int* err,
+                                                              unsigned long long* runs) {
     __shared__ unsigned long long win[4 * kPjWin];  // planes [TS | CS | S | count] of the window
     __shared__ int box[4];
     const int nx1 = cK.nx + 1;
@@ -354,8 +387,10 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
     long long aT[4], aC[4], aS[4];
     uint32_t cnt = 0;  // four 8-bit counters, one per corner (a run holds at most kPjPer tracers)
     int ri = -1, rk = -1;
+    unsigned nflush = 0;  // runs of this thread (the tracer order's locality, reported in runs)
     auto flush = [&]() {
         if (ri < 0) return;
+        nflush++;
         int wi, wk, W, H, P;
         const bool use_win = geometry(wi, wk, W, H, P);
         const int li = ri - wi, lk = rk - wk;
@@ -414,6 +449,10 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
     if (t < t1) add(r[t], s[t], Tt[t], comp ? Ct[t] : 0.0);
     flush();
     if (bad) atomicOr(err, bad);
+    if (runs) {
+        const unsigned wr = __reduce_add_sync(0xffffffffu, nflush);
+        if ((threadIdx.x & 31) == 0) atomicAdd(runs, (unsigned long long)wr);
+    }
     int wi, wk, W, H, P;
     if (!geometry(wi, wk, W, H, P)) return;
     __syncthreads();
@@ -448,6 +487,7 @@ struct ProjScratch {
     int32_t *tcell, *clist, *ccount, *cstart, *scan_tmp;
     double* cpart;
     int* derr;
+    unsigned long long* runs;  // runs counter of the mixed projection (nullptr: not counted)
 };
 
 static int project_with(Engine& E, const ProjScratch& W, const double* r, const double* s, const double* Tt,
@@ -472,13 +512,15 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
             unsigned long long* acc = reinterpret_cast<unsigned long long*>(W.cpart);
             CK(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 4 * (size_t)ncell, E.st));
             auto kern = E.K.exact_div ? k_project_fx<true> : k_project_fx<false>;
-            PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, E.cfg.comp, W.derr);
+            if (W.runs) CK(cudaMemsetAsync(W.runs, 0, sizeof(unsigned long long), E.st));
+            PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, E.cfg.comp, W.derr,
+                                                                         W.runs);
             PT_COUNT(), k_node_fx<<<grid, 128, 0, E.st>>>(acc, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
         } else {  // the reference's association: ascending tracer ID per cell, FP64
             PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, W.tcell, W.ccount, W.derr);
             int nb = (int)nblk(ncell, 1024);
             PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(W.ccount, W.cstart, W.scan_tmp, ncell);
-            PT_COUNT(), k_scan_totals<<<1, 32, 0, E.st>>>(W.scan_tmp, nb);
+            PT_COUNT(), k_scan_totals<<<1, kScanTotThreads, 0, E.st>>>(W.scan_tmp, nb);
             PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(W.cstart, W.scan_tmp, ncell);
             int32_t* cursor = W.scan_tmp + nb + 32;
             CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
@@ -492,9 +534,19 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
         CKL("projection");
     }
     int herr = 0;
+    unsigned long long hruns = 0;
     CK(cudaMemcpyAsync(&herr, W.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+    const bool counted = W.runs && E.cfg.precision == PT_PREC_MIXED;
+    if (counted) CK(cudaMemcpyAsync(&hruns, W.runs, sizeof hruns, cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
     if (herr & 1) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
+    // a thread's kPjPer consecutive tracers make one run when they share a cell; at more than
+    // kResortRuns runs per thread on average the tracer order has lost its locality: re-sort them
+    // by cell before the next step (mixed precision, where the order does not enter any result)
+    if (counted) {
+        E.last_runs = (double)hruns * (double)kPjPer / (double)E.ntr;
+        if (E.last_runs > kResortRuns) E.want_resort = true;
+    }
     if (herr & 2)
         return fail(PT_ERR_CONFIG, "mixed-precision projection: a tracer's T or C is outside (-4, 4) (FP64 precision "
                                    "has no such limit)");
@@ -508,7 +560,7 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
 }
 
 int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f, int smooth) {
-    ProjScratch W{E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp, E.cpart, E.derr};
+    ProjScratch W{E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp, E.cpart, E.derr, E.proj_runs};
     return project_with(E, W, r, s, Tt, T0f, smooth);
 }
 
@@ -559,10 +611,116 @@ int project_noalloc(Engine& E, const double* T0f, int smooth) {
     ProjScratch W{reinterpret_cast<int32_t*>(b + kNaOffCell), reinterpret_cast<int32_t*>(b + kNaOffList),
                   reinterpret_cast<int32_t*>(b + kNaOffCount), reinterpret_cast<int32_t*>(b + kNaOffStart),
                   reinterpret_cast<int32_t*>(b + kNaOffScan), reinterpret_cast<double*>(b + kNaOffPart),
-                  reinterpret_cast<int*>(b + kNaOffFlag)};
+                  reinterpret_cast<int*>(b + kNaOffFlag), nullptr};
     // project_with clears the counts, the scatter cursors and the flag before use; every other
     // part is fully written before it is read
     return project_with(E, W, E.rtr, E.str, E.Ttr, T0f, smooth);
+}
+
+// ---------------------------------------------------------------- tracer locality (mixed precision)
+// The mixed path's results do not depend on the order of the tracers (integer projection sums,
+// per-tracer RK stages), but its speed does: k_project_fx keeps per-cell runs in registers and the
+// RK stage's table gathers hit L1 when neighbouring tracers share cells.  Advection scatters the
+// seeding order, so when the projection reports lost locality the tracers are re-sorted by cell
+// and sub-cell (counting sort) at the start of the next step.  perm[p] is the user's index of the
+// tracer held at position p; tracer fields are exchanged in the user's order (tracer_user_order).
+
+// sort key of each tracer: its cell, column by column (k fastest: the RK stage's 7-row stencils
+// then overlap from one warp to the next), times 16 plus its 4x4 sub-cell (row-major), so that
+// tracers of one cell stay together and, inside the cell, close tracers stay close.  0 for a
+// tracer outside the domain (the projection reports it).  Per-key counts.
+constexpr int kSubKeys = 16;
+template <bool EXACT>
+__global__ void k_tracer_keys(const double* __restrict__ r, const double* __restrict__ s, int64_t n,
+                              int32_t* __restrict__ key, int32_t* __restrict__ count) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1;
+    if (t < n) {
+        TracerCell tc;
+        c = 0;
+        if (locate<EXACT>(r[t], s[t], tc)) {
+            const int sx = min((int)(tc.fx >> 26), 3), sz = min((int)(tc.fz >> 26), 3);
+            c = (tc.k0 + (cK.nz + 1) * tc.i0) * kSubKeys + 4 * sz + sx;
+        }
+        key[t] = c;
+    }
+    const unsigned group = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && (int)(threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(&count[c], __popc(group));
+}
+
+// out_q[p] = in_q[src[p]] for the four tracer arrays, and the user index with them
+__global__ void k_permute_tracers(const int32_t* __restrict__ src, int64_t n, const double* __restrict__ a0,
+                                  const double* __restrict__ a1, const double* __restrict__ a2,
+                                  const double* __restrict__ a3, double* __restrict__ b0, double* __restrict__ b1,
+                                  double* __restrict__ b2, double* __restrict__ b3, const int32_t* __restrict__ pin,
+                                  int32_t* __restrict__ pout) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t t = src[p];
+    b0[p] = a0[t]; b1[p] = a1[t]; b2[p] = a2[t]; b3[p] = a3[t];
+    pout[p] = pin[t];
+}
+
+__global__ void k_iota(int32_t* p, int64_t n) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) p[q] = (int32_t)q;
+}
+
+int tracer_order_reset(Engine& E) {
+    E.perm_active = false;
+    E.want_resort = false;
+    E.resorts = 0;
+    if (!E.perm) return 0;
+    PT_COUNT(), k_iota<<<nblk(E.ntr, 256), 256, 0, E.st>>>(E.perm, E.ntr);
+    CKL("k_iota");
+    return 0;
+}
+
+// counting sort of the tracers by key; the four tracer arrays and perm move together (into the
+// RK stage buffers, then the pointers swap)
+int resort_tracers(Engine& E) {
+    E.want_resort = false;
+    if (!E.perm) return 0;
+    const int nkey = (int)resort_nkey(E.K.nx, E.K.nz);
+    const int64_t n = E.ntr;
+    CK(cudaMemsetAsync(E.rs_count, 0, sizeof(int32_t) * (size_t)nkey, E.st));
+    auto kk = E.K.exact_div ? k_tracer_keys<true> : k_tracer_keys<false>;
+    PT_COUNT(), kk<<<nblk(n, 256), 256, 0, E.st>>>(E.rtr, E.str, n, E.tcell, E.rs_count);
+    const int nb = (int)nblk(nkey, 1024);
+    PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(E.rs_count, E.rs_start, E.rs_tot, nkey);
+    PT_COUNT(), k_scan_totals<<<1, kScanTotThreads, 0, E.st>>>(E.rs_tot, nb);
+    PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(E.rs_start, E.rs_tot, nkey);
+    CK(cudaMemsetAsync(E.rs_count, 0, sizeof(int32_t) * (size_t)nkey, E.st));  // now the cursors
+    PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.rs_start, E.rs_count, E.clist);
+    PT_COUNT(), k_permute_tracers<<<nblk(n, 256), 256, 0, E.st>>>(E.clist, n, E.rtr, E.str, E.Ttr, E.Ctr, E.rtr1,
+                                                                   E.str1, E.Ttr1, E.rtr2, E.perm, E.perm2);
+    CKL("resort_tracers");
+    std::swap(E.rtr, E.rtr1);
+    std::swap(E.str, E.str1);
+    std::swap(E.Ttr, E.Ttr1);
+    std::swap(E.Ctr, E.rtr2);
+    std::swap(E.perm, E.perm2);
+    E.perm_active = true;
+    E.resorts++;
+    return 0;
+}
+
+// user-order exchange of one tracer array: to_user: user[perm[p]] = in[p]; else in[p] = user[perm[p]]
+__global__ void k_perm_scatter(const int32_t* __restrict__ perm, const double* __restrict__ in, double* __restrict__ out,
+                               int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) out[perm[p]] = in[p];
+}
+__global__ void k_perm_gather(const int32_t* __restrict__ perm, const double* __restrict__ in, double* __restrict__ out,
+                              int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) out[p] = in[perm[p]];
+}
+int tracer_user_order(Engine& E, double* internal, double* staging, bool to_user) {
+    if (to_user) PT_COUNT(), k_perm_scatter<<<nblk(E.ntr, 256), 256, 0, E.st>>>(E.perm, internal, staging, E.ntr);
+    else PT_COUNT(), k_perm_gather<<<nblk(E.ntr, 256), 256, 0, E.st>>>(E.perm, staging, internal, E.ntr);
+    CKL("tracer_user_order");
+    return 0;
 }
 
 // ---------------------------------------------------------------- RK4 stage loops

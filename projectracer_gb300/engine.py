@@ -93,6 +93,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_prof_enable.argtypes = [i32]
     L.pt_prof_kernel.argtypes = [i32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
     L.pt_prof_launches.restype = ctypes.c_int64
+    L.pt_prof_tracer_order.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
     L.pt_prof_region.argtypes = [i32, ctypes.POINTER(f64)]
     _LIB = L
     return L
@@ -190,6 +191,16 @@ class Engine:
 
     def launches(self) -> int:
         return int(self.L.pt_prof_launches())
+
+    def tracer_order(self) -> tuple[int, float]:
+        """(re-sorts by cell since the upload, cell runs per projection thread in the last
+        projection); mixed precision, where the tracer order is internal."""
+        n, runs = ctypes.c_int64(), ctypes.c_double()
+        self._check(self.L.pt_prof_tracer_order(ctypes.byref(n), ctypes.byref(runs)))
+        return n.value, runs.value
+
+    def resorts(self) -> int:
+        return self.tracer_order()[0]
 
     def phase_times(self) -> list[float]:
         v = (ctypes.c_double * 8)()
