@@ -10,6 +10,7 @@
 // uses explicit round-to-nearest intrinsics, no contraction).  Mixed precision: one pass with
 // per-tracer fixed-point contributions and integer sums (k_project_fx), deterministic without a
 // sort and independent of the tracer order; counts bit-exact, sums to 2^-28.
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 #include <cstdio>
@@ -313,12 +314,12 @@ __device__ __forceinline__ int fix28(double v, int& bad) {
     return (hw >> 31) ? -a : a;
 }
 
-// average runs per projection thread above which the mixed path re-sorts its tracers by cell.
-// Measured at 1024x512 with 32 tracers per cell: one step of advection takes a sorted order to
-// about 4 runs of 16, the seeding order reaches 7 within ten steps, a random order has 16; the
-// projection costs about the same from 1 to 7 runs (0.47-0.53 ms), the RK stage rises from 0.42 to
-// 1.25 ms and the projection to 0.93 ms in a random order, and a re-sort costs about 0.35 ms.
-constexpr double kResortRuns = 8.0;
+// Re-sort threshold of the mixed path, as a fraction of the way from cell order to a random order
+// in runs (cells) per 16 consecutive tracers.  Measured at 1024x512 with 32 tracers per cell:
+// the seeding order loses about half of its locality within ten steps; a random order costs the RK
+// stage 1.25 ms instead of 0.42 ms and the projection 0.93 ms instead of about 0.5 ms, and a
+// re-sort costs about 0.35 ms.
+constexpr double kResortFrac = 0.5;
 
 // cell and fractions of a tracer; false outside the domain (composition.f90:1007-1010).  EXACT:
 // dr and ds are powers of two (integer decoding only, no FP64 arithmetic)
@@ -338,24 +339,38 @@ __device__ __forceinline__ bool locate(double rr, double ss, TracerCell& c) {
     return true;
 }
 
-// One CTA per chunk of kPjChunk consecutive tracers, kPjPer consecutive tracers per thread.
-// Tracer IDs are spatially grouped (seeding order), so a thread's tracers mostly share a cell: it
-// keeps the running sums of the current cell in registers and adds them, when the cell changes,
-// to a shared-memory window of the grid (64-bit integer shared atomics); at the end the window is
+// One CTA per chunk of kPjChunk consecutive tracers, kPjPer consecutive tracers per lane.  The
+// tracers are kept in cell order, so a lane's tracers mostly share a cell: it keeps the running
+// sums of its current cell (a run) in registers.  A finished run is appended to its warp's run
+// queue in shared memory (slots by ballot rank: all lanes that finish a run in the same step write
+// at once), and when the queue is full the whole warp drains it, one run per lane, into a
+// shared-memory window of the grid (64-bit integer shared atomics).  At the end the window is
 // added to the global sums with one integer atomic per non-zero value.  The window is the box of
-// the cells of every thread's first and last tracer plus one cell of margin; runs outside it (and
+// the cells of every lane's first and last tracer plus one cell of margin; runs outside it (and
 // every run when the box is too large for the window) go to the global sums directly.
-// acc: [node][TS, CS, S, count] int64.
+// acc: [node][TS, CS, S, count] int64; window planes [TS | CS | S + (count << 44)] (a chunk's S
+// stays below 2^44, its counts below 2^20).  runs (optional): the number of runs.
 constexpr int kPjThreads = 256, kPjPer = 16, kPjChunk = kPjThreads * kPjPer, kPjWin = 1280;
-template <bool EXACT>
+constexpr int kPjCountShift = 44;
+constexpr int kPjWarps = kPjThreads / 32;
+
+struct RunQueue {                   // one per warp, structure of arrays (conflict-free slots)
+    int node[32];                   // lower-left node of the run's cell
+    unsigned long long v[13][32];   // TS[4], CS[4], S[4], packed corner counts
+};
+
+template <bool EXACT, bool COMP>
 __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __restrict__ r, const double* __restrict__ s,
                                                               const double* __restrict__ Tt,
                                                               const double* __restrict__ Ct, int64_t n,
-                                                              unsigned long long* __restrict__ acc, int comp, int* err,
+                                                              unsigned long long* __restrict__ acc, int* err,
                                                               unsigned long long* runs) {
-    __shared__ unsigned long long win[4 * kPjWin];  // planes [TS | CS | S | count] of the window
+    __shared__ unsigned long long win[3 * kPjWin];  // planes [TS | CS | S + count << 44] of the window
+    __shared__ RunQueue rq[kPjWarps];
     __shared__ int box[4];
     const int nx1 = cK.nx + 1;
+    const int lane = threadIdx.x & 31;
+    RunQueue& Q = rq[threadIdx.x >> 5];
     const int64_t t0 = (int64_t)blockIdx.x * kPjChunk + (int64_t)threadIdx.x * kPjPer;
     const int64_t t1 = t0 + kPjPer < n ? t0 + kPjPer : n;
     int bad = 0;
@@ -371,7 +386,7 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
     }
     __syncthreads();
     // window: cells box +- 1, i.e. nodes [imin-1, imax+2] x [kmin-1, kmax+2], odd row pitch; its
-    // geometry is re-derived from box[] where needed (fewer live registers in the tracer loop)
+    // geometry is re-derived from box[] in the drains (fewer live registers in the tracer loop)
     auto geometry = [&](int& wi, int& wk, int& W, int& H, int& P) {
         wi = box[0] - 1; wk = box[2] - 1;
         W = box[1] - box[0] + 4; H = box[3] - box[2] + 4; P = W | 1;
@@ -380,88 +395,137 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
     {
         int wi, wk, W, H, P;
         if (geometry(wi, wk, W, H, P)) {
-            for (int q = threadIdx.x; q < 4 * kPjWin; q += kPjThreads) win[q] = 0ull;
+            for (int q = threadIdx.x; q < 3 * kPjWin; q += kPjThreads) win[q] = 0ull;
             __syncthreads();
         }
     }
+    int nq = 0;              // queued runs of this warp (warp-uniform)
+    unsigned nruns = 0;      // runs of this lane
+    // the warp adds its nq queued runs, one per lane
+    auto drain = [&]() {
+        __syncwarp();
+        if (lane < nq) {
+            int wi, wk, W, H, P;
+            const bool use_win = geometry(wi, wk, W, H, P);
+            const int nd = Q.node[lane];
+            const int ci = nd % nx1, ck = nd / nx1;
+            const int li = ci - wi, lk = ck - wk;
+            const unsigned cnt = (unsigned)Q.v[12][lane];
+            if (use_win && li >= 0 && lk >= 0 && li + 1 < W && lk + 1 < H) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int o = (li + (j & 1)) + P * (lk + (j >> 1));
+                    const unsigned long long vT = Q.v[j][lane], vC = Q.v[4 + j][lane];
+                    const unsigned long long vS = Q.v[8 + j][lane] +
+                                                  ((unsigned long long)((cnt >> (8 * j)) & 255u) << kPjCountShift);
+                    if (vT) atomicAdd(&win[o], vT);
+                    if (vC) atomicAdd(&win[kPjWin + o], vC);
+                    if (vS) atomicAdd(&win[2 * kPjWin + o], vS);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const size_t node = (size_t)(ci + (j & 1)) + (size_t)nx1 * (size_t)(ck + (j >> 1));
+                    const unsigned long long v[4] = {Q.v[j][lane], Q.v[4 + j][lane], Q.v[8 + j][lane],
+                                                     (cnt >> (8 * j)) & 255u};
+#pragma unroll
+                    for (int p = 0; p < 4; p++)
+                        if (v[p]) atomicAdd(&acc[4 * node + p], v[p]);
+                }
+            }
+        }
+        __syncwarp();
+        nq = 0;
+    };
     long long aT[4], aC[4], aS[4];
     uint32_t cnt = 0;  // four 8-bit counters, one per corner (a run holds at most kPjPer tracers)
     int ri = -1, rk = -1;
-    unsigned nflush = 0;  // runs of this thread (the tracer order's locality, reported in runs)
-    auto flush = [&]() {
-        if (ri < 0) return;
-        nflush++;
-        int wi, wk, W, H, P;
-        const bool use_win = geometry(wi, wk, W, H, P);
-        const int li = ri - wi, lk = rk - wk;
-        const bool inside = use_win && li >= 0 && lk >= 0 && li + 1 < W && lk + 1 < H;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int a = j & 1, b = j >> 1;
-            const long long v[4] = {aT[j], aC[j], aS[j], (long long)((cnt >> (8 * j)) & 255u)};
-            if (inside) {
-                const int o = (li + a) + P * (lk + b);
-#pragma unroll
-                for (int p = 0; p < 4; p++)
-                    if (v[p]) atomicAdd(&win[p * kPjWin + o], (unsigned long long)v[p]);
-            } else {
-                const size_t node = (size_t)(ri + a) + (size_t)nx1 * (size_t)(rk + b);
-#pragma unroll
-                for (int p = 0; p < 4; p++)
-                    if (v[p]) atomicAdd(&acc[4 * node + p], (unsigned long long)v[p]);
-            }
-        }
-    };
-    auto add = [&](double rr, double ss, double tv, double cv) {
+    // one warp-synchronous step: lane tracer (valid: a tracer to add, fin: the lane's last call)
+    auto step = [&](bool valid, double rr, double ss, double tv, double cv, bool fin) {
         TracerCell c;
-        if (!locate<EXACT>(rr, ss, c)) {
-            bad |= 1;
-            return;
+        bool inside = false;
+        if (valid) {
+            inside = locate<EXACT>(rr, ss, c);
+            if (!inside) bad |= 1;
         }
-        if (c.i0 != ri || c.k0 != rk) {
-            flush();
+        const bool close = ri >= 0 && (fin || (inside && (c.i0 != ri || c.k0 != rk)));
+        const unsigned m = __ballot_sync(0xffffffffu, close);
+        if (m) {
+            if (nq + __popc(m) > 32) drain();
+            if (close) {
+                const int slot = nq + __popc(m & ((1u << lane) - 1u));
+                Q.node[slot] = ri + nx1 * rk;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    Q.v[j][slot] = (unsigned long long)aT[j];
+                    Q.v[4 + j][slot] = (unsigned long long)aC[j];
+                    Q.v[8 + j][slot] = (unsigned long long)aS[j];
+                }
+                Q.v[12][slot] = cnt;
+                nruns++;
+                ri = -1;
+            }
+            nq += __popc(m);
+        }
+        if (!inside) return;
+        if (ri < 0) {
             ri = c.i0;
             rk = c.k0;
 #pragma unroll
             for (int j = 0; j < 4; j++) aT[j] = aC[j] = aS[j] = 0;
             cnt = 0;
         }
-        const int T28 = fix28(tv, bad), C28 = comp ? fix28(cv, bad) : 0;
+        const int T28 = fix28(tv, bad), C28 = COMP ? fix28(cv, bad) : 0;
         const uint32_t wx[2] = {(uint32_t)kFixOne - c.fx, c.fx}, wz[2] = {(uint32_t)kFixOne - c.fz, c.fz};
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int S = (int)(((unsigned long long)wx[j & 1] * wz[j >> 1] + (1ull << 27)) >> 28);
             aS[j] += S;
             aT[j] += (int)(((long long)T28 * S + (1ll << 27)) >> 28);  // |.| <= |T28|: fits
-            if (comp) aC[j] += (int)(((long long)C28 * S + (1ll << 27)) >> 28);
+            if (COMP) aC[j] += (int)(((long long)C28 * S + (1ll << 27)) >> 28);
         }
         cnt += 1u << (8 * c.near);
     };
-    // consecutive pairs with 16-byte loads (t0 is even; the arrays are 16-byte aligned)
+    // consecutive pairs with 16-byte loads (t0 is even; the arrays are 16-byte aligned); every
+    // lane runs the same number of steps (the warp's last lanes may hold fewer tracers)
     auto ld2 = [](const double* a, int64_t i) { return __ldg(reinterpret_cast<const double2*>(a + i)); };
-    int64_t t = t0;
-    for (; t + 1 < t1; t += 2) {
-        const double2 r2 = ld2(r, t), s2 = ld2(s, t), T2 = ld2(Tt, t);
-        const double2 C2 = comp ? ld2(Ct, t) : make_double2(0.0, 0.0);
-        add(r2.x, s2.x, T2.x, C2.x);
-        add(r2.y, s2.y, T2.y, C2.y);
+    for (int q = 0; q < kPjPer; q += 2) {
+        const int64_t t = t0 + q;
+        if (t + 1 < t1) {
+            const double2 r2 = ld2(r, t), s2 = ld2(s, t), T2 = ld2(Tt, t);
+            const double2 C2 = COMP ? ld2(Ct, t) : make_double2(0.0, 0.0);
+            step(true, r2.x, s2.x, T2.x, C2.x, false);
+            step(true, r2.y, s2.y, T2.y, C2.y, false);
+        } else {
+            const bool v = t < t1;
+            step(v, v ? r[t] : 0.0, v ? s[t] : 0.0, v ? Tt[t] : 0.0, v && COMP ? Ct[t] : 0.0, false);
+            step(false, 0.0, 0.0, 0.0, 0.0, false);
+        }
     }
-    if (t < t1) add(r[t], s[t], Tt[t], comp ? Ct[t] : 0.0);
-    flush();
+    step(false, 0.0, 0.0, 0.0, 0.0, true);  // close the open runs
+    if (nq) drain();
     if (bad) atomicOr(err, bad);
     if (runs) {
-        const unsigned wr = __reduce_add_sync(0xffffffffu, nflush);
-        if ((threadIdx.x & 31) == 0) atomicAdd(runs, (unsigned long long)wr);
+        const unsigned wr = __reduce_add_sync(0xffffffffu, nruns);
+        if (lane == 0 && wr) atomicAdd(runs, (unsigned long long)wr);
     }
     int wi, wk, W, H, P;
     if (!geometry(wi, wk, W, H, P)) return;
     __syncthreads();
     const int nw = W * H;
-    for (int q = threadIdx.x; q < 4 * nw; q += kPjThreads) {
-        const int p = q & 3, cell = q >> 2;
+    const unsigned long long smask = (1ull << kPjCountShift) - 1ull;
+    for (int q = threadIdx.x; q < 3 * nw; q += kPjThreads) {
+        const int p = q % 3, cell = q / 3;
         const int row = cell / W, col = cell - row * W;
         const unsigned long long v = win[p * kPjWin + row * P + col];
-        if (v) atomicAdd(&acc[4 * ((size_t)(wi + col) + (size_t)nx1 * (size_t)(wk + row)) + p], v);
+        if (!v) continue;
+        unsigned long long* a = &acc[4 * ((size_t)(wi + col) + (size_t)nx1 * (size_t)(wk + row))];
+        if (p < 2) {
+            atomicAdd(&a[p], v);
+        } else {
+            if (v & smask) atomicAdd(&a[2], v & smask);
+            if (v >> kPjCountShift) atomicAdd(&a[3], v >> kPjCountShift);
+        }
     }
 }
 
@@ -511,10 +575,10 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
                     return fail(PT_ERR_ARG, "mixed-precision projection: tracer arrays must be 16-byte aligned");
             unsigned long long* acc = reinterpret_cast<unsigned long long*>(W.cpart);
             CK(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 4 * (size_t)ncell, E.st));
-            auto kern = E.K.exact_div ? k_project_fx<true> : k_project_fx<false>;
+            auto kern = E.K.exact_div ? (E.cfg.comp ? k_project_fx<true, true> : k_project_fx<true, false>)
+                                      : (E.cfg.comp ? k_project_fx<false, true> : k_project_fx<false, false>);
             if (W.runs) CK(cudaMemsetAsync(W.runs, 0, sizeof(unsigned long long), E.st));
-            PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, E.cfg.comp, W.derr,
-                                                                         W.runs);
+            PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, W.derr, W.runs);
             PT_COUNT(), k_node_fx<<<grid, 128, 0, E.st>>>(acc, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
         } else {  // the reference's association: ascending tracer ID per cell, FP64
             PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, W.tcell, W.ccount, W.derr);
@@ -540,12 +604,14 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
     if (counted) CK(cudaMemcpyAsync(&hruns, W.runs, sizeof hruns, cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
     if (herr & 1) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
-    // a thread's kPjPer consecutive tracers make one run when they share a cell; at more than
-    // kResortRuns runs per thread on average the tracer order has lost its locality: re-sort them
-    // by cell before the next step (mixed precision, where the order does not enter any result)
+    // runs per kPjPer consecutive tracers: from about kPjPer / (tracers per cell) in cell order to
+    // kPjPer in a random order; past kResortFrac of the way the tracers are re-sorted by cell
+    // before the next step (mixed precision, where the order does not enter any result)
     if (counted) {
         E.last_runs = (double)hruns * (double)kPjPer / (double)E.ntr;
-        if (E.last_runs > kResortRuns) E.want_resort = true;
+        const double per_cell = (double)E.ntr / ((double)E.K.nx * (double)E.K.nz);
+        const double sorted = std::max(1.0, (double)kPjPer / std::max(per_cell, 1.0));
+        if (E.last_runs > sorted + kResortFrac * ((double)kPjPer - sorted)) E.want_resort = true;
     }
     if (herr & 2)
         return fail(PT_ERR_CONFIG, "mixed-precision projection: a tracer's T or C is outside (-4, 4) (FP64 precision "
