@@ -33,18 +33,65 @@ int cuda_check(cudaError_t e, const char* what) {
     return PT_ERR_CUDA;
 }
 
-PhaseTimer::PhaseTimer(Engine& e, int s) : E(e), slot(s) {
-    if (E.pev[slot][0]) cudaEventRecord(E.pev[slot][0], E.st);
+static cudaEvent_t take_event(Engine& E) {
+    cudaEvent_t ev = nullptr;
+    if (!E.ev_pool.empty()) {
+        ev = E.ev_pool.back();
+        E.ev_pool.pop_back();
+    } else if (cudaEventCreate(&ev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        ev = nullptr;
+    }
+    return ev;
 }
-PhaseTimer::~PhaseTimer() {
-    if (!E.pev[slot][0]) return;
-    cudaEventRecord(E.pev[slot][1], E.st);
-    if (cudaEventSynchronize(E.pev[slot][1]) == cudaSuccess) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, E.pev[slot][0], E.pev[slot][1]);
-        E.phase_ms[slot] += ms;
+
+static void push_span(Engine& E, int slot, int kid, int n, cudaEvent_t a) {
+    if (!a) return;
+    cudaEvent_t b = take_event(E);
+    if (!b) {
+        E.ev_pool.push_back(a);
+        return;
+    }
+    cudaEventRecord(b, E.st);
+    E.spans.push_back({slot, kid, n, a, b});
+    if (E.spans.size() > 8192) {  // bound the pending list
+        cudaStreamSynchronize(E.st);
+        harvest_spans(E);
     }
 }
+
+void harvest_spans(Engine& E) {
+    size_t keep = 0;
+    for (size_t q = 0; q < E.spans.size(); q++) {
+        const Engine::Span s = E.spans[q];
+        float ms = 0.f;
+        const cudaError_t e = cudaEventElapsedTime(&ms, s.a, s.b);
+        if (e == cudaErrorNotReady) {  // still running: keep for a later harvest
+            (void)cudaGetLastError();
+            E.spans[keep++] = s;
+            continue;
+        }
+        if (e == cudaSuccess) {
+            if (s.slot >= 0) {
+                E.phase_ms[s.slot] += ms;
+            } else {
+                E.kms[s.kid] += ms;
+                E.kcount[s.kid] += s.n;
+            }
+        } else {
+            (void)cudaGetLastError();  // a timing miss must not surface as the next launch's error
+        }
+        E.ev_pool.push_back(s.a);
+        E.ev_pool.push_back(s.b);
+    }
+    E.spans.resize(keep);
+}
+
+PhaseTimer::PhaseTimer(Engine& e, int s) : E(e), slot(s) {
+    a = take_event(E);
+    if (a) cudaEventRecord(a, E.st);
+}
+PhaseTimer::~PhaseTimer() { push_span(E, slot, 0, 0, a); }
 
 // cudaEventRecordExternal makes the record a timing node of the captured graph (a plain record
 // during capture only expresses a dependency)
@@ -69,18 +116,11 @@ void harvest_graph_timer(Engine& E, int which) {
 }
 
 KernelTimer::KernelTimer(Engine& e, int i, int count) : E(e), id(i), n(count) {
-    if (E.prof) cudaEventRecord(E.kev0, E.st);
-}
-KernelTimer::~KernelTimer() {
     if (!E.prof) return;
-    cudaEventRecord(E.kev1, E.st);
-    if (cudaEventSynchronize(E.kev1) == cudaSuccess) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, E.kev0, E.kev1);
-        E.kms[id] += ms;
-        E.kcount[id] += n;
-    }
+    a = take_event(E);
+    if (a) cudaEventRecord(a, E.st);
 }
+KernelTimer::~KernelTimer() { push_span(E, -1, id, n, a); }
 
 static int dalloc(Engine& E, double** p, size_t n) {
     CK(cudaMalloc(p, n * sizeof(double)));
@@ -200,9 +240,13 @@ static void engine_free(Engine& E) {
     if (E.st2) cudaStreamDestroy(E.st2);
     if (E.derr) cudaFree(E.derr);
     if (E.hscal) cudaFreeHost(E.hscal);
-    for (int q = 0; q < PT_NPHASE; q++)
-        for (int j = 0; j < 2; j++)
-            if (E.pev[q][j]) cudaEventDestroy(E.pev[q][j]);
+    for (const Engine::Span& s : E.spans) {
+        cudaEventDestroy(s.a);
+        cudaEventDestroy(s.b);
+    }
+    E.spans.clear();
+    for (cudaEvent_t ev : E.ev_pool) cudaEventDestroy(ev);
+    E.ev_pool.clear();
     for (int q = 0; q < 2; q++)
         for (int j = 0; j < 2; j++)
             if (E.gev[q][j]) cudaEventDestroy(E.gev[q][j]);
@@ -210,10 +254,8 @@ static void engine_free(Engine& E) {
     if (E.gM2) cudaGraphExecDestroy(E.gM2);
     if (E.gA) cudaGraphExecDestroy(E.gA);
     if (E.gB) cudaGraphExecDestroy(E.gB);
-    if (E.kev0) cudaEventDestroy(E.kev0);
     if (E.rev0) cudaEventDestroy(E.rev0);
     if (E.rev1) cudaEventDestroy(E.rev1);
-    if (E.kev1) cudaEventDestroy(E.kev1);
     if (E.st) cudaStreamDestroy(E.st);
 }
 
@@ -309,12 +351,8 @@ int pt_init(const pt_config* cfg) {
     E->g1 = make_geo(cfg->nx, cfg->nz);
     for (int l = 1; l <= E->grids; l++) E->gl[l] = make_geo(E->L[l].nx, E->L[l].nz);
     if ((rc = cuda_check(cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking), "stream"))) { delete E; return rc; }
-    for (int q = 0; q < PT_NPHASE; q++)
-        for (int j = 0; j < 2; j++) cudaEventCreate(&E->pev[q][j]);
     for (int q = 0; q < 2; q++)
         for (int j = 0; j < 2; j++) cudaEventCreate(&E->gev[q][j]);
-    cudaEventCreate(&E->kev0);
-    cudaEventCreate(&E->kev1);
     g_eng = E;
     TRACE("pt_init: device allocations and constants");
     if ((rc = engine_alloc(*E)) || (rc = upload_consts_fields(*E)) || (rc = upload_consts_tracers(*E)) ||
@@ -515,6 +553,7 @@ static int solve_psi(Engine& E, pt_solve_info* info) {
     cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    harvest_spans(E);
     if (info) {
         info->ms += ms;
         info->n_temp = E.n_temp;
@@ -582,6 +621,7 @@ int pt_step(double* dt_out, pt_solve_info* info) {
     if (dt_out) *dt_out = E.dt;
     if (info) info->n_temp = E.n_temp;
     CK(cudaStreamSynchronize(E.st));
+    harvest_spans(E);
     return 0;
 }
 
@@ -645,6 +685,8 @@ int pt_prof_enable(int on) {
 
 int pt_prof_reset(void) {
     if (int rc = need(g_eng != nullptr)) return rc;
+    CK(cudaStreamSynchronize(g_eng->st));
+    harvest_spans(*g_eng);
     for (int q = 0; q < 8; q++) { g_eng->kcount[q] = 0; g_eng->kms[q] = 0.0; }
     g_launches = 0;
     return 0;
@@ -653,6 +695,8 @@ int pt_prof_reset(void) {
 int pt_prof_kernel(int id, int64_t* launches, double* total_ms) {
     if (int rc = need(g_eng != nullptr)) return rc;
     if (id < 0 || id >= 8) return fail(PT_ERR_ARG, "kernel id out of range");
+    CK(cudaStreamSynchronize(g_eng->st));
+    harvest_spans(*g_eng);
     if (launches) *launches = g_eng->kcount[id];
     if (total_ms) *total_ms = g_eng->kms[id];
     return 0;
@@ -691,6 +735,8 @@ int pt_prof_region(int end, double* ms) {
 int pt_phase_times(double* ms8) {
     if (int rc = need(g_eng != nullptr)) return rc;
     if (!ms8) return fail(PT_ERR_ARG, "null pointer");
+    CK(cudaStreamSynchronize(g_eng->st));
+    harvest_spans(*g_eng);
     for (int q = 0; q < PT_NPHASE; q++) ms8[q] = g_eng->phase_ms[q];
     return 0;
 }

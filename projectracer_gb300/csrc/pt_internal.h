@@ -185,7 +185,15 @@ struct Engine {
     int n_eta = 0, n_temp = 0, cycles = 0, refinements = 0;
     double eig_fine = 0, resid_ratio = 0, res_ref[PT_MAXLEV] = {}, residual_mag1 = 0;
     double phase_ms[PT_NPHASE] = {};
-    cudaEvent_t pev[PT_NPHASE][2] = {};  // one start/stop pair per phase slot (slots nest)
+    // timed spans (phase slots, and kernel classes when profiling is on) whose events have been
+    // recorded but not yet read: read at the library's existing synchronisation points
+    // (harvest_spans), so that timing adds no host wait of its own
+    struct Span {
+        int slot, kid, n;  // slot >= 0: phase slot; else kernel class kid with n launches
+        cudaEvent_t a, b;
+    };
+    std::vector<Span> spans;
+    std::vector<cudaEvent_t> ev_pool;
     // events recorded inside the captured level-1 smoothing batch (graph nodes), read after the
     // graph's synchronisation when profiling is on: [0] FP64 batch, [1] FP32 batch
     cudaEvent_t gev[2][2] = {};
@@ -196,7 +204,6 @@ struct Engine {
     cudaGraphExec_t gA = nullptr, gB = nullptr;  // captured multigrid cycle (parts A and B)
     int64_t nA = 0, nB = 0;
     int prof = 0;
-    cudaEvent_t kev0 = nullptr, kev1 = nullptr;
     cudaEvent_t rev0 = nullptr, rev1 = nullptr;  // pt_prof_region
     int64_t kcount[8] = {};
     double kms[8] = {};
@@ -210,9 +217,12 @@ extern std::atomic<int64_t> g_launches;
 struct KernelTimer {
     Engine& E;
     int id, n;
+    cudaEvent_t a = nullptr;
     KernelTimer(Engine& e, int i, int count);
     ~KernelTimer();
 };
+// adds the completed spans to phase_ms / kms (call after a synchronisation of the stream)
+void harvest_spans(Engine& E);
 enum { KT_RKC_FP64_L1 = 0, KT_RKC_FP32_L1 = 1, KT_RK_STAGE = 2, KT_PROJECT = 3 };
 // Event pair around the level-1 smoothing batch of a cycle; recorded into the CUDA graph when the
 // batch is captured, read by harvest_graph_timer after the graph has run.
@@ -306,6 +316,7 @@ int reduce_max_smoothness(Engine& E, const double* f, double* out);
 struct PhaseTimer {
     Engine& E;
     int slot;
+    cudaEvent_t a = nullptr;
     PhaseTimer(Engine& e, int s);
     ~PhaseTimer();
 };

@@ -1237,6 +1237,7 @@ int multigrid(Engine& E, pt_solve_info* info) {
             if ((rc = run_part(E, 0))) return rc;
             CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
         }
+        CK(cudaStreamSynchronize(E.st));
         harvest_graph_timer(E, 0);
         mag1 = E.hscal[0] / (double)(E.gl[1].nx - 2) / (double)(E.gl[1].nz - 2);
         (void)norm;

@@ -710,6 +710,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
             if ((rc = run_mixed(E, 0))) return rc;
             CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
         }
+        CK(cudaStreamSynchronize(E.st));
         harvest_graph_timer(E, 1);
         mag1 = E.hscal[0] / norm;
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite residual in the mixed-precision solve");
