@@ -425,7 +425,7 @@ def algorithmic_bytes(kid: int, cfg) -> float:
 NCU_TRAFFIC = {
     1: ("per launch", 17.05e6, "profiles/k_rkc_stage_f_C3_1024x512.md"),
     2: ("per tracer", 109.9e6 / 2097152, "profiles/k_rk_stage_f_C3_1024x512.md"),
-    3: ("per tracer", 91.3e6 / 2097152, "profiles/k_project_fx_C3_1024x512.md"),
+    3: ("per tracer", (555.24e6 + 19.88e6) / 16777216, "profiles/k_project_fx_C3_1024x512.md"),
 }
 
 
