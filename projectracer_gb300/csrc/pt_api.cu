@@ -573,12 +573,17 @@ static int stage_tables(Engine& E) {
     PhaseTimer tm(E, PH_GRID);
     int rc;
     if ((rc = load_tracer_space(E))) return rc;
+    if (use_tables_fx(E)) return tables_fx(E, 2, E.tsa);
     if ((rc = compute_derivatives(E, E.tsa, 2))) return rc;
     return tables_to_f32(E, 2, E.tsa);
 }
 static int velocity_tables(Engine& E) {
     PhaseTimer tm(E, PH_GRID);
     int rc;
+    if (use_tables_fx(E)) {
+        if ((rc = tables_fx(E, 0, E.u))) return rc;
+        return tables_fx(E, 1, E.w);
+    }
     if ((rc = compute_derivatives(E, E.u, 0))) return rc;
     if ((rc = compute_derivatives(E, E.w, 1))) return rc;
     if ((rc = tables_to_f32(E, 0, E.u))) return rc;

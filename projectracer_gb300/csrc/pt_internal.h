@@ -271,6 +271,9 @@ int coarse_scale_fit(Engine& E, double* alpha);   // pt_mg.cu
 int unet_engine_release(Engine& E);
 int unet_engine_load(Engine& E, const char* path);  // PT_GUESS_UNET weights
 int tables_to_f32(Engine& E, int which, const double* f);  // FP32 copies for the mixed RK stage
+// the mixed RK stage's FP32 table of f straight from exact integer stencil sums (no FP64 table)
+bool use_tables_fx(const Engine& E);
+int tables_fx(Engine& E, int which, const double* f);
 int compute_derivatives(Engine& E, const double* f, int which);  // composition.f90:1457-1478
 int compute_velocities(Engine& E);                   // momentum.f90:655-710
 int stability_dt(Engine& E, double* dt);             // energy.f90:756-810

@@ -12,6 +12,7 @@
 // sort and independent of the tracer order; counts bit-exact, sums to 2^-28.
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -979,6 +980,140 @@ __global__ void k_tables_to_f32(float4* out, const double* F, const double* D1, 
     if (q >= n) return;
     out[q] = make_float4((float)F[q], (float)D1[q], (float)D2[q], (float)D3[q]);
 }
+
+// ---- the same table from exact integer stencil sums (mixed path)
+// The x-derivative stencils are small rationals (D1 = [1,-8,0,8,-1]/12, D2 = [-1,16,-30,16,-1]/12,
+// D3 = [1,-8,13,0,-13,8,-1]/8, checked on the host), so with a row segment of f in fixed point
+// (X = round(f 2^s), |X| < 2^62 from the segment's largest exponent, split as Xh 2^31 + Xl) each
+// derivative is an exact integer sum; only its conversion to FP32 rounds.  The conversions are
+// integer operations, so the table costs no FP64 arithmetic (the FP64 path's k_derivs takes 45
+// FP64 operations per node and its FP32 copy four more).
+constexpr int kTbX = 128;
+
+// v 2^e2 rounded to FP32 (to nearest, ties away from zero; below the normal range: 0)
+__device__ __forceinline__ float i64_to_float_scaled(long long v, int e2) {
+    if (v == 0) return 0.f;
+    const unsigned sgn = v < 0 ? 0x80000000u : 0u;
+    unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+    const int lz = __clzll(a);
+    a <<= lz;                                             // leading one at bit 63
+    unsigned long long m = (a >> 39) + 1;                 // 25 bits, rounding bit added
+    int ex = 127 + 63 - lz + e2;
+    if (m >> 25) { m >>= 1; ex++; }                       // the rounding carried into bit 25
+    m >>= 1;                                              // 24 bits, leading one at bit 23
+    if (ex <= 0) return 0.f;
+    if (ex >= 255) return __uint_as_float(sgn | 0x7F800000u);
+    return __uint_as_float(sgn | ((unsigned)ex << 23) | ((unsigned)m & 0x7FFFFFu));
+}
+// FP64 to FP32 from the bit pattern (to nearest, ties away from zero; FP32-subnormal results: 0)
+__device__ __forceinline__ float d2f_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0x7FF) return __uint_as_float(sgn | 0x7F800000u | (unsigned)((b & 0xFFFFFFFFFFFFFull) != 0) << 22);
+    unsigned long long m = ((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) + (1ull << 28);  // round at bit 29
+    int ex = e - 1023 + 127;
+    if (m >> 53) { m >>= 1; ex++; }
+    if (e == 0 || ex <= 0) return __uint_as_float(sgn);
+    if (ex >= 255) return __uint_as_float(sgn | 0x7F800000u);
+    return __uint_as_float(sgn | ((unsigned)ex << 23) | ((unsigned)(m >> 29) & 0x7FFFFFu));
+}
+
+// one CTA per kTbX nodes of a row k in [-3, nz+3]; nodes i in [0, nx]
+__global__ void __launch_bounds__(kTbX) k_tables_fx(float4* __restrict__ out, const double* __restrict__ f, Geo g,
+                                                    float c1, float c2, float c3) {
+    __shared__ int2 X[kTbX + 6];
+    __shared__ int emax_s;
+    const int nx = cK.nx;
+    const int i0 = blockIdx.x * kTbX, k = (int)blockIdx.y - 3;
+    if (threadIdx.x == 0) emax_s = 0;
+    __syncthreads();
+    unsigned long long raw[2];
+    int em = 0;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int idx = threadIdx.x + kTbX * q;
+        unsigned long long b = 0;
+        if (idx < kTbX + 6) {
+            const int i = i0 - 3 + idx;
+            if (i <= nx + 3) b = (unsigned long long)__double_as_longlong(f[g.at(i, k)]);
+        }
+        raw[q] = b;
+        em = max(em, (int)((b >> 52) & 0x7FF));
+    }
+    em = __reduce_max_sync(0xffffffffu, em);
+    if ((threadIdx.x & 31) == 0) atomicMax(&emax_s, em);
+    __syncthreads();
+    const int emax = emax_s;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int idx = threadIdx.x + kTbX * q;
+        if (idx >= kTbX + 6) break;
+        const unsigned long long b = raw[q];
+        const int e = (int)((b >> 52) & 0x7FF);
+        long long v = 0;
+        if (e != 0 && emax != 0x7FF) {
+            const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+            const int sh = emax - 9 - e;  // X = m 2^-sh, |X| < 2^62
+            unsigned long long a;
+            if (sh <= 0) a = m << (-sh);
+            else if (sh < 64) a = (m + (1ull << (sh - 1))) >> sh;
+            else a = 0;
+            v = (b >> 63) ? -(long long)a : (long long)a;
+        }
+        const long long h = v >> 31;  // floor
+        X[idx] = make_int2((int)h, (int)(v - (h << 31)));
+    }
+    __syncthreads();
+    const int i = i0 + (int)threadIdx.x;
+    if (i > nx) return;
+    const double fv = f[g.at(i, k)];
+    if (emax == 0x7FF) {  // Inf/NaN in the segment: NaN derivatives, as the FP64 stencil gives
+        const float nan = __uint_as_float(0x7FC00000u);
+        out[g.at(i, k)] = make_float4(d2f_bits(fv), nan, nan, nan);
+        return;
+    }
+    constexpr int w1[7] = {0, 1, -8, 0, 8, -1, 0}, w2[7] = {0, -1, 16, -30, 16, -1, 0},
+                  w3[7] = {1, -8, 13, 0, -13, 8, -1};
+    long long h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0;
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        const int2 x = X[threadIdx.x + j];
+        if (w1[j]) { h1 += (long long)w1[j] * x.x; l1 += (long long)w1[j] * x.y; }
+        if (w2[j]) { h2 += (long long)w2[j] * x.x; l2 += (long long)w2[j] * x.y; }
+        if (w3[j]) { h3 += (long long)w3[j] * x.x; l3 += (long long)w3[j] * x.y; }
+    }
+    // sum = (h 2^31 + l) 2^-s with s = 1084 - emax; h 2^23 + (l >> 8) keeps 2^-54 of the
+    // segment's scale and fits 64 bits
+    const int e2 = 8 - (1084 - emax);
+    const float d1 = i64_to_float_scaled((h1 << 23) + (l1 >> 8), e2) * c1;
+    const float d2 = i64_to_float_scaled((h2 << 23) + (l2 >> 8), e2) * c2;
+    const float d3 = i64_to_float_scaled((h3 << 23) + (l3 >> 8), e2) * c3;
+    out[g.at(i, k)] = make_float4(d2f_bits(fv), d1, d2, d3);
+}
+
+// the integer stencils above are the run's x-derivative stencils (checked once per call: 21
+// comparisons on the host)
+static bool tables_exact_ok(const Consts& K) {
+    const int w[4][7] = {{}, {0, 1, -8, 0, 8, -1, 0}, {0, -1, 16, -30, 16, -1, 0}, {1, -8, 13, 0, -13, 8, -1}};
+    const double den[4] = {1.0, 12.0, 12.0, 8.0};
+    for (int m = 1; m <= 3; m++)
+        for (int j = 0; j < 7; j++)
+            if (std::fabs(K.Dm[m][j] * den[m] - w[m][j]) > 1e-12) return false;
+    return true;
+}
+
+int tables_fx(Engine& E, int which, const double* f) {
+    const Consts& K = E.K;
+    const float c1 = (float)(1.0 / (12.0 * K.dr_pow[1])), c2 = (float)(1.0 / (12.0 * K.dr_pow[2])),
+                c3 = (float)(1.0 / (8.0 * K.dr_pow[3]));
+    dim3 grid(nblk(K.nx + 1, kTbX), K.nz + 7);
+    PT_COUNT(), k_tables_fx<<<grid, kTbX, 0, E.st>>>(E.ftab[which], f, E.g1, c1, c2, c3);
+    CKL("k_tables_fx");
+    return 0;
+}
+
+bool use_tables_fx(const Engine& E) { return E.ftab[0] != nullptr && tables_exact_ok(E.K); }
 
 int tables_to_f32(Engine& E, int which, const double* f) {
     if (!E.ftab[which]) return 0;
