@@ -36,6 +36,10 @@ int pt_prof_region(int end, double* ms);
  * order): re-sorts by cell since the last pt_upload_state, and the average number of cell runs per
  * projection thread (of 16 consecutive tracers) in the last projection. */
 int pt_prof_tracer_order(int64_t* resorts, double* runs_per_thread);
+/* Mixed precision: the RK stage's FP32 interpolation table `which` (0 u, 1 w, 2 the tracer-space
+ * term) as last built, nodes i = 0..nx of rows k = -3..nz+3, row-major, four floats per node
+ * (value and x-derivatives of order 1, 2, 3): (nz+7)(nx+1)*4 floats. */
+int pt_prof_table(int which, float* host);
 
 #ifdef __cplusplus
 }

@@ -709,6 +709,18 @@ int pt_prof_kernel(int id, int64_t* launches, double* total_ms) {
 
 int64_t pt_prof_launches(void) { return g_launches.load(); }
 
+int pt_prof_table(int which, float* host) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    Engine& E = *g_eng;
+    if (which < 0 || which > 2 || !host) return fail(PT_ERR_ARG, "table id out of range or null pointer");
+    if (!E.ftab[which]) return fail(PT_ERR_STATE, "the FP32 tables exist in mixed precision only");
+    const size_t w = (size_t)(E.K.nx + 1) * sizeof(float4);
+    CK(cudaMemcpy2DAsync(host, w, E.ftab[which] + E.g1.at(0, -3), E.g1.pitch * sizeof(float4), w,
+                         (size_t)(E.K.nz + 7), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    return 0;
+}
+
 int pt_prof_tracer_order(int64_t* resorts, double* runs_per_thread) {
     if (int rc = need(g_eng != nullptr)) return rc;
     if (resorts) *resorts = g_eng->resorts;

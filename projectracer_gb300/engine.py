@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_prof_kernel.argtypes = [i32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
     L.pt_prof_launches.restype = ctypes.c_int64
     L.pt_prof_tracer_order.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
+    L.pt_prof_table.argtypes = [i32, vp]
     L.pt_prof_region.argtypes = [i32, ctypes.POINTER(f64)]
     _LIB = L
     return L
@@ -201,6 +202,13 @@ class Engine:
 
     def resorts(self) -> int:
         return self.tracer_order()[0]
+
+    def table(self, which: int) -> np.ndarray:
+        """The mixed RK stage's FP32 table `which` (0 u, 1 w, 2 tracer-space term): array of
+        shape (nz+7, nx+1, 4), rows k = -3..nz+3, [value, d/dx, d2/dx2, d3/dx3]."""
+        out = np.empty((self.nz + 7, self.nx + 1, 4), dtype=np.float32)
+        self._check(self.L.pt_prof_table(which, _ptr(out)))
+        return out
 
     def phase_times(self) -> list[float]:
         v = (ctypes.c_double * 8)()

@@ -332,3 +332,35 @@ def test_extrapolated_guess_steps_close_to_previous_guess():
     for a, b in zip(out[PT_GUESS_PREVIOUS], out[PT_GUESS_EXTRAPOLATE]):
         assert rel_err(b, a) < 1e-6
     assert cycles[PT_GUESS_EXTRAPOLATE] <= cycles[PT_GUESS_PREVIOUS]
+
+
+def test_mixed_tables_match_fp64_stencils():
+    """The mixed RK stage's FP32 tables (value and x-derivatives 1..3 of u and w, built from exact
+    integer stencil sums) against the same stencils in FP64 on the downloaded velocities: the
+    values to FP32 rounding, the derivatives to 1e-6 of their largest magnitude."""
+    from projectracer_gb300.config import PT_PREC_MIXED
+
+    cfg, st = small_case("c3")
+    cfg.precision = PT_PREC_MIXED
+    e = eng.Engine(cfg)
+    e.upload(st)
+    e.solve_psi()
+    e.step()
+    nx, nz = cfg.nx, cfg.nz
+    dr = cfg.aspect / nx
+    taps = {1: ([1, -8, 0, 8, -1], 12.0, 2), 2: ([-1, 16, -30, 16, -1], 12.0, 2),
+            3: ([1, -8, 13, 0, -13, 8, -1], 8.0, 3)}
+    for which, field in ((0, eng.F_U), (1, eng.F_W)):
+        f = e.get(field)  # rows k = -3..nz+3, columns i = -3..nx+3
+        tab = e.table(which).astype(np.float64)
+        assert np.array_equal(tab[..., 0], f[:, 3:nx + 4].astype(np.float32).astype(np.float64))
+        for m, (w, den, half) in taps.items():
+            ref = np.zeros((nz + 7, nx + 1))
+            for j, c in enumerate(w):
+                off = j - half
+                ref += c * f[:, 3 + off:3 + off + nx + 1]
+            ref /= den * dr ** m
+            scale = np.abs(ref).max()
+            assert scale > 0
+            assert np.abs(tab[..., m] - ref).max() <= 1e-6 * scale, (which, m)
+    e.close()
