@@ -922,13 +922,10 @@ __device__ __forceinline__ int nearest_off_pow2(double x, int p, int& off28) {
     return fl;
 }
 
-// One RK4 stage (energy.f90:258-536) with FP32 interpolation: the cell and the offsets come from
-// the positions' bit patterns, the slopes are summed in FP32, and only the position/value updates
-// (FP64 state + an FP32 increment) use the FP64 pipe.
-__global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.n) return;
-    const double r = A.xr[t], s = A.xs[t];
+// The slopes (dr/dt, ds/dt, dT/dt) of energy.f90:258-536 at (r, s) by FP32 interpolation: the cell
+// and the offsets come from the position's bit pattern.
+__device__ __forceinline__ void rk_slopes(const StageArgsF& A, Geo g, double r, double s, float& tr, float& ts,
+                                          float& tT) {
     int i, k;
     float hr, hs;
     if (cK.exact_div) {
@@ -951,10 +948,24 @@ __global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
     }
     const float a1 = hr, a2 = 0.5f * hr * hr, a3 = hr * hr * hr * (1.0f / 6.0f);
     const float b1 = hs, b2 = 0.5f * hs * hs, b3 = hs * hs * hs * (1.0f / 6.0f);
-    const float tr = interp_f(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
-    const float ts = interp_f(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
-    const float tT = interp_f(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
+    tr = interp_f(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
+    ts = interp_f(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
+    tT = interp_f(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
+}
+
+// One RK4 stage (energy.f90:258-536) with FP32 interpolation and FP32 slope sums; only the
+// position/value updates (FP64 state + an FP32 increment) use the FP64 pipe.  Every load that does
+// not depend on the position (step-start values, slope sums) is issued before the table gathers,
+// so that its latency overlaps theirs.
+__global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    const double r = A.xr[t], s = A.xs[t];
     const double r0 = A.r0[t], s0 = A.s0[t], T0 = A.T0[t];
+    float pr = 0.f, ps = 0.f, pT = 0.f;
+    if (A.stage > 1) { pr = A.ar[t]; ps = A.as[t]; pT = A.aT[t]; }
+    float tr, ts, tT;
+    rk_slopes(A, g, r, s, tr, ts, tT);
     switch (A.stage) {
         case 1:
             A.ar[t] = tr; A.as[t] = ts; A.aT[t] = tT;
@@ -962,13 +973,13 @@ __global__ void __launch_bounds__(256) k_rk_stage_f(StageArgsF A, Geo g) {
             break;
         case 2:
         case 3:
-            A.ar[t] += 2.0f * tr; A.as[t] += 2.0f * ts; A.aT[t] += 2.0f * tT;
+            A.ar[t] = pr + 2.0f * tr; A.as[t] = ps + 2.0f * ts; A.aT[t] = pT + 2.0f * tT;
             A.rn[t] = r0 + (double)(A.dtf * tr); A.sn[t] = s0 + (double)(A.dtf * ts); A.Tn[t] = T0 + (double)(A.dtf * tT);
             break;
         default:
-            A.rtr[t] = r0 + (double)(A.dtf * (A.ar[t] + tr));
-            A.str[t] = s0 + (double)(A.dtf * (A.as[t] + ts));
-            A.Ttr[t] = T0 + (double)(A.dtf * (A.aT[t] + tT));
+            A.rtr[t] = r0 + (double)(A.dtf * (pr + tr));
+            A.str[t] = s0 + (double)(A.dtf * (ps + ts));
+            A.Ttr[t] = T0 + (double)(A.dtf * (pT + tT));
             break;
     }
 }
