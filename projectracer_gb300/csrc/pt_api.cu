@@ -598,12 +598,14 @@ int pt_step(double* dt_out, pt_solve_info* info) {
     if (E.want_resort && (rc = resort_tracers(E))) return rc;
     if ((rc = stability_dt(E, &E.dt))) return rc;
     const int comp = E.cfg.comp;
-    const size_t nb = sizeof(double) * (size_t)E.ntr;
     if (comp && (rc = copy_field(E, E.C0, E.Cnew))) return rc;
     if ((rc = copy_field(E, E.T0, E.Tratio))) return rc;
-    CK(cudaMemcpyAsync(E.Ttr0, E.Ttr, nb, cudaMemcpyDeviceToDevice, E.st));
-    CK(cudaMemcpyAsync(E.rtr0, E.rtr, nb, cudaMemcpyDeviceToDevice, E.st));
-    CK(cudaMemcpyAsync(E.str0, E.str, nb, cudaMemcpyDeviceToDevice, E.st));
+    // the step-start tracers (energy.f90:262-266) by exchanging buffers instead of copying them:
+    // the RK stages write rtr/str/Ttr before reading them (stage 1 starts the FP64 path's slope
+    // sums there; the mixed path writes them at stage 4)
+    std::swap(E.rtr0, E.rtr);
+    std::swap(E.str0, E.str);
+    std::swap(E.Ttr0, E.Ttr);
     // stage 1
     if ((rc = stage_tables(E)) || (rc = velocity_tables(E)) || (rc = rk_stage(E, 1))) return rc;
     // stages 2-4: project the stage positions, re-solve psi, advance
