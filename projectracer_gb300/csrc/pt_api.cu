@@ -572,8 +572,11 @@ int pt_solve_psi(pt_solve_info* info) {
 static int stage_tables(Engine& E) {
     PhaseTimer tm(E, PH_GRID);
     int rc;
+    if (use_tables_fx(E)) {
+        if ((rc = tracer_space_fx(E))) return rc;
+        return tables_fx(E, 2, E.tsa);
+    }
     if ((rc = load_tracer_space(E))) return rc;
-    if (use_tables_fx(E)) return tables_fx(E, 2, E.tsa);
     if ((rc = compute_derivatives(E, E.tsa, 2))) return rc;
     return tables_to_f32(E, 2, E.tsa);
 }

@@ -247,6 +247,14 @@ __global__ void k_tracer_space(double* tsa, const double* X, const double* cd, c
     tsa[a] = cd[a] * (Txx + Tzz) + (cr[a] * Tx + cs[a] * Tz) + h;
 }
 
+// extendT (energy.f90:595-630): Tratio with its span-5 ghosts into Text
+int extend_T(Engine& E) {
+    const int tot = (E.K.nx + 11) * (E.K.nz + 11);
+    PT_COUNT(), k_bc_T<<<nblk(tot, 256), 256, 0, E.st>>>(E.Text, E.Tratio, E.Cvis, E.g1, 5, 1);
+    CKL("extendT");
+    return 0;
+}
+
 int load_tracer_space(Engine& E) {
     int tot = (E.K.nx + 11) * (E.K.nz + 11);
     PT_COUNT(), k_bc_T<<<nblk(tot, 256), 256, 0, E.st>>>(E.Text, E.Tratio, E.Cvis, E.g1, 5, 1);

@@ -274,6 +274,8 @@ int tables_to_f32(Engine& E, int which, const double* f);  // FP32 copies for th
 // the mixed RK stage's FP32 table of f straight from exact integer stencil sums (no FP64 table)
 bool use_tables_fx(const Engine& E);
 int tables_fx(Engine& E, int which, const double* f);
+int extend_T(Engine& E);              // Text from Tratio (extendT)
+int tracer_space_fx(Engine& E);       // tsa from Text with exact integer stencil sums (mixed path)
 int compute_derivatives(Engine& E, const double* f, int which);  // composition.f90:1457-1478
 int compute_velocities(Engine& E);                   // momentum.f90:655-710
 int stability_dt(Engine& E, double* dt);             // energy.f90:756-810

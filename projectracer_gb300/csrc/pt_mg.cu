@@ -128,6 +128,9 @@ __global__ void k_vis_grad(VisSet S, Geo g, int l, int full, int ivis) {
 }
 
 // test_eigenvalues (RKC1 branch): ratio, local pseudo-time step, min ratio
+// FEW (mixed precision): the pseudo-time step with two divisions instead of four, by the
+// reciprocals of ae and be (the step feeds an FP32 smoother there); the ratio keeps its division
+template <bool FEW>
 __global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double ctemp, unsigned long long* rmin) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     const LevConst& L = cL[l];
@@ -140,7 +143,7 @@ __global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double 
         double eR = S.vxxmzz[o] * L.SR1 + vg * L.SR2 + S.vxz[o] * L.SR4 + S.vx[o] * L.SR5 + S.vz[o] * L.SR6;
         ratio = fabs(eR / eI);
         S.ratio[o] = ratio;
-        double a = eR / ae, b = eI / be;
+        const double a = FEW ? eR * ae : eR / ae, b = FEW ? eI * be : eI / be;  // FEW: ae, be are 1/ae, 1/be
         S.dtst[o] = ctemp * eR / (a * a + b * b);
     }
     double m = fmin(ratio, 1.0e100);
@@ -201,7 +204,10 @@ static int smoother_vis(Engine& E, const VisCtx& C, int l, int interpolate, VisS
                 unsigned long long init = (unsigned long long)__builtin_bit_cast(long long, 1.0e100);
                 CK(cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, C.st));
                 dim3 ge(nblk(nx - 1, 128), nz - 1);
-                PT_COUNT(), k_test_eig<<<ge, 128, 0, C.st>>>(S, g, l, ae, be, ctemp, d);
+                if (E.cfg.precision == PT_PREC_MIXED)
+                    PT_COUNT(), k_test_eig<true><<<ge, 128, 0, C.st>>>(S, g, l, 1.0 / ae, 1.0 / be, ctemp, d);
+                else
+                    PT_COUNT(), k_test_eig<false><<<ge, 128, 0, C.st>>>(S, g, l, ae, be, ctemp, d);
                 CKL("k_test_eig");
                 CK(cudaMemcpyAsync(C.hscal, d, 8, cudaMemcpyDeviceToHost, C.st));
                 CK(cudaStreamSynchronize(C.st));

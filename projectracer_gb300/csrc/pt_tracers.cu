@@ -1001,6 +1001,19 @@ __global__ void k_tables_to_f32(float4* out, const double* F, const double* D1, 
 // FP64 operations per node and its FP32 copy four more).
 constexpr int kTbX = 128;
 
+// v 2^e2 as a double from integer operations: the leading 53 bits of |v| (truncated; the callers'
+// sums already carry 2^-54 of their scale), 0 below the normal range
+__device__ __forceinline__ double i64_to_double_trunc(long long v, int e2) {
+    if (v == 0) return 0.0;
+    const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
+    const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+    const int lz = __clzll(a);
+    const unsigned long long mant = (a << lz) >> 11;  // leading one at bit 52
+    const long long ex = (long long)(1023 + 63 - lz + e2);
+    if (ex <= 0) return 0.0;
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 // v 2^e2 rounded to FP32 (to nearest, ties away from zero; below the normal range: 0)
 __device__ __forceinline__ float i64_to_float_scaled(long long v, int e2) {
     if (v == 0) return 0.f;
@@ -1103,14 +1116,119 @@ __global__ void __launch_bounds__(kTbX) k_tables_fx(float4* __restrict__ out, co
     out[g.at(i, k)] = make_float4(d2f_bits(fv), d1, d2, d3);
 }
 
-// the integer stencils above are the run's x-derivative stencils (checked once per call: 21
-// comparisons on the host)
+// load_tracer_space (energy.f90:59-179) for the mixed path: Tx, Tz, Txx, Tzz of Text as exact
+// integer sums (D1 = [1,-8,0,8,-1]/12, D2 = [-1,16,-30,16,-1]/12) on a tile in 62-bit fixed point,
+// so that only the combination with the conductivity fields is FP64 arithmetic (about 10
+// operations per node instead of about 50).  Nodes i in [-3, nx+3], k in [-3, nz+3].
+constexpr int kTsX = 32, kTsZ = 8, kTsW = kTsX + 4, kTsH = kTsZ + 4;
+__global__ void __launch_bounds__(kTsX * kTsZ) k_tracer_space_fx(double* __restrict__ tsa, const double* __restrict__ X,
+                                                                 const double* __restrict__ cd,
+                                                                 const double* __restrict__ cr,
+                                                                 const double* __restrict__ cs,
+                                                                 const double* __restrict__ Cvis, Geo g, double sx,
+                                                                 double sxx, double sz, double szz) {
+    __shared__ int2 Xf[kTsH][kTsW];
+    __shared__ int emax_s;
+    const int nx = cK.nx, nz = cK.nz;
+    const int tid = threadIdx.y * kTsX + threadIdx.x;
+    const int i0 = -3 + (int)blockIdx.x * kTsX, k0 = -3 + (int)blockIdx.y * kTsZ;
+    if (tid == 0) emax_s = 0;
+    __syncthreads();
+    constexpr int NT = kTsW * kTsH, PER = (NT + kTsX * kTsZ - 1) / (kTsX * kTsZ);
+    unsigned long long raw[PER];
+    int em = 0;
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        const int idx = tid + kTsX * kTsZ * q;
+        unsigned long long b = 0;
+        if (idx < NT) {
+            const int i = i0 - 2 + idx % kTsW, k = k0 - 2 + idx / kTsW;  // i, k >= -5
+            if (i <= nx + 5 && k <= nz + 5) b = (unsigned long long)__double_as_longlong(X[g.at(i, k)]);
+        }
+        raw[q] = b;
+        em = max(em, (int)((b >> 52) & 0x7FF));
+    }
+    em = __reduce_max_sync(0xffffffffu, em);
+    if ((tid & 31) == 0) atomicMax(&emax_s, em);
+    __syncthreads();
+    const int emax = emax_s;
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        const int idx = tid + kTsX * kTsZ * q;
+        if (idx >= NT) break;
+        const unsigned long long b = raw[q];
+        const int e = (int)((b >> 52) & 0x7FF);
+        long long v = 0;
+        if (e != 0 && emax != 0x7FF) {
+            const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+            const int sh = emax - 9 - e;  // X = m 2^-sh, |X| < 2^62
+            unsigned long long a;
+            if (sh <= 0) a = m << (-sh);
+            else if (sh < 64) a = (m + (1ull << (sh - 1))) >> sh;
+            else a = 0;
+            v = (b >> 63) ? -(long long)a : (long long)a;
+        }
+        const long long h = v >> 31;
+        Xf[idx / kTsW][idx % kTsW] = make_int2((int)h, (int)(v - (h << 31)));
+    }
+    __syncthreads();
+    const int i = i0 + (int)threadIdx.x, k = k0 + (int)threadIdx.y;
+    if (i > nx + 3 || k > nz + 3) return;
+    const size_t o = g.at(i, k);
+    double Tx, Tz, Txx, Tzz;
+    if (emax == 0x7FF) {
+        Tx = Tz = Txx = Tzz = __longlong_as_double(0x7FF8000000000000ll);
+    } else {
+        constexpr int w1[5] = {1, -8, 0, 8, -1}, w2[5] = {-1, 16, -30, 16, -1};
+        long long h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0;
+        const int cx = threadIdx.x + 2, cz = threadIdx.y + 2;
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            const int2 ax = Xf[cz][cx + j - 2], az = Xf[cz + j - 2][cx];
+            if (w1[j]) {
+                h1 += (long long)w1[j] * ax.x; l1 += (long long)w1[j] * ax.y;
+                h3 += (long long)w1[j] * az.x; l3 += (long long)w1[j] * az.y;
+            }
+            h2 += (long long)w2[j] * ax.x; l2 += (long long)w2[j] * ax.y;
+            h4 += (long long)w2[j] * az.x; l4 += (long long)w2[j] * az.y;
+        }
+        // (h 2^31 + l) 2^-s, s = 1084 - emax, as h 2^23 + (l >> 8) at 2^(8-s) (|.| < 2^60)
+        const int e2 = 8 - (1084 - emax);
+        Tx = i64_to_double_trunc((h1 << 23) + (l1 >> 8), e2) * sx;
+        Txx = i64_to_double_trunc((h2 << 23) + (l2 >> 8), e2) * sxx;
+        Tz = i64_to_double_trunc((h3 << 23) + (l3 >> 8), e2) * sz;
+        Tzz = i64_to_double_trunc((h4 << 23) + (l4 >> 8), e2) * szz;
+    }
+    double h = cK.H;  // compute_heating, energy.f90:19-40 (iheattype=0)
+    if (cK.comp != 0) {
+        const double cv = Cvis[o];
+        h = cK.Htype * cv + cK.H * (1.0 - cv);
+    }
+    tsa[o] = cd[o] * (Txx + Tzz) + (cr[o] * Tx + cs[o] * Tz) + h;
+}
+
+int tracer_space_fx(Engine& E) {
+    if (int rc = extend_T(E)) return rc;
+    const Consts& K = E.K;
+    dim3 grid(nblk(K.nx + 7, kTsX), nblk(K.nz + 7, kTsZ)), block(kTsX, kTsZ);
+    PT_COUNT(), k_tracer_space_fx<<<grid, block, 0, E.st>>>(E.tsa, E.Text, E.cond, E.cond_r, E.cond_s, E.Cvis, E.g1,
+                                                            1.0 / (12.0 * K.dr), 1.0 / (12.0 * K.dr2),
+                                                            1.0 / (12.0 * K.ds), 1.0 / (12.0 * K.ds2));
+    CKL("k_tracer_space_fx");
+    return 0;
+}
+
+// the integer stencils above are the run's derivative stencils (checked on the host at every
+// call: 35 comparisons)
 static bool tables_exact_ok(const Consts& K) {
     const int w[4][7] = {{}, {0, 1, -8, 0, 8, -1, 0}, {0, -1, 16, -30, 16, -1, 0}, {1, -8, 13, 0, -13, 8, -1}};
     const double den[4] = {1.0, 12.0, 12.0, 8.0};
     for (int m = 1; m <= 3; m++)
         for (int j = 0; j < 7; j++)
             if (std::fabs(K.Dm[m][j] * den[m] - w[m][j]) > 1e-12) return false;
+    // the first and second derivatives of the tracer-space term (k_tracer_space_fx)
+    for (int j = 0; j < 7; j++)
+        if (std::fabs(12.0 * K.D1[j] - w[1][j]) > 1e-12 || std::fabs(12.0 * K.D2[j] - w[2][j]) > 1e-12) return false;
     return true;
 }
 
