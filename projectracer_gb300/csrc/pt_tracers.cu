@@ -1029,13 +1029,15 @@ __device__ __forceinline__ float i64_to_float_scaled(long long v, int e2) {
     if (ex >= 255) return __uint_as_float(sgn | 0x7F800000u);
     return __uint_as_float(sgn | ((unsigned)ex << 23) | ((unsigned)m & 0x7FFFFFu));
 }
-// FP64 to FP32 from the bit pattern (to nearest, ties away from zero; FP32-subnormal results: 0)
+// FP64 to FP32 from the bit pattern (to nearest, ties to even, as the conversion instruction;
+// FP32-subnormal results: 0)
 __device__ __forceinline__ float d2f_bits(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
     const int e = (int)((b >> 52) & 0x7FF);
     if (e == 0x7FF) return __uint_as_float(sgn | 0x7F800000u | (unsigned)((b & 0xFFFFFFFFFFFFFull) != 0) << 22);
-    unsigned long long m = ((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) + (1ull << 28);  // round at bit 29
+    unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    m += (1ull << 28) - 1 + ((m >> 29) & 1);  // round at bit 29, ties to the even result
     int ex = e - 1023 + 127;
     if (m >> 53) { m >>= 1; ex++; }
     if (e == 0 || ex <= 0) return __uint_as_float(sgn);
