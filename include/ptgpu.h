@@ -37,7 +37,7 @@ extern "C" {
 #define PT_ERR_ARG (-9)                  /* bad argument (null pointer, size, field id) */
 #define PT_ERR_NOT_FINITE (-10)          /* NaN/Inf detected in a residual */
 
-/* Precision of the stream-function solve (spec extension; not in the reference). */
+/* Precision of the stream-function solve (an extension; not in the reference). */
 #define PT_PREC_FP64 0  /* plain FP64 multigrid: the reference algorithm on the GPU */
 #define PT_PREC_MIXED 1 /* FP32 smoothing/transfers, FP64 residual + defect correction, FP64 coarse LU */
 
@@ -54,7 +54,7 @@ extern "C" {
 #define PT_CYCLE_REFERENCE 0
 #define PT_CYCLE_V 1
 
-/* Initial-guess mode of the stream-function solve (spec extension). */
+/* Initial-guess mode of the stream-function solve (an extension; not in the reference). */
 #define PT_GUESS_PREVIOUS 0 /* previous psi (the reference's warm start, iterative_solver.f90:134) */
 #define PT_GUESS_ZERO 1
 #define PT_GUESS_UNET 2

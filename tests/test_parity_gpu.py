@@ -3,7 +3,7 @@
 Integer work (cell indices, tracer counts) and the projection / boundary-condition / smoother
 kernels are compared bit for bit (the oracle runs the projection in the engine's canonical
 summation order).  Floating-point results that pass through the FMA-contracted kernels (psi
-solve, tracer interpolation) are compared at the benchmark spec's tolerance of 1e-10 relative to the
+solve, tracer interpolation) are compared at the required tolerance of 1e-10 relative to the
 field's maximum (per single solve / step, typically 1e-13).
 """
 import numpy as np
