@@ -166,8 +166,9 @@ static int engine_alloc(Engine& E) {
     if (E.cfg.precision == PT_PREC_MIXED) {  // tracer order (re-sorted by cell when locality is lost)
         if ((rc = ialloc(E, &E.perm, nt)) || (rc = ialloc(E, &E.perm2, nt))) return rc;
         const size_t nkey = resort_nkey(E.K.nx, E.K.nz);
-        if ((rc = ialloc(E, &E.rs_count, nkey)) || (rc = ialloc(E, &E.rs_start, nkey)) ||
-            (rc = ialloc(E, &E.rs_tot, nkey / 1024 + 64)))
+        if (nkey <= (size_t)INT32_MAX &&  // int32 sort keys; larger grids keep the upload order
+            ((rc = ialloc(E, &E.rs_count, nkey)) || (rc = ialloc(E, &E.rs_start, nkey)) ||
+             (rc = ialloc(E, &E.rs_tot, nkey / 1024 + 64))))
             return rc;
         CK(cudaMalloc(&E.proj_runs, sizeof(unsigned long long)));
         if ((rc = tracer_order_reset(E))) return rc;

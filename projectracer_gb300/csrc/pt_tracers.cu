@@ -747,7 +747,7 @@ int tracer_order_reset(Engine& E) {
 // RK stage buffers, then the pointers swap)
 int resort_tracers(Engine& E) {
     E.want_resort = false;
-    if (!E.perm) return 0;
+    if (!E.perm || !E.rs_count) return 0;
     const int nkey = (int)resort_nkey(E.K.nx, E.K.nz);
     const int64_t n = E.ntr;
     CK(cudaMemsetAsync(E.rs_count, 0, sizeof(int32_t) * (size_t)nkey, E.st));
