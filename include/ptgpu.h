@@ -4,8 +4,8 @@
  * The reference (Fortran 90 + OpenMP) has no plugin interface: its hot-path subroutines take no
  * arguments and exchange data through the module globals of basics.f90 and arrays.f90.  The entry
  * points below replace the bodies of those subroutines; a Fortran driver binds them with
- * iso_c_binding (the binding is shown in INTEGRATION.md).  Each declaration cites the reference
- * routine it replaces (file:line inside ProjecTracer_Source/).
+ * iso_c_binding.  Each declaration cites the reference routine it replaces (file:line inside
+ * ProjecTracer_Source/).
  *
  * Conventions
  *  - Every function returns 0 (PT_OK) or a negative PT_ERR_* code; pt_last_error() describes it.
@@ -39,7 +39,9 @@ extern "C" {
 
 /* Precision of the stream-function solve (an extension; not in the reference). */
 #define PT_PREC_FP64 0  /* plain FP64 multigrid: the reference algorithm on the GPU */
-#define PT_PREC_MIXED 1 /* FP32 smoothing/transfers, FP64 residual + defect correction, FP64 coarse LU */
+#define PT_PREC_MIXED 1 /* FP32 smoothing and transfers, FP64 residual and defect correction, FP64 coarse LU
+                          and FP64 coarse solve; FP64 tracer positions and RK update, with the velocities
+                          interpolated from FP32 tables; integer fixed-point (2^-28) projection sums */
 
 /* Coarse-level initial guess inside a multigrid cycle.  The reference never resets
  * error(:,:,2:grids) (zeroed once, main.f90:229), so each coarse visit starts from the previous
@@ -71,7 +73,7 @@ extern "C" {
  * the &gpu extension group.  Supported subset: order=4, uniform grid (gridX=gridZ=0), Database=2,
  * ntype<=1 with continuous C (iC_continuous=1), temperature tracers (tracer=1), RK4 (torder=4) with
  * RK_update=1, multigrid with the RKC1 smoother (iterate=1, MG=1, RKC1=1, splitting=0), Newtonian
- * viscosity (non_Newtonian=0, plastic=0), constant internal heating (iheattype=0), CFL=0.
+ * viscosity (non_Newtonian=0, plastic=0), constant internal heating (iheattype=0), CFL=0 or 1.
  */
 typedef struct pt_config {
     /* grid (&inputs) */
@@ -153,7 +155,7 @@ typedef struct pt_stats {
  * (compute_basics basics.f90:204-333, storage basics.f90:70-202, multigrid_setup
  * multigrid_cycle.f90:1-99, FD_coefficients main.f90:499-642, derivative_eigenvalues
  * energy.f90:632-744, eigenvalue_prep iterative_solver.f90:1232-1362, Chebyshev_prep_stream
- * Chebyshev.f90:182-210).  Allocates all device buffers. */
+ * Chebyshev.f90:82-110).  Allocates all device buffers. */
 int pt_init(const pt_config* cfg);
 
 /* Releases everything pt_init allocated. */

@@ -40,6 +40,11 @@ int pt_prof_tracer_order(int64_t* resorts, double* runs_per_thread);
  * term) as last built, nodes i = 0..nx of rows k = -3..nz+3, row-major, four floats per node
  * (value and x-derivatives of order 1, 2, 3): (nz+7)(nx+1)*4 floats. */
 int pt_prof_table(int which, float* host);
+/* Relative residual mean|r| / mean|RHS| of the last psi solve at each convergence test, in order
+ * (the reference logs the final one, iterative_solver.f90:338): the first min(count, cap) values
+ * go to out, *count receives the number of tests.  Kept when the solve fails (cycle cap,
+ * divergence), so a caller can read how far it got. */
+int pt_prof_residuals(double* out, int cap, int* count);
 
 #ifdef __cplusplus
 }

@@ -231,8 +231,6 @@ static void engine_free(Engine& E) {
     if (E.Ginv) cudaFree(E.Ginv);
     for (double* p : {E.Ginv2, E.Mc2, E.RowB2})
         if (p) cudaFree(p);
-    for (float* p : {E.Gf, E.Gf2})
-        if (p) cudaFree(p);
     if (E.ipiv2) cudaFree(E.ipiv2);
     if (E.derr2) cudaFree(E.derr2);
     if (E.hflag2) cudaFreeHost(E.hflag2);
@@ -357,7 +355,7 @@ int pt_init(const pt_config* cfg) {
     g_eng = E;
     TRACE("pt_init: device allocations and constants");
     if ((rc = engine_alloc(*E)) || (rc = upload_consts_fields(*E)) || (rc = upload_consts_tracers(*E)) ||
-        (rc = upload_consts_mg(*E)) || (rc = upload_consts_mixed(*E)) || (rc = noalloc_scratch_setup())) {
+        (rc = upload_consts_mg(*E)) || (rc = upload_consts_mixed(*E)) || (rc = noalloc_scratch_setup(nullptr))) {
         std::string msg = g_err;
         pt_finalize();
         g_err = msg;
@@ -731,6 +729,15 @@ int pt_prof_tracer_order(int64_t* resorts, double* runs_per_thread) {
     if (int rc = need(g_eng != nullptr)) return rc;
     if (resorts) *resorts = g_eng->resorts;
     if (runs_per_thread) *runs_per_thread = g_eng->last_runs;
+    return 0;
+}
+
+int pt_prof_residuals(double* out, int cap, int* count) {
+    if (int rc = need(g_eng != nullptr)) return rc;
+    const std::vector<double>& h = g_eng->res_hist;
+    if (count) *count = (int)h.size();
+    if (out)
+        for (int q = 0; q < cap && q < (int)h.size(); q++) out[q] = h[(size_t)q];
     return 0;
 }
 

@@ -125,7 +125,6 @@ struct Engine {
     // mixed precision: the next time level's coarse factorisation, built on st2 while the
     // top-of-step solve runs with the previous one, then copied into Mc/RowB/ipiv/Ginv
     double *Mc2 = nullptr, *RowB2 = nullptr, *Ginv2 = nullptr;
-    float *Gf = nullptr, *Gf2 = nullptr;  // FP32 copies of the inverse (the mixed V-cycle's coarse solve)
     int *ipiv2 = nullptr, *derr2 = nullptr, *hflag2 = nullptr;
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_in = nullptr, ev_fact = nullptr;
@@ -185,6 +184,7 @@ struct Engine {
     int n_eta = 0, n_temp = 0, cycles = 0, refinements = 0;
     double eig_fine = 0, resid_ratio = 0, res_ref[PT_MAXLEV] = {}, residual_mag1 = 0;
     double phase_ms[PT_NPHASE] = {};
+    std::vector<double> res_hist;  // relative residual at each convergence test of the last solve
     // timed spans (phase slots, and kernel classes when profiling is on) whose events have been
     // recorded but not yet read: read at the library's existing synchronisation points
     // (harvest_spans), so that timing adds no host wait of its own
@@ -262,7 +262,7 @@ int smoother_time_T(Engine& E, const double* Tin);   // smoother.f90:638-672
 int smoother_time_C(Engine& E);                      // smoother.f90:582-636
 int load_conductivity(Engine& E);                    // energy.f90:59-86
 int load_tracer_space(Engine& E);                    // energy.f90:154-179 (+extendT 595-630)
-int noalloc_scratch_setup();  // static scratch address of the current device (before any capture)
+int noalloc_scratch_setup(unsigned char** base);  // static scratch of the current device (before any capture)
 int project_noalloc(Engine& E, const double* T0f, int smooth);
 // learned initial psi (pt_unet.cu): after mg_setup_solve; fallback check after the first cycle
 int unet_guess(Engine& E);

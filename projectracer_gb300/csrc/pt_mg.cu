@@ -692,7 +692,9 @@ __global__ void __launch_bounds__(1024) k_band_lu(double* ab, int* ipiv, int n, 
         if (j + kv <= n)
             for (int i = 1 + tid; i <= kl; i += nt) AB(i, j + kv) = 0.0;
         const int km = kl < n - j ? kl : n - j;
-        // pivot: first index of the maximum |a| in AB(kv+1..kv+1+km, j)
+        // pivot: first index of the maximum |a| in AB(kv+1..kv+1+km, j).  A NaN never wins the
+        // comparison; the search starts from row 1 so the index stays inside the band even for a
+        // column of NaNs, which is then reported like a zero pivot.
         if (tid < 32) {
             double best = -1.0;
             int bi = 1 << 30;
@@ -700,6 +702,7 @@ __global__ void __launch_bounds__(1024) k_band_lu(double* ab, int* ipiv, int n, 
                 double a = fabs(AB(kv + i, j));
                 if (a > best) { best = a; bi = i; }
             }
+            if (bi > km + 1) bi = 1;
             for (int o = 16; o > 0; o >>= 1) {
                 double ob = __shfl_xor_sync(0xffffffffu, best, o);
                 int oi = __shfl_xor_sync(0xffffffffu, bi, o);
@@ -708,7 +711,8 @@ __global__ void __launch_bounds__(1024) k_band_lu(double* ab, int* ipiv, int n, 
             if (tid == 0) {
                 s_jp = bi;
                 ipiv[j - 1] = bi + j - 1;
-                s_nz = (AB(kv + bi, j) != 0.0);
+                const double piv = AB(kv + bi, j);
+                s_nz = (piv != 0.0 && piv == piv);
                 if (s_nz) {
                     int jue = j + ku + bi - 1 < n ? j + ku + bi - 1 : n;
                     if (jue > s_ju) s_ju = jue;
@@ -898,7 +902,7 @@ __global__ void __launch_bounds__(32 * kInvWarps) k_band_inverse(const double* a
 
 // coarse solve through the explicit inverse: b = RowB * RHS on interior nodes (0 on the
 // boundary), x = G b (one warp per row, lanes stride the row, fixed-order shuffle reduction),
-// scattered into the level array.  R = float for the mixed-precision cycle.
+// scattered into the level array.
 template <typename R>
 __global__ void __launch_bounds__(256) k_coarse_apply(R* Eout, const R* RHS, const double* G, const double* RowB, Geo g,
                                                       int nxc, int nzc) {
@@ -919,25 +923,25 @@ __global__ void __launch_bounds__(256) k_coarse_apply(R* Eout, const R* RHS, con
     if (lane == 0) Eout[g.at(p / N, p % N)] = (R)a;
 }
 
-// The mixed-precision V-cycle's coarse solve: x = G b in FP32 with the FP32 copy of the inverse.
-// The result is a coarse correction inside an FP32 preconditioner of the FP64 defect correction;
-// FP32 rounding of G and of the sum (relative 1e-5 or so for this small, smooth inverse) leaves
-// the cycle count unchanged (measured), and the GEMV no longer runs on the FP64 pipe.
-__global__ void __launch_bounds__(256) k_coarse_apply32(float* Eout, const float* RHS, const float* G,
-                                                        const double* RowB, Geo g, int nxc, int nzc, float sz) {
-    extern __shared__ float bsf[];
+// The mixed-precision V-cycle's coarse solve: x = G b with the FP64 inverse and FP64 sums (the
+// coarsest level stays FP64), from the FP32 restricted residual, into the FP32 correction with
+// its boundary values.  A GEMV of n^2 FMAs (n = 561 at 1024x512) spread over n warps costs a few
+// microseconds on the FP64 pipe.
+__global__ void __launch_bounds__(256) k_coarse_apply_mixed(float* Eout, const float* RHS, const double* G,
+                                                            const double* RowB, Geo g, int nxc, int nzc, float sz) {
+    extern __shared__ double bsm[];
     const int N = nzc + 1, n = (nxc + 1) * N;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         int ip = q / N, kp = q % N;
-        bsf[q] = (ip > 0 && ip < nxc && kp > 0 && kp < nzc) ? (float)((double)RHS[g.at(ip, kp)] * RowB[q]) : 0.0f;
+        bsm[q] = (ip > 0 && ip < nxc && kp > 0 && kp < nzc) ? (double)RHS[g.at(ip, kp)] * RowB[q] : 0.0;
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int p = blockIdx.x * (blockDim.x >> 5) + warp;
     if (p >= n) return;
-    const float* row = G + (size_t)p * n;
-    float a = 0.0f;
-    for (int q = lane; q < n; q += 32) a = fmaf(row[q], bsf[q], a);
+    const double* row = G + (size_t)p * n;
+    double a = 0.0;
+    for (int q = lane; q < n; q += 32) a = fma(row[q], bsm[q], a);
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
     if (lane != 0) return;
     // the correction with its boundary values: wall nodes zero, interior nodes with their free-slip
@@ -947,6 +951,7 @@ __global__ void __launch_bounds__(256) k_coarse_apply32(float* Eout, const float
         Eout[g.at(ip, kp)] = 0.0f;
         return;
     }
+    const float v = (float)a;
     int xs[3], zs[3];
     float xf[3], zf[3];
     int nxp = 0, nzp = 0;
@@ -957,12 +962,7 @@ __global__ void __launch_bounds__(256) k_coarse_apply32(float* Eout, const float
     if (kp <= 3) { zs[nzp] = -kp; zf[nzp++] = sz; }
     if (kp >= nzc - 3) { zs[nzp] = 2 * nzc - kp; zf[nzp++] = sz; }
     for (int u = 0; u < nxp; u++)
-        for (int v = 0; v < nzp; v++) Eout[g.at(xs[u], zs[v])] = (xf[u] * zf[v]) * a;
-}
-
-__global__ void k_g_to_f32(float* out, const double* in, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = (float)in[i];
+        for (int w = 0; w < nzp; w++) Eout[g.at(xs[u], zs[w])] = (xf[u] * zf[w]) * v;
 }
 
 __global__ void k_coarse_rhs(double* B, const double* RHS, const double* RowB, Geo g, int nxc, int nzc) {
@@ -994,8 +994,6 @@ static int coarse_factor(Engine& E) {
     if (E.Ginv) {
         PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st>>>(
             E.Mc, E.ipiv, E.Ginv, n, E.kl, E.ku);
-        const size_t nn = (size_t)n * n;
-        PT_COUNT(), k_g_to_f32<<<nblk(nn, 256), 256, 0, E.st>>>(E.Gf, E.Ginv, nn);
         CKL("k_band_inverse");
     }
     return 0;
@@ -1013,7 +1011,6 @@ static int coarse_factor_async(Engine& E, const VisLevels& V) {
     PT_COUNT(), k_band_lu<<<1, 1024, 0, E.st2>>>(E.Mc2, E.ipiv2, n, E.kl, E.ku, E.derr2);
     PT_COUNT(), k_band_inverse<<<nblk(n, kInvWarps), 32 * kInvWarps, inv_smem(n, E.kl, E.ku), E.st2>>>(
         E.Mc2, E.ipiv2, E.Ginv2, n, E.kl, E.ku);
-    PT_COUNT(), k_g_to_f32<<<nblk((size_t)n * n, 256), 256, 0, E.st2>>>(E.Gf2, E.Ginv2, (size_t)n * n);
     CKL("async coarse factorisation");
     CK(cudaMemcpyAsync(E.hflag2, E.derr2, sizeof(int), cudaMemcpyDeviceToHost, E.st2));
     E.fact_pending = true;
@@ -1073,7 +1070,6 @@ int coarse_resolve(Engine& E) {
     CK(cudaMemcpyAsync(E.RowB, E.RowB2, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, E.st));
     CK(cudaMemcpyAsync(E.ipiv, E.ipiv2, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, E.st));
     CK(cudaMemcpyAsync(E.Ginv, E.Ginv2, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
-    CK(cudaMemcpyAsync(E.Gf, E.Gf2, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
     return 0;
 }
 
@@ -1084,7 +1080,7 @@ int coarse_apply(Engine& E, double* out64, float* out32, const double* rhs64, co
     const unsigned blocks = nblk(n, 8);
     const size_t smem = sizeof(double) * (size_t)n;
     if (out64) PT_COUNT(), k_coarse_apply<double><<<blocks, 256, smem, E.st>>>(out64, rhs64, E.Ginv, E.RowB, g, g.nx, g.nz);
-    else PT_COUNT(), k_coarse_apply32<<<blocks, 256, smem / 2, E.st>>>(out32, rhs32, E.Gf, E.RowB, g, g.nx, g.nz,
+    else PT_COUNT(), k_coarse_apply_mixed<<<blocks, 256, smem, E.st>>>(out32, rhs32, E.Ginv, E.RowB, g, g.nx, g.nz,
                                                                        E.cfg.Vbc == 0 ? -1.f : 1.f);
     CKL("k_coarse_apply");
     return 0;
@@ -1237,6 +1233,7 @@ int multigrid(Engine& E, pt_solve_info* info) {
     const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int q = 1;
     double mag1 = 0.0;
+    E.res_hist.clear();
     for (;;) {
         {
             PhaseTimer tp(E, PH_CYCLE_L1);
@@ -1247,6 +1244,7 @@ int multigrid(Engine& E, pt_solve_info* info) {
         harvest_graph_timer(E, 0);
         mag1 = E.hscal[0] / (double)(E.gl[1].nx - 2) / (double)(E.gl[1].nz - 2);
         (void)norm;
+        if (E.res_hist.size() < 100000) E.res_hist.push_back(mag1 / E.res_ref[1]);
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite multigrid residual");
         if (mag1 > 1.0e10 * E.res_ref[1])
             return fail(PT_ERR_MG_DIVERGED, "Multigrid Convergence Problem: Abnormally High Residual Detected");
@@ -1310,7 +1308,7 @@ int mg_alloc(Engine& E) {
     CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)band_solve_smem(E.ngc, E.kl, E.ku)));
     CK(cudaFuncSetAttribute(k_coarse_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_coarse_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_coarse_apply_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // explicit coarse inverse (both precisions): the coarse solve becomes a GEMV spread over the
     // SMs instead of two sequential banded substitutions on one warp of this part's narrow FP64
     // pipe; n^2 doubles, kept while it is small next to the level arrays (n <= 4096: <= 134 MB)
@@ -1318,9 +1316,6 @@ int mg_alloc(Engine& E) {
         CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
         E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
         CK(cudaMalloc(&E.Ginv2, sizeof(double) * (size_t)E.ngc * E.ngc));
-        CK(cudaMalloc(&E.Gf, sizeof(float) * (size_t)E.ngc * E.ngc));
-        CK(cudaMalloc(&E.Gf2, sizeof(float) * (size_t)E.ngc * E.ngc));
-        CK(cudaFuncSetAttribute(k_coarse_apply32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2)));
         CK(cudaMalloc(&E.Mc2, sizeof(double) * (size_t)ldab * E.ngc));
         CK(cudaMalloc(&E.RowB2, sizeof(double) * (size_t)E.ngc));
         CK(cudaMalloc(&E.ipiv2, sizeof(int) * (size_t)E.ngc));

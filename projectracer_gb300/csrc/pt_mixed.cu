@@ -704,6 +704,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
     const double norm = (double)(E.gl[1].nx - 2) * (double)(E.gl[1].nz - 2);
     int cycles = 0;
     double mag1 = 0.0;
+    E.res_hist.clear();
     for (;;) {
         {
             PhaseTimer tp(E, PH_CYCLE_L1);
@@ -713,6 +714,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
         CK(cudaStreamSynchronize(E.st));
         harvest_graph_timer(E, 1);
         mag1 = E.hscal[0] / norm;
+        if (E.res_hist.size() < 100000) E.res_hist.push_back(mag1 / E.res_ref[1]);
         if (!std::isfinite(mag1)) return fail(PT_ERR_NOT_FINITE, "non-finite residual in the mixed-precision solve");
         if (mag1 > 1.0e10 * E.res_ref[1])
             return fail(PT_ERR_MG_DIVERGED, "mixed-precision solve: abnormally high residual");
@@ -731,6 +733,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
             CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
             CK(cudaStreamSynchronize(E.st));
             mag1 = E.hscal[0] / norm;
+            if (E.res_hist.size() < 100000) E.res_hist.push_back(mag1 / E.res_ref[1]);
             if (mag1 / E.res_ref[1] <= E.cfg.tolerance) break;
         }
         if (cycles >= E.cfg.max_cycles)

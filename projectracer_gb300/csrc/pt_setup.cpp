@@ -3,7 +3,7 @@
 // Computes what the reference's start-up computes before the time loop (main.f90:168-198):
 // finite-difference stencils (FD_coefficients, main.f90:499-642), Fourier-symbol maxima
 // (derivative_eigenvalues, energy.f90:632-744), RKC1 coefficients (Chebyshev_prep_stream,
-// Chebyshev.f90:182-210), the multigrid hierarchy and schedule (optimize_grid,
+// Chebyshev.f90:82-110), the multigrid hierarchy and schedule (optimize_grid,
 // iterative_solver.f90:1-61; multigrid_setup, multigrid_cycle.f90:1-99), per-level eigenvalue
 // symbols (eigenvalue_prep, iterative_solver.f90:1232-1362), the coarse stencil matrices
 // (stream_space_matrix_prep, 692-743) and the coarse band width (Compute_Matrix_coarse with

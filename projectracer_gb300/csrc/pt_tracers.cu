@@ -11,6 +11,7 @@
 // per-tracer fixed-point contributions and integer sums (k_project_fx), deterministic without a
 // sort and independent of the tracer order; counts bit-exact, sums to 2^-28.
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -649,19 +650,24 @@ static constexpr size_t kNaBytes = kNaOffFlag + 256;
 static_assert(kNaBytes <= 16u * 1024u * 1024u, "no-alloc projection scratch stays below 16 MB");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
-static unsigned char* s_noalloc_base[64] = {};  // per device, from cudaGetSymbolAddress
+// per device, from cudaGetSymbolAddress; threads that resolve the same device at once store the
+// same address
+static std::atomic<unsigned char*> s_noalloc_base[64];
 
-// Resolves the scratch address of the current device.  pt_init calls it, so the lookup (which may
-// load the module) never happens inside a stream capture.
-int noalloc_scratch_setup() {
+// Resolves (once per device) and returns the scratch address of the current device.  pt_init
+// calls it, so the lookup (which may load the module) never happens inside a stream capture.
+int noalloc_scratch_setup(unsigned char** base) {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail(PT_ERR_CUDA, "device index out of range for the no-alloc scratch table");
-    if (!s_noalloc_base[dev]) {
+    unsigned char* b = s_noalloc_base[dev].load(std::memory_order_acquire);
+    if (!b) {
         void* p = nullptr;
         CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        s_noalloc_base[dev] = static_cast<unsigned char*>(p);
+        b = static_cast<unsigned char*>(p);
+        s_noalloc_base[dev].store(b, std::memory_order_release);
     }
+    if (base) *base = b;
     return 0;
 }
 
@@ -670,11 +676,8 @@ int project_noalloc(Engine& E, const double* T0f, int smooth) {
     if ((size_t)E.ntr > kNaTracers || ncell > kNaNodes)
         return fail(PT_ERR_ARG, "pt_tracers_to_corners_noalloc: more than " + std::to_string(kNaTracers) +
                                     " tracers or " + std::to_string(kNaNodes) + " grid nodes");
-    int rc;
-    if ((rc = noalloc_scratch_setup())) return rc;
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    unsigned char* b = s_noalloc_base[dev];
+    unsigned char* b = nullptr;
+    if (int rc = noalloc_scratch_setup(&b)) return rc;
     ProjScratch W{reinterpret_cast<int32_t*>(b + kNaOffCell), reinterpret_cast<int32_t*>(b + kNaOffList),
                   reinterpret_cast<int32_t*>(b + kNaOffCount), reinterpret_cast<int32_t*>(b + kNaOffStart),
                   reinterpret_cast<int32_t*>(b + kNaOffScan), reinterpret_cast<double*>(b + kNaOffPart),

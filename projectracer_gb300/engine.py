@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_prof_tracer_order.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(f64)]
     L.pt_prof_table.argtypes = [i32, vp]
     L.pt_prof_region.argtypes = [i32, ctypes.POINTER(f64)]
+    L.pt_prof_residuals.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int)]
     _LIB = L
     return L
 
@@ -209,6 +210,15 @@ class Engine:
         out = np.empty((self.nz + 7, self.nx + 1, 4), dtype=np.float32)
         self._check(self.L.pt_prof_table(which, _ptr(out)))
         return out
+
+    def residuals(self) -> list[float]:
+        """Relative residual at each convergence test of the last psi solve (kept after a failed
+        solve)."""
+        n = ctypes.c_int()
+        self._check(self.L.pt_prof_residuals(None, 0, ctypes.byref(n)))
+        out = np.zeros(max(1, n.value))
+        self._check(self.L.pt_prof_residuals(_ptr(out), n.value, ctypes.byref(n)))
+        return list(out[:n.value])
 
     def phase_times(self) -> list[float]:
         v = (ctypes.c_double * 8)()

@@ -23,6 +23,7 @@ def small_case(kind: str = "iso", nx: int = 64, nz: int = 64, tpc: int = 8, seed
         c.nx, c.nz = nx, nz
         c.RaT, c.RaC, c.visT = 1e5, 5e4, 1e3
         c.courant = 0.1
+        c.CFL, c.grids = 0, 6  # diffusive time step and the reference's level count at this low Ra
     elif kind == "depth":
         c, _ = workload("C3")
         c.nx, c.nz = nx, nz

@@ -27,9 +27,15 @@ def pair(kind, **kw):
     return cfg, o, e
 
 
-@pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
-def test_upload_projection_bit_exact(kind):
-    cfg, o, e = pair(kind)
+# (kind, nx, nz): the power-of-two grids of the physics cases, and 96x48 (spacing 1/48, not a power
+# of two: the general branches of the cell index, the shape functions and the multigrid constants)
+GRIDS = [("iso", 64, 64), ("chem", 64, 64), ("depth", 64, 64), ("chem", 96, 48), ("depth", 96, 48)]
+GRID_IDS = [f"{k}-{nx}x{nz}" for k, nx, nz in GRIDS]
+
+
+@pytest.mark.parametrize("kind,nx,nz", GRIDS, ids=GRID_IDS)
+def test_upload_projection_bit_exact(kind, nx, nz):
+    cfg, o, e = pair(kind, nx=nx, nz=nz)
     assert np.array_equal(e.get(eng.F_NEMPTY), o.get(11))
     for fid in (eng.F_TRATIO, eng.F_TVIS, eng.F_TBUOY, eng.F_T):
         g, r = e.get(fid), o.get(fid)
@@ -39,15 +45,16 @@ def test_upload_projection_bit_exact(kind):
     e.close()
 
 
-@pytest.mark.parametrize("kind", ["iso", "chem", "c3"])
-def test_mixed_projection_bit_exact(kind):
+@pytest.mark.parametrize("kind,nx,nz", [("iso", 64, 64), ("chem", 64, 64), ("c3", 64, 64), ("chem", 96, 48)],
+                         ids=["iso", "chem", "c3", "chem-96x48"])
+def test_mixed_projection_bit_exact(kind, nx, nz):
     """The one-pass fixed-point projection of the mixed-precision path equals its integer
     restatement bit for bit (counts, Tratio and Cnew on every node with tracers), tracers on the
     walls and corners included."""
     from oracle.project_fx import project_fx, ratios
     from projectracer_gb300.config import PT_PREC_MIXED
 
-    cfg, st = small_case(kind)
+    cfg, st = small_case(kind, nx=nx, nz=nz)
     st = walls(cfg, st)
     cfg.precision = PT_PREC_MIXED
     e = eng.Engine(cfg)
@@ -122,9 +129,9 @@ def test_mixed_steps_independent_of_tracer_order():
         assert np.array_equal(a[perm], b)
 
 
-@pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
-def test_solve_psi_matches_oracle(kind):
-    cfg, o, e = pair(kind)
+@pytest.mark.parametrize("kind,nx,nz", GRIDS, ids=GRID_IDS)
+def test_solve_psi_matches_oracle(kind, nx, nz):
+    cfg, o, e = pair(kind, nx=nx, nz=nz)
     info = e.solve_psi()
     o.solve_psi()
     assert info["cycles"] == int(o.scalar("cycles"))
@@ -136,9 +143,9 @@ def test_solve_psi_matches_oracle(kind):
     e.close()
 
 
-@pytest.mark.parametrize("kind", ["iso", "chem", "depth"])
-def test_step_matches_oracle(kind):
-    cfg, o, e = pair(kind)
+@pytest.mark.parametrize("kind,nx,nz", GRIDS, ids=GRID_IDS)
+def test_step_matches_oracle(kind, nx, nz):
+    cfg, o, e = pair(kind, nx=nx, nz=nz)
     e.solve_psi()
     o.solve_psi()
     dt, info = e.step()

@@ -1,8 +1,10 @@
 """pt_tracers_to_corners_noalloc, the projection for drivers that cannot allocate device memory
 (their pool owns the GPU, or cudaMalloc would stall other streams), against pt_tracers_to_corners
-on the same engine and tracer state: two consecutive calls of each give bit-identical T, C and
-tracer counts; states above the static scratch limits are rejected.  Collected last (file name)
-so that it also runs after the rest of the suite has used the device."""
+on the same engine and tracer state, in both precisions: two consecutive calls of each give
+bit-identical T, C and tracer counts (FP64: the sorted sums; mixed precision: the integer
+fixed-point sums, which reuse the same static scratch as their accumulator); states above the
+static scratch limits are rejected.  Collected last (file name) so that it also runs after the
+rest of the suite has used the device."""
 import ctypes
 
 import numpy as np
@@ -18,8 +20,10 @@ def _fields(e):
     return [e.get(f) for f in (eng.F_TRATIO, eng.F_CNEW, eng.F_NEMPTY, eng.F_T)]
 
 
-def test_noalloc_projection_matches_existing_entry_point():
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_noalloc_projection_matches_existing_entry_point(precision):
     cfg, st = small_case("chem")
+    cfg.precision = precision
     e = eng.Engine(cfg)
     e.upload(st)
     e.solve_psi()
