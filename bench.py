@@ -208,6 +208,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the headline workload (no error, residual-floor, 1e-8 and per-configuration sections)")
     ap.add_argument("--tpc", type=int, default=0,
                     help="tracers per cell override (profiling captures of a smaller tracer state only)")
     args = ap.parse_args()
@@ -270,20 +272,31 @@ def main():
     phases = {nm: (ph1[q] - ph0[q]) / args.steps for q, nm in enumerate(phase_names)}
     # the plain FP64 GPU path from the same state: psi-solve ms at the same tolerance
     fp64 = None
+    extra = {}
     if args.precision == "mixed" and not args.no_fp64_compare:
         snap = snapshot(e, eng, st)
         e.close()
         e = None
         fp64 = fp64_comparison(eng, cfg, snap)
         fp64_same = fp64_comparison(eng, cfg, snap, same_schedule=True)
+        if not args.quick:
+            extra["mixed_error_vs_fp64"] = mixed_error_vs_fp64(eng, cfg, snap)
+            extra[f"psi_residual_floor_{cfg.nx}x{cfg.nz}"] = residual_floor(eng, cfg, snap)
+        del snap
+    if not args.quick and rank == 0:
+        if e is not None:
+            e.close()
+            e = None
+        extra["psi_solve_at_1e-8"] = psi_at_1e8(eng)
+        extra["per_config"] = per_config(eng)
     line = {"metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": args.steps,
             "warmup": W, "ms_per_step": elapsed / args.steps * 1e3, "host_ms_per_step": host_s / args.steps * 1e3,
             "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
             "data": "synthetic",
-            "config": {"workload": f"{args.workload} {cfg.nx}x{cfg.nz} {cfg.ntr} tracers",
-                       "precision": args.precision, "tolerance": cfg.tolerance, "grids": grids,
-                       "courant": cfg.courant, "replicas": world, "l2_flush": "inputs larger than L2"},
+            "config": dict({"workload": f"{args.workload} {cfg.nx}x{cfg.nz} {cfg.ntr} tracers",
+                            "precision": args.precision, "replicas": world, "l2_flush": "inputs larger than L2"},
+                           **solver_keys(cfg, grids)),
             "psi_solve_ms": solve_ms / max(1, nsolve), "mg_cycles_per_solve": cycles / max(1, nsolve),
             "tracers_per_s": value * cfg.ntr, "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
             "roofline": roof, "phase_ms_per_step": phases}
@@ -292,6 +305,7 @@ def main():
         line["psi_solve_speedup_vs_fp64"] = fp64["psi_solve_ms"] / max(1e-9, line["psi_solve_ms"])
         line["fp64_same_schedule"] = fp64_same
         line["psi_solve_speedup_vs_fp64_same_schedule"] = fp64_same["psi_solve_ms"] / max(1e-9, line["psi_solve_ms"])
+    line.update(extra)
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args.workload).items()
@@ -304,6 +318,191 @@ def main():
     dist.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+GUESS_NAMES = {0: "previous psi", 1: "zero", 2: "learned", 3: "time-extrapolated"}
+
+
+def solver_keys(cfg, grids=None) -> dict:
+    """The solver settings that define the timed method (the workload text fixes the physics; these
+    say where the timed run differs from the reference's shipped settings)."""
+    from projectracer_gb300.config import PT_CYCLE_V, PT_MG_CORRECTION, PT_PREC_MIXED
+
+    mixed = cfg.precision == PT_PREC_MIXED
+    return {"tolerance": cfg.tolerance, "grids": grids if grids is not None else cfg.grids, "courant": cfg.courant,
+            "CFL": cfg.CFL, "mg_scheme": "correction" if cfg.mg_scheme == PT_MG_CORRECTION else "reference",
+            "mg_cycle": "V" if (mixed and cfg.mg_cycle == PT_CYCLE_V) else "reference W-type",
+            "nstageS": cfg.nstageS, "nstageC": (cfg.nstageC or cfg.nstageS) if mixed else cfg.nstageS,
+            "dampingS": cfg.dampingS, "guess": GUESS_NAMES[cfg.guess_mode],
+            "coarse_solve": "FP64 explicit inverse of the FP64 banded LU"}
+
+
+def fp64_reference_method(cfg):
+    """The plain FP64 GPU path with the reference's solver (W-type schedule, 35-stage RKC1 smoother
+    with damping 1000, previous-psi start) on cfg's physics, grid and tolerance."""
+    from projectracer_gb300.config import PT_CYCLE_REFERENCE, PT_PREC_FP64, PtConfig
+
+    c = cfg.copy()
+    c.precision = PT_PREC_FP64
+    ref = PtConfig.defaults()
+    c.nstageS, c.dampingS, c.nstageC = ref.nstageS, ref.dampingS, 0
+    c.guess_mode = ref.guess_mode
+    c.mg_cycle = PT_CYCLE_REFERENCE
+    return c
+
+
+def _rel(a, b) -> float:
+    import numpy as np
+
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b))) / max(float(np.max(np.abs(b))), 1e-300)
+
+
+def mixed_error_vs_fp64(eng, cfg, snap) -> dict:
+    """The mixed path's error against the plain FP64 GPU path from the same state: in each
+    precision one psi solve, one step (three more solves, four projections) and the psi solve of
+    the next step, at the same tolerance; then the largest difference of each result relative to
+    the FP64 field's largest magnitude."""
+    out = {}
+    for tag, c in (("mixed", cfg.copy()), ("fp64", fp64_reference_method(cfg))):
+        e = eng.Engine(c)
+        e.upload(snap)
+        e.solve_psi()
+        dt, _ = e.step()
+        info = e.solve_psi()
+        out[tag] = {"dt": dt, "resid_ratio": info["resid_ratio"], "stats": e.stats(),
+                    "fields": {nm: e.get(fid) for nm, fid in (("psi", eng.F_SF), ("u", eng.F_U), ("w", eng.F_W),
+                                                              ("T", eng.F_T), ("C", eng.F_CNEW),
+                                                              ("tracer_r", eng.F_TRACER_R),
+                                                              ("tracer_s", eng.F_TRACER_S),
+                                                              ("tracer_T", eng.F_TRACER_T),
+                                                              ("tracer_C", eng.F_TRACER_C))}}
+        e.close()
+    m, f = out["mixed"], out["fp64"]
+    err = {nm: _rel(m["fields"][nm], f["fields"][nm]) for nm in f["fields"]}
+    for k in ("Nu", "vrms", "Tavg", "Cavg"):
+        err[k] = abs(m["stats"][k] - f["stats"][k]) / max(abs(f["stats"][k]), 1e-300)
+    err["dt"] = abs(m["dt"] - f["dt"]) / f["dt"]
+    err["nempty_equal"] = bool((m["stats"]["empty_cells"], m["stats"]["tracer_min"], m["stats"]["tracer_max"]) ==
+                               (f["stats"]["empty_cells"], f["stats"]["tracer_min"], f["stats"]["tracer_max"]))
+    return {"relative_error": err, "tolerance": cfg.tolerance,
+            "resid_ratio": {"mixed": m["resid_ratio"], "fp64": f["resid_ratio"]},
+            "how": "from the same state: psi solve + one RK4 step + the next psi solve in each precision; "
+                   "max |mixed - fp64| / max |fp64| per field (the FP64 path runs the reference's solver)"}
+
+
+def residual_floor(eng, cfg, snap, cycles: int = 40) -> dict:
+    """The lowest relative residual a top-of-step psi solve reaches within `cycles` cycles at a
+    tolerance it cannot meet (1e-14), for the FP64 path (reference solver) and the mixed path."""
+    out = {}
+    for tag, c in (("fp64", fp64_reference_method(cfg)), ("mixed", cfg.copy())):
+        c.tolerance, c.max_cycles = 1e-14, cycles
+        e = eng.Engine(c)
+        e.upload(snap)
+        try:
+            e.solve_psi()
+            status = "converged"
+        except eng.PtError as ex:
+            status = {-4: "cycle cap", -3: "diverged"}.get(ex.code, str(ex))
+        h = e.residuals()
+        e.close()
+        if not h:
+            out[tag] = {"status": status}
+            continue
+        q = min(range(len(h)), key=lambda j: h[j])
+        out[tag] = {"min_resid_ratio": h[q], "at_test": q + 1, "tests": len(h), "last": h[-1], "status": status,
+                    "reaches_1e-8": bool(h[q] <= 1e-8)}
+    return out
+
+
+def timed_steps(eng, cfg, st, steps: int, warmup: int) -> dict:
+    """Device-timed steps (psi solve + energy_time) of one configuration from a fresh upload (at
+    most 100 cycles per solve: a solve that cannot reach the tolerance fails instead of running on)."""
+    cfg = cfg.copy()
+    cfg.max_cycles = min(cfg.max_cycles, 100)
+    e = eng.Engine(cfg)
+    e.upload(st)
+    for _ in range(warmup):
+        e.solve_psi()
+        e.step()
+    e.region_begin()
+    cyc, ms, ns, worst = 0, 0.0, 0, 0.0
+    for _ in range(steps):
+        i0 = e.solve_psi()
+        _, i1 = e.step()
+        cyc += i0["cycles"] + i1["cycles"]
+        ms += i0["ms"] + i1["ms"]
+        ns += 4
+        worst = max(worst, i0["resid_ratio"], i1["resid_ratio"])
+    el = e.region_end() * 1e-3
+    e.close()
+    return {"timesteps_per_s": steps / el, "ms_per_step": el / steps * 1e3, "tracers_per_s": steps / el * cfg.ntr,
+            "psi_solve_ms": ms / ns, "mg_cycles_per_solve": cyc / ns, "max_resid_ratio": worst, "steps": steps}
+
+
+def per_config(eng, steps: int = 3) -> dict:
+    """Throughput of the other stated configurations on one GPU (device-timed, after 2 warm-up
+    steps): C1 and C2 in plain FP64 (the reference's solver), C5 in both precisions; the CPU
+    restatement beside C1 (the configuration the CPU can run in full)."""
+    from projectracer_gb300.config import PT_PREC_FP64, PT_PREC_MIXED, workload
+    from projectracer_gb300.inputs import make_state
+
+    res = {}
+    for name, precs in (("C1", (PT_PREC_FP64,)), ("C2", (PT_PREC_FP64,)), ("C5", (PT_PREC_MIXED, PT_PREC_FP64))):
+        cfg0, w = workload(name)
+        st = make_state(cfg0, 1, noise=0.0 if name == "C1" else 1e-3)
+        entry = {"grid": f"{cfg0.nx}x{cfg0.nz}", "tracers": int(cfg0.ntr)}
+        for prec in precs:
+            cfg, w = workload(name, 1.0, prec)
+            apply_bench_solver(cfg, w)
+            if prec == PT_PREC_FP64:
+                cfg = fp64_reference_method(cfg)
+            tag = "mixed" if prec == PT_PREC_MIXED else "fp64"
+            try:
+                r = timed_steps(eng, cfg, st, steps if name != "C5" else 2, 2)
+                r["config"] = solver_keys(cfg)
+            except Exception as ex:  # a configuration that fails is reported, not fatal
+                r = {"failed": str(ex)}
+            entry[tag] = r
+        res[name] = entry
+        del st
+    try:
+        cb = cpu_baseline("C1", steps=3)
+        res["C1"]["cpu_baseline"] = {k: v for k, v in cb.items() if k != "sample_seconds_per_step"}
+    except Exception as ex:
+        res["C1"]["cpu_baseline"] = {"failed": str(ex)}
+    return res
+
+
+def psi_at_1e8(eng, steps: int = 2) -> dict:
+    """psi-solve time at the metric's 1e-8 relative residual where the FP64 path reaches it: the
+    1024x512 workload's physics on a 512x256 grid (six levels down to 16x8), and the 256x128
+    thermochemical workload; plain FP64 (reference solver) against mixed precision from the same
+    seeded state, 2 warm-up steps then `steps` timed steps (4 solves each)."""
+    from projectracer_gb300.config import PT_PREC_MIXED, workload
+    from projectracer_gb300.inputs import make_state
+
+    res = {}
+    for name, scale in (("C3", 0.5), ("C2", 1.0)):
+        cfg, w = workload(name, scale, PT_PREC_MIXED)
+        cfg.tolerance = 1e-8
+        if name == "C3":
+            cfg.ntr = cfg.nx * cfg.nz * 8
+            cfg.grids = 6
+        st = make_state(cfg, 2, noise=1e-3)
+        entry = {"grid": f"{cfg.nx}x{cfg.nz}", "tolerance": 1e-8}
+        for tag, c in (("fp64", fp64_reference_method(cfg)), ("mixed", cfg.copy())):
+            try:
+                r = timed_steps(eng, c, st, steps, 2)
+                r["reached"] = bool(r["max_resid_ratio"] <= 1e-8)
+                entry[tag] = r
+            except Exception as ex:
+                entry[tag] = {"failed": str(ex)}
+        if "psi_solve_ms" in entry.get("fp64", {}) and "psi_solve_ms" in entry.get("mixed", {}):
+            entry["psi_solve_speedup"] = entry["fp64"]["psi_solve_ms"] / entry["mixed"]["psi_solve_ms"]
+            entry["step_speedup"] = entry["fp64"]["ms_per_step"] / entry["mixed"]["ms_per_step"]
+        res[f"{name} physics {cfg.nx}x{cfg.nz}"] = entry
+    return res
 
 
 def snapshot(e, eng, st) -> dict:

@@ -35,6 +35,8 @@ typedef struct {
 
 typedef struct ptref_state {
     pt_config cfg;
+    int iheattype_boundary; /* 1: comp=1 iheattype=1 boundary heating (the shipped run's start-up only) */
+    double klayer, dlayer;  /* the shipped run's initial layer profile (initial_conditions.f90) */
     int nparts;        /* emulated OpenMP thread partitions (sum order of the reference) */
     int iterate;       /* 1 multigrid, 0 direct banded */
     int nx, nz, grids, nsteps;
@@ -152,7 +154,6 @@ int ref_coarse_bandwidth(ptref_state* s);
 rfld ref_fld_alloc(int nx, int nz, int g);
 int ref_fail(ptref_state* s, int code, const char* msg);
 
-extern int ref_iheattype_boundary; /* 1: comp=1 iheattype=1 boundary heating (golden init only) */
-extern double ref_klayer, ref_dlayer;
+
 
 #endif

@@ -9,8 +9,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-int ref_iheattype_boundary = 0;
-double ref_klayer = 35.0, ref_dlayer = 0.5;
 
 static const double pii = 3.1415926535897932; /* basics.f90:32 */
 
@@ -557,10 +555,10 @@ static double H_horizontal_boundaries(double z, double RaC, double RaT, double k
 double ref_heating(ptref_state* s, int i, int k) {
     const pt_config* c = &s->cfg;
     if (c->comp == 0) return c->H;
-    if (ref_iheattype_boundary) {
+    if (s->iheattype_boundary) {
         double z = s->zg[k + 6], x = s->xg[i + 6];
         (void)x;
-        if (z == 0.0 || z == 1.0) return H_horizontal_boundaries(z, c->RaC, c->RaT, ref_klayer, ref_dlayer);
+        if (z == 0.0 || z == 1.0) return H_horizontal_boundaries(z, c->RaC, c->RaT, s->klayer, s->dlayer);
         s->status = PT_ERR_CONFIG;
         return 0.0;
     }
@@ -577,19 +575,19 @@ static double golden_temperature(ptref_state* s, double x, double z) {
     double f0 = 0.0;
     double a = c->aspect;
     double t1 = -(pii * pii * pii) * ((a * a + 1.0) * (a * a + 1.0)) / (a * a * a) * cos(pii * x / a) * sin(pii * z) * f0;
-    return (t1 + c->RaC / (1.0 + exp(-2.0 * ref_klayer * (ref_dlayer - z))) + (c->RaT - c->RaC) * (1.0 - z)) / c->RaT;
+    return (t1 + c->RaC / (1.0 + exp(-2.0 * s->klayer * (s->dlayer - z))) + (c->RaT - c->RaC) * (1.0 - z)) / c->RaT;
 }
-static double golden_composition(double x, double z) {
+static double golden_composition(const ptref_state* s, double x, double z) {
     (void)x;
-    return 1.0 / (1.0 + exp(-2.0 * ref_klayer * (ref_dlayer - z)));
+    return 1.0 / (1.0 + exp(-2.0 * s->klayer * (s->dlayer - z)));
 }
 
 /* initial_temperature (basics.f90:335-361) + initialize_tracers (composition.f90:776-858). */
 int ptref_init_reference(ptref_state* s, int tpc, int nthreads_rng, double klayer, double dlayer,
                          int iheattype_boundary) {
-    ref_klayer = klayer;
-    ref_dlayer = dlayer;
-    ref_iheattype_boundary = iheattype_boundary;
+    s->klayer = klayer;
+    s->dlayer = dlayer;
+    s->iheattype_boundary = iheattype_boundary;
     int nx = s->nx, nz = s->nz;
     double* xg = s->xg + 6;
     double* zg = s->zg + 6;
@@ -637,7 +635,7 @@ int ptref_init_reference(ptref_state* s, int tpc, int nthreads_rng, double klaye
                     if (st >= 1.0) st = 1.0;
                     s->rtr[id - 1] = rt;
                     s->str[id - 1] = st;
-                    if (s->cfg.comp == 1) s->Ctr[id - 1] = golden_composition(rt, st);
+                    if (s->cfg.comp == 1) s->Ctr[id - 1] = golden_composition(s, rt, st);
                     s->Ttr[id - 1] = golden_temperature(s, rt, st);
                     id++;
                 }

@@ -200,8 +200,11 @@ WORKLOADS = {
     "C4": dict(nx=512, nz=256, aspect=2.0, RaT=1e6, RaC=2e5, comp=1, ivis=1, visT=1e2, visP=1.0,
                tpc=16, courant=0.5, tolerance=1e-8, steps=1),
     # 2048x1024, Ra_T=1e8, Ra_C=2e7, contrast 1e6, 30 tracers per cell, H=5, 100 steps
+    # (timed, like 1024x512, at bench_tolerance with the mixed method's V-cycle settings)
     "C5": dict(nx=2048, nz=1024, aspect=2.0, RaT=1e8, RaC=2e7, comp=1, ivis=1, visT=1e5, visP=10.0,
-               tpc=30, courant=0.5, tolerance=1e-8, steps=100, H=5.0, CFL=1, mg_scheme=1),
+               tpc=30, courant=0.5, tolerance=1e-8, steps=100, H=5.0, CFL=1, mg_scheme=1, bench_tolerance=1e-6,
+               mg_cycle=PT_CYCLE_V, mixed_nstageS=10, mixed_nstageC=8, mixed_dampingS=30.0,
+               mixed_guess=PT_GUESS_EXTRAPOLATE),
 }
 
 

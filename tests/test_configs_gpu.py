@@ -50,7 +50,10 @@ def test_config_fp64_matches_oracle_over_steps(name, steps):
                 worst = max(worst, abs(se[k] - so[k]) / abs(so[k]))
         dt, _ = e.step()
         o.step()
-        assert dt == o.scalar("dt"), n
+        if cfg.CFL:  # velocity-limited: dt carries the velocity's rounding
+            assert abs(dt - o.scalar("dt")) <= TOL * o.scalar("dt"), n
+        else:
+            assert dt == o.scalar("dt"), n
     e.solve_psi()
     o.solve_psi()
     se, so = e.stats(), o.stats()

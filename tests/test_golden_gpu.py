@@ -4,8 +4,12 @@ The shipped run (100x100, 612,060 tracers, 2 OpenMP threads) wrote its t=0 stati
 stats.dat (basics.f90:427-428) and its t=0 snapshot to T10000 (main.f90:396-397); both are
 fixtures in tests/golden.  The t=0 state is rebuilt by the oracle's restatement of the start-up
 (initial T, mzran tracer seeding split over 2 threads, composition.f90:776-858), pinned by
-tests/test_oracle_golden.py, and uploaded into the engine as a restart (pt_upload_state).  The
-engine then projects the tracers, smooths T, solves for psi and computes the statistics itself.
+tests/test_oracle_golden.py, and uploaded into the engine as a restart (pt_upload_state): the
+engine projects the tracers itself (counts, Cnew).  The reference's fresh start-up builds T_vis
+and T_buoy differently from its restart read (main.f90:168-230 against grid.f90:93-95 with
+main.f90:204-210), so the start-up's T, T_vis, T_buoy, C_vis and C_buoy are then set through
+pt_set_field, as a driver that starts fresh would.  The engine then solves for psi and computes
+the velocities and the statistics.
 
 The grid spacing 0.01 is not a power of two, so these cases run the general branches of the
 projection and the RK stage (cell index by llround(x/h), the FP64 division in the shape
@@ -42,35 +46,40 @@ def golden_state(golden):
     inp = golden["namelist"]["inputs"]
     o = Oracle(cfg, iterate=1, nparts=golden["stdout"]["Nthreads"])
     o.init_reference(int(inp["tpc"]), golden["stdout"]["Nthreads"], float(inp["klayer"]), float(inp["dlayer"]), 1)
+    cfg.Tbot_iso, cfg.Ttop_iso = o.scalar("Tbot_iso"), o.scalar("Ttop_iso")  # set by initial_temperature
     xg, zg = grid_coords(cfg)
     st = dict(xg=xg, zg=zg, T=o.get(0), Cnew=o.get(4), SF=o.get(7), rtr=o.get(20), str=o.get(21), Ttr=o.get(22),
               Ctr=o.get(23))
-    return cfg, st
+    start = {eng.F_T: o.get(0), eng.F_TVIS: o.get(2), eng.F_TBUOY: o.get(3), eng.F_CVIS: o.get(5),
+             eng.F_CBUOY: o.get(6)}
+    return cfg, st, start
 
 
 @pytest.fixture(scope="module")
 def engine_t0(golden_state):
-    cfg, st = golden_state
+    cfg, st, start = golden_state
     e = eng.Engine(cfg)
     e.upload(st)
+    projected = {f: e.get(f) for f in (eng.F_NEMPTY, eng.F_TRATIO, eng.F_CNEW, eng.F_TVIS)}
+    for f, v in start.items():
+        e.set(f, v)
     before = e.stats()
     info = e.solve_psi()
     after = e.stats()
-    fields = {f: e.get(f) for f in (eng.F_T, eng.F_SF, eng.F_U, eng.F_W, eng.F_NEMPTY, eng.F_CNEW, eng.F_TVIS,
-                                    eng.F_TRATIO)}
+    fields = {f: e.get(f) for f in (eng.F_T, eng.F_SF, eng.F_U, eng.F_W, eng.F_NEMPTY, eng.F_CNEW)}
     e.close()
-    return before, after, info, fields
+    return before, after, info, fields, projected
 
 
 def test_golden_state_is_the_shipped_run(golden, golden_state):
-    cfg, st = golden_state
+    cfg, st, _ = golden_state
     assert cfg.nx == 100 and cfg.nz == 100 and len(st["rtr"]) == golden["stdout"]["ntr"] == 612060
     assert cfg.aspect / cfg.nx == 0.01
 
 
 def test_stats_t0_without_psi(golden, engine_t0):
     """Columns that need no psi solve, straight after the restart upload."""
-    st, _, _, _ = engine_t0
+    st = engine_t0[0]
     ref = golden["stats"][0]
     for k in ("empty_cells", "tracer_min", "tracer_max"):
         assert st[k] == ref[k], k
@@ -79,7 +88,7 @@ def test_stats_t0_without_psi(golden, engine_t0):
 
 
 def test_stats_t0_through_psi_solve(golden, engine_t0):
-    _, st, info, _ = engine_t0
+    _, st, info, _, _ = engine_t0
     ref = golden["stats"][0]
     assert info["resid_ratio"] <= 1e-12
     for k in ("vrms", "mobility", "strain_max"):
@@ -90,7 +99,7 @@ def test_stats_t0_through_psi_solve(golden, engine_t0):
 
 def test_snapshot_t0_fields(engine_t0):
     """T10000 (x, z, T, SF, u, w, stress, vis, Tvis, nempty, Cnew, Cvis; 5 printed digits)."""
-    _, _, _, f = engine_t0
+    f = engine_t0[3]
     d = np.load(os.path.join(HERE, "golden", "T10000_subset.npz"))
     i, k, cols = d["i"], d["k"], d["cols"]
     mine = {2: f[eng.F_T][k + 3, i + 3], 3: f[eng.F_SF][k + 3, i + 3], 4: f[eng.F_U][k + 3, i + 3],
@@ -105,8 +114,8 @@ def test_projection_bit_exact_at_non_power_of_two_spacing(golden_state, engine_t
     """The FP64 projection of the shipped run's tracers (dr = ds = 0.01) against the oracle in
     the engine's canonical summation order: counts, Tratio, Cnew and the smoothed Tvis bit for
     bit."""
-    cfg, st = golden_state
-    _, _, _, f = engine_t0
+    cfg, st, _ = golden_state
+    f = engine_t0[4]  # straight after the upload's projection and smoothing
     o = Oracle(cfg, iterate=1, nparts=0)
     o.load_restart(st["xg"], st["zg"], st["T"], st["Cnew"], st["SF"], st["rtr"], st["str"], st["Ctr"], st["Ttr"])
     assert np.array_equal(f[eng.F_NEMPTY], o.get(11))
@@ -120,7 +129,7 @@ def test_mixed_projection_at_non_power_of_two_spacing(golden_state):
     its integer restatement, bit for bit, on the shipped run's tracers."""
     from oracle.project_fx import project_fx, ratios
 
-    cfg, st = golden_state
+    cfg, st, _ = golden_state
     c = cfg.copy()
     c.precision = PT_PREC_MIXED
     e = eng.Engine(c)
@@ -138,7 +147,7 @@ def test_mixed_projection_at_non_power_of_two_spacing(golden_state):
 def test_step_at_non_power_of_two_spacing(golden_state):
     """One RK4 step from the shipped run's t=0 state (isoviscous, multigrid at 1e-12), engine
     against oracle: dt, tracers and T to 1e-10, counts bit-exact."""
-    cfg, st = golden_state
+    cfg, st, _ = golden_state
     o = Oracle(cfg, iterate=1, nparts=0)
     o.load_restart(st["xg"], st["zg"], st["T"], st["Cnew"], st["SF"], st["rtr"], st["str"], st["Ctr"], st["Ttr"])
     e = eng.Engine(cfg)
