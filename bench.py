@@ -578,7 +578,7 @@ def end_to_end(e, eng, cfg, st, steps, dist, world):
             e._check(e.L.pt_set_field(fid, ptr(a)))
         e.solve_psi()
         e.step()
-        e._check(e.L.pt_download_state(ptr(grid_T), ptr(grid_C), ptr(grid_S), ptr(h_r), ptr(h_s), ptr(h_C), ptr(h_T)))
+        e._check(e.L.pt_download_state(ptr(grid_T), ptr(grid_C), ptr(grid_S), ptr(h_r), ptr(h_s), ptr(h_C), ptr(h_T), None))
     dist.barrier()
     el = dist.max(time.perf_counter() - t0)
     h2d = 4 * n * 8

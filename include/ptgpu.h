@@ -110,6 +110,17 @@ typedef struct pt_config {
     int32_t mg_cycle;      /* PT_CYCLE_*: level schedule of the mixed-precision solve (&gpu group) */
     int32_t nstageC;       /* RKC1 stages on levels 2..grids of the mixed-precision V-cycle; 0 = nstageS
                               (&gpu group; the FP64 path always uses nstageS) */
+    int32_t discrete_types; /* 1: tracers carry an integer type 0/1 instead of a continuous C
+                              (iC_continuous=0, ntype=1, bilinear shape_function=1: the projection of
+                              tracers_to_corners_OG, composition.f90:1090-1276); 0: continuous C */
+    int32_t reference_rounding; /* FP64 precision only (&gpu group).  0: the RKC1 stages and residuals
+                              form their stencil sums exactly in integer arithmetic and the coarsest
+                              grid is solved through the explicit inverse of its LU (fast, and at
+                              least as accurate as the reference's FP64 sums).  1: the reference's
+                              FP64 operations in its order (stream_derivatives/stream_space,
+                              iterative_solver.f90:890-1073; DGBTRS substitutions), no fused
+                              multiply-adds, so that results follow the CPU reference to its own
+                              rounding over many steps; slower */
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */
@@ -127,10 +138,13 @@ enum pt_field_id {
     PT_F_VIS = 10,    /* vis_grid(-3:nx+3,-3:nz+3,1) smoothed viscosity (get only) arrays.f90:665 */
     PT_F_NEMPTY = 11, /* nempty(0:nx,0:nz) int32 tracer count per dual cell (get only) */
     PT_F_RHS = 12,    /* RHS(1:nx-1,1:nz-1,1) buoyancy (get only)               arrays.f90:662 */
+    PT_F_COUNT_TYPE = 13, /* count_type(1,0:nx,0:nz) int32 tracers of type 1 per dual cell (get only;
+                             discrete types)                                   composition.f90:1141,1173 */
     PT_F_TRACER_R = 20, /* rtr(1:ntr) */
     PT_F_TRACER_S = 21, /* str(1:ntr) */
     PT_F_TRACER_T = 22, /* Ttr(1:ntr) */
-    PT_F_TRACER_C = 23  /* Ctr(1:ntr) */
+    PT_F_TRACER_C = 23, /* Ctr(1:ntr) (with discrete types: the type as 0.0 / 1.0) */
+    PT_F_TRACER_TYPE = 24 /* Ttype(1:ntr) int32, 0 or 1 (discrete types only)     basics.f90:110 */
 };
 
 /* Per-step solver telemetry (logged by the reference to stdout at iterative_solver.f90:197,338). */
@@ -180,14 +194,17 @@ int pt_get_field(int field, void* host);
  * main.f90:204-210: host arrays in the layout of the Trestart / restart_tracers records
  * (xg,zg,T,Cnew,SF and rtr,str,Ctr,Ttr).  Applies the T, psi and C boundary conditions, projects
  * the tracers (tracers_to_corners without smoothing), then runs smoother_time_T(T), smoother_time
- * and load_conductivity_array.  xg/zg are checked against the uniform grid.  Sets time=0. */
+ * and load_conductivity_array.  xg/zg are checked against the uniform grid.  Sets time=0.
+ * Ttype: the tracer types 0/1 (restart_tracers with iC_continuous=0) when cfg.discrete_types is
+ * 1, in which case Ctr may be NULL; must be NULL otherwise. */
 int pt_upload_state(const double* xg, const double* zg, const double* T, const double* Cnew,
                     const double* SF, const double* rtr, const double* str, const double* Ctr,
-                    const double* Ttr);
+                    const double* Ttr, const int32_t* Ttype);
 
-/* Download of the restart records written by print_restart (main.f90:457-496). */
+/* Download of the restart records written by print_restart (main.f90:457-496); any pointer may
+ * be NULL.  Ttype: the tracer types (discrete types only). */
 int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* str, double* Ctr,
-                      double* Ttr);
+                      double* Ttr, int32_t* Ttype);
 
 /* Velocity solve at the top of a time step (main.f90:246-259): multigrid
  * (iterative_solver.f90:124-341) then compute_velocities (momentum.f90:655-710).

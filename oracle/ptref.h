@@ -92,6 +92,8 @@ typedef struct ptref_state {
     /* tracers */
     int64_t ntr;
     double *rtr, *str, *Ttr, *Ctr;
+    int32_t* Ttype;       /* discrete tracer types 0/1 (iC_continuous=0), NULL for continuous C */
+    int32_t* count_type1; /* count_type(1, 0:nx, 0:nz) of the last discrete-type projection */
     double *rtr0, *str0, *Ttr0, *rtr1, *str1, *Ttr1, *rtr2, *str2, *Ttr2;
     double time, dt;
     double mass; int kent; int have_mass;
@@ -115,6 +117,10 @@ int ptref_init_reference(ptref_state* s, int tpc, int nthreads_rng, double klaye
 int ptref_load_restart(ptref_state* s, const double* xg, const double* zg, const double* T,
                        const double* Cnew, const double* SF, const double* rtr, const double* str,
                        const double* Ctr, const double* Ttr);
+
+/* discrete tracer types (iC_continuous=0, ntype=1): the types 0/1 of the tracers, set before
+ * ptref_load_restart; the projection is then tracers_to_corners_OG */
+int ptref_set_types(ptref_state* s, const int32_t* Ttype);
 
 int ptref_solve_psi(ptref_state* s);   /* update_velocities */
 int ptref_step(ptref_state* s);        /* energy_time */

@@ -40,6 +40,7 @@ def lib() -> ctypes.CDLL:
         L.ptref_error.argtypes = [vp]
         L.ptref_init_reference.argtypes = [vp, i32, i32, f64, f64, i32]
         L.ptref_load_restart.argtypes = [vp] + [vp] * 9
+        L.ptref_set_types.argtypes = [vp, vp]
         L.ptref_solve_psi.argtypes = [vp]
         L.ptref_step.argtypes = [vp]
         L.ptref_stats.argtypes = [vp, vp]
@@ -101,8 +102,10 @@ class Oracle:
         return (self.nz + 2 * g + 1, self.nx + 2 * g + 1)
 
     def get(self, field_id: int) -> np.ndarray:
-        if field_id == 11:
+        if field_id in (11, 13):
             out = np.zeros((self.nz + 1, self.nx + 1), dtype=np.int32)
+        elif field_id == 24:
+            out = np.zeros(self.cfg.ntr, dtype=np.int32)
         elif field_id == 12:
             out = np.zeros((self.nz - 1, self.nx - 1), dtype=np.float64)
         elif field_id >= 20:
@@ -124,6 +127,12 @@ class Oracle:
     def init_reference(self, tpc: int, nthreads_rng: int, klayer: float, dlayer: float,
                        boundary_heating: int = 1):
         self.check(self.L.ptref_init_reference(self.h, tpc, nthreads_rng, klayer, dlayer, boundary_heating))
+
+    def set_types(self, Ttype):
+        """Discrete tracer types 0/1 (call before load_restart): the projection becomes
+        tracers_to_corners_OG."""
+        self._types = np.ascontiguousarray(Ttype, dtype=np.int32)
+        self.check(self.L.ptref_set_types(self.h, _ptr(self._types)))
 
     def load_restart(self, xg, zg, T, Cnew, SF, rtr, str_, Ctr, Ttr):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (xg, zg, T, Cnew, SF, rtr, str_, Ctr, Ttr)]

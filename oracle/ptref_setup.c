@@ -526,6 +526,18 @@ ptref_state* ptref_create(const pt_config* cfg, int iterate, int nparts) {
     return s;
 }
 
+int ptref_set_types(ptref_state* s, const int32_t* Ttype) {
+    if (!s->cfg.comp) return ref_fail(s, PT_ERR_CONFIG, "discrete tracer types need comp=1");
+    if (!s->Ttype) s->Ttype = (int32_t*)malloc(sizeof(int32_t) * (size_t)(s->ntr > 0 ? s->ntr : 1));
+    if (!s->count_type1) s->count_type1 = (int32_t*)calloc((size_t)(s->nx + 1) * (size_t)(s->nz + 1), sizeof(int32_t));
+    for (int64_t t = 0; t < s->ntr; t++) {
+        if (Ttype[t] != 0 && Ttype[t] != 1) return ref_fail(s, PT_ERR_ARG, "tracer types must be 0 or 1 (ntype=1)");
+        s->Ttype[t] = Ttype[t];
+        s->Ctr[t] = (double)Ttype[t]; /* the type as a composition value (Ctr is unused by OG) */
+    }
+    return 0;
+}
+
 void ptref_destroy(ptref_state* s) {
     if (!s) return;
     /* process-lifetime test helper: the OS reclaims the remaining buffers */
@@ -671,7 +683,7 @@ int ptref_load_restart(ptref_state* s, const double* xg, const double* zg, const
     memcpy(s->rtr, rtr, nt * sizeof(double));
     memcpy(s->str, str, nt * sizeof(double));
     memcpy(s->Ttr, Ttr, nt * sizeof(double));
-    if (s->cfg.comp == 1) memcpy(s->Ctr, Ctr, nt * sizeof(double));
+    if (s->cfg.comp == 1 && !s->Ttype) memcpy(s->Ctr, Ctr, nt * sizeof(double)); /* types: Ctr already holds them */
     int rc = ref_project(s, s->rtr, s->str, s->Ttr, &s->T, 0);
     if (rc) return rc;
     ref_smoother_time_T(s, &s->T);

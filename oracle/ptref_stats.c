@@ -215,6 +215,16 @@ static rfld* field_of(ptref_state* s, int id) {
 int ptref_get_field(ptref_state* s, int id, void* out) {
     int nx = s->nx, nz = s->nz;
     if (id == PT_F_NEMPTY) { memcpy(out, s->nempty, sizeof(int32_t) * (size_t)(nx + 1) * (nz + 1)); return 0; }
+    if (id == PT_F_COUNT_TYPE) {
+        if (!s->count_type1) return PT_ERR_ARG;
+        memcpy(out, s->count_type1, sizeof(int32_t) * (size_t)(nx + 1) * (nz + 1));
+        return 0;
+    }
+    if (id == PT_F_TRACER_TYPE) {
+        if (!s->Ttype) return PT_ERR_ARG;
+        memcpy(out, s->Ttype, sizeof(int32_t) * (size_t)s->ntr);
+        return 0;
+    }
     if (id == PT_F_RHS) {
         double* o = (double*)out;
         for (int k = 1; k <= nz - 1; k++)

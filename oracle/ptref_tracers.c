@@ -253,6 +253,131 @@ static inline double shape_1d(double x, int i, double h) {
     return a > 0.0 ? a : 0.0;
 }
 
+/* tracers_to_corners_OG, composition.f90:1090-1276, with ntype=1 and the bilinear shape function
+ * (shape_function=1; shape_fn, composition.f90:888-894): per node the shape-weighted sum of T
+ * (T1), the shape sums of the type-0 and the type-1 tracers (count_type_real), and the per-type
+ * counts of the tracers whose nearest node it is (count_type).  nempty_real is the sum over the
+ * types (1221), C = count_type_real(1)/nempty_real and T = T1/nempty_real where nempty_real > 0
+ * (1243-1258).  Summation orders as in ref_project: nparts >= 1 the reference's per-thread ranges
+ * added in rank order (1110-1177); nparts == 0 the GPU's canonical order (per cell in ID order,
+ * then the 9 cells of a node in a fixed order). */
+static void project_og_sums(ptref_state* s, const double* r, const double* sv, const double* Tt, double* T1,
+                            double* cr0, double* cr1, int32_t* cnt, int32_t* cnt1, size_t nn) {
+    int nx = s->nx, nz = s->nz;
+    int64_t ntr = s->ntr;
+    const int32_t* ty = s->Ttype;
+#define NI(i, k) ((size_t)((i) + 1) + (size_t)((k) + 1) * (size_t)(nx + 3))
+    if (s->nparts >= 1) {
+        int P = s->nparts;
+        int64_t Nshare = ntr / P;
+        double* tw = (double*)calloc(nn * (size_t)P, sizeof(double));
+        double* w0 = (double*)calloc(nn * (size_t)P, sizeof(double));
+        double* w1 = (double*)calloc(nn * (size_t)P, sizeof(double));
+        int32_t* c0 = (int32_t*)calloc(nn * (size_t)P, sizeof(int32_t));
+        int32_t* c1 = (int32_t*)calloc(nn * (size_t)P, sizeof(int32_t));
+#pragma omp parallel for schedule(static, 1)
+        for (int rank = 0; rank < P; rank++) {
+            int64_t id_min = 1 + (int64_t)rank * Nshare;
+            int64_t id_max = (rank == P - 1) ? ((rank + 1) * Nshare > ntr ? (rank + 1) * Nshare : ntr) : (rank + 1) * Nshare;
+            size_t o = nn * (size_t)rank;
+            for (int64_t id = id_min; id <= id_max; id++) {
+                double rr = r[id - 1], ss = sv[id - 1];
+                int i = (int)lround(rr / s->dr), k = (int)lround(ss / s->ds);
+                int t1 = ty[id - 1] == 1;
+                if (t1) c1[o + NI(i, k)]++;
+                else c0[o + NI(i, k)]++;
+                for (int di = -1; di <= 1; di++)
+                    for (int dk = -1; dk <= 1; dk++) {
+                        double S = shape_1d(rr, i + di, s->dr) * shape_1d(ss, k + dk, s->ds);
+                        tw[o + NI(i + di, k + dk)] = tw[o + NI(i + di, k + dk)] + Tt[id - 1] * S;
+                        double* w = t1 ? w1 : w0;
+                        w[o + NI(i + di, k + dk)] = w[o + NI(i + di, k + dk)] + S;
+                    }
+            }
+        }
+        for (int k = 0; k <= nz; k++)
+            for (int i = 0; i <= nx; i++) {
+                double a = 0.0, b0 = 0.0, b1 = 0.0;
+                int32_t n0 = 0, n1 = 0;
+                for (int rank = 0; rank < P; rank++) {
+                    size_t q = nn * (size_t)rank + NI(i, k);
+                    a = a + tw[q];
+                    b0 = b0 + w0[q];
+                    b1 = b1 + w1[q];
+                    n0 += c0[q];
+                    n1 += c1[q];
+                }
+                T1[NI(i, k)] = a;
+                cr0[NI(i, k)] = b0;
+                cr1[NI(i, k)] = b1;
+                cnt[NI(i, k)] = n0 + n1;
+                cnt1[NI(i, k)] = n1;
+            }
+        free(tw); free(w0); free(w1); free(c0); free(c1);
+    } else {
+        size_t ncell = (size_t)(nx + 1) * (size_t)(nz + 1);
+        int64_t* start = (int64_t*)calloc(ncell + 1, sizeof(int64_t));
+        int64_t* list = (int64_t*)malloc(sizeof(int64_t) * (size_t)(ntr > 0 ? ntr : 1));
+        int32_t* cell = (int32_t*)malloc(sizeof(int32_t) * (size_t)(ntr > 0 ? ntr : 1));
+        for (int64_t id = 0; id < ntr; id++) {
+            int i = (int)lround(r[id] / s->dr), k = (int)lround(sv[id] / s->ds);
+            cell[id] = i + (nx + 1) * k;
+            start[cell[id] + 1]++;
+        }
+        for (size_t q = 0; q < ncell; q++) start[q + 1] += start[q];
+        int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (ncell + 1));
+        memcpy(fill, start, sizeof(int64_t) * (ncell + 1));
+        for (int64_t id = 0; id < ntr; id++) list[fill[cell[id]]++] = id;
+        free(fill);
+        double* Pc = (double*)calloc(ncell * 27, sizeof(double)); /* [cell][T, S type 1, S type 0][3x3] */
+        int32_t* n1c = (int32_t*)calloc(ncell, sizeof(int32_t));
+#pragma omp parallel for schedule(dynamic, 64)
+        for (size_t q = 0; q < ncell; q++) {
+            int ci = (int)(q % (size_t)(nx + 1)), ck = (int)(q / (size_t)(nx + 1));
+            double* pc = Pc + q * 27;
+            for (int64_t t = start[q]; t < start[q + 1]; t++) {
+                int64_t id = list[t];
+                double rr = r[id], ss = sv[id];
+                int t1 = ty[id] == 1;
+                n1c[q] += t1;
+                double wx[3], wz[3];
+                for (int d = 0; d < 3; d++) {
+                    wx[d] = shape_1d(rr, ci + d - 1, s->dr);
+                    wz[d] = shape_1d(ss, ck + d - 1, s->ds);
+                }
+                for (int dz = 0; dz < 3; dz++)
+                    for (int dx = 0; dx < 3; dx++) {
+                        double S = wx[dx] * wz[dz];
+                        pc[0 * 9 + dz * 3 + dx] = pc[0 * 9 + dz * 3 + dx] + Tt[id] * S;
+                        int plane = t1 ? 1 : 2;
+                        pc[plane * 9 + dz * 3 + dx] = pc[plane * 9 + dz * 3 + dx] + S;
+                    }
+            }
+        }
+        for (int k = 0; k <= nz; k++)
+            for (int i = 0; i <= nx; i++) {
+                double a = 0.0, b1 = 0.0, b0 = 0.0;
+                for (int ck = k - 1; ck <= k + 1; ck++)
+                    for (int ci = i - 1; ci <= i + 1; ci++) {
+                        if (ci < 0 || ci > nx || ck < 0 || ck > nz) continue;
+                        const double* pc = Pc + ((size_t)ci + (size_t)(nx + 1) * (size_t)ck) * 27;
+                        int dz = k - ck + 1, dx = i - ci + 1;
+                        a = a + pc[0 * 9 + dz * 3 + dx];
+                        b1 = b1 + pc[1 * 9 + dz * 3 + dx];
+                        b0 = b0 + pc[2 * 9 + dz * 3 + dx];
+                    }
+                size_t q = (size_t)i + (size_t)(nx + 1) * (size_t)k;
+                T1[NI(i, k)] = a;
+                cr0[NI(i, k)] = b0;
+                cr1[NI(i, k)] = b1;
+                cnt[NI(i, k)] = (int32_t)(start[q + 1] - start[q]);
+                cnt1[NI(i, k)] = n1c[q];
+            }
+        free(Pc); free(n1c); free(start); free(list); free(cell);
+    }
+#undef NI
+}
+
 /* tracers_to_corners_iC_continuous, composition.f90:942-1087.
  * nparts>=1: the reference's order -- tracer IDs split into nparts contiguous ranges (one per
  *            OpenMP thread), each summed in ID order, then the ranges added in rank order.
@@ -279,7 +404,17 @@ int ref_project(ptref_state* s, const double* r, const double* sv, const double*
             return ref_fail(s, PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
         }
     }
-    if (s->nparts >= 1) {
+    if (s->Ttype) { /* discrete types: tracers_to_corners_OG */
+        double* cr0 = (double*)calloc(nn, sizeof(double));
+        int32_t* cnt1 = (int32_t*)calloc(nn, sizeof(int32_t));
+        project_og_sums(s, r, sv, Tt, TxS, cr0, CxS, cnt, cnt1, nn);
+        for (int k = 0; k <= nz; k++)
+            for (int i = 0; i <= nx; i++) {
+                s->count_type1[i + (nx + 1) * k] = cnt1[NI(i, k)];
+                shape_sum[NI(i, k)] = cr0[NI(i, k)] + CxS[NI(i, k)];
+            }
+        free(cr0); free(cnt1);
+    } else if (s->nparts >= 1) {
         int P = s->nparts;
         int64_t Nshare = ntr / P;
         double* ssw = (double*)calloc(nn * (size_t)P, sizeof(double));

@@ -1,7 +1,8 @@
 """Builds libptgpu.so (the CUDA engine behind include/ptgpu.h) in-tree with nvcc for sm_103a.
 
-Translation units compile in parallel; the field kernels are compiled without FMA contraction so
-that they round exactly like the reference's expressions (see csrc/pt_fields.cu).
+Translation units compile in parallel; the field kernels and the FP64 multigrid kernels are
+compiled without FMA contraction so that they round exactly like the reference's expressions (see
+csrc/pt_fields.cu, csrc/pt_mg.cu); kernels that want a fused multiply-add call fma() explicitly.
 """
 
 from __future__ import annotations
@@ -20,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
           "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
-EXTRA = {"pt_fields.cu": ["--fmad=false"]}
+EXTRA = {"pt_fields.cu": ["--fmad=false"], "pt_mg.cu": ["--fmad=false"]}
 SOURCES = ["pt_setup.cpp", "pt_fields.cu", "pt_tracers.cu", "pt_mg.cu", "pt_mixed.cu", "pt_api.cu", "pt_unet.cu"]
 
 

@@ -147,6 +147,7 @@ static int engine_alloc(Engine& E) {
             if ((rc = dalloc(E, &E.der[f][j], n1))) return rc;
     const int ncell = (E.K.nx + 1) * (E.K.nz + 1);
     if ((rc = ialloc(E, &E.nempty, (size_t)ncell))) return rc;
+    if (E.cfg.discrete_types && (rc = ialloc(E, &E.count1, (size_t)ncell))) return rc;
     if ((rc = dalloc(E, &E.red, (size_t)(4 * (E.K.nz + 1) + 64)))) return rc;
     if ((rc = dalloc(E, &E.dscal, 32))) return rc;
     CK(cudaMallocHost(&E.hscal, 64 * sizeof(double)));
@@ -209,7 +210,7 @@ static void engine_free(Engine& E) {
     for (int q = 0; q < 11; q++)
         if (E.visw[q]) cudaFree(E.visw[q]);
     if (E.proj_runs) cudaFree(E.proj_runs);
-    int32_t* ia[] = {E.nempty, E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp, E.perm, E.perm2, E.rs_count, E.rs_start, E.rs_tot};
+    int32_t* ia[] = {E.nempty, E.count1, E.tcell, E.clist, E.ccount, E.cstart, E.scan_tmp, E.perm, E.perm2, E.rs_count, E.rs_start, E.rs_tot};
     for (auto a : ia)
         if (a) cudaFree(a);
     if (E.ipiv) cudaFree(E.ipiv);
@@ -346,6 +347,14 @@ int pt_init(const pt_config* cfg) {
         return fail(PT_ERR_CONFIG, "precision must be PT_PREC_FP64 or PT_PREC_MIXED");
     }
     if ((int64_t)cfg->ntr > 2000000000LL) { delete E; return fail(PT_ERR_CONFIG, "ntr above 2e9 is not supported"); }
+    if (cfg->reference_rounding != 0 && (cfg->reference_rounding != 1 || cfg->precision != PT_PREC_FP64)) {
+        delete E;
+        return fail(PT_ERR_CONFIG, "reference_rounding = 1 applies to PT_PREC_FP64 only");
+    }
+    if (cfg->discrete_types != 0 && (cfg->discrete_types != 1 || cfg->comp != 1)) {
+        delete E;
+        return fail(PT_ERR_CONFIG, "discrete_types = 1 needs comp = 1 (one dense type, ntype = 1)");
+    }
     TRACE("pt_init: geometry and stream");
     E->g1 = make_geo(cfg->nx, cfg->nz);
     for (int l = 1; l <= E->grids; l++) E->gl[l] = make_geo(E->L[l].nx, E->L[l].nz);
@@ -381,7 +390,8 @@ int pt_field_extent(int field, int32_t* lo_x, int32_t* hi_x, int32_t* lo_z, int3
     Engine& E = *g_eng;
     int32_t a = 0, b = 0, c = 0, d = 0, eb = 8;
     if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) { a = 1; b = (int32_t)E.ntr; }
-    else if (field == PT_F_NEMPTY) { a = 0; b = E.K.nx; c = 0; d = E.K.nz; eb = 4; }
+    else if (field == PT_F_NEMPTY || (field == PT_F_COUNT_TYPE && E.count1)) { a = 0; b = E.K.nx; c = 0; d = E.K.nz; eb = 4; }
+    else if (field == PT_F_TRACER_TYPE && E.cfg.discrete_types) { a = 1; b = (int32_t)E.ntr; eb = 4; }
     else if (field == PT_F_RHS) { a = 1; b = E.K.nx - 1; c = 1; d = E.K.nz - 1; }
     else if (field_ptr(E, field)) { int g = field_ghost(field); a = -g; b = E.K.nx + g; c = -g; d = E.K.nz + g; }
     else return fail(PT_ERR_ARG, "unknown field id");
@@ -406,7 +416,19 @@ int pt_set_field(int field, const void* host) {
     if (int rc = need(g_eng != nullptr)) return rc;
     if (!host) return fail(PT_ERR_ARG, "null pointer");
     Engine& E = *g_eng;
-    if (field == PT_F_NEMPTY || field == PT_F_VIS || field == PT_F_RHS) return fail(PT_ERR_ARG, "field is read-only");
+    if (field == PT_F_NEMPTY || field == PT_F_VIS || field == PT_F_RHS || field == PT_F_COUNT_TYPE)
+        return fail(PT_ERR_ARG, "field is read-only");
+    if (field == PT_F_TRACER_TYPE) {
+        if (!E.cfg.discrete_types) return fail(PT_ERR_ARG, "tracer types exist with discrete_types = 1 only");
+        CK(cudaMemcpyAsync(E.tcell, host, sizeof(int32_t) * (size_t)E.ntr, cudaMemcpyHostToDevice, E.st));
+        if (!E.perm_active) return types_to_c(E, E.tcell, E.Ctr);
+        if (int rc = types_to_c(E, E.tcell, E.str2)) return rc;  // user order, staged
+        if (int rc = tracer_user_order(E, E.Ctr, E.str2, false)) return rc;
+        CK(cudaStreamSynchronize(E.st));
+        return 0;
+    }
+    if (field == PT_F_TRACER_C && E.cfg.discrete_types)
+        return fail(PT_ERR_ARG, "discrete_types = 1: set the tracer types (PT_F_TRACER_TYPE), not C");
     if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) {
         const size_t nb = sizeof(double) * (size_t)E.ntr;
         if (!E.perm_active) {
@@ -427,8 +449,22 @@ int pt_get_field(int field, void* host) {
     if (!host) return fail(PT_ERR_ARG, "null pointer");
     Engine& E = *g_eng;
     CK(cudaStreamSynchronize(E.st));
-    if (field == PT_F_NEMPTY) {
-        CK(cudaMemcpy(host, E.nempty, sizeof(int32_t) * (size_t)(E.K.nx + 1) * (E.K.nz + 1), cudaMemcpyDeviceToHost));
+    if (field == PT_F_NEMPTY || field == PT_F_COUNT_TYPE) {
+        const int32_t* src = field == PT_F_NEMPTY ? E.nempty : E.count1;
+        if (!src) return fail(PT_ERR_ARG, "count_type exists with discrete_types = 1 only");
+        CK(cudaMemcpy(host, src, sizeof(int32_t) * (size_t)(E.K.nx + 1) * (E.K.nz + 1), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+    if (field == PT_F_TRACER_TYPE) {
+        if (!E.cfg.discrete_types) return fail(PT_ERR_ARG, "tracer types exist with discrete_types = 1 only");
+        const double* c = E.Ctr;
+        if (E.perm_active) {  // back to the user's order
+            if (int rc = tracer_user_order(E, E.Ctr, E.str2, true)) return rc;
+            c = E.str2;
+        }
+        if (int rc = c_to_types(E, c, E.tcell)) return rc;
+        CK(cudaMemcpyAsync(host, E.tcell, sizeof(int32_t) * (size_t)E.ntr, cudaMemcpyDeviceToHost, E.st));
+        CK(cudaStreamSynchronize(E.st));
         return 0;
     }
     if (field >= PT_F_TRACER_R && field <= PT_F_TRACER_C) {
@@ -446,11 +482,14 @@ int pt_get_field(int field, void* host) {
 }
 
 int pt_upload_state(const double* xg, const double* zg, const double* T, const double* Cnew, const double* SF,
-                    const double* rtr, const double* str, const double* Ctr, const double* Ttr) {
+                    const double* rtr, const double* str, const double* Ctr, const double* Ttr, const int32_t* Ttype) {
     if (int rc = need(g_eng != nullptr)) return rc;
     Engine& E = *g_eng;
-    if (!xg || !zg || !T || !SF || !rtr || !str || !Ttr || (E.cfg.comp && (!Cnew || !Ctr)))
+    const bool og = E.cfg.discrete_types != 0;
+    if (!xg || !zg || !T || !SF || !rtr || !str || !Ttr || (E.cfg.comp && !Cnew) || (E.cfg.comp && !og && !Ctr))
         return fail(PT_ERR_ARG, "null pointer in restart arrays");
+    if (og != (Ttype != nullptr))
+        return fail(PT_ERR_ARG, og ? "discrete_types = 1: Ttype is required" : "Ttype given without discrete_types = 1");
     const int nx = E.K.nx, nz = E.K.nz;
     for (int i = 0; i <= nx; i++)
         if (std::fabs(xg[i + 6] - E.K.dr * i) > 1e-12 * E.K.aspect)
@@ -468,7 +507,12 @@ int pt_upload_state(const double* xg, const double* zg, const double* T, const d
     CK(cudaMemcpyAsync(E.rtr, rtr, nb, cudaMemcpyHostToDevice, E.st));
     CK(cudaMemcpyAsync(E.str, str, nb, cudaMemcpyHostToDevice, E.st));
     CK(cudaMemcpyAsync(E.Ttr, Ttr, nb, cudaMemcpyHostToDevice, E.st));
-    if (E.cfg.comp) CK(cudaMemcpyAsync(E.Ctr, Ctr, nb, cudaMemcpyHostToDevice, E.st));
+    if (og) {  // the types, held as 0.0 / 1.0 in the composition array
+        CK(cudaMemcpyAsync(E.tcell, Ttype, sizeof(int32_t) * (size_t)E.ntr, cudaMemcpyHostToDevice, E.st));
+        if ((rc = types_to_c(E, E.tcell, E.Ctr))) return rc;
+    } else if (E.cfg.comp) {
+        CK(cudaMemcpyAsync(E.Ctr, Ctr, nb, cudaMemcpyHostToDevice, E.st));
+    }
     if ((rc = tracer_order_reset(E))) return rc;
     TRACE("upload: boundary conditions");
     // grid.f90:67-73: boundary conditions on the restart fields
@@ -490,7 +534,8 @@ int pt_upload_state(const double* xg, const double* zg, const double* T, const d
     return 0;
 }
 
-int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* str, double* Ctr, double* Ttr) {
+int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* str, double* Ctr, double* Ttr,
+                      int32_t* Ttype) {
     if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
     int rc;
     if (T && (rc = pt_get_field(PT_F_T, T))) return rc;
@@ -500,6 +545,7 @@ int pt_download_state(double* T, double* Cnew, double* SF, double* rtr, double* 
     if (str && (rc = pt_get_field(PT_F_TRACER_S, str))) return rc;
     if (Ctr && (rc = pt_get_field(PT_F_TRACER_C, Ctr))) return rc;
     if (Ttr && (rc = pt_get_field(PT_F_TRACER_T, Ttr))) return rc;
+    if (Ttype && (rc = pt_get_field(PT_F_TRACER_TYPE, Ttype))) return rc;
     return 0;
 }
 

@@ -103,6 +103,7 @@ struct Engine {
     float* facc[3] = {};     // mixed precision: per tracer FP32 sums of the RK slopes of r, s, T
     double* coef[3] = {};    // 16 Taylor coefficients per node per field (advection)
     int32_t* nempty = nullptr;
+    int32_t* count1 = nullptr;  // discrete types: count_type(1, 0:nx, 0:nz) of the last projection
     // multigrid
     double *err[PT_MAXLEV] = {}, *S0[PT_MAXLEV] = {}, *S1[PT_MAXLEV] = {}, *S2[PT_MAXLEV] = {},
            *RHS[PT_MAXLEV] = {}, *res[PT_MAXLEV] = {}, *dtst[PT_MAXLEV] = {}, *ratio[PT_MAXLEV] = {},
@@ -293,6 +294,9 @@ int tracer_user_order(Engine& E, double* internal, double* staging, bool to_user
 int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f,
             int smooth);                              // composition.f90:923-1087
 int rk_stage(Engine& E, int stage);                   // energy.f90:258-536 tracer loops
+// discrete tracer types: int32 0/1 on the device <-> the type as 0.0 / 1.0 in a composition array
+int types_to_c(Engine& E, const int32_t* dev_types, double* c);
+int c_to_types(Engine& E, const double* c, int32_t* dev_types);
 
 // multigrid (pt_mg.cu)
 bool trace_on();  // PTGPU_TRACE set in the environment

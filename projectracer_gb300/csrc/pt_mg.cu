@@ -340,43 +340,33 @@ struct StreamOp {
     const double *vis, *vx, *vz, *vxz, *vxxmzz, *rhs, *dtst;
 };
 
-// -(stream operator - RHS) at node (i,k) of S (stream_derivatives + stream_space)
+// -(stream operator - RHS) at node (i,k) of S: stream_derivatives (iterative_solver.f90:973-1073)
+// and stream_space (890-911) with the reference's operations in the reference's order -- each
+// derivative a sum over its full stencil (zero weights included) divided by the spacing power,
+// the cross derivatives as 25-point sums, no fused multiply-adds (this file is compiled with
+// --fmad=false) -- so that the FP64 path with reference_rounding rounds like the reference.
 __device__ __forceinline__ double stream_F(const double* __restrict__ S, Geo g, const LevConst& L,
                                            const StreamOp& op, int i, int k, int ivis) {
-    // x and z lines through the node
-    double sx[7], sz[7];
-#pragma unroll
-    for (int j = 0; j < 7; j++) {
-        sx[j] = S[g.at(i + j - 3, k)];
-        sz[j] = S[g.at(i, k + j - 3)];
-    }
-    double Sxx = 0, Sxxx = 0, Sxxxx = 0, Szz = 0, Szzz = 0, Szzzz = 0;
-#pragma unroll
-    for (int j = 1; j <= 5; j++) { Sxx += cK.D2[j] * sx[j]; Szz += cK.D2[j] * sz[j]; }
-#pragma unroll
-    for (int j = 0; j < 7; j++) {
-        Sxxx += cK.D3[j] * sx[j]; Sxxxx += cK.D4[j] * sx[j];
-        Szzz += cK.D3[j] * sz[j]; Szzzz += cK.D4[j] * sz[j];
-    }
-    Sxx *= L.idr2; Sxxx *= L.idr3; Sxxxx *= L.idr4;  // reciprocals: see LevConst
-    Szz *= L.ids2; Szzz *= L.ids3; Szzzz *= L.ids4;
-    // cross derivatives: x-derivatives of the 5 rows, combined in z
-    double Sxz = 0, Sxxz = 0, Sxzz = 0, Sxxzz = 0;
-#pragma unroll
-    for (int kk = -2; kk <= 2; kk++) {
-        double d1 = 0, d2 = 0;
-#pragma unroll
-        for (int ii = -2; ii <= 2; ii++) {
-            double v = (kk == 0) ? sx[ii + 3] : S[g.at(i + ii, k + kk)];
-            d1 += cK.D1[3 + ii] * v;
-            d2 += cK.D2[3 + ii] * v;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int j = -2; j <= 2; j++) a += cK.D2[j + 3] * S[g.at(i + j, k)];
+    for (int j = -3; j <= 3; j++) b += cK.D3[j + 3] * S[g.at(i + j, k)];
+    for (int j = -3; j <= 3; j++) c += cK.D4[j + 3] * S[g.at(i + j, k)];
+    const double Sxx = a / L.dr2, Sxxx = b / L.dr3, Sxxxx = c / L.dr4;
+    a = 0.0; b = 0.0; c = 0.0;
+    for (int j = -2; j <= 2; j++) a += cK.D2[j + 3] * S[g.at(i, k + j)];
+    for (int j = -3; j <= 3; j++) b += cK.D3[j + 3] * S[g.at(i, k + j)];
+    for (int j = -3; j <= 3; j++) c += cK.D4[j + 3] * S[g.at(i, k + j)];
+    const double Szz = a / L.ds2, Szzz = b / L.ds3, Szzzz = c / L.ds4;
+    double xz = 0.0, xxz = 0.0, xzz = 0.0, xxzz = 0.0;
+    for (int k2 = -2; k2 <= 2; k2++)
+        for (int i2 = -2; i2 <= 2; i2++) {
+            const double v = S[g.at(i + i2, k + k2)];
+            xz += cK.Drs[i2 + 2][k2 + 2] * v;
+            xxz += cK.Drrs[i2 + 2][k2 + 2] * v;
+            xzz += cK.Drss[i2 + 2][k2 + 2] * v;
+            xxzz += cK.Drrss[i2 + 2][k2 + 2] * v;
         }
-        Sxz += cK.D1[3 + kk] * d1;
-        Sxzz += cK.D2[3 + kk] * d1;
-        Sxxz += cK.D1[3 + kk] * d2;
-        Sxxzz += cK.D2[3 + kk] * d2;
-    }
-    Sxz *= L.idrds; Sxxz *= L.idr2ds; Sxzz *= L.idrds2; Sxxzz *= L.idr2ds2;
+    const double Sxz = xz / L.drds, Sxxz = xxz / L.dr2ds, Sxzz = xzz / L.drds2, Sxxzz = xxzz / L.dr2ds2;
     size_t o = g.at(i, k);
     double r;
     double t2 = op.vis[o] * (Sxxxx + Szzzz + 2.0 * Sxxzz);
@@ -1295,7 +1285,8 @@ int mg_alloc(Engine& E) {
     }
     for (int q = 0; q < 11; q++)
         if (int rc = alloc(&E.visw[q], E.gl[1].elems())) return rc;
-    E.res_int = exact_stencils_setup(E);
+    // exact integer stencil sums unless the FP64 path is asked to round like the reference
+    E.res_int = !E.cfg.reference_rounding && exact_stencils_setup(E);
     int ldab = 2 * E.kl + E.ku + 1;
     if (int rc = alloc(&E.Mc, (size_t)ldab * E.ngc)) return rc;
     if (int rc = alloc(&E.Bc, E.ngc)) return rc;
@@ -1312,7 +1303,7 @@ int mg_alloc(Engine& E) {
     // explicit coarse inverse (both precisions): the coarse solve becomes a GEMV spread over the
     // SMs instead of two sequential banded substitutions on one warp of this part's narrow FP64
     // pipe; n^2 doubles, kept while it is small next to the level arrays (n <= 4096: <= 134 MB)
-    if (E.ngc <= 4096 && inv_smem(E.ngc, E.kl, E.ku) <= 200 * 1024) {
+    if (!E.cfg.reference_rounding && E.ngc <= 4096 && inv_smem(E.ngc, E.kl, E.ku) <= 200 * 1024) {
         CK(cudaMalloc(&E.Ginv, sizeof(double) * (size_t)E.ngc * E.ngc));
         E.bytes_allocated += sizeof(double) * (size_t)E.ngc * E.ngc;
         CK(cudaMalloc(&E.Ginv2, sizeof(double) * (size_t)E.ngc * E.ngc));

@@ -196,6 +196,12 @@ __device__ __forceinline__ double shape1(double x, int i, double h, double inv, 
 }
 
 // per-cell partial sums for the 3x3 nodes around the cell; planes of ncell: [q*9 + dz*3 + dx]
+// Continuous C (tracers_to_corners_iC_continuous): T*S, C*S, S.  Discrete types (OG,
+// tracers_to_corners_OG, composition.f90:1139-1166, the type held in Ct as 0.0 / 1.0): T*S, the
+// shape sum of the type-1 tracers (count_type_real(1)) and that of the type-0 tracers
+// (count_type_real(0)); a tracer of the other type leaves a plane's partial unchanged (+0.0 and
+// x 1.0 are exact), so the sums are those of the reference's per-type loops in ID order.
+template <bool OG>
 __global__ void k_cell_partials(const double* __restrict__ r, const double* __restrict__ s,
                                 const double* __restrict__ Tt, const double* __restrict__ Ct,
                                 const int32_t* __restrict__ list, const int32_t* __restrict__ start,
@@ -212,6 +218,7 @@ __global__ void k_cell_partials(const double* __restrict__ r, const double* __re
     for (int a = 0; a < n; a++) {
         int32_t t = list[b + a];
         double rr = r[t], ss = s[t], tv = Tt[t], cv = comp ? Ct[t] : 0.0;
+        const bool type1 = OG && cv != 0.0;
         double wx[3], wz[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -225,8 +232,13 @@ __global__ void k_cell_partials(const double* __restrict__ r, const double* __re
                 double S = __dmul_rn(wx[dx], wz[dz]);
                 int q = dz * 3 + dx;
                 aT[q] = __dadd_rn(aT[q], __dmul_rn(tv, S));
-                aC[q] = __dadd_rn(aC[q], __dmul_rn(cv, S));
-                aS[q] = __dadd_rn(aS[q], S);
+                if (OG) {
+                    if (type1) aC[q] = __dadd_rn(aC[q], S);
+                    else aS[q] = __dadd_rn(aS[q], S);
+                } else {
+                    aC[q] = __dadd_rn(aC[q], __dmul_rn(cv, S));
+                    aS[q] = __dadd_rn(aS[q], S);
+                }
             }
     }
 #pragma unroll
@@ -237,7 +249,10 @@ __global__ void k_cell_partials(const double* __restrict__ r, const double* __re
     }
 }
 
-// per node: fixed-order sum of the partials of the 3x3 surrounding cells, then the ratio
+// per node: fixed-order sum of the partials of the 3x3 surrounding cells, then the ratio.
+// OG: the shape sum is nempty_real = count_type_real(0) + count_type_real(1)
+// (composition.f90:1221), C = count_type_real(1) / nempty_real, T = T1 / nempty_real (1253-1256).
+template <bool OG>
 __global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restrict__ count, int ncell,
                             double* Tratio, double* Cnew, int32_t* nempty, Geo g, int comp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
@@ -253,12 +268,62 @@ __global__ void k_node_sums(const double* __restrict__ P, const int32_t* __restr
             sC = __dadd_rn(sC, P[(size_t)(9 + q) * ncell + c]);
             sS = __dadd_rn(sS, P[(size_t)(18 + q) * ncell + c]);
         }
+    if (OG) sS = __dadd_rn(sS, sC);
     int c = i + (nx + 1) * k;
     nempty[c] = count[c];
     if (sS > 0.0) {
         Tratio[g.at(i, k)] = __ddiv_rn(sT, sS);
         if (comp) Cnew[g.at(i, k)] = __ddiv_rn(sC, sS);
     }
+}
+
+// count_type(1, i, k) of tracers_to_corners_OG (composition.f90:1141, 1173): type-1 tracers
+// (Ct != 0) per nearest node, one atomic per distinct node of a warp.  Positions were checked by
+// the projection that runs before it; a tracer outside the domain is skipped.
+__global__ void k_count_type1(const double* __restrict__ r, const double* __restrict__ s,
+                              const double* __restrict__ Ct, int64_t n, int32_t* __restrict__ count1) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1;
+    if (t < n && Ct[t] != 0.0) {
+        const double rr = r[t], ss = s[t];
+        if (in_range(rr, cK.aspect) && in_range(ss, 1.0)) {
+            const int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
+            const int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
+            c = i + (cK.nx + 1) * k;
+        }
+    }
+    const unsigned group = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && (int)(threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(&count1[c], __popc(group));
+}
+
+// tracer types (int32 0/1) <-> the type as 0.0 / 1.0 in the composition array; a type other
+// than 0 and 1 sets bad (ntype = 1)
+__global__ void k_types_to_c(const int32_t* __restrict__ ty, double* __restrict__ c, int64_t n, int* bad) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int32_t v = ty[t];
+    if (v != 0 && v != 1) atomicOr(bad, 4);
+    c[t] = v == 1 ? 1.0 : 0.0;
+}
+__global__ void k_c_to_types(const double* __restrict__ c, int32_t* __restrict__ ty, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) ty[t] = c[t] != 0.0 ? 1 : 0;
+}
+
+int types_to_c(Engine& E, const int32_t* dev_types, double* c) {
+    CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
+    PT_COUNT(), k_types_to_c<<<nblk(E.ntr, 256), 256, 0, E.st>>>(dev_types, c, E.ntr, E.derr);
+    CKL("k_types_to_c");
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    if (h) return fail(PT_ERR_ARG, "tracer types must be 0 or 1 (ntype = 1)");
+    return 0;
+}
+int c_to_types(Engine& E, const double* c, int32_t* dev_types) {
+    PT_COUNT(), k_c_to_types<<<nblk(E.ntr, 256), 256, 0, E.st>>>(c, dev_types, E.ntr);
+    CKL("k_c_to_types");
+    return 0;
 }
 
 // ---------------------------------------------------------------- projection, mixed precision
@@ -592,12 +657,18 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
             CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
             PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(W.tcell, n, W.cstart, cursor, W.clist);
             PT_COUNT(), k_sort_cells<<<nblk(ncell, 128), 128, 0, E.st>>>(W.clist, W.cstart, W.ccount, ncell);
-            PT_COUNT(), k_cell_partials<<<nblk(ncell, 128), 128, 0, E.st>>>(r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount,
-                                                                            ncell, W.cpart, E.cfg.comp);
-            PT_COUNT(), k_node_sums<<<grid, 128, 0, E.st>>>(W.cpart, W.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1,
-                                                            E.cfg.comp);
+            const bool og = E.cfg.discrete_types != 0;
+            PT_COUNT(), (og ? k_cell_partials<true> : k_cell_partials<false>)<<<nblk(ncell, 128), 128, 0, E.st>>>(
+                r, s, Tt, E.Ctr, W.clist, W.cstart, W.ccount, ncell, W.cpart, E.cfg.comp);
+            PT_COUNT(), (og ? k_node_sums<true> : k_node_sums<false>)<<<grid, 128, 0, E.st>>>(
+                W.cpart, W.ccount, ncell, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
         }
         CKL("projection");
+        if (E.cfg.discrete_types && E.count1) {  // count_type(1, :, :) of the same projection
+            CK(cudaMemsetAsync(E.count1, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+            PT_COUNT(), k_count_type1<<<nblk(n, 256), 256, 0, E.st>>>(r, s, E.Ctr, n, E.count1);
+            CKL("k_count_type1");
+        }
     }
     int herr = 0;
     unsigned long long hruns = 0;

@@ -20,8 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libptgpu.so")
 HEADER = os.path.join(HERE, "..", "include", "ptgpu.h")
 
-F_T, F_TRATIO, F_TVIS, F_TBUOY, F_CNEW, F_CVIS, F_CBUOY, F_SF, F_U, F_W, F_VIS, F_NEMPTY, F_RHS = range(13)
-F_TRACER_R, F_TRACER_S, F_TRACER_T, F_TRACER_C = 20, 21, 22, 23
+F_T, F_TRATIO, F_TVIS, F_TBUOY, F_CNEW, F_CVIS, F_CBUOY, F_SF, F_U, F_W, F_VIS, F_NEMPTY, F_RHS, F_COUNT_TYPE = range(14)
+F_TRACER_R, F_TRACER_S, F_TRACER_T, F_TRACER_C, F_TRACER_TYPE = 20, 21, 22, 23, 24
 
 ERRORS = {-1: "PT_ERR_CONFIG", -2: "PT_ERR_TRACER_OUT_OF_DOMAIN", -3: "PT_ERR_MG_DIVERGED",
           -4: "PT_ERR_MG_MAX_CYCLES", -5: "PT_ERR_SINGULAR_COARSE", -6: "PT_ERR_CUDA", -7: "PT_ERR_STATE",
@@ -81,8 +81,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_field_extent.argtypes = [i32] + [ctypes.POINTER(ctypes.c_int32)] * 5
     L.pt_set_field.argtypes = [i32, vp]
     L.pt_get_field.argtypes = [i32, vp]
-    L.pt_upload_state.argtypes = [vp] * 9
-    L.pt_download_state.argtypes = [vp] * 7
+    L.pt_upload_state.argtypes = [vp] * 10
+    L.pt_download_state.argtypes = [vp] * 8
     L.pt_solve_psi.argtypes = [ctypes.POINTER(SolveInfo)]
     L.pt_step.argtypes = [ctypes.POINTER(f64), ctypes.POINTER(SolveInfo)]
     L.pt_stats.argtypes = [ctypes.POINTER(StatsRow)]
@@ -129,20 +129,25 @@ class Engine:
     def get(self, field: int) -> np.ndarray:
         lox, hix, loz, hiz, eb = self.extent(field)
         if field >= F_TRACER_R:
-            out = np.empty(hix, dtype=np.float64)
+            out = np.empty(hix, dtype=np.int32 if eb == 4 else np.float64)
         else:
             out = np.empty((hiz - loz + 1, hix - lox + 1), dtype=np.int32 if eb == 4 else np.float64)
         self._check(self.L.pt_get_field(field, _ptr(out)))
         return out
 
     def set(self, field: int, arr: np.ndarray):
-        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        arr = np.ascontiguousarray(arr, dtype=np.int32 if field == F_TRACER_TYPE else np.float64)
         self._check(self.L.pt_set_field(field, _ptr(arr)))
 
     def upload(self, st: dict):
+        """Restart upload; st holds the restart arrays, and "Ttype" (int32 0/1) for an engine with
+        discrete tracer types (its "Ctr" is then ignored)."""
         arrs = [np.ascontiguousarray(st[k], dtype=np.float64)
                 for k in ("xg", "zg", "T", "Cnew", "SF", "rtr", "str", "Ctr", "Ttr")]
-        self._check(self.L.pt_upload_state(*[_ptr(a) for a in arrs]))
+        ty = None
+        if self.cfg.discrete_types:
+            ty = np.ascontiguousarray(st["Ttype"], dtype=np.int32)
+        self._check(self.L.pt_upload_state(*[_ptr(a) for a in arrs], None if ty is None else _ptr(ty)))
 
     def solve_psi(self) -> dict:
         info = SolveInfo()

@@ -83,7 +83,7 @@ def test_stats_t0_without_psi(golden, engine_t0):
     ref = golden["stats"][0]
     for k in ("empty_cells", "tracer_min", "tracer_max"):
         assert st[k] == ref[k], k
-    for k in ("time", "Tavg", "Nu", "Nu_bot", "RaT_avg", "q1", "q2", "q3", "q4", "Cavg", "entrainment"):
+    for k in ("time", "Tavg", "Nu", "Nu_bot", "q1", "q2", "q3", "q4", "Cavg", "entrainment"):
         assert st[k] == pytest.approx(ref[k], rel=2e-14, abs=1e-15), k
 
 
@@ -93,6 +93,7 @@ def test_stats_t0_through_psi_solve(golden, engine_t0):
     assert info["resid_ratio"] <= 1e-12
     for k in ("vrms", "mobility", "strain_max"):
         assert st[k] == pytest.approx(ref[k], rel=1e-9), k
+    assert st["RaT_avg"] == pytest.approx(ref["RaT_avg"], rel=2e-14)  # needs the viscosity of the solve
     for k in ("empty_cells", "tracer_min", "tracer_max"):
         assert st[k] == ref[k], k
 
