@@ -94,7 +94,15 @@ static int vis_bcs(Engine& E, double* v, int l, cudaStream_t st) {
     return 0;
 }
 
+// c + a b: fused (fma) for the fast paths, two roundings in the reference's order for the FP64
+// path with reference_rounding (this file is compiled with --fmad=false, so only fma() fuses)
+template <bool FUSED>
+__device__ __forceinline__ double madd(double a, double b, double c) {
+    return FUSED ? fma(a, b, c) : c + a * b;
+}
+
 // viscosity_gradients, second-order stencils (uniform grid)
+template <bool FUSED>
 __global__ void k_vis_grad(VisSet S, Geo g, int l, int full, int ivis) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
     const LevConst& L = cL[l];
@@ -106,16 +114,16 @@ __global__ void k_vis_grad(VisSet S, Geo g, int l, int full, int ivis) {
     }
     const double* v = S.vis;
     double xx = 0.0, zz = 0.0;
-    for (int j = -1; j <= 1; j++) xx = xx + cK.D2so[j + 1] * v[g.at(i + j, k)];
+    for (int j = -1; j <= 1; j++) xx = madd<FUSED>(cK.D2so[j + 1], v[g.at(i + j, k)], xx);
     xx = qdiv(xx, L.dr2, L.idr2);
-    for (int j = -1; j <= 1; j++) zz = zz + cK.D2so[j + 1] * v[g.at(i, k + j)];
+    for (int j = -1; j <= 1; j++) zz = madd<FUSED>(cK.D2so[j + 1], v[g.at(i, k + j)], zz);
     zz = qdiv(zz, L.ds2, L.ids2);
     if (full) {
         double xz = 0.0, x = 0.0, z = 0.0;
         for (int k2 = -1; k2 <= 1; k2++)
-            for (int i2 = -1; i2 <= 1; i2++) xz = xz + cK.Drsso[i2 + 1][k2 + 1] * v[g.at(i + i2, k + k2)];
-        for (int j = -1; j <= 1; j++) x = x + cK.D1so[j + 1] * v[g.at(i + j, k)];
-        for (int j = -1; j <= 1; j++) z = z + cK.D1so[j + 1] * v[g.at(i, k + j)];
+            for (int i2 = -1; i2 <= 1; i2++) xz = madd<FUSED>(cK.Drsso[i2 + 1][k2 + 1], v[g.at(i + i2, k + k2)], xz);
+        for (int j = -1; j <= 1; j++) x = madd<FUSED>(cK.D1so[j + 1], v[g.at(i + j, k)], x);
+        for (int j = -1; j <= 1; j++) z = madd<FUSED>(cK.D1so[j + 1], v[g.at(i, k + j)], z);
         S.vxz[o] = qdiv(xz, L.drds, L.idrds);
         S.vx[o] = qdiv(x, L.dr, L.idr);
         S.vz[o] = qdiv(z, L.ds, L.ids);
@@ -129,8 +137,9 @@ __global__ void k_vis_grad(VisSet S, Geo g, int l, int full, int ivis) {
 
 // test_eigenvalues (RKC1 branch): ratio, local pseudo-time step, min ratio
 // FEW (mixed precision): the pseudo-time step with two divisions instead of four, by the
-// reciprocals of ae and be (the step feeds an FP32 smoother there); the ratio keeps its division
-template <bool FEW>
+// reciprocals of ae and be (the step feeds an FP32 smoother there); the ratio keeps its division.
+// FUSED: the sums as fused multiply-adds (not with reference_rounding).
+template <bool FEW, bool FUSED>
 __global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double ctemp, unsigned long long* rmin) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
     const LevConst& L = cL[l];
@@ -138,13 +147,16 @@ __global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double 
     if (i <= L.nx - 1) {
         size_t o = g.at(i, k);
         double vg = S.vis[o];
-        double eI = fabs(S.vxxpzz[o] * L.SI1) + vg * L.SI2 + fabs(S.vxz[o] * L.SI4) + fabs(S.vx[o] * L.SI5) +
+        double eI = madd<FUSED>(vg, L.SI2, fabs(S.vxxpzz[o] * L.SI1)) + fabs(S.vxz[o] * L.SI4) + fabs(S.vx[o] * L.SI5) +
                     fabs(S.vz[o] * L.SI6);
-        double eR = S.vxxmzz[o] * L.SR1 + vg * L.SR2 + S.vxz[o] * L.SR4 + S.vx[o] * L.SR5 + S.vz[o] * L.SR6;
+        double eR = madd<FUSED>(vg, L.SR2, S.vxxmzz[o] * L.SR1);
+        eR = madd<FUSED>(S.vxz[o], L.SR4, eR);
+        eR = madd<FUSED>(S.vx[o], L.SR5, eR);
+        eR = madd<FUSED>(S.vz[o], L.SR6, eR);
         ratio = fabs(eR / eI);
         S.ratio[o] = ratio;
         const double a = FEW ? eR * ae : eR / ae, b = FEW ? eI * be : eI / be;  // FEW: ae, be are 1/ae, 1/be
-        S.dtst[o] = ctemp * eR / (a * a + b * b);
+        S.dtst[o] = ctemp * eR / madd<FUSED>(a, a, b * b);
     }
     double m = fmin(ratio, 1.0e100);
     for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
@@ -156,12 +168,13 @@ __global__ void k_test_eig(VisSet S, Geo g, int l, double ae, double be, double 
 // phase copies from the row ghost of the mirrored column, which still holds what the previous
 // call wrote there: the mirrored node's value before this update.  (The first call of a smoothing
 // pass is a plain vis_bcs, so that previous call always exists.)
+template <bool FUSED>
 __global__ void k_vis_update_bc(double* v, const double* vsm, Geo g, int nx, int nz, double c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
     if (i > nx) return;
     const size_t o = g.at(i, k);
     const double old = v[o];
-    const double nv = old + c * vsm[o];
+    const double nv = madd<FUSED>(c, vsm[o], old);
     v[o] = nv;
     int xs[2], zs[2], nxm = 0, nzm = 0;
     if (i >= 1 && i <= 3) xs[nxm++] = -i;
@@ -194,10 +207,12 @@ static int smoother_vis(Engine& E, const VisCtx& C, int l, int interpolate, VisS
     const double stab = coarse_smoother ? E.RKC1_stability_c : E.RKC1_stability;
     const double ae = -stab / 2.0, be = (double)(coarse_smoother ? E.nstageC : E.cfg.nstageS);
     const double ctemp = E.cfg.courant_stream * (stab / (ae * ae));
+    const bool fused = !E.cfg.reference_rounding;
     dim3 gg(nblk(nx + 1, 128), nz + 1);
     for (int guard = 0; guard < 100000; guard++) {
         for (int nn = nn_store; nn <= Niter; nn++) {
-            PT_COUNT(), k_vis_grad<<<gg, 128, 0, C.st>>>(S, g, l, Nvis_store != 0, ivis);
+            PT_COUNT(), (fused ? k_vis_grad<true> : k_vis_grad<false>)<<<gg, 128, 0, C.st>>>(S, g, l, Nvis_store != 0,
+                                                                                        ivis);
             CKL("k_vis_grad");
             if (interpolate == 0 && (Nvis_store >= 1 || ivis == 0)) {
                 unsigned long long* d = (unsigned long long*)C.dscal;
@@ -205,9 +220,11 @@ static int smoother_vis(Engine& E, const VisCtx& C, int l, int interpolate, VisS
                 CK(cudaMemcpyAsync(d, &init, 8, cudaMemcpyHostToDevice, C.st));
                 dim3 ge(nblk(nx - 1, 128), nz - 1);
                 if (E.cfg.precision == PT_PREC_MIXED)
-                    PT_COUNT(), k_test_eig<true><<<ge, 128, 0, C.st>>>(S, g, l, 1.0 / ae, 1.0 / be, ctemp, d);
+                    PT_COUNT(), k_test_eig<true, true><<<ge, 128, 0, C.st>>>(S, g, l, 1.0 / ae, 1.0 / be, ctemp, d);
+                else if (fused)
+                    PT_COUNT(), k_test_eig<false, true><<<ge, 128, 0, C.st>>>(S, g, l, ae, be, ctemp, d);
                 else
-                    PT_COUNT(), k_test_eig<false><<<ge, 128, 0, C.st>>>(S, g, l, ae, be, ctemp, d);
+                    PT_COUNT(), k_test_eig<false, false><<<ge, 128, 0, C.st>>>(S, g, l, ae, be, ctemp, d);
                 CKL("k_test_eig");
                 CK(cudaMemcpyAsync(C.hscal, d, 8, cudaMemcpyDeviceToHost, C.st));
                 CK(cudaStreamSynchronize(C.st));
@@ -228,7 +245,8 @@ static int smoother_vis(Engine& E, const VisCtx& C, int l, int interpolate, VisS
             int ntemp = Niter - nn + 1;
             double c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
             c = 0.99 * c;
-            PT_COUNT(), k_vis_update_bc<<<gg, 128, 0, C.st>>>(S.vis, S.vsm, g, nx, nz, c);
+            PT_COUNT(), (fused ? k_vis_update_bc<true> : k_vis_update_bc<false>)<<<gg, 128, 0, C.st>>>(S.vis, S.vsm, g, nx,
+                                                                                                  nz, c);
             CKL("k_vis_update_bc");
         }
         if (trigger) return 0;
