@@ -121,6 +121,11 @@ typedef struct pt_config {
                               iterative_solver.f90:890-1073; DGBTRS substitutions), no fused
                               multiply-adds, so that results follow the CPU reference to its own
                               rounding over many steps; slower */
+    int32_t direct;        /* &inputs iterate=0: the psi solve is the direct banded solve of
+                              build_SF_matrix/solve_SF_equation (momentum.f90:319-653): assembly,
+                              row equilibration and band LU once (the operator of an isoviscous run
+                              does not change), then per solve the banded substitutions.  FP64,
+                              ivis=0 only.  0: multigrid (iterate=1, MG=1) */
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

@@ -74,6 +74,7 @@ class PtConfig(ctypes.Structure):
         ("nstageC", ctypes.c_int32),
         ("discrete_types", ctypes.c_int32),
         ("reference_rounding", ctypes.c_int32),
+        ("direct", ctypes.c_int32),
     ]
 
     @staticmethod
@@ -156,6 +157,7 @@ class PtConfig(ctypes.Structure):
         c.precision = int(gpu.get("precision", c.precision))
         c.guess_mode = int(gpu.get("guess_mode", c.guess_mode))
         c.discrete_types = 1 if int(inp.get("ic_continuous", 1)) == 0 else 0
+        c.direct = 1 if int(inp.get("iterate", 1)) == 0 else 0
         c.mg_scheme = int(gpu.get("mg_scheme", PT_MG_REFERENCE))
         c.mg_cycle = int(gpu.get("mg_cycle", PT_CYCLE_REFERENCE))
         tpc = int(inp.get("tpc", 0))

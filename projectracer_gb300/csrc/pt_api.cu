@@ -176,11 +176,13 @@ static int engine_alloc(Engine& E) {
     }
     if ((rc = mg_alloc(E))) return rc;
     if (E.cfg.precision == PT_PREC_MIXED && (rc = mixed_alloc(E))) return rc;
+    if (E.cfg.direct && (rc = direct_alloc(E))) return rc;
     return 0;
 }
 
 static void engine_free(Engine& E) {
     unet_engine_release(E);
+    direct_free(E);
     if (E.psi_a) cudaFree(E.psi_a);
     if (E.psi_b) cudaFree(E.psi_b);
     double** fine[] = {&E.T, &E.Tratio, &E.Tvis, &E.Tbuoy, &E.Cnew, &E.Cvis, &E.Cbuoy, &E.SF, &E.u, &E.w,
@@ -347,6 +349,10 @@ int pt_init(const pt_config* cfg) {
         return fail(PT_ERR_CONFIG, "precision must be PT_PREC_FP64 or PT_PREC_MIXED");
     }
     if ((int64_t)cfg->ntr > 2000000000LL) { delete E; return fail(PT_ERR_CONFIG, "ntr above 2e9 is not supported"); }
+    if (cfg->direct != 0 && (cfg->direct != 1 || cfg->precision != PT_PREC_FP64 || cfg->ivis != 0)) {
+        delete E;
+        return fail(PT_ERR_CONFIG, "direct = 1 (banded direct solve) runs in PT_PREC_FP64 with ivis = 0");
+    }
     if (cfg->reference_rounding != 0 && (cfg->reference_rounding != 1 || cfg->precision != PT_PREC_FP64)) {
         delete E;
         return fail(PT_ERR_CONFIG, "reference_rounding = 1 applies to PT_PREC_FP64 only");
@@ -589,7 +595,8 @@ static int solve_psi(Engine& E, pt_solve_info* info) {
     cudaEventRecord(a, E.st);
     if (E.cfg.guess_mode == PT_GUESS_ZERO) CK(cudaMemsetAsync(E.SF, 0, E.g1.elems() * 8, E.st));
     if (E.cfg.guess_mode == PT_GUESS_EXTRAPOLATE && (rc = extrapolated_guess(E))) return rc;
-    rc = (E.cfg.precision == PT_PREC_MIXED) ? multigrid_mixed(E, info) : multigrid(E, info);
+    rc = E.cfg.direct ? direct_solve(E, info)
+                      : (E.cfg.precision == PT_PREC_MIXED) ? multigrid_mixed(E, info) : multigrid(E, info);
     if (!rc && E.cfg.guess_mode == PT_GUESS_EXTRAPOLATE) rc = record_psi(E);
     if (!rc) rc = compute_velocities(E);
     cudaEventRecord(b, E.st);

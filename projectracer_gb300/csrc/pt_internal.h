@@ -104,6 +104,13 @@ struct Engine {
     double* coef[3] = {};    // 16 Taylor coefficients per node per field (advection)
     int32_t* nempty = nullptr;
     int32_t* count1 = nullptr;  // discrete types: count_type(1, 0:nx, 0:nz) of the last projection
+    // direct banded solve (cfg.direct, pt_direct.cu): band matrix and LU, row factors, right-hand
+    // side, pivots, the LU kernel's barrier state and error words
+    int dn = 0, dkl = 0, dku = 0, dchunk = 0;
+    double *dMB = nullptr, *dRow = nullptr, *dB = nullptr;
+    int *dipiv = nullptr, *dluerr = nullptr;
+    void* dlu = nullptr;
+    bool direct_ready = false;
     // multigrid
     double *err[PT_MAXLEV] = {}, *S0[PT_MAXLEV] = {}, *S1[PT_MAXLEV] = {}, *S2[PT_MAXLEV] = {},
            *RHS[PT_MAXLEV] = {}, *res[PT_MAXLEV] = {}, *dtst[PT_MAXLEV] = {}, *ratio[PT_MAXLEV] = {},
@@ -297,6 +304,11 @@ int rk_stage(Engine& E, int stage);                   // energy.f90:258-536 trac
 // discrete tracer types: int32 0/1 on the device <-> the type as 0.0 / 1.0 in a composition array
 int types_to_c(Engine& E, const int32_t* dev_types, double* c);
 int c_to_types(Engine& E, const double* c, int32_t* dev_types);
+
+// direct banded solve (pt_direct.cu)
+int direct_alloc(Engine& E);
+void direct_free(Engine& E);
+int direct_solve(Engine& E, pt_solve_info* info);  // momentum.f90:258-317, 636-653
 
 // multigrid (pt_mg.cu)
 bool trace_on();  // PTGPU_TRACE set in the environment

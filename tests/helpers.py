@@ -63,3 +63,28 @@ def walls(cfg, st):
     r[-3:], s[-2:] = cfg.aspect, 1.0
     st["rtr"], st["str"] = r, s
     return st
+
+
+def golden_t0(golden: dict, direct: int = 0):
+    """The reference's shipped run (100x100, 612,060 tracers) at t=0, rebuilt by the oracle's
+    restatement of its start-up: (cfg, restart arrays, start-up fields by field id, oracle).
+    direct=1 keeps the run's own psi solver (iterate=0, the banded direct solve); direct=0 uses
+    multigrid at a relative residual of 1e-12."""
+    from oracle.ptref import Oracle
+    from projectracer_gb300 import engine as eng
+    from projectracer_gb300.inputs import grid_coords
+
+    cfg = PtConfig.from_groups(golden["namelist"])
+    cfg.iheattype = 0  # interior H is never evaluated before the first stats row
+    cfg.direct = direct
+    cfg.tolerance = 1e-12
+    inp = golden["namelist"]["inputs"]
+    o = Oracle(cfg, iterate=0 if direct else 1, nparts=golden["stdout"]["Nthreads"])
+    o.init_reference(int(inp["tpc"]), golden["stdout"]["Nthreads"], float(inp["klayer"]), float(inp["dlayer"]), 1)
+    cfg.Tbot_iso, cfg.Ttop_iso = o.scalar("Tbot_iso"), o.scalar("Ttop_iso")  # set by initial_temperature
+    xg, zg = grid_coords(cfg)
+    st = dict(xg=xg, zg=zg, T=o.get(0), Cnew=o.get(4), SF=o.get(7), rtr=o.get(20), str=o.get(21), Ttr=o.get(22),
+              Ctr=o.get(23))
+    start = {eng.F_T: o.get(0), eng.F_TVIS: o.get(2), eng.F_TBUOY: o.get(3), eng.F_CVIS: o.get(5),
+             eng.F_CBUOY: o.get(6)}
+    return cfg, st, start, o

@@ -28,8 +28,8 @@ def test_library_exports_all_declared_symbols(lib):
 
 
 def test_config_struct_layout_matches_header():
-    # pt_config: 16 int32, one int64, 24 doubles, 6 int32 (no padding on LP64)
-    assert ctypes.sizeof(PtConfig) == 16 * 4 + 8 + 24 * 8 + 6 * 4
+    # pt_config: 16 int32, one int64, 24 doubles, 7 int32, padded to the 8-byte alignment (LP64)
+    assert ctypes.sizeof(PtConfig) == 16 * 4 + 8 + 24 * 8 + 7 * 4 + 4
     assert PtConfig.discrete_types.offset == 16 * 4 + 8 + 24 * 8 + 4 * 4
     assert PtConfig.reference_rounding.offset == 16 * 4 + 8 + 24 * 8 + 5 * 4
 

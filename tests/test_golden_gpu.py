@@ -11,7 +11,8 @@ main.f90:204-210), so the start-up's T, T_vis, T_buoy, C_vis and C_buoy are then
 pt_set_field, as a driver that starts fresh would.  The engine then solves for psi and computes
 the velocities and the statistics.
 
-The grid spacing 0.01 is not a power of two, so these cases run the general branches of the
+These cases solve for psi by multigrid; tests/test_direct_gpu.py runs the shipped run's own direct
+banded solve.  The grid spacing 0.01 is not a power of two, so these cases run the general branches of the
 projection and the RK stage (cell index by llround(x/h), the FP64 division in the shape
 functions, floor(x/h) in the fixed-point projection) that the power-of-two test grids skip.
 
@@ -30,8 +31,8 @@ import pytest
 
 from oracle.ptref import Oracle
 from projectracer_gb300 import engine as eng
-from projectracer_gb300.config import PT_PREC_MIXED, PtConfig
-from projectracer_gb300.inputs import grid_coords
+from projectracer_gb300.config import PT_PREC_MIXED
+from tests.helpers import golden_t0
 
 pytestmark = pytest.mark.gpu
 
@@ -40,18 +41,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 @pytest.fixture(scope="module")
 def golden_state(golden):
-    cfg = PtConfig.from_groups(golden["namelist"])
-    cfg.iheattype = 0  # interior H is never evaluated before the first stats row
-    cfg.tolerance = 1e-12
-    inp = golden["namelist"]["inputs"]
-    o = Oracle(cfg, iterate=1, nparts=golden["stdout"]["Nthreads"])
-    o.init_reference(int(inp["tpc"]), golden["stdout"]["Nthreads"], float(inp["klayer"]), float(inp["dlayer"]), 1)
-    cfg.Tbot_iso, cfg.Ttop_iso = o.scalar("Tbot_iso"), o.scalar("Ttop_iso")  # set by initial_temperature
-    xg, zg = grid_coords(cfg)
-    st = dict(xg=xg, zg=zg, T=o.get(0), Cnew=o.get(4), SF=o.get(7), rtr=o.get(20), str=o.get(21), Ttr=o.get(22),
-              Ctr=o.get(23))
-    start = {eng.F_T: o.get(0), eng.F_TVIS: o.get(2), eng.F_TBUOY: o.get(3), eng.F_CVIS: o.get(5),
-             eng.F_CBUOY: o.get(6)}
+    cfg, st, start, _ = golden_t0(golden, direct=0)
     return cfg, st, start
 
 
