@@ -126,6 +126,12 @@ typedef struct pt_config {
                               row equilibration and band LU once (the operator of an isoviscous run
                               does not change), then per solve the banded substitutions.  FP64,
                               ivis=0 only.  0: multigrid (iterate=1, MG=1) */
+    int32_t chebyshev;     /* &inputs Chebyshev=1: the energy step is the nstage-stage RKC2 Chebyshev
+                              method of energy_time_Chebyshev (Chebyshev.f90:113-243) with the RK2
+                              time step (torder=2, energy.f90:787-793); 0: RK4 (energy_time).  FP64
+                              precision only */
+    int32_t nstage;        /* RKC2 stages (2..60) */
+    double damping, aRK2;  /* RKC2 damping and the free parameter b1 = aRK2/omega1 (Chebyshev.f90:55) */
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

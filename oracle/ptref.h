@@ -63,6 +63,9 @@ typedef struct ptref_state {
     double SM1[7][7], SM2[7][7], SM4[7][7], SM5[7][7], SM6[7][7]; /* [di+3][dk+3] */
     /* RKC1 coefficients (Chebyshev.f90:182-210) */
     double mewtS[64], mewS[64], vS[64], cS[64], bS[64];
+    /* RKC2 energy stepper (Chebyshev_prep, Chebyshev.f90:38-80) */
+    double cCheb[64], mewCheb[64], vCheb[64], mewtCheb[64], gtCheb[64];
+    double* u0; double* w0; double* dT0; /* stage-1 slopes (1:ntr) */
     double RKC1_stability;
     double delta_T, delta_C;
     int kl, ku, ngrid_coarse;

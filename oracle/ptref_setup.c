@@ -219,6 +219,37 @@ static void derivative_eigenvalues(ptref_state* s) {
 }
 
 /* Chebyshev_prep_stream, Chebyshev.f90:182-210 (with Chebyshev_coefficients_stream 120-134). */
+/* Chebyshev_prep (Chebyshev.f90:38-80) with Chebyshev_coefficients (1-18): the RKC2 coefficients
+ * of the nstage-stage energy stepper; TCheb_x(j)**2 as TCheb_x(j)*TCheb_x(j) */
+static void chebyshev_prep(ptref_state* s) {
+    int N = s->cfg.nstage;
+    double T[64], Tx[64], Txx[64], b[64], a[64];
+    double w0 = 1.0 + s->cfg.damping / (double)(N * N);
+    T[0] = 1.0; T[1] = w0; Tx[0] = 0.0; Tx[1] = 1.0; Txx[0] = 0.0; Txx[1] = 0.0;
+    for (int j = 2; j <= N; j++) {
+        T[j] = 2.0 * w0 * T[j - 1] - T[j - 2];
+        Tx[j] = 2.0 * T[j - 1] + 2.0 * w0 * Tx[j - 1] - Tx[j - 2];
+        Txx[j] = 4.0 * Tx[j - 1] + 2.0 * w0 * Txx[j - 1] - Txx[j - 2];
+    }
+    double w1 = Tx[N] / Txx[N];
+    for (int j = 2; j <= N; j++) b[j] = Txx[j] / (Tx[j] * Tx[j]);
+    b[0] = -b[2];
+    b[1] = s->cfg.aRK2 / w1;
+    a[0] = 1.0 - b[0];
+    a[1] = 1.0 - b[1] * w0;
+    for (int j = 2; j <= N; j++) a[j] = 1.0 - b[j] * T[j];
+    s->mewtCheb[1] = b[1] * w1;
+    for (int j = 2; j <= N; j++) {
+        s->mewCheb[j] = 2.0 * b[j] * w0 / b[j - 1];
+        s->vCheb[j] = -b[j] / b[j - 2];
+        s->cCheb[j] = 1.0 - s->mewCheb[j] - s->vCheb[j];
+    }
+    for (int j = 2; j <= N; j++) {
+        s->mewtCheb[j] = 2.0 * b[j] * w1 / b[j - 1];
+        s->gtCheb[j] = -a[j - 1] * s->mewtCheb[j];
+    }
+}
+
 static void chebyshev_prep_stream(ptref_state* s) {
     int N = s->cfg.nstageS;
     double T[64], Tx[64];
@@ -511,6 +542,16 @@ ptref_state* ptref_create(const pt_config* cfg, int iterate, int nparts) {
     double** tr[] = {&s->rtr, &s->str, &s->Ttr, &s->Ctr, &s->rtr0, &s->str0, &s->Ttr0, &s->rtr1,
                      &s->str1, &s->Ttr1, &s->rtr2, &s->str2, &s->Ttr2};
     for (size_t i = 0; i < sizeof tr / sizeof tr[0]; i++) *tr[i] = (double*)calloc(nt, sizeof(double));
+    if (cfg->chebyshev) { /* RKC2 energy stepper: coefficients and the stage-1 slopes */
+        if (cfg->nstage < 2 || cfg->nstage > 60) {
+            ref_fail(s, PT_ERR_CONFIG, "nstage must be 2..60");
+        } else {
+            chebyshev_prep(s);
+            s->u0 = (double*)calloc(nt, sizeof(double));
+            s->w0 = (double*)calloc(nt, sizeof(double));
+            s->dT0 = (double*)calloc(nt, sizeof(double));
+        }
+    }
     /* uniform grid, grid.f90:46-54 and 105-116 */
     double* xg = s->xg + 6;
     double* zg = s->zg + 6;

@@ -559,7 +559,16 @@ static double stability_RK4(ptref_state* s) {
                 if (eA > eigA_max) eigA_max = eA;
                 if (eD > eigD_max) eigD_max = eD;
             }
-        double dtA = 2.8 / eigA_max, dtD = 2.8 / eigD_max;
+        double dtA, dtD;
+        if (s->cfg.chebyshev) { /* torder=2 (energy.f90:787-793), required by the RKC2 stepper */
+            if (eigA_max >= eigD_max)
+                return ref_fail(s, PT_ERR_CONFIG, "Advective Eigenvalues Exceed Diffusive Eigenvalues -- this does not work for RK2"), 0.0;
+            dtA = 1.0 / eigA_max;
+            dtD = 2.0 / eigD_max;
+        } else {
+            dtA = 2.8 / eigA_max;
+            dtD = 2.8 / eigD_max;
+        }
         dt = (eigA_max == 0.0) ? dtD : 1.0 / (1.0 / dtA + 1.0 / dtD);
         dt = s->cfg.courant * dt;
         if (s->cfg.CFL == 1 && 2.0 / eigD_max < dt) dt = 2.0 / eigD_max;
@@ -621,8 +630,87 @@ static int update_velocities(ptref_state* s) {
     return 0;
 }
 
+/* energy_time_Chebyshev, Chebyshev.f90:113-243 (tracer=1, RK_update=1, equalize=0, uniform grid) */
+static int step_chebyshev(ptref_state* s) {
+    int nx = s->nx, nz = s->nz;
+    int64_t ntr = s->ntr;
+    int comp = s->cfg.comp, N = s->cfg.nstage;
+    if (!s->u0) return ref_fail(s, PT_ERR_STATE, "RKC2 stepper not set up (chebyshev=1 at create)");
+    double dt = stability_RK4(s);
+    if (s->status) return s->status;
+    s->dt = dt;
+    rfld C0 = ref_fld_alloc(nx, nz, 5);
+    rfld T0 = ref_fld_alloc(nx, nz, 3);
+    if (comp) copy_fld(&C0, &s->Cnew);
+    copy_fld(&T0, &s->Tratio);
+    size_t nb = sizeof(double) * (size_t)ntr;
+    memcpy(s->Ttr0, s->Ttr, nb);
+    memcpy(s->rtr0, s->rtr, nb);
+    memcpy(s->str0, s->str, nb);
+    int rc = 0;
+    /* stage 1 */
+    load_tracer_space(s);
+    compute_derivatives(s, &s->tsa, s->DERr_t);
+    compute_derivatives(s, &s->u, s->DERr_u);
+    compute_derivatives(s, &s->w, s->DERr_w);
+    double dtstage = s->mewtCheb[1] * dt;
+#pragma omp parallel for
+    for (int64_t id = 0; id < ntr; id++) {
+        double tr = interpolate(s, s->rtr0[id], s->str0[id], s->DERr_u, &s->u);
+        double ts = interpolate(s, s->rtr0[id], s->str0[id], s->DERr_w, &s->w);
+        double tT = interpolate(s, s->rtr0[id], s->str0[id], s->DERr_t, &s->tsa);
+        s->u0[id] = tr;
+        s->w0[id] = ts;
+        s->dT0[id] = tT;
+        s->rtr1[id] = s->rtr0[id] + dtstage * tr;
+        s->str1[id] = s->str0[id] + dtstage * ts;
+        s->Ttr1[id] = s->Ttr0[id] + dtstage * tT;
+        s->rtr2[id] = s->rtr0[id];
+        s->str2[id] = s->str0[id];
+        s->Ttr2[id] = s->Ttr0[id];
+    }
+    /* stages 2..nstage */
+    for (int j = 2; j <= N; j++) {
+        if (comp) copy_fld(&s->Cnew, &C0);
+        if ((rc = ref_project(s, s->rtr1, s->str1, s->Ttr1, &T0, 1))) goto done;
+        load_tracer_space(s);
+        compute_derivatives(s, &s->tsa, s->DERr_t);
+        if ((rc = update_velocities(s))) goto done;
+        compute_derivatives(s, &s->u, s->DERr_u);
+        compute_derivatives(s, &s->w, s->DERr_w);
+        dtstage = s->mewtCheb[j] * dt;
+        double dtstage2 = s->gtCheb[j] * dt;
+        double cj = s->cCheb[j], mj = s->mewCheb[j], vj = s->vCheb[j];
+#pragma omp parallel for
+        for (int64_t id = 0; id < ntr; id++) {
+            double tr = interpolate(s, s->rtr1[id], s->str1[id], s->DERr_u, &s->u);
+            double ts = interpolate(s, s->rtr1[id], s->str1[id], s->DERr_w, &s->w);
+            double tT = interpolate(s, s->rtr1[id], s->str1[id], s->DERr_t, &s->tsa);
+            s->rtr[id] = cj * s->rtr0[id] + mj * s->rtr1[id] + vj * s->rtr2[id] + dtstage * tr + dtstage2 * s->u0[id];
+            s->str[id] = cj * s->str0[id] + mj * s->str1[id] + vj * s->str2[id] + dtstage * ts + dtstage2 * s->w0[id];
+            s->Ttr[id] = cj * s->Ttr0[id] + mj * s->Ttr1[id] + vj * s->Ttr2[id] + dtstage * tT + dtstage2 * s->dT0[id];
+            s->rtr2[id] = s->rtr1[id];
+            s->str2[id] = s->str1[id];
+            s->Ttr2[id] = s->Ttr1[id];
+            s->rtr1[id] = s->rtr[id];
+            s->str1[id] = s->str[id];
+            s->Ttr1[id] = s->Ttr[id];
+        }
+    }
+    /* wrap-up */
+    if (comp) copy_fld(&s->Cnew, &C0);
+    if ((rc = ref_project(s, s->rtr, s->str, s->Ttr, &T0, 1))) goto done;
+    copy_fld(&s->T, &s->Tratio);
+    s->time = s->time + dt;
+done:
+    free(C0.p);
+    free(T0.p);
+    return rc;
+}
+
 /* energy_time, energy.f90:181-556 (tracer=1, torder=4, RK_update=1, local_time=0) */
 int ptref_step(ptref_state* s) {
+    if (s->cfg.chebyshev) return step_chebyshev(s);
     int nx = s->nx, nz = s->nz;
     int64_t ntr = s->ntr;
     int comp = s->cfg.comp;

@@ -75,6 +75,10 @@ class PtConfig(ctypes.Structure):
         ("discrete_types", ctypes.c_int32),
         ("reference_rounding", ctypes.c_int32),
         ("direct", ctypes.c_int32),
+        ("chebyshev", ctypes.c_int32),
+        ("nstage", ctypes.c_int32),
+        ("damping", ctypes.c_double),
+        ("aRK2", ctypes.c_double),
     ]
 
     @staticmethod
@@ -120,6 +124,9 @@ class PtConfig(ctypes.Structure):
         c.Ttop_iso = 0.0
         c.dent = 0.5
         c.mg_scheme = PT_MG_REFERENCE
+        c.nstage = 3
+        c.damping = 100.0
+        c.aRK2 = 0.5
         return c
 
     @staticmethod
@@ -134,6 +141,12 @@ class PtConfig(ctypes.Structure):
                     "nstageS", "comp", "Tbot", "Vbc", "CFL"):
             if key.lower() in inp:
                 setattr(c, key, int(inp[key.lower()]))
+        for key in ("nstage", "chebyshev"):
+            if key in inp:
+                setattr(c, key, int(inp[key]))
+        for key in ("damping", "aRK2"):
+            if key.lower() in inp:
+                setattr(c, key, float(inp[key.lower()]))
         for key in ("aspect", "tolerance", "eig_ratio", "dampingS", "c_2", "c_1", "courant",
                     "courantT", "courantC", "courant_stream", "dent"):
             if key.lower() in inp:

@@ -158,6 +158,9 @@ static int engine_alloc(Engine& E) {
                       &E.rtr1, &E.str1, &E.Ttr1, &E.rtr2, &E.str2, &E.Ttr2};
     for (auto p : trc)
         if ((rc = dalloc(E, p, nt))) return rc;
+    if (E.cfg.chebyshev)
+        for (double** p : {&E.k0r, &E.k0s, &E.k0T})
+            if ((rc = dalloc(E, p, nt))) return rc;
     if ((rc = ialloc(E, &E.tcell, nt))) return rc;
     if ((rc = ialloc(E, &E.clist, nt))) return rc;
     if ((rc = ialloc(E, &E.ccount, (size_t)ncell))) return rc;
@@ -188,7 +191,8 @@ static void engine_free(Engine& E) {
     double** fine[] = {&E.T, &E.Tratio, &E.Tvis, &E.Tbuoy, &E.Cnew, &E.Cvis, &E.Cbuoy, &E.SF, &E.u, &E.w,
                        &E.cond, &E.cond_r, &E.cond_s, &E.tsa, &E.Text, &E.T0, &E.C0, &E.scratch, &E.psi_keep,
                        &E.red, &E.dscal, &E.cpart, &E.rtr, &E.str, &E.Ttr, &E.Ctr, &E.rtr0, &E.str0,
-                       &E.Ttr0, &E.rtr1, &E.str1, &E.Ttr1, &E.rtr2, &E.str2, &E.Ttr2, &E.Mc, &E.Bc, &E.RowB};
+                       &E.Ttr0, &E.rtr1, &E.str1, &E.Ttr1, &E.rtr2, &E.str2, &E.Ttr2, &E.Mc, &E.Bc, &E.RowB,
+                       &E.k0r, &E.k0s, &E.k0T};
     for (auto p : fine)
         if (*p) { cudaFree(*p); *p = nullptr; }
     for (int f = 0; f < 3; f++)
@@ -645,10 +649,45 @@ static int velocity_tables(Engine& E) {
     return tables_to_f32(E, 1, E.w);
 }
 
+// energy_time_Chebyshev (Chebyshev.f90:113-243): stage 1 from the step-start tracers (their slopes
+// kept), stages 2..nstage each after a projection of the previous stage's tracers, a fresh psi
+// (RK_update=1) and new tables; the last stage's tracers are the step's result
+static int step_rkc2(Engine& E, double* dt_out, pt_solve_info* info) {
+    int rc;
+    if ((rc = stability_dt(E, &E.dt))) return rc;
+    const int comp = E.cfg.comp;
+    if (comp && (rc = copy_field(E, E.C0, E.Cnew))) return rc;
+    if ((rc = copy_field(E, E.T0, E.Tratio))) return rc;
+    std::swap(E.rtr0, E.rtr);  // the step-start tracers (the stages write rtr/str/Ttr last)
+    std::swap(E.str0, E.str);
+    std::swap(E.Ttr0, E.Ttr);
+    if ((rc = stage_tables(E)) || (rc = velocity_tables(E)) || (rc = rkc2_stage(E, 1))) return rc;
+    double tstage = E.time + E.mewtCheb[1] * E.dt;
+    for (int j = 2; j <= E.cfg.nstage; j++) {
+        if (comp && (rc = copy_field(E, E.Cnew, E.C0))) return rc;
+        if ((rc = project(E, E.rtr1, E.str1, E.Ttr1, E.T0, 1))) return rc;
+        if ((rc = stage_tables(E))) return rc;
+        E.solve_tau = tstage;
+        if ((rc = solve_psi(E, info))) return rc;
+        if ((rc = velocity_tables(E)) || (rc = rkc2_stage(E, j))) return rc;
+        tstage = E.time + E.mewtCheb[j] * E.dt;
+    }
+    if (comp && (rc = copy_field(E, E.Cnew, E.C0))) return rc;
+    if ((rc = project(E, E.rtr, E.str, E.Ttr, E.T0, 1))) return rc;
+    if ((rc = copy_field(E, E.T, E.Tratio))) return rc;
+    E.time = E.time + E.dt;
+    if (dt_out) *dt_out = E.dt;
+    if (info) info->n_temp = E.n_temp;
+    CK(cudaStreamSynchronize(E.st));
+    harvest_spans(E);
+    return 0;
+}
+
 int pt_step(double* dt_out, pt_solve_info* info) {
     if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
     Engine& E = *g_eng;
     if (info) std::memset(info, 0, sizeof *info);
+    if (E.cfg.chebyshev) return step_rkc2(E, dt_out, info);
     int rc;
     if (E.want_resort && (rc = resort_tracers(E))) return rc;
     if ((rc = stability_dt(E, &E.dt))) return rc;

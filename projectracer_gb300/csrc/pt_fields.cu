@@ -382,6 +382,12 @@ int stability_dt(Engine& E, double* dt) {
     CK(cudaStreamSynchronize(E.st));
     double eA = E.hscal[0], eD = E.hscal[1];
     double dtA = 2.8 / eA, dtD = 2.8 / eD;
+    if (E.cfg.chebyshev) {  // torder=2 (energy.f90:787-793), which the RKC2 stepper requires
+        if (eA >= eD)
+            return fail(PT_ERR_CONFIG, "Advective Eigenvalues Exceed Diffusive Eigenvalues -- this does not work for RK2");
+        dtA = 1.0 / eA;
+        dtD = 2.0 / eD;
+    }
     double v = (eA == 0.0) ? dtD : 1.0 / (1.0 / dtA + 1.0 / dtD);
     *dt = E.cfg.courant * v;
     if (E.cfg.CFL == 1 && 2.0 / eD < *dt) *dt = 2.0 / eD;  // energy.f90:809

@@ -87,6 +87,9 @@ struct Engine {
     // the coarse-level RKC1 smoother of the mixed V-cycle (nstageC stages, same damping)
     int nstageC = 0;
     double RKC1_stability_c = 0, mew_c[64] = {}, vv_c[64] = {}, mewt_c[64] = {};
+    // the RKC2 energy stepper (cfg.chebyshev): coefficients and the stage-1 slopes of each tracer
+    double cCheb[64] = {}, mewCheb[64] = {}, vCheb[64] = {}, mewtCheb[64] = {}, gtCheb[64] = {};
+    double *k0r = nullptr, *k0s = nullptr, *k0T = nullptr;
     double Tr_base = 0, Trr_base = 0, Trrr_base = 0, Trrrr_base = 0, Trs_base = 0, Trrs_base = 0,
            Trrss_base = 0, Tr_base_so = 0, Trr_base_so = 0;
     int kl = 0, ku = 0, ngc = 0, kent = 0;
@@ -301,6 +304,7 @@ int tracer_user_order(Engine& E, double* internal, double* staging, bool to_user
 int project(Engine& E, const double* r, const double* s, const double* Tt, const double* T0f,
             int smooth);                              // composition.f90:923-1087
 int rk_stage(Engine& E, int stage);                   // energy.f90:258-536 tracer loops
+int rkc2_stage(Engine& E, int stage);                 // Chebyshev.f90:151-227 tracer loops
 // discrete tracer types: int32 0/1 on the device <-> the type as 0.0 / 1.0 in a composition array
 int types_to_c(Engine& E, const int32_t* dev_types, double* c);
 int c_to_types(Engine& E, const double* c, int32_t* dev_types);

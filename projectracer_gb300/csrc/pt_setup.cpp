@@ -206,6 +206,38 @@ static void rkc1_coefficients(Engine& E) {
     E.RKC1_stability = -2.0 * w0 / w1;
 }
 
+// RKC2 coefficients of the nstage-stage Chebyshev energy stepper (Chebyshev_prep,
+// Chebyshev.f90:38-80, with the recursions of Chebyshev_coefficients, 1-18); TCheb_x(j)**2 as a
+// product
+static void rkc2_coefficients(Engine& E) {
+    const int N = E.cfg.nstage;
+    double T[64], Tx[64], Txx[64], b[64], a[64];
+    const double w0 = 1.0 + E.cfg.damping / (double)(N * N);
+    T[0] = 1.0; T[1] = w0; Tx[0] = 0.0; Tx[1] = 1.0; Txx[0] = 0.0; Txx[1] = 0.0;
+    for (int j = 2; j <= N; j++) {
+        T[j] = 2.0 * w0 * T[j - 1] - T[j - 2];
+        Tx[j] = 2.0 * T[j - 1] + 2.0 * w0 * Tx[j - 1] - Tx[j - 2];
+        Txx[j] = 4.0 * Tx[j - 1] + 2.0 * w0 * Txx[j - 1] - Txx[j - 2];
+    }
+    const double w1 = Tx[N] / Txx[N];
+    for (int j = 2; j <= N; j++) b[j] = Txx[j] / (Tx[j] * Tx[j]);
+    b[0] = -b[2];
+    b[1] = E.cfg.aRK2 / w1;
+    a[0] = 1.0 - b[0];
+    a[1] = 1.0 - b[1] * w0;
+    for (int j = 2; j <= N; j++) a[j] = 1.0 - b[j] * T[j];
+    E.mewtCheb[1] = b[1] * w1;
+    for (int j = 2; j <= N; j++) {
+        E.mewCheb[j] = 2.0 * b[j] * w0 / b[j - 1];
+        E.vCheb[j] = -b[j] / b[j - 2];
+        E.cCheb[j] = 1.0 - E.mewCheb[j] - E.vCheb[j];
+    }
+    for (int j = 2; j <= N; j++) {
+        E.mewtCheb[j] = 2.0 * b[j] * w1 / b[j - 1];
+        E.gtCheb[j] = -a[j - 1] * E.mewtCheb[j];
+    }
+}
+
 static int choose_levels(Engine& E) {
     int nx = E.cfg.nx, nz = E.cfg.nz, grids = E.cfg.grids;
     const int small = nx < nz ? nx : nz;
@@ -268,6 +300,10 @@ int setup_constants(Engine& E) {
     if (c.comp != 0 && c.comp != 1) return fail(PT_ERR_CONFIG, "comp must be 0 or 1");
     if (c.RaT == 0.0) return fail(PT_ERR_CONFIG, "RaT=0 (manual dt) is not supported");
     if (c.ntr <= 0) return fail(PT_ERR_CONFIG, "ntr must be positive");
+    if (c.chebyshev != 0 && (c.chebyshev != 1 || c.precision != PT_PREC_FP64))
+        return fail(PT_ERR_CONFIG, "chebyshev = 1 (RKC2 energy stepper) runs in PT_PREC_FP64");
+    if (c.chebyshev && (c.nstage < 2 || c.nstage > 60)) return fail(PT_ERR_CONFIG, "nstage must be 2..60");
+    if (c.chebyshev) rkc2_coefficients(E);
     int rc = choose_levels(E);
     if (rc) return rc;
     fd_stencils(K);

@@ -946,6 +946,50 @@ __global__ void __launch_bounds__(256) k_rk_stage(StageArgs A, Geo g) {
     }
 }
 
+// One stage of the RKC2 energy stepper (Chebyshev.f90:151-227), FP64 interpolation as in
+// k_rk_stage.  Stage 1 at the step-start position x0: keeps the slopes k0, x1 = x0 + mewt_1 dt k,
+// x2 = x0.  Stage j at x1: x = c_j x0 + mew_j x1 + v_j x2 + mewt_j dt k + gt_j dt k0, then x2 = x1,
+// x1 = x (the last stage's x is the step's result).
+struct Rkc2Args {
+    Tables u, w, t;
+    const double *r0, *s0, *T0;      // step start
+    double *r1, *s1, *T1, *r2, *s2, *T2;
+    double *r, *s, *T;               // this stage's result
+    double *kr, *ks, *kT;            // stage-1 slopes
+    double c, mew, v, dtst, dtst2;
+    int stage;
+    int64_t n;
+};
+__global__ void __launch_bounds__(256) k_rkc2_stage(Rkc2Args A, Geo g) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    const double r = A.stage == 1 ? A.r0[t] : A.r1[t], s = A.stage == 1 ? A.s0[t] : A.s1[t];
+    int i = cell_index(r, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
+    int k = cell_index(s, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
+    i = min(max(i, 0), cK.nx);  // positions were validated by the projection; clamp keeps reads in bounds
+    k = min(max(k, 0), cK.nz);
+    const double hr = r - (double)i * cK.dr, hs = s - (double)k * cK.ds;
+    const double a1 = hr * cK.inv_fact[1], a2 = hr * hr * cK.inv_fact[2], a3 = hr * hr * hr * cK.inv_fact[3];
+    const double b1 = hs * cK.inv_fact[1], b2 = hs * hs * cK.inv_fact[2], b3 = hs * hs * hs * cK.inv_fact[3];
+    const double tr = interp(A.u, g, i, k, a1, a2, a3, b1, b2, b3);
+    const double ts = interp(A.w, g, i, k, a1, a2, a3, b1, b2, b3);
+    const double tT = interp(A.t, g, i, k, a1, a2, a3, b1, b2, b3);
+    const double r0 = A.r0[t], s0 = A.s0[t], T0 = A.T0[t];
+    if (A.stage == 1) {
+        A.kr[t] = tr; A.ks[t] = ts; A.kT[t] = tT;
+        A.r1[t] = r0 + A.dtst * tr; A.s1[t] = s0 + A.dtst * ts; A.T1[t] = T0 + A.dtst * tT;
+        A.r2[t] = r0; A.s2[t] = s0; A.T2[t] = T0;
+        return;
+    }
+    const double r1 = A.r1[t], s1 = A.s1[t], T1 = A.T1[t];
+    const double x = A.c * r0 + A.mew * r1 + A.v * A.r2[t] + A.dtst * tr + A.dtst2 * A.kr[t];
+    const double z = A.c * s0 + A.mew * s1 + A.v * A.s2[t] + A.dtst * ts + A.dtst2 * A.ks[t];
+    const double y = A.c * T0 + A.mew * T1 + A.v * A.T2[t] + A.dtst * tT + A.dtst2 * A.kT[t];
+    A.r[t] = x; A.s[t] = z; A.T[t] = y;
+    A.r2[t] = r1; A.s2[t] = s1; A.T2[t] = T1;
+    A.r1[t] = x; A.s1[t] = z; A.T1[t] = y;
+}
+
 // ---------------------------------------------------------------- mixed-precision stage
 // The same stage with the Taylor interpolation in FP32 from FP32 copies of the velocity and
 // dT/dt tables: positions, step-start values and the RK accumulators stay FP64.  Interpolated
@@ -1326,6 +1370,30 @@ int tables_to_f32(Engine& E, int which, const double* f) {
     PT_COUNT(), k_tables_to_f32<<<nblk(n, 256), 256, 0, E.st>>>(E.ftab[which], f, E.der[which][0], E.der[which][1],
                                                                 E.der[which][2], n);
     CKL("k_tables_to_f32");
+    return 0;
+}
+
+int rkc2_stage(Engine& E, int stage) {
+    PhaseTimer tm(E, PH_RK);
+    Rkc2Args A;
+    A.u = {E.u, E.der[0][0], E.der[0][1], E.der[0][2]};
+    A.w = {E.w, E.der[1][0], E.der[1][1], E.der[1][2]};
+    A.t = {E.tsa, E.der[2][0], E.der[2][1], E.der[2][2]};
+    A.r0 = E.rtr0; A.s0 = E.str0; A.T0 = E.Ttr0;
+    A.r1 = E.rtr1; A.s1 = E.str1; A.T1 = E.Ttr1;
+    A.r2 = E.rtr2; A.s2 = E.str2; A.T2 = E.Ttr2;
+    A.r = E.rtr; A.s = E.str; A.T = E.Ttr;
+    A.kr = E.k0r; A.ks = E.k0s; A.kT = E.k0T;
+    A.stage = stage;
+    A.n = E.ntr;
+    A.c = stage > 1 ? E.cCheb[stage] : 0.0;
+    A.mew = stage > 1 ? E.mewCheb[stage] : 0.0;
+    A.v = stage > 1 ? E.vCheb[stage] : 0.0;
+    A.dtst = E.mewtCheb[stage] * E.dt;
+    A.dtst2 = stage > 1 ? E.gtCheb[stage] * E.dt : 0.0;
+    KernelTimer kt(E, KT_RK_STAGE, 1);
+    PT_COUNT(), k_rkc2_stage<<<nblk(E.ntr, 256), 256, 0, E.st>>>(A, E.g1);
+    CKL("k_rkc2_stage");
     return 0;
 }
 
