@@ -424,7 +424,7 @@ __global__ void k_stats_rows(const double* T, const double* C, const double* u, 
 // single-thread tail: z integrals, fluxes, strain maximum, tracer counts
 __global__ void k_stats_tail(const double* rows, const double* T, const double* u, const double* w,
                              const double* cd, const double* E1, const int32_t* nempty, Geo g,
-                             double* out, int kent) {
+                             double* out, int kent, int direct) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int nx = cK.nx, nz = cK.nz;
     double I[4] = {0, 0, 0, 0}, Ient = 0.0;
@@ -450,9 +450,26 @@ __global__ void k_stats_tail(const double* rows, const double* T, const double* 
         }
         pst = st; psb = sb; pT0 = t0; pm = m;
     }
-    // strain-rate invariant on the top row from psi (compute_strain_rate_invariant_direct)
+    // strain-rate invariant on the top row: from the multigrid's psi (compute_strain_rate_invariant_direct,
+    // momentum.f90:73-92), or for the direct solve from the velocities (compute_strain_rate_invariant,
+    // momentum.f90:1-34)
     double smax = -1.0 / 0.0;
-    for (int i = 0; i <= nx; i++) {
+    for (int i = 0; i <= nx && direct; i++) {
+        const int k = nz;
+        double ur = 0, us = 0, wr = 0, ws = 0;
+        for (int j = -2; j <= 2; j++) ur = ur + cK.D1[3 + j] * u[g.at(i + j, k)];
+        ur = ur / cK.dr;
+        for (int j = -2; j <= 2; j++) us = us + cK.D1[3 + j] * u[g.at(i, k + j)];
+        us = us / cK.ds;
+        for (int j = -2; j <= 2; j++) wr = wr + cK.D1[3 + j] * w[g.at(i + j, k)];
+        wr = wr / cK.dr;
+        for (int j = -2; j <= 2; j++) ws = ws + cK.D1[3 + j] * w[g.at(i, k + j)];
+        ws = ws / cK.ds;
+        const double ux = ur / 1.0, uz = us / 1.0, wx = wr / 1.0, wz = ws / 1.0;
+        const double s = pow(0.5 * (2.0 * (ux * ux + wz * wz) + (uz + wx) * (uz + wx)), 0.5);
+        if (s > smax) smax = s;
+    }
+    for (int i = 0; i <= nx && !direct; i++) {
         int k = nz;
         double Sxx = 0, Szz = 0, Sxz = 0;
         for (int j = -2; j <= 2; j++) Sxx = Sxx + cK.D2[3 + j] * E1[g.at(i + j, k)];
@@ -497,7 +514,8 @@ int stats(Engine& E, pt_stats_row* o) {
     const double* C = E.cfg.comp ? E.Cnew : E.T;
     PT_COUNT(), k_stats_rows<<<nblk(nz + 1, 64), 64, 0, E.st>>>(E.T, C, E.u, E.w, E.cond, E.vis[1], E.g1, rows);
     double* out = rows + 4 * (nz + 1) + 8;
-    PT_COUNT(), k_stats_tail<<<1, 32, 0, E.st>>>(rows, E.T, E.u, E.w, E.cond, E.err[1], E.nempty, E.g1, out, E.kent);
+    PT_COUNT(), k_stats_tail<<<1, 32, 0, E.st>>>(rows, E.T, E.u, E.w, E.cond, E.err[1], E.nempty, E.g1, out, E.kent,
+                                                  E.cfg.direct);
     CKL("stats");
     CK(cudaMemcpyAsync(E.hscal, out, 17 * sizeof(double), cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
