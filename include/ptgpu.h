@@ -251,6 +251,24 @@ int pt_tracers_to_corners(const double* T0, int smooth_vis);
 #define PT_NOALLOC_MAX_NODES 33153
 int pt_tracers_to_corners_noalloc(const double* T0, int smooth_vis);
 
+/* Output and restart files of the current state, written asynchronously: the device-to-host copies
+ * are queued in order after the work that produced the state (later calls may start at once and do
+ * not change what is written), then a host thread formats and writes the files.  pt_io_wait waits
+ * for that thread and returns its status; every writer and reader waits for the previous one.
+ * pt_write_snapshot: snapshots (main.f90:377-424), the files T<10000+fcount> (x, z, T, SF, u, w,
+ *   2 vis strain, vis, T_vis, nempty and, with composition, C and C_vis per node, i outer, edit
+ *   descriptors G14.5E3 and I6) and P<10000+fcount> (lateral averages of T, strain rate and
+ *   stress per row) in directory dir.
+ * pt_write_restart: print_restart (main.f90:457-496), the records Trestart (xg, zg, T, [Cnew], SF)
+ *   and restart_tracers (rtr, str, [Ctr or Ttype], Ttr) in gfortran's sequential unformatted form
+ *   (4-byte length markers; records longer than 2^31-9 bytes split into sub-records).
+ * pt_read_restart: the restart read (grid.f90:55-104) of those two files from dir, then
+ *   pt_upload_state. */
+int pt_write_snapshot(const char* dir, int fcount);
+int pt_write_restart(const char* dir);
+int pt_read_restart(const char* dir);
+int pt_io_wait(void);
+
 /* Current simulation time and the RK4 time step of stability_RK4 (energy.f90:756-810). */
 int pt_time(double* time, double* dt);
 

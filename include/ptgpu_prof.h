@@ -45,6 +45,9 @@ int pt_prof_table(int which, float* host);
  * go to out, *count receives the number of tests.  Kept when the solve fails (cycle cap,
  * divergence), so a caller can read how far it got. */
 int pt_prof_residuals(double* out, int cap, int* count);
+/* Largest sub-record payload of the restart writer in bytes (0: gfortran's 2^31-9), so that tests
+ * can exercise the sub-record form on small files. */
+int pt_prof_record_limit(int64_t bytes);
 
 #ifdef __cplusplus
 }

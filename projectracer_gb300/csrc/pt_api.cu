@@ -185,6 +185,7 @@ static int engine_alloc(Engine& E) {
 
 static void engine_free(Engine& E) {
     unet_engine_release(E);
+    io_release(E);
     direct_free(E);
     if (E.psi_a) cudaFree(E.psi_a);
     if (E.psi_b) cudaFree(E.psi_b);

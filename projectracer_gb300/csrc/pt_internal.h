@@ -114,6 +114,7 @@ struct Engine {
     int *dipiv = nullptr, *dluerr = nullptr;
     void* dlu = nullptr;
     bool direct_ready = false;
+    void* io = nullptr;  // snapshot / restart writer state (pt_io.cu)
     // multigrid
     double *err[PT_MAXLEV] = {}, *S0[PT_MAXLEV] = {}, *S1[PT_MAXLEV] = {}, *S2[PT_MAXLEV] = {},
            *RHS[PT_MAXLEV] = {}, *res[PT_MAXLEV] = {}, *dtst[PT_MAXLEV] = {}, *ratio[PT_MAXLEV] = {},
@@ -308,6 +309,9 @@ int rkc2_stage(Engine& E, int stage);                 // Chebyshev.f90:151-227 t
 // discrete tracer types: int32 0/1 on the device <-> the type as 0.0 / 1.0 in a composition array
 int types_to_c(Engine& E, const int32_t* dev_types, double* c);
 int c_to_types(Engine& E, const double* c, int32_t* dev_types);
+
+// output and restart files (pt_io.cu): joins a pending writer and frees its staging
+void io_release(Engine& E);
 
 // direct banded solve (pt_direct.cu)
 int direct_alloc(Engine& E);

@@ -97,6 +97,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_prof_table.argtypes = [i32, vp]
     L.pt_prof_region.argtypes = [i32, ctypes.POINTER(f64)]
     L.pt_prof_residuals.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int)]
+    L.pt_write_snapshot.argtypes = [ctypes.c_char_p, i32]
+    L.pt_write_restart.argtypes = [ctypes.c_char_p]
+    L.pt_read_restart.argtypes = [ctypes.c_char_p]
+    L.pt_prof_record_limit.argtypes = [ctypes.c_int64]
     _LIB = L
     return L
 
@@ -215,6 +219,21 @@ class Engine:
         out = np.empty((self.nz + 7, self.nx + 1, 4), dtype=np.float32)
         self._check(self.L.pt_prof_table(which, _ptr(out)))
         return out
+
+    def write_snapshot(self, directory: str, fcount: int = 0):
+        """T<10000+fcount> and P<10000+fcount> of the current state (asynchronous: see io_wait)."""
+        self._check(self.L.pt_write_snapshot(directory.encode(), fcount))
+
+    def write_restart(self, directory: str):
+        """Trestart and restart_tracers of the current state (asynchronous: see io_wait)."""
+        self._check(self.L.pt_write_restart(directory.encode()))
+
+    def read_restart(self, directory: str):
+        """Restart read of Trestart and restart_tracers, then the upload (pt_read_restart)."""
+        self._check(self.L.pt_read_restart(directory.encode()))
+
+    def io_wait(self):
+        self._check(self.L.pt_io_wait())
 
     def residuals(self) -> list[float]:
         """Relative residual at each convergence test of the last psi solve (kept after a failed

@@ -149,7 +149,15 @@ def read_restart(directory: str, cfg: PtConfig) -> dict:
     out["SF"] = out["SF"].reshape(nz + 7, nx + 7)
     out["Cnew"] = out["Cnew"].reshape(nz + 11, nx + 11) if comp else np.zeros((nz + 11, nx + 11))
     with open(os.path.join(directory, "restart_tracers"), "rb") as fh:
-        buf = np.frombuffer(_read_record(fh), dtype="<f8")
+        raw = _read_record(fh)
+    if comp and getattr(cfg, "discrete_types", 0):  # rtr, str, Ttype (integer*4), Ttr
+        out["rtr"] = np.frombuffer(raw, dtype="<f8", count=n).copy()
+        out["str"] = np.frombuffer(raw, dtype="<f8", count=n, offset=8 * n).copy()
+        out["Ttype"] = np.frombuffer(raw, dtype="<i4", count=n, offset=16 * n).copy()
+        out["Ttr"] = np.frombuffer(raw, dtype="<f8", count=n, offset=20 * n).copy()
+        out["Ctr"] = out["Ttype"].astype(np.float64)
+        return out
+    buf = np.frombuffer(raw, dtype="<f8")
     names = ["rtr", "str"] + (["Ctr"] if comp else []) + ["Ttr"]
     for j, name in enumerate(names):
         out[name] = buf[j * n:(j + 1) * n].copy()

@@ -7,7 +7,7 @@ Run once in a checkout that has the reference next to it:
 Inputs (all produced by the reference's own run of its shipped inputs.nml with 2 OpenMP threads):
 stdout (known-answer values), stats.dat (basics.f90:427-428 format), T10000 (t=0 snapshot,
 main.f90:396-397 format), P10000 (lateral averages, main.f90:414-422) and inputs.nml.
-Outputs: reference_run.json and T10000_subset.npz in this directory.
+Outputs: reference_run.json, T10000_subset.npz and snapshot_t0_lines.json in this directory.
 """
 
 from __future__ import annotations
@@ -77,6 +77,15 @@ def main(ref: str) -> None:
     k = np.tile(np.arange(n), n)
     keep = ((i % 5) == 0) & ((k % 5) == 0) | (k == 1) | (k == n - 2)
     np.savez_compressed(os.path.join(HERE, "T10000_subset.npz"), i=i[keep], k=k[keep], cols=A[keep])
+    # the snapshot files as printed (every 37th line of T10000 with its line number, all of P10000),
+    # for the snapshot writer's edit descriptors
+    with open(os.path.join(ref, "T10000")) as fh:
+        tl = fh.read().split("\n")
+    with open(os.path.join(ref, "P10000")) as fh:
+        pl = fh.read().split("\n")
+    sample = {"T10000": [[n, tl[n]] for n in range(0, len(tl), 37) if tl[n]], "P10000": [ln for ln in pl if ln]}
+    with open(os.path.join(HERE, "snapshot_t0_lines.json"), "w") as fh:
+        json.dump(sample, fh, indent=0)
 
 
 if __name__ == "__main__":
