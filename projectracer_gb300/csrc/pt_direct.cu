@@ -3,7 +3,7 @@
 // banded LU with partial pivoting (DGBTRF), and per solve the buoyancy right-hand side (258-289),
 // the banded substitutions (DGBTRS, solve_SF_equation 636-653) and Stream_grid (291-317).
 //
-// The matrix has one row per grid node, p = (nz+1) i + k + 1 (Database=2), with the 33-point
+// The matrix has one row per grid node, p = (nz+1) i + k + 1 (Database=2), with the 29-point
 // biharmonic stencil folded at the walls (free-slip images carry a sign) and identity rows at the
 // corners; its band is kl = ku = 3 (nz+1) wide.  For an isoviscous run (ivis=0, the only case the
 // reference builds once) every stencil value depends only on the stencil offset, the two image
@@ -27,10 +27,12 @@ namespace pt {
 
 namespace {
 
-// the 33 stencil points of build_SF_matrix in the reference's order (momentum.f90:397-470)
+// the 29 stencil points of build_SF_matrix in the reference's order (momentum.f90:397-470): the
+// x and z arms at distance 3, then the 5 x 5 block
+constexpr int kStencilPts = 29;
 struct StencilPts {
     int n = 0;
-    int di[33], dk[33];
+    int di[kStencilPts], dk[kStencilPts];
     StencilPts() {
         for (int i = -3; i <= 3; i += 6) { di[n] = i; dk[n++] = 0; }
         for (int k = -3; k <= 3; k += 6) { di[n] = 0; dk[n++] = k; }
@@ -103,8 +105,8 @@ static double matrix_element(const Engine& E, int i, int k, int rsym, int ssym, 
 
 // element table [point][rsym][ssym][row]; kind 0 entries carry NaN and are skipped
 struct ElemTable {
-    double v[33][2][2][3];
-    int di[33], dk[33];
+    double v[kStencilPts][2][2][3];
+    int di[kStencilPts], dk[kStencilPts];
 };
 __constant__ ElemTable cET;
 
@@ -123,7 +125,7 @@ __global__ void k_direct_assemble(double* MB, int n, int ldab, int kl, int ku, i
         return;
     }
     const int row = (ip == 0 || ip == nx) ? 1 : ((kp == 0 || kp == nz) ? 2 : 0);
-    for (int q0 = 0; q0 < 33; q0++) {
+    for (int q0 = 0; q0 < kStencilPts; q0++) {
         int iq = ip + cET.di[q0], rsym = 0;
         if (iq < 0) { iq = -iq; rsym = 1; }
         else if (iq > nx) { iq = nx - (iq - nx); rsym = 1; }
@@ -478,7 +480,7 @@ int direct_alloc(Engine& E) {
     // Matrix_element for every (stencil point, image signs, row kind)
     static const StencilPts P;
     ElemTable T;
-    for (int q = 0; q < 33; q++) {
+    for (int q = 0; q < kStencilPts; q++) {
         T.di[q] = P.di[q];
         T.dk[q] = P.dk[q];
         for (int rs = 0; rs < 2; rs++)
