@@ -88,7 +88,11 @@ int ptref_band_lu(int n, int kl, int ku, double* ab, int ldab, int* ipiv) {
     return info;
 }
 
-/* dgbtrs.f (TRANS='N', one right-hand side) with dtbsv.f (upper, no transpose, non-unit). */
+/* dgbtrs.f (TRANS='N', one right-hand side) with dtbsv.f (upper, no transpose, non-unit).  Every
+ * column is updated and every entry divided, zeros included, like the optimized BLAS that the
+ * shipped run linked: its snapshot T10000 prints psi = -0 on every wall node that is not a corner
+ * (0 divided by a negative pivot).  The reference dtbsv.f/dger.f skip zero entries, which leaves
+ * those +0; nonzero results are the same either way. */
 int ptref_band_solve(int n, int kl, int ku, const double* ab, int ldab, const int* ipiv, double* b) {
     int kd = ku + kl + 1;
     if (kl > 0)
@@ -96,20 +100,16 @@ int ptref_band_solve(int n, int kl, int ku, const double* ab, int ldab, const in
             int lm = kl < n - j ? kl : n - j;
             int l = ipiv[j - 1];
             if (l != j) { double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
-            if (b[j - 1] != 0.0) {
-                double temp = -1.0 * b[j - 1];
-                for (int i = 1; i <= lm; i++) b[j + i - 1] = b[j + i - 1] + AB(kd + i, j) * temp;
-            }
+            double temp = -1.0 * b[j - 1];
+            for (int i = 1; i <= lm; i++) b[j + i - 1] = b[j + i - 1] + AB(kd + i, j) * temp;
         }
     int k = kl + ku, kplus1 = k + 1;
     for (int j = n; j >= 1; j--) {
-        if (b[j - 1] != 0.0) {
-            int l = kplus1 - j;
-            b[j - 1] = b[j - 1] / AB(kplus1, j);
-            double temp = b[j - 1];
-            int i0 = 1 > j - k ? 1 : j - k;
-            for (int i = j - 1; i >= i0; i--) b[i - 1] = b[i - 1] - temp * AB(l + i, j);
-        }
+        int l = kplus1 - j;
+        b[j - 1] = b[j - 1] / AB(kplus1, j);
+        double temp = b[j - 1];
+        int i0 = 1 > j - k ? 1 : j - k;
+        for (int i = j - 1; i >= i0; i--) b[i - 1] = b[i - 1] - temp * AB(l + i, j);
     }
     return 0;
 }

@@ -307,7 +307,8 @@ __global__ void __launch_bounds__(kLuThreads) k_direct_lu(double* ab, int* ipiv,
 // DGBTRS (TRANS='N', one right-hand side): forward substitution with the interchanges and L,
 // back substitution with U (dtbsv), one warp carrying the sequential column steps, the band
 // columns staged through shared memory `chunk` at a time by the whole CTA.  Same operations in the
-// same order as the column-by-column DGBTRS.
+// same order as the column-by-column DGBTRS; zero entries are divided and propagated too, like the
+// optimized BLAS of the shipped run (psi = -0 on the non-corner wall nodes of its snapshots).
 constexpr int kDsThreads = 128;
 static size_t direct_solve_smem(int n, int kl, int ku, int chunk) {
     return sizeof(double) * ((size_t)n + (size_t)chunk * (size_t)(kl + ku + 1)) + sizeof(int) * (size_t)chunk;
@@ -337,11 +338,8 @@ __global__ void __launch_bounds__(kDsThreads) k_direct_solve(const double* ab, c
                 const int l = cp[jj];
                 if (l != j && lane == 0) { const double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
                 __syncwarp();
-                const double bj = b[j - 1];
-                if (bj != 0.0) {
-                    const double temp = -1.0 * bj;
-                    for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + cb[jj * kl + i - 1] * temp;
-                }
+                const double temp = -1.0 * b[j - 1];
+                for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + cb[jj * kl + i - 1] * temp;
                 __syncwarp();
             }
         }
@@ -355,14 +353,11 @@ __global__ void __launch_bounds__(kDsThreads) k_direct_solve(const double* ab, c
             for (int jj = 0; jj < cn; jj++) {
                 const int j = c1 - jj;
                 const double* col = cb + (size_t)jj * kp1;
-                const double bj = b[j - 1];
-                if (bj != 0.0) {
-                    const double x = bj / col[kp1 - 1];
-                    __syncwarp();
-                    if (lane == 0) b[j - 1] = x;
-                    const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
-                    for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * col[l + i - 1];
-                }
+                const double x = b[j - 1] / col[kp1 - 1];
+                __syncwarp();
+                if (lane == 0) b[j - 1] = x;
+                const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+                for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * col[l + i - 1];
                 __syncwarp();
             }
         }

@@ -767,7 +767,8 @@ __global__ void __launch_bounds__(1024) k_band_lu(double* ab, int* ipiv, int n, 
 // them, its lanes splitting each column's band update; the band columns (and pivots) a chunk of
 // steps needs are staged in shared memory by the whole CTA beforehand, so each step works from
 // shared memory instead of waiting on a global load.  Same operations in the same order as the
-// column-by-column DGBTRS.
+// column-by-column DGBTRS, zero entries divided and propagated too (the optimized-BLAS behaviour
+// of the shipped run, which only decides the sign of exact zeros).
 constexpr int kBsChunk = 32, kBsThreads = 128;
 __host__ __device__ constexpr size_t band_solve_smem(int n, int kl, int ku) {
     return sizeof(double) * ((size_t)n + (size_t)kBsChunk * (kl + ku + 1)) + sizeof(int) * kBsChunk;
@@ -795,11 +796,8 @@ __global__ void __launch_bounds__(kBsThreads) k_band_solve(const double* ab, con
                 const int l = cp[jj];
                 if (l != j && lane == 0) { double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
                 __syncwarp();
-                const double bj = b[j - 1];
-                if (bj != 0.0) {
-                    const double temp = -1.0 * bj;
-                    for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + cb[jj * kl + i - 1] * temp;
-                }
+                const double temp = -1.0 * b[j - 1];
+                for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + cb[jj * kl + i - 1] * temp;
                 __syncwarp();
             }
         }
@@ -814,14 +812,11 @@ __global__ void __launch_bounds__(kBsThreads) k_band_solve(const double* ab, con
             for (int jj = 0; jj < cn; jj++) {
                 const int j = c1 - jj;
                 const double* col = cb + (size_t)jj * kp1;  // col[r - 1] = AB(r, j)
-                const double bj = b[j - 1];
-                if (bj != 0.0) {
-                    const double x = bj / col[kp1 - 1];
-                    __syncwarp();
-                    if (lane == 0) b[j - 1] = x;
-                    const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
-                    for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * col[l + i - 1];
-                }
+                const double x = b[j - 1] / col[kp1 - 1];
+                __syncwarp();
+                if (lane == 0) b[j - 1] = x;
+                const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+                for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * col[l + i - 1];
                 __syncwarp();
             }
         }

@@ -75,3 +75,39 @@ def test_lateral_profile_t0(golden, golden_run):
         for ii in range(nx):
             fint = fint + 0.5 * (row[ii] * 1.0 + row[ii + 1] * 1.0) * dr
         assert fint / o.cfg.aspect == pytest.approx(tlat, rel=5.01e-5, abs=1e-300)
+
+
+def _g14_5e3(x: float) -> str:
+    """Fortran g14.5E3 as gfortran prints it (F form for 0.1 <= |x| < 1e5, else E form)."""
+    if x == 0.0:
+        return "%9.4f     " % x  # '-0.0000' for a negative zero
+    k = int(("%.4e" % x).split("e")[1]) + 1
+    if 0 <= k <= 5:
+        return "%9.*f     " % (5 - k, x)
+    m = "%.4e" % abs(x)
+    return "%14s" % ("%s0.%s%sE%s%03d" % ("-" if x < 0 else "", m[0], m[2:6], "-" if k < 0 else "+", abs(k)))
+
+
+def test_snapshot_t0_text(golden_run):
+    """The sampled lines of the shipped T10000 as printed, every column but the stress one: T, psi
+    (with the sign of its zeros: -0 on the non-corner wall nodes), u, w, vis, Tvis, nempty, Cnew,
+    Cvis."""
+    import json
+    import os
+    o, _ = golden_run
+    with open(os.path.join(os.path.dirname(__file__), "golden", "snapshot_t0_lines.json")) as fh:
+        ref = json.load(fh)["T10000"]
+    nz = o.cfg.nz
+    f3 = [o.get(q) for q in (0, 7, 8, 9, 10, 2)]
+    ne, C, Cv = o.get(11), o.get(4), o.get(5)
+    checked = 0
+    for n, line in ref:
+        i, k = divmod(n, nz + 2)
+        if k > nz:
+            continue
+        cols = [line[14 * j:14 * (j + 1)] for j in (2, 3, 4, 5, 7, 8)]
+        assert [_g14_5e3(f[k + 3, i + 3]) for f in f3] == cols, n
+        assert "%6d" % ne[k, i] == line[126:132], n
+        assert _g14_5e3(C[k + 5, i + 5]) + _g14_5e3(Cv[k + 5, i + 5]) == line[132:160], n
+        checked += 1
+    assert checked > 250
