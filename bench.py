@@ -210,6 +210,8 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="only the headline workload (no error, residual-floor, 1e-8 and per-configuration sections)")
+    ap.add_argument("--krylov", type=int, default=-1,
+                    help="GCR directions of the mixed solve (default: the workload's setting; 0 = defect correction)")
     ap.add_argument("--tpc", type=int, default=0,
                     help="tracers per cell override (profiling captures of a smaller tracer state only)")
     args = ap.parse_args()
@@ -229,6 +231,8 @@ def main():
     apply_bench_solver(cfg, w)
     if args.tpc > 0:
         cfg.ntr = cfg.nx * cfg.nz * args.tpc
+    if args.krylov >= 0 and args.precision == "mixed":
+        cfg.krylov = args.krylov
     st = make_state(cfg, 3 + rank, noise=w.get("noise", 1e-3))
     e = eng.Engine(cfg)
     e.upload(st)
@@ -334,7 +338,9 @@ def solver_keys(cfg, grids=None) -> dict:
             "mg_cycle": "V" if (mixed and cfg.mg_cycle == PT_CYCLE_V) else "reference W-type",
             "nstageS": cfg.nstageS, "nstageC": (cfg.nstageC or cfg.nstageS) if mixed else cfg.nstageS,
             "dampingS": cfg.dampingS, "guess": GUESS_NAMES[cfg.guess_mode],
-            "coarse_solve": "FP64 explicit inverse of the FP64 banded LU"}
+            "coarse_solve": "FP64 explicit inverse of the FP64 banded LU",
+            "outer": f"GCR({cfg.krylov}) with the cycle as preconditioner" if (mixed and cfg.krylov > 0)
+            else "defect correction (x += cycle correction)"}
 
 
 def fp64_reference_method(cfg):
@@ -344,6 +350,7 @@ def fp64_reference_method(cfg):
 
     c = cfg.copy()
     c.precision = PT_PREC_FP64
+    c.krylov = 0
     ref = PtConfig.defaults()
     c.nstageS, c.dampingS, c.nstageC = ref.nstageS, ref.dampingS, 0
     c.guess_mode = ref.guess_mode
@@ -523,6 +530,7 @@ def fp64_comparison(eng, cfg, snap, steps: int = 2, same_schedule: bool = False)
 
     c = cfg.copy()
     c.precision = PT_PREC_FP64
+    c.krylov = 0  # the FP64 path is the plain cycle
     if not same_schedule:
         ref = PtConfig.defaults()  # the reference's smoother (35 stages, damping 1000), warm start
         c.nstageS, c.dampingS = ref.nstageS, ref.dampingS

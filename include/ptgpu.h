@@ -132,6 +132,11 @@ typedef struct pt_config {
                               precision only */
     int32_t nstage;        /* RKC2 stages (2..60) */
     double damping, aRK2;  /* RKC2 damping and the free parameter b1 = aRK2/omega1 (Chebyshev.f90:55) */
+    int32_t krylov;        /* mixed precision only (&gpu group).  0: each cycle adds its correction to
+                              psi (defect correction).  m in 1..8: the cycle is the preconditioner of
+                              a flexible GCR iteration that keeps the last m search directions
+                              (restarted after m); same convergence test */
+    int32_t pad_;
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */

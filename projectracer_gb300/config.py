@@ -79,6 +79,8 @@ class PtConfig(ctypes.Structure):
         ("nstage", ctypes.c_int32),
         ("damping", ctypes.c_double),
         ("aRK2", ctypes.c_double),
+        ("krylov", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
     ]
 
     @staticmethod
@@ -173,6 +175,7 @@ class PtConfig(ctypes.Structure):
         c.direct = 1 if int(inp.get("iterate", 1)) == 0 else 0
         c.mg_scheme = int(gpu.get("mg_scheme", PT_MG_REFERENCE))
         c.mg_cycle = int(gpu.get("mg_cycle", PT_CYCLE_REFERENCE))
+        c.krylov = int(gpu.get("krylov", 0))
         tpc = int(inp.get("tpc", 0))
         c.ntr = ntr if ntr is not None else (c.nx + 1) * (c.nz + 1) * tpc
         return c
@@ -257,6 +260,8 @@ def workload(name: str, scale: float = 1.0, precision: int = PT_PREC_FP64) -> tu
         c.dampingS = w["mixed_dampingS"]
     if precision == PT_PREC_MIXED and "mixed_guess" in w:
         c.guess_mode = w["mixed_guess"]
+    if precision == PT_PREC_MIXED:
+        c.krylov = w.get("mixed_krylov", 0)
     c.precision = precision
     c.ntr = c.nx * c.nz * w["tpc"]
     return c, w

@@ -259,6 +259,14 @@ static void engine_free(Engine& E) {
             if (E.gev[q][j]) cudaEventDestroy(E.gev[q][j]);
     if (E.gM1) cudaGraphExecDestroy(E.gM1);
     if (E.gM2) cudaGraphExecDestroy(E.gM2);
+    for (int j = 0; j < kGcrMax; j++) {
+        if (E.gG0[j]) cudaGraphExecDestroy(E.gG0[j]);
+        if (E.gG1[j]) cudaGraphExecDestroy(E.gG1[j]);
+        if (E.gz[j]) cudaFree(E.gz[j]);
+        if (E.gv[j]) cudaFree(E.gv[j]);
+    }
+    for (double* p : {E.gr1, E.gzero, E.gpart, E.gsc})
+        if (p) cudaFree(p);
     if (E.gA) cudaGraphExecDestroy(E.gA);
     if (E.gB) cudaGraphExecDestroy(E.gB);
     if (E.rev0) cudaEventDestroy(E.rev0);
@@ -365,6 +373,10 @@ int pt_init(const pt_config* cfg) {
     if (cfg->discrete_types != 0 && (cfg->discrete_types != 1 || cfg->comp != 1)) {
         delete E;
         return fail(PT_ERR_CONFIG, "discrete_types = 1 needs comp = 1 (one dense type, ntype = 1)");
+    }
+    if (cfg->krylov != 0 && (cfg->krylov < 0 || cfg->krylov > kGcrMax || cfg->precision != PT_PREC_MIXED)) {
+        delete E;
+        return fail(PT_ERR_CONFIG, "krylov = 1..8 (GCR directions) applies to PT_PREC_MIXED only");
     }
     TRACE("pt_init: geometry and stream");
     E->g1 = make_geo(cfg->nx, cfg->nz);

@@ -21,6 +21,7 @@
 
 #define GH 5
 #define PT_MAXLEV 8
+constexpr int kGcrMax = 8;  // most GCR search directions of the mixed-precision solve (pt_config.krylov)
 
 enum { PH_RK = 0, PH_PROJECT, PH_SOLVE, PH_SETUP, PH_CYCLE_L1, PH_CYCLE_COARSE, PH_GRID, PH_FACTOR, PT_NPHASE };
 
@@ -128,6 +129,14 @@ struct Engine {
     float* fcoef[PT_MAXLEV][6] = {};  // vis, vx, vz, vxz, vxxmzz, dt_stream in FP32
     cudaGraphExec_t gM1 = nullptr, gM2 = nullptr;
     int64_t nM1 = 0, nM2 = 0;
+    // GCR acceleration of the mixed solve (krylov > 0): search directions z_j (FP64, with their
+    // ghost images) and v_j = -A z_j, the level-1 residual of the smoothing (r - A e), a zero
+    // right-hand side, per-row partial sums and the device scalars [|v_j|^2 (kGcrMax) | c_j
+    // (kGcrMax) | alpha]; one pair of captured graphs per direction slot
+    double *gz[kGcrMax] = {}, *gv[kGcrMax] = {};
+    double *gr1 = nullptr, *gzero = nullptr, *gpart = nullptr, *gsc = nullptr;
+    cudaGraphExec_t gG0[kGcrMax] = {}, gG1[kGcrMax] = {};
+    int64_t nG0[kGcrMax] = {}, nG1[kGcrMax] = {};
     double* psi_keep = nullptr;
     // coarse band LU
     double *Mc = nullptr, *Bc = nullptr, *RowB = nullptr;

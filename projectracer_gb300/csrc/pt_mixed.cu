@@ -471,6 +471,179 @@ __global__ void k_coarse_scatter_f(float* e, const double* B, Geo g, int nxc, in
     e[g.at((p - 1) / N, (p - 1) % N)] = (float)B[p - 1];
 }
 
+// ---------------------------------------------------------------- GCR acceleration (krylov > 0)
+// Flexible GCR with the mixed cycle as its preconditioner: per iteration j (direction slot j
+// since the last restart)
+//   z_j = M r        the level-1 FP32 smoothing of A e = r from zero, then the V-cycle below
+//                    level 1 on r - A e, prolongated (FP64 accumulation, ghost images included)
+//   v_j = -A z_j     FP64 operator (exact integer stencil sums)
+//   v_j -= sum_i c_i v_i,  z_j -= sum_i c_i z_i,  c_i = (v_j, v_i) / (v_i, v_i)    (i < j)
+//   alpha = -(r, v_j) / (v_j, v_j);   x += alpha z_j;   r += alpha v_j
+// so that r stays the residual of x (up to FP64 rounding) and |r| is minimised over the span of
+// the directions.  Dot products are per-row partial sums (one CTA per padded row, interior nodes
+// only) reduced in a fixed order: the iteration is deterministic.  The scalars stay on the
+// device: gsc = [|v_i|^2 (kGcrMax) | c_i (kGcrMax) | alpha].
+struct GcrSet {
+    const double* v[kGcrMax];
+    double* z[kGcrMax];
+};
+constexpr int kGcrThreads = 256;
+
+// block sum of nq (<= kGcrMax + 2) per-thread values, in a fixed order; thread 0 writes
+// out[q * stride]
+__device__ __forceinline__ void gcr_block_sums(double* a, int nq, double* out, int stride) {
+    __shared__ double sh[kGcrThreads / 32][kGcrMax + 2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kGcrMax + 2; q++) {
+        if (q >= nq) break;
+        double v = a[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int q = 0; q < nq; q++) {
+            double t = 0.0;
+            for (int w = 0; w < kGcrThreads / 32; w++) t += sh[w][q];
+            out[(size_t)q * stride] = t;
+        }
+}
+
+// per padded row b: partial dots (vn, v_i) over the interior, i < nk -> part[i * R + b]
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_dots(const double* __restrict__ vn, GcrSet S, int nk, Geo g,
+                                                          int nx, int nz, double* part) {
+    pdl_begin();
+    const int R = gridDim.x, b = blockIdx.x, k = b - GH;
+    double a[kGcrMax] = {};
+    if (k >= 1 && k <= nz - 1)
+        for (int i = 1 + threadIdx.x; i <= nx - 1; i += kGcrThreads) {
+            const size_t o = g.at(i, k);
+            const double v = vn[o];
+#pragma unroll
+            for (int q = 0; q < kGcrMax; q++)
+                if (q < nk) a[q] += v * S.v[q][o];
+        }
+    gcr_block_sums(a, nk, part + b, R);
+}
+
+// c_i = (sum over rows of part[i]) / |v_i|^2 into sc[kGcrMax + i]
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_coef(const double* __restrict__ part, int R, int nk, double* sc) {
+    pdl_begin();
+    double a[kGcrMax] = {};
+#pragma unroll
+    for (int q = 0; q < kGcrMax; q++)
+        if (q < nk)
+            for (int b = threadIdx.x; b < R; b += kGcrThreads) a[q] += part[(size_t)q * R + b];
+    __shared__ double tot[kGcrMax];
+    gcr_block_sums(a, nk, tot, 1);
+    __syncthreads();
+    if (threadIdx.x < (unsigned)nk) {
+        const double n2 = sc[threadIdx.x];
+        sc[kGcrMax + threadIdx.x] = n2 > 0.0 ? tot[threadIdx.x] / n2 : 0.0;
+    }
+}
+
+// vn -= sum c_i v_i, zn -= sum c_i z_i over the whole padded row (ghost images stay images);
+// then partial (vn, vn) -> part[b], (r, vn) -> part[R + b] over the interior
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_orth(double* __restrict__ vn, double* __restrict__ zn, GcrSet S,
+                                                          int nk, const double* __restrict__ sc,
+                                                          const double* __restrict__ r, Geo g, int nx, int nz,
+                                                          double* part) {
+    pdl_begin();
+    const int R = gridDim.x, b = blockIdx.x, k = b - GH;
+    double c[kGcrMax];
+#pragma unroll
+    for (int q = 0; q < kGcrMax; q++) c[q] = q < nk ? sc[kGcrMax + q] : 0.0;
+    double a[2] = {0.0, 0.0};
+    const size_t row = (size_t)b * g.pitch;
+    for (int col = threadIdx.x; col < g.pitch; col += kGcrThreads) {
+        const size_t o = row + col;
+        double v = vn[o];
+        if (nk > 0) {
+            double z = zn[o];
+#pragma unroll
+            for (int q = 0; q < kGcrMax; q++)
+                if (q < nk) {
+                    v -= c[q] * S.v[q][o];
+                    z -= c[q] * S.z[q][o];
+                }
+            vn[o] = v;
+            zn[o] = z;
+        }
+        const int i = col - GH;
+        if (k >= 1 && k <= nz - 1 && i >= 1 && i <= nx - 1) {
+            a[0] += v * v;
+            a[1] += r[o] * v;
+        }
+    }
+    gcr_block_sums(a, 2, part + b, R);
+}
+
+// |v_j|^2 -> sc[j];  alpha = -(r, v_j) / |v_j|^2 -> sc[2 kGcrMax] (0 for a vanishing direction)
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_alpha(const double* __restrict__ part, int R, int j, double* sc) {
+    pdl_begin();
+    double a[2] = {0.0, 0.0};
+    for (int b = threadIdx.x; b < R; b += kGcrThreads) {
+        a[0] += part[b];
+        a[1] += part[R + b];
+    }
+    __shared__ double tot[2];
+    gcr_block_sums(a, 2, tot, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double n2 = tot[0];
+        const bool ok = n2 > 0.0 && isfinite(n2) && isfinite(tot[1]);
+        sc[j] = ok ? n2 : 0.0;
+        sc[2 * kGcrMax] = ok ? -tot[1] / n2 : 0.0;
+    }
+}
+
+// x += alpha z (whole padded row), r += alpha v (interior), partial sum |r| -> part[b]
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_update(double* __restrict__ x, double* __restrict__ r,
+                                                            const double* __restrict__ zn,
+                                                            const double* __restrict__ vn,
+                                                            const double* __restrict__ sc, Geo g, int nx, int nz,
+                                                            double* part) {
+    pdl_begin();
+    const int b = blockIdx.x, k = b - GH;
+    const double al = sc[2 * kGcrMax];
+    double a[1] = {0.0};
+    const size_t row = (size_t)b * g.pitch;
+    for (int col = threadIdx.x; col < g.pitch; col += kGcrThreads) {
+        const size_t o = row + col;
+        x[o] += al * zn[o];
+        const int i = col - GH;
+        if (k >= 1 && k <= nz - 1 && i >= 1 && i <= nx - 1) {
+            const double rv = r[o] + al * vn[o];
+            r[o] = rv;
+            a[0] += fabs(rv);
+        }
+    }
+    gcr_block_sums(a, 1, part + b, 0);
+}
+
+// the sum of the R row partials of |r| into *out
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_sum(const double* __restrict__ part, int R, double* out) {
+    pdl_begin();
+    double a[1] = {0.0};
+    for (int b = threadIdx.x; b < R; b += kGcrThreads) a[0] += part[b];
+    gcr_block_sums(a, 1, out, 0);
+}
+
+// z = e (FP64, with the ghost images) and r1 = r - A e (FP32 stencil, FP64 update): the start of
+// z_j = M r and the residual that the levels below 1 see
+__global__ void __launch_bounds__(128) k_gcr_first(double* __restrict__ z, double* __restrict__ r1,
+                                                   const double* __restrict__ r, const float* __restrict__ e, FOp op,
+                                                   Geo g, int nx, int nz, int ivis, double sz) {
+    pdl_begin();
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    const size_t o = g.at(i, k);
+    r1[o] = r[o] - (double)apply_A<float>(e, g, 1, op, i, k, ivis);
+    store_ghosts_d(z, g, i, k, nx, nz, (double)e[o], sz);
+}
+
 // FP64 level-1 residual (and optionally the sum of |r| into dscal[8])
 static int residual64(Engine& E, bool want_sum, float* res32 = nullptr) {
     const Geo& g = E.gl[1];
@@ -517,7 +690,8 @@ static int bcs_f(Engine& E, int l, float* f) {
 // FP32 iterate_stream on the correction of level l, RKC1 in increment form (k_rkc_first_f).
 // zero: the correction is zero on entry (first visit after a descent); want_res: the residual is
 // needed (the next step descends).
-static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in = false) {
+static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in = false,
+                    const double* res1 = nullptr) {
     const Geo& g = E.gl[l];
     // level 1: the nstageS-stage smoother; levels 2..grids: the nstageC-stage one
     const bool coarse = l >= 2;
@@ -546,7 +720,8 @@ static int smooth_f(Engine& E, int l, bool zero, bool want_res, bool restrict_in
             int rc;
             if (l == 2)
                 rc = launch_pdl("k_restrict_first_f", k_restrict_first_f<double>, grd, blk, 0, E.st, Dm1, F0, e,
-                                E.fRHS[l], (const double*)E.res[1], gf, op, g, l, g.nx, g.nz, mewtc1, ivis, sz);
+                                E.fRHS[l], res1 ? res1 : (const double*)E.res[1], gf, op, g, l, g.nx, g.nz, mewtc1,
+                                ivis, sz);
             else
                 rc = launch_pdl("k_restrict_first_f", k_restrict_first_f<float>, grd, blk, 0, E.st, Dm1, F0, e,
                                 E.fRHS[l], (const float*)E.fres[l - 1], gf, op, g, l, g.nx, g.nz, mewtc1, ivis, sz);
@@ -599,9 +774,29 @@ static int coarse_solve_f(Engine& E) {
 //         the same point (after the level-1 smoothing), as in the FP64 cycle;
 // part 1: the rest of the schedule on the correction, from the restriction of that FP64
 //         residual onwards; the closing prolongation (level 2 -> 1) is added to x in FP64.
-static int mixed_part(Engine& E, int part) {
+static int gcr_tail(Engine& E, int slot);
+
+// slot >= 0: the GCR form (krylov > 0) for direction slot `slot`: part 0 smooths the current
+// residual into z_slot and forms r - A e for the levels below; part 1 prolongates into z_slot
+// instead of x and ends with the GCR update of x and r (gcr_tail)
+static int mixed_part(Engine& E, int part, int slot = -1) {
     int rc;
     const Geo& g1 = E.gl[1];
+    const bool gcr = slot >= 0;
+    if (part == 0 && gcr) {
+        const size_t n1 = g1.elems();
+        if ((rc = launch_pdl("k_res_to_f32", k_res_to_f32, dim3(nblk(n1, 256)), dim3(256), 0, E.st, E.fRHS[1],
+                             (const double*)E.res[1], n1)))
+            return rc;
+        if ((rc = smooth_f(E, 1, true, false))) return rc;
+        dim3 blk(32, 4), grd(nblk(g1.nx - 1, 32), nblk(g1.nz - 1, 4));
+        return launch_pdl("k_gcr_first", k_gcr_first, grd, blk, 0, E.st, E.gz[slot], E.gr1, (const double*)E.res[1],
+                          (const float*)E.ferr[1], fop(E, 1), g1, g1.nx, g1.nz, E.cfg.ivis,
+                          E.cfg.Vbc == 0 ? -1.0 : 1.0);
+    }
+    // the level-1 residual the levels below see: r - A e
+    const double* r1 = gcr ? E.gr1 : E.res[1];
+    double* xdst = gcr ? E.gz[slot] : E.err[1];
     if (part == 0) {
         if ((rc = residual64(E, false, E.fRHS[1]))) return rc;
         if ((rc = smooth_f(E, 1, true, false))) return rc;
@@ -627,23 +822,25 @@ static int mixed_part(Engine& E, int part) {
             // the correction of level l restarts from zero: cleared by the first smoothing stage
             // (or overwritten whole by the coarse solve)
             if (l == 2)
-                rc = launch_pdl("k_restrict_f", k_restrict_f<double>, gr, dim3(128), 0, E.st, E.fRHS[l],
-                                (const double*)E.res[1], g, gf, g.nx, g.nz);
+                rc = launch_pdl("k_restrict_f", k_restrict_f<double>, gr, dim3(128), 0, E.st, E.fRHS[l], r1, g, gf,
+                                g.nx, g.nz);
             else
                 rc = launch_pdl("k_restrict_f", k_restrict_f<float>, gr, dim3(128), 0, E.st, E.fRHS[l],
                                 (const float*)E.fres[l - 1], g, gf, g.nx, g.nz);
             if (rc) return rc;
         }
         if (l < grids) {
-            if ((rc = smooth_f(E, l, descend, multi[p + 1] > multi[p], descend))) return rc;
+            if ((rc = smooth_f(E, l, descend, multi[p + 1] > multi[p], descend, r1))) return rc;
         } else if ((rc = coarse_solve_f(E))) {
             return rc;
         }
         if (multi[p + 1] < multi[p]) {
-            if (l == 2) {  // closing prolongation, added to x in FP64
-                return launch_pdl("k_prolong_add", k_prolong_add, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0,
-                                  E.st, E.err[1], (const float*)E.ferr[2], g1, g, g1.nx, g1.nz,
-                                  E.cfg.Vbc == 0 ? -1.0 : 1.0);
+            if (l == 2) {  // closing prolongation, added to x (or to z_slot) in FP64
+                if ((rc = launch_pdl("k_prolong_add", k_prolong_add, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128),
+                                     0, E.st, xdst, (const float*)E.ferr[2], g1, g, g1.nx, g1.nz,
+                                     E.cfg.Vbc == 0 ? -1.0 : 1.0)))
+                    return rc;
+                return gcr ? gcr_tail(E, slot) : 0;
             }
             const Geo& gf = E.gl[l - 1];
             if ((rc = launch_pdl("k_prolong_bc_f", k_prolong_bc_f, dim3(nblk(gf.nx - 1, 128), gf.nz - 1), dim3(128), 0,
@@ -653,6 +850,75 @@ static int mixed_part(Engine& E, int part) {
         }
     }
     return fail(PT_ERR_CONFIG, "mixed-precision cycle: schedule does not return to level 1");
+}
+
+// v_j = -A z_j (FP64), orthogonalisation against the slot's predecessors, then x += alpha z_j,
+// r += alpha v_j and the sum of |r| into dscal[8]
+static int gcr_tail(Engine& E, int slot) {
+    const Geo& g = E.gl[1];
+    int rc;
+    DOp op0{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.gzero};
+    if (E.res_int) {
+        dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
+        auto kern = E.resfx[1].square ? k_residual_fx<true> : k_residual_fx<false>;
+        rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.gv[slot], (float*)nullptr,
+                        (const double*)E.gz[slot], op0, g, g.nx, g.nz, E.cfg.ivis, E.resfx[1]);
+    } else {
+        dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
+        rc = launch_pdl("k_residual64", k_residual64, grd, blk, 0, E.st, E.gv[slot], (const double*)E.gz[slot], op0, g,
+                        g.nx, g.nz, E.cfg.ivis);
+    }
+    if (rc) return rc;
+    GcrSet S{};
+    for (int q = 0; q < slot; q++) {
+        S.v[q] = E.gv[q];
+        S.z[q] = E.gz[q];
+    }
+    const int R = g.nz + 2 * GH + 1;
+    if (slot > 0) {
+        if ((rc = launch_pdl("k_gcr_dots", k_gcr_dots, dim3(R), dim3(kGcrThreads), 0, E.st, (const double*)E.gv[slot], S,
+                             slot, g, g.nx, g.nz, E.gpart)))
+            return rc;
+        if ((rc = launch_pdl("k_gcr_coef", k_gcr_coef, dim3(1), dim3(kGcrThreads), 0, E.st, (const double*)E.gpart, R,
+                             slot, E.gsc)))
+            return rc;
+    }
+    if ((rc = launch_pdl("k_gcr_orth", k_gcr_orth, dim3(R), dim3(kGcrThreads), 0, E.st, E.gv[slot], E.gz[slot], S, slot,
+                         (const double*)E.gsc, (const double*)E.res[1], g, g.nx, g.nz, E.gpart)))
+        return rc;
+    if ((rc = launch_pdl("k_gcr_alpha", k_gcr_alpha, dim3(1), dim3(kGcrThreads), 0, E.st, (const double*)E.gpart, R,
+                         slot, E.gsc)))
+        return rc;
+    if ((rc = launch_pdl("k_gcr_update", k_gcr_update, dim3(R), dim3(kGcrThreads), 0, E.st, E.err[1], E.res[1],
+                         (const double*)E.gz[slot], (const double*)E.gv[slot], (const double*)E.gsc, g, g.nx, g.nz,
+                         E.gpart)))
+        return rc;
+    return launch_pdl("k_gcr_sum", k_gcr_sum, dim3(1), dim3(kGcrThreads), 0, E.st, (const double*)E.gpart, R,
+                      E.dscal + 8);
+}
+
+static int run_gcr(Engine& E, int part, int slot) {
+    cudaGraphExec_t& ex = part == 0 ? E.gG0[slot] : E.gG1[slot];
+    int64_t& n = part == 0 ? E.nG0[slot] : E.nG1[slot];
+    if (!ex) {
+        cudaGraph_t graph = nullptr;
+        int64_t before = g_launches.load();
+        CK(cudaStreamBeginCapture(E.st, cudaStreamCaptureModeThreadLocal));
+        int rc = mixed_part(E, part, slot);
+        cudaError_t e = cudaStreamEndCapture(E.st, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        CK(e);
+        CK(cudaGraphInstantiate(&ex, graph, 0));
+        cudaGraphDestroy(graph);
+        n = g_launches - before;
+        g_launches = before;
+    }
+    CK(cudaGraphLaunch(ex, E.st));
+    g_launches += n;
+    return 0;
 }
 
 static int run_mixed(Engine& E, int part) {
@@ -676,6 +942,71 @@ static int run_mixed(Engine& E, int part) {
     }
     CK(cudaGraphLaunch(ex, E.st));
     g_launches += n;
+    return 0;
+}
+
+// |r| / |RHS| of the current residual: the sum written to dscal[8], read back
+static int read_ratio(Engine& E, double norm, double* ratio) {
+    CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    *ratio = E.hscal[0] / norm / E.res_ref[1];
+    if (E.res_hist.size() < 100000) E.res_hist.push_back(*ratio);
+    if (!std::isfinite(*ratio)) return fail(PT_ERR_NOT_FINITE, "non-finite residual in the mixed-precision solve");
+    if (*ratio > 1.0e10) return fail(PT_ERR_MG_DIVERGED, "mixed-precision solve: abnormally high residual");
+    return 0;
+}
+
+// The GCR-accelerated solve (krylov = m > 0): the FP64 residual of the start, then per iteration
+// one preconditioning cycle and the GCR update (both captured graphs, slot j = iterations since
+// the last restart, restarted after m).  The updated residual is tested after every iteration;
+// when it passes, the residual is recomputed from x and tested again (a failed confirmation
+// restarts the directions from that residual).
+static int gcr_solve(Engine& E, pt_solve_info* info, double norm) {
+    int rc, cycles = 0, slot = 0;
+    double ratio = 0.0;
+    if ((rc = residual64(E, true)) || (rc = read_ratio(E, norm, &ratio))) return rc;
+    bool confirmed = ratio <= E.cfg.tolerance;
+    while (!confirmed) {
+        if (cycles >= E.cfg.max_cycles) return fail(PT_ERR_MG_MAX_CYCLES, "mixed-precision solve: too many cycles");
+        {
+            PhaseTimer tp(E, PH_CYCLE_L1);
+            if ((rc = run_gcr(E, 0, slot))) return rc;
+        }
+        {
+            PhaseTimer tp(E, PH_CYCLE_COARSE);
+            if ((rc = run_gcr(E, 1, slot))) return rc;
+        }
+        if ((rc = read_ratio(E, norm, &ratio))) return rc;
+        harvest_graph_timer(E, 1);
+        cycles++;
+        if (trace_on()) fprintf(stderr, "[ptgpu] gcr iteration %d residual ratio %.4e\n", cycles, ratio);
+        slot = (slot + 1) % E.cfg.krylov;
+        if (cycles == 1) {  // one iteration from a learned guess: keep it or restart from the previous psi
+            const int fb = unet_check_fallback(E, ratio);
+            if (fb < 0) return fail(PT_ERR_CUDA, "learned-guess fallback copy");
+            if (fb) {
+                if ((rc = residual64(E, true)) || (rc = read_ratio(E, norm, &ratio))) return rc;
+                slot = 0;
+                confirmed = ratio <= E.cfg.tolerance;
+                continue;
+            }
+        }
+        if (ratio <= E.cfg.tolerance) {  // confirm with the FP64 residual of x
+            if ((rc = residual64(E, true)) || (rc = read_ratio(E, norm, &ratio))) return rc;
+            confirmed = ratio <= E.cfg.tolerance;
+            slot = 0;
+        }
+    }
+    E.cycles = cycles;
+    E.refinements = cycles;
+    E.resid_ratio = ratio;
+    CK(cudaMemcpyAsync(E.SF, E.err[1], E.g1.elems() * 8, cudaMemcpyDeviceToDevice, E.st));
+    if (info) {
+        info->cycles += cycles;
+        info->resid_ratio = ratio;
+        info->n_eta = E.n_eta;
+        info->eig_fine = E.eig_fine;
+    }
     return 0;
 }
 
@@ -705,6 +1036,7 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
     int cycles = 0;
     double mag1 = 0.0;
     E.res_hist.clear();
+    if (E.cfg.krylov > 0) return gcr_solve(E, info, norm);
     for (;;) {
         {
             PhaseTimer tp(E, PH_CYCLE_L1);
@@ -759,6 +1091,21 @@ int multigrid_mixed(Engine& E, pt_solve_info* info) {
 
 int mixed_alloc(Engine& E) {
     if (E.res_int && !exact_stencils_setup(E)) return fail(PT_ERR_CUDA, "exact-stencil constants (mixed kernels)");
+    if (E.cfg.krylov > 0) {
+        const size_t n = E.g1.elems(), R = (size_t)E.g1.nz + 2 * GH + 1;
+        auto get = [&](double** p, size_t cnt) {
+            CK(cudaMalloc(p, cnt * sizeof(double)));
+            CK(cudaMemsetAsync(*p, 0, cnt * sizeof(double), E.st));
+            E.bytes_allocated += cnt * sizeof(double);
+            return 0;
+        };
+        int rc;
+        for (int j = 0; j < E.cfg.krylov; j++)
+            if ((rc = get(&E.gz[j], n)) || (rc = get(&E.gv[j], n))) return rc;
+        if ((rc = get(&E.gr1, n)) || (rc = get(&E.gzero, n)) || (rc = get(&E.gpart, (size_t)(kGcrMax + 2) * R)) ||
+            (rc = get(&E.gsc, 2 * kGcrMax + 1)))
+            return rc;
+    }
     for (int f = 0; f < 3; f++) {
         const size_t n = E.g1.elems();
         CK(cudaMalloc(&E.ftab[f], n * sizeof(float4)));
