@@ -314,6 +314,7 @@ __global__ void __launch_bounds__(256) k_residual_fx(double* __restrict__ res, f
                                                      int ivis, ResFxK K) {
     __shared__ int2 X[kRfHt][kRfW];
     __shared__ int emax_s;
+    pdl_begin();
     const int i0 = blockIdx.x * kRfTX + 1, k0 = blockIdx.y * kRfTZ + 1;
     const int emax = load_tile_fx<TileBig>(X, &emax_s, x, g, i0, k0, nx, nz);
 #pragma unroll 1
