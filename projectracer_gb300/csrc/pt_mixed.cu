@@ -475,9 +475,14 @@ __global__ void k_coarse_scatter_f(float* e, const double* B, Geo g, int nxc, in
 // ---------------------------------------------------------------- GCR acceleration (krylov > 0)
 // Flexible GCR with the mixed cycle as its preconditioner: per iteration j (direction slot j
 // since the last restart)
-//   z_j = M r        the level-1 FP32 smoothing of A e = r from zero, then the V-cycle below
-//                    level 1 on r - A e, prolongated (FP64 accumulation, ghost images included)
-//   v_j = -A z_j     FP64 operator (exact integer stencil sums)
+//   z_j = M r        the V-cycle below level 1 on r, prolongated: z_0 = P e_2 (FP64); then the
+//                    FP32 level-1 smoothing e_3 of A e = r_2, r_2 = r - A z_0 (FP64, exact
+//                    integer stencil sums), from zero: z_j = z_0 + e_3.  The smoothing comes last
+//                    because A applied to an unsmoothed prolongation is dominated by its grid-scale
+//                    interpolation error (the plain cycle, too, tests its residual after the level-1
+//                    smoothing, never right after a prolongation)
+//   v_j = -A z_j = (r_2 - A e_3) - r     (A e_3: FP32 stencil, FP64 update; e_3 was built from r_2,
+//                    so its rounding is relative to |r_2|)
 //   v_j -= sum_i c_i v_i,  z_j -= sum_i c_i z_i,  c_i = (v_j, v_i) / (v_i, v_i)    (i < j)
 //   alpha = -(r, v_j) / (v_j, v_j);   x += alpha z_j;   r += alpha v_j
 // so that r stays the residual of x (up to FP64 rounding) and |r| is minimised over the span of
@@ -632,17 +637,17 @@ __global__ void __launch_bounds__(kGcrThreads) k_gcr_sum(const double* __restric
     gcr_block_sums(a, 1, out, 0);
 }
 
-// z = e (FP64, with the ghost images) and r1 = r - A e (FP32 stencil, FP64 update): the start of
-// z_j = M r and the residual that the levels below 1 see
-__global__ void __launch_bounds__(128) k_gcr_first(double* __restrict__ z, double* __restrict__ r1,
-                                                   const double* __restrict__ r, const float* __restrict__ e, FOp op,
-                                                   Geo g, int nx, int nz, int ivis, double sz) {
+// z += e (FP64, with the ghost images) and v = (r2 - A e) - r: the end of z_j = M r and -A z_j
+__global__ void __launch_bounds__(128) k_gcr_post(double* __restrict__ z, double* __restrict__ v,
+                                                  const double* __restrict__ r, const double* __restrict__ r2,
+                                                  const float* __restrict__ e, FOp op, Geo g, int nx, int nz, int ivis,
+                                                  double sz) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx - 1 || k > nz - 1) return;
     const size_t o = g.at(i, k);
-    r1[o] = r[o] - (double)apply_A<float>(e, g, 1, op, i, k, ivis);
-    store_ghosts_d(z, g, i, k, nx, nz, (double)e[o], sz);
+    v[o] = (r2[o] - (double)apply_A<float>(e, g, 1, op, i, k, ivis)) - r[o];
+    store_ghosts_d(z, g, i, k, nx, nz, z[o] + (double)e[o], sz);
 }
 
 // FP64 level-1 residual (and optionally the sum of |r| into dscal[8])
@@ -777,26 +782,19 @@ static int coarse_solve_f(Engine& E) {
 //         residual onwards; the closing prolongation (level 2 -> 1) is added to x in FP64.
 static int gcr_tail(Engine& E, int slot);
 
-// slot >= 0: the GCR form (krylov > 0) for direction slot `slot`: part 0 smooths the current
-// residual into z_slot and forms r - A e for the levels below; part 1 prolongates into z_slot
-// instead of x and ends with the GCR update of x and r (gcr_tail)
+// slot >= 0: the GCR form (krylov > 0) for direction slot `slot` (part 1 runs first): part 1 is
+// the V-cycle below level 1 on the current residual, prolongated into z_slot = P e_2; part 0 the
+// level-1 smoothing of r - A z_slot added to z_slot, v_slot, and the GCR update of x and r
+// (gcr_tail)
 static int mixed_part(Engine& E, int part, int slot = -1) {
     int rc;
     const Geo& g1 = E.gl[1];
     const bool gcr = slot >= 0;
-    if (part == 0 && gcr) {
-        const size_t n1 = g1.elems();
-        if ((rc = launch_pdl("k_res_to_f32", k_res_to_f32, dim3(nblk(n1, 256)), dim3(256), 0, E.st, E.fRHS[1],
-                             (const double*)E.res[1], n1)))
-            return rc;
-        if ((rc = smooth_f(E, 1, true, false))) return rc;
-        dim3 blk(32, 4), grd(nblk(g1.nx - 1, 32), nblk(g1.nz - 1, 4));
-        return launch_pdl("k_gcr_first", k_gcr_first, grd, blk, 0, E.st, E.gz[slot], E.gr1, (const double*)E.res[1],
-                          (const float*)E.ferr[1], fop(E, 1), g1, g1.nx, g1.nz, E.cfg.ivis,
-                          E.cfg.Vbc == 0 ? -1.0 : 1.0);
-    }
-    // the level-1 residual the levels below see: r - A e
-    const double* r1 = gcr ? E.gr1 : E.res[1];
+    if (part == 0 && gcr) return gcr_tail(E, slot);
+    if (part == 1 && gcr) CK(cudaMemsetAsync(E.gz[slot], 0, g1.elems() * sizeof(double), E.st));
+    // the level-1 residual the levels below see (after the pre-smoothing of part 0, or the GCR
+    // residual) and where the closing prolongation goes
+    const double* r1 = E.res[1];
     double* xdst = gcr ? E.gz[slot] : E.err[1];
     if (part == 0) {
         if ((rc = residual64(E, false, E.fRHS[1]))) return rc;
@@ -841,7 +839,7 @@ static int mixed_part(Engine& E, int part, int slot = -1) {
                                      0, E.st, xdst, (const float*)E.ferr[2], g1, g, g1.nx, g1.nz,
                                      E.cfg.Vbc == 0 ? -1.0 : 1.0)))
                     return rc;
-                return gcr ? gcr_tail(E, slot) : 0;
+                return 0;
             }
             const Geo& gf = E.gl[l - 1];
             if ((rc = launch_pdl("k_prolong_bc_f", k_prolong_bc_f, dim3(nblk(gf.nx - 1, 128), gf.nz - 1), dim3(128), 0,
@@ -858,18 +856,31 @@ static int mixed_part(Engine& E, int part, int slot = -1) {
 static int gcr_tail(Engine& E, int slot) {
     const Geo& g = E.gl[1];
     int rc;
-    DOp op0{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.gzero};
+    // r2 = r - A z_0 in FP64 (and its FP32 copy, the right-hand side of the level-1 smoothing)
+    DOp opr{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.res[1]};
     if (E.res_int) {
         dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
         auto kern = E.resfx[1].square ? k_residual_fx<true> : k_residual_fx<false>;
-        rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.gv[slot], (float*)nullptr,
-                        (const double*)E.gz[slot], op0, g, g.nx, g.nz, E.cfg.ivis, E.resfx[1]);
+        rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.gr1, E.fRHS[1], (const double*)E.gz[slot], opr, g,
+                        g.nx, g.nz, E.cfg.ivis, E.resfx[1]);
     } else {
         dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
-        rc = launch_pdl("k_residual64", k_residual64, grd, blk, 0, E.st, E.gv[slot], (const double*)E.gz[slot], op0, g,
+        rc = launch_pdl("k_residual64", k_residual64, grd, blk, 0, E.st, E.gr1, (const double*)E.gz[slot], opr, g,
                         g.nx, g.nz, E.cfg.ivis);
+        const size_t n1 = g.elems();
+        if (!rc)
+            rc = launch_pdl("k_res_to_f32", k_res_to_f32, dim3(nblk(n1, 256)), dim3(256), 0, E.st, E.fRHS[1],
+                            (const double*)E.gr1, n1);
     }
     if (rc) return rc;
+    if ((rc = smooth_f(E, 1, true, false))) return rc;
+    {
+        dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
+        if ((rc = launch_pdl("k_gcr_post", k_gcr_post, grd, blk, 0, E.st, E.gz[slot], E.gv[slot],
+                             (const double*)E.res[1], (const double*)E.gr1, (const float*)E.ferr[1], fop(E, 1), g, g.nx,
+                             g.nz, E.cfg.ivis, E.cfg.Vbc == 0 ? -1.0 : 1.0)))
+            return rc;
+    }
     GcrSet S{};
     for (int q = 0; q < slot; q++) {
         S.v[q] = E.gv[q];
@@ -958,8 +969,8 @@ static int read_ratio(Engine& E, double norm, double* ratio) {
 }
 
 // The GCR-accelerated solve (krylov = m > 0): the FP64 residual of the start, then per iteration
-// one preconditioning cycle and the GCR update (both captured graphs, slot j = iterations since
-// the last restart, restarted after m).  The updated residual is tested after every iteration;
+// the preconditioning cycle (the levels below 1, then level 1) and the GCR update (two captured
+// graphs per slot j = iterations since the last restart, restarted after m).  The updated residual is tested after every iteration;
 // when it passes, the residual is recomputed from x and tested again (a failed confirmation
 // restarts the directions from that residual).
 static int gcr_solve(Engine& E, pt_solve_info* info, double norm) {
@@ -970,12 +981,12 @@ static int gcr_solve(Engine& E, pt_solve_info* info, double norm) {
     while (!confirmed) {
         if (cycles >= E.cfg.max_cycles) return fail(PT_ERR_MG_MAX_CYCLES, "mixed-precision solve: too many cycles");
         {
-            PhaseTimer tp(E, PH_CYCLE_L1);
-            if ((rc = run_gcr(E, 0, slot))) return rc;
-        }
-        {
             PhaseTimer tp(E, PH_CYCLE_COARSE);
             if ((rc = run_gcr(E, 1, slot))) return rc;
+        }
+        {
+            PhaseTimer tp(E, PH_CYCLE_L1);
+            if ((rc = run_gcr(E, 0, slot))) return rc;
         }
         if ((rc = read_ratio(E, norm, &ratio))) return rc;
         harvest_graph_timer(E, 1);
@@ -1103,7 +1114,7 @@ int mixed_alloc(Engine& E) {
         int rc;
         for (int j = 0; j < E.cfg.krylov; j++)
             if ((rc = get(&E.gz[j], n)) || (rc = get(&E.gv[j], n))) return rc;
-        if ((rc = get(&E.gr1, n)) || (rc = get(&E.gzero, n)) || (rc = get(&E.gpart, (size_t)(kGcrMax + 2) * R)) ||
+        if ((rc = get(&E.gr1, n)) || (rc = get(&E.gpart, (size_t)(kGcrMax + 2) * R)) ||
             (rc = get(&E.gsc, 2 * kGcrMax + 1)))
             return rc;
     }
