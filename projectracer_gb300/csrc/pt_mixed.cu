@@ -433,7 +433,9 @@ __device__ __forceinline__ void store_ghosts_d(double* out, Geo g, int i, int k,
 }
 
 // x += P e2 on the interior in FP64: the closing prolongation of a cycle (level 2 -> 1) fused
-// with the update, so the level-1 correction is never rounded to FP32
+// with the update, so the level-1 correction is never rounded to FP32.  SET: x = P e2 (the GCR
+// direction), with the ghost images; wall nodes are not written
+template <bool SET>
 __global__ void k_prolong_add(double* x, const float* C, Geo gf, Geo gc, int nxf, int nzf, double sz) {
     pdl_begin();
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y + 1;
@@ -446,7 +448,7 @@ __global__ void k_prolong_add(double* x, const float* C, Geo gf, Geo gc, int nxf
         add = ((double)C[gc.at((i - 1) / 2, (k - 1) / 2)] + (double)C[gc.at((i + 1) / 2, (k - 1) / 2)] +
                (double)C[gc.at((i + 1) / 2, (k + 1) / 2)] + (double)C[gc.at((i - 1) / 2, (k + 1) / 2)]) * 0.25;
     size_t o = gf.at(i, k);
-    store_ghosts_d(x, gf, i, k, nxf, nzf, x[o] + add, sz);
+    store_ghosts_d(x, gf, i, k, nxf, nzf, SET ? add : x[o] + add, sz);
 }
 
 // x += e on the interior (FP64 accumulate of the FP32 correction), with the ghost images
@@ -486,22 +488,26 @@ __global__ void k_coarse_scatter_f(float* e, const double* B, Geo g, int nxc, in
 //   v_j -= sum_i c_i v_i,  z_j -= sum_i c_i z_i,  c_i = (v_j, v_i) / (v_i, v_i)    (i < j)
 //   alpha = -(r, v_j) / (v_j, v_j);   x += alpha z_j;   r += alpha v_j
 // so that r stays the residual of x (up to FP64 rounding) and |r| is minimised over the span of
-// the directions.  Dot products are per-row partial sums (one CTA per padded row, interior nodes
-// only) reduced in a fixed order: the iteration is deterministic.  The scalars stay on the
-// device: gsc = [|v_i|^2 (kGcrMax) | c_i (kGcrMax) | alpha].
+// the directions.  Three kernels after the smoothing, one CTA per padded grid row: k_gcr_post
+// (z_j, v_j, the dots (v_j, v_i)), k_gcr_orth (the orthogonalisation, (v_j, v_j), (r, v_j)) and
+// k_gcr_update (x, r, sum |r|).  Each writes per-row partial sums over the interior nodes, and its
+// last CTA to finish (a counter, reset by that CTA) reduces them in row order into the device
+// scalars gsc = [|v_i|^2 (kGcrMax) | c_i (kGcrMax) | alpha | sum |r|]: the iteration is
+// deterministic and the scalars never leave the device.
 struct GcrSet {
     const double* v[kGcrMax];
     double* z[kGcrMax];
 };
 constexpr int kGcrThreads = 256;
+constexpr int kGcrScAlpha = 2 * kGcrMax, kGcrScRes = 2 * kGcrMax + 1, kGcrSc = 2 * kGcrMax + 2;
 
-// block sum of nq (<= kGcrMax + 2) per-thread values, in a fixed order; thread 0 writes
+// block sum of nq (<= kGcrMax) per-thread values, in a fixed order; thread 0 writes
 // out[q * stride]
-__device__ __forceinline__ void gcr_block_sums(double* a, int nq, double* out, int stride) {
-    __shared__ double sh[kGcrThreads / 32][kGcrMax + 2];
+__device__ __forceinline__ void gcr_block_sums(const double* a, int nq, double* out, int stride) {
+    __shared__ double sh[kGcrThreads / 32][kGcrMax];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < kGcrMax + 2; q++) {
+    for (int q = 0; q < kGcrMax; q++) {
         if (q >= nq) break;
         double v = a[q];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -516,46 +522,89 @@ __device__ __forceinline__ void gcr_block_sums(double* a, int nq, double* out, i
         }
 }
 
-// per padded row b: partial dots (vn, v_i) over the interior, i < nk -> part[i * R + b]
-__global__ void __launch_bounds__(kGcrThreads) k_gcr_dots(const double* __restrict__ vn, GcrSet S, int nk, Geo g,
-                                                          int nx, int nz, double* part) {
+// After the CTA's partials are written: true in the last CTA of the grid to get here (it then
+// sees every CTA's partials); that CTA resets the counter for the next launch.
+__device__ __forceinline__ bool gcr_last_block(unsigned* count) {
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(count, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        if (threadIdx.x == 0) *count = 0u;
+    }
+    return last;
+}
+
+// the totals of nq partial planes part[q * R + b] (b < R) in row order into tot[q] (all threads)
+__device__ __forceinline__ void gcr_totals(const double* part, int R, int nq, double* tot) {
+    double a[kGcrMax] = {};
+#pragma unroll
+    for (int q = 0; q < kGcrMax; q++)
+        if (q < nq)
+            for (int b = threadIdx.x; b < R; b += kGcrThreads) a[q] += __ldcg(part + (size_t)q * R + b);
+    gcr_block_sums(a, nq, tot, 1);
+    __syncthreads();
+}
+
+// alpha from the totals (v_j, v_j), (r, v_j): |v_j|^2 -> sc[j], alpha -> sc[kGcrScAlpha] (0 for a
+// vanishing or non-finite direction)
+__device__ __forceinline__ void gcr_alpha(const double* tot, int j, double* sc) {
+    if (threadIdx.x == 0) {
+        const double n2 = tot[0];
+        const bool ok = n2 > 0.0 && isfinite(n2) && isfinite(tot[1]);
+        sc[j] = ok ? n2 : 0.0;
+        sc[kGcrScAlpha] = ok ? -tot[1] / n2 : 0.0;
+    }
+}
+
+// z += e (FP64, with the ghost images) and v = (r2 - A e) - r: the end of z_j = M r and -A z_j.
+// nk > 0: partial dots (v, v_i), i < nk, then (last CTA) c_i = (v, v_i) / |v_i|^2;
+// nk = 0: partial (v, v) and (r, v), then (last CTA) alpha.
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_post(double* __restrict__ z, double* __restrict__ v,
+                                                          const double* __restrict__ r, const double* __restrict__ r2,
+                                                          const float* __restrict__ e, FOp op, GcrSet S, int nk,
+                                                          Geo g, int nx, int nz, int ivis, double sz, double* part,
+                                                          double* sc, unsigned* count) {
     pdl_begin();
     const int R = gridDim.x, b = blockIdx.x, k = b - GH;
     double a[kGcrMax] = {};
     if (k >= 1 && k <= nz - 1)
         for (int i = 1 + threadIdx.x; i <= nx - 1; i += kGcrThreads) {
             const size_t o = g.at(i, k);
-            const double v = vn[o];
+            const double rv = r[o];
+            const double vv = (r2[o] - (double)apply_A<float>(e, g, 1, op, i, k, ivis)) - rv;
+            v[o] = vv;
+            store_ghosts_d(z, g, i, k, nx, nz, z[o] + (double)e[o], sz);
+            if (nk == 0) {
+                a[0] += vv * vv;
+                a[1] += rv * vv;
+            } else {
 #pragma unroll
-            for (int q = 0; q < kGcrMax; q++)
-                if (q < nk) a[q] += v * S.v[q][o];
+                for (int q = 0; q < kGcrMax; q++)
+                    if (q < nk) a[q] += vv * S.v[q][o];
+            }
         }
-    gcr_block_sums(a, nk, part + b, R);
-}
-
-// c_i = (sum over rows of part[i]) / |v_i|^2 into sc[kGcrMax + i]
-__global__ void __launch_bounds__(kGcrThreads) k_gcr_coef(const double* __restrict__ part, int R, int nk, double* sc) {
-    pdl_begin();
-    double a[kGcrMax] = {};
-#pragma unroll
-    for (int q = 0; q < kGcrMax; q++)
-        if (q < nk)
-            for (int b = threadIdx.x; b < R; b += kGcrThreads) a[q] += part[(size_t)q * R + b];
+    const int nq = nk == 0 ? 2 : nk;
+    gcr_block_sums(a, nq, part + b, R);
+    if (!gcr_last_block(count)) return;
     __shared__ double tot[kGcrMax];
-    gcr_block_sums(a, nk, tot, 1);
-    __syncthreads();
-    if (threadIdx.x < (unsigned)nk) {
+    gcr_totals(part, R, nq, tot);
+    if (nk == 0) {
+        gcr_alpha(tot, 0, sc);
+    } else if (threadIdx.x < (unsigned)nk) {
         const double n2 = sc[threadIdx.x];
         sc[kGcrMax + threadIdx.x] = n2 > 0.0 ? tot[threadIdx.x] / n2 : 0.0;
     }
 }
 
 // vn -= sum c_i v_i, zn -= sum c_i z_i over the whole padded row (ghost images stay images);
-// then partial (vn, vn) -> part[b], (r, vn) -> part[R + b] over the interior
+// partial (vn, vn) and (r, vn) over the interior, then (last CTA) alpha for slot nk
 __global__ void __launch_bounds__(kGcrThreads) k_gcr_orth(double* __restrict__ vn, double* __restrict__ zn, GcrSet S,
-                                                          int nk, const double* __restrict__ sc,
-                                                          const double* __restrict__ r, Geo g, int nx, int nz,
-                                                          double* part) {
+                                                          int nk, double* sc, const double* __restrict__ r, Geo g,
+                                                          int nx, int nz, double* part, unsigned* count) {
     pdl_begin();
     const int R = gridDim.x, b = blockIdx.x, k = b - GH;
     double c[kGcrMax];
@@ -565,18 +614,15 @@ __global__ void __launch_bounds__(kGcrThreads) k_gcr_orth(double* __restrict__ v
     const size_t row = (size_t)b * g.pitch;
     for (int col = threadIdx.x; col < g.pitch; col += kGcrThreads) {
         const size_t o = row + col;
-        double v = vn[o];
-        if (nk > 0) {
-            double z = zn[o];
+        double v = vn[o], z = zn[o];
 #pragma unroll
-            for (int q = 0; q < kGcrMax; q++)
-                if (q < nk) {
-                    v -= c[q] * S.v[q][o];
-                    z -= c[q] * S.z[q][o];
-                }
-            vn[o] = v;
-            zn[o] = z;
-        }
+        for (int q = 0; q < kGcrMax; q++)
+            if (q < nk) {
+                v -= c[q] * S.v[q][o];
+                z -= c[q] * S.z[q][o];
+            }
+        vn[o] = v;
+        zn[o] = z;
         const int i = col - GH;
         if (k >= 1 && k <= nz - 1 && i >= 1 && i <= nx - 1) {
             a[0] += v * v;
@@ -584,36 +630,21 @@ __global__ void __launch_bounds__(kGcrThreads) k_gcr_orth(double* __restrict__ v
         }
     }
     gcr_block_sums(a, 2, part + b, R);
-}
-
-// |v_j|^2 -> sc[j];  alpha = -(r, v_j) / |v_j|^2 -> sc[2 kGcrMax] (0 for a vanishing direction)
-__global__ void __launch_bounds__(kGcrThreads) k_gcr_alpha(const double* __restrict__ part, int R, int j, double* sc) {
-    pdl_begin();
-    double a[2] = {0.0, 0.0};
-    for (int b = threadIdx.x; b < R; b += kGcrThreads) {
-        a[0] += part[b];
-        a[1] += part[R + b];
-    }
+    if (!gcr_last_block(count)) return;
     __shared__ double tot[2];
-    gcr_block_sums(a, 2, tot, 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const double n2 = tot[0];
-        const bool ok = n2 > 0.0 && isfinite(n2) && isfinite(tot[1]);
-        sc[j] = ok ? n2 : 0.0;
-        sc[2 * kGcrMax] = ok ? -tot[1] / n2 : 0.0;
-    }
+    gcr_totals(part, R, 2, tot);
+    gcr_alpha(tot, nk, sc);
 }
 
-// x += alpha z (whole padded row), r += alpha v (interior), partial sum |r| -> part[b]
+// x += alpha z (whole padded row), r += alpha v (interior); partial sum |r|, then (last CTA) the
+// total into sc[kGcrScRes]
 __global__ void __launch_bounds__(kGcrThreads) k_gcr_update(double* __restrict__ x, double* __restrict__ r,
                                                             const double* __restrict__ zn,
-                                                            const double* __restrict__ vn,
-                                                            const double* __restrict__ sc, Geo g, int nx, int nz,
-                                                            double* part) {
+                                                            const double* __restrict__ vn, double* sc, Geo g, int nx,
+                                                            int nz, double* part, unsigned* count) {
     pdl_begin();
-    const int b = blockIdx.x, k = b - GH;
-    const double al = sc[2 * kGcrMax];
+    const int R = gridDim.x, b = blockIdx.x, k = b - GH;
+    const double al = sc[kGcrScAlpha];
     double a[1] = {0.0};
     const size_t row = (size_t)b * g.pitch;
     for (int col = threadIdx.x; col < g.pitch; col += kGcrThreads) {
@@ -626,28 +657,11 @@ __global__ void __launch_bounds__(kGcrThreads) k_gcr_update(double* __restrict__
             a[0] += fabs(rv);
         }
     }
-    gcr_block_sums(a, 1, part + b, 0);
-}
-
-// the sum of the R row partials of |r| into *out
-__global__ void __launch_bounds__(kGcrThreads) k_gcr_sum(const double* __restrict__ part, int R, double* out) {
-    pdl_begin();
-    double a[1] = {0.0};
-    for (int b = threadIdx.x; b < R; b += kGcrThreads) a[0] += part[b];
-    gcr_block_sums(a, 1, out, 0);
-}
-
-// z += e (FP64, with the ghost images) and v = (r2 - A e) - r: the end of z_j = M r and -A z_j
-__global__ void __launch_bounds__(128) k_gcr_post(double* __restrict__ z, double* __restrict__ v,
-                                                  const double* __restrict__ r, const double* __restrict__ r2,
-                                                  const float* __restrict__ e, FOp op, Geo g, int nx, int nz, int ivis,
-                                                  double sz) {
-    pdl_begin();
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i > nx - 1 || k > nz - 1) return;
-    const size_t o = g.at(i, k);
-    v[o] = (r2[o] - (double)apply_A<float>(e, g, 1, op, i, k, ivis)) - r[o];
-    store_ghosts_d(z, g, i, k, nx, nz, z[o] + (double)e[o], sz);
+    gcr_block_sums(a, 1, part + b, R);
+    if (!gcr_last_block(count)) return;
+    __shared__ double tot[1];
+    gcr_totals(part, R, 1, tot);
+    if (threadIdx.x == 0) sc[kGcrScRes] = tot[0];
 }
 
 // FP64 level-1 residual (and optionally the sum of |r| into dscal[8])
@@ -791,7 +805,6 @@ static int mixed_part(Engine& E, int part, int slot = -1) {
     const Geo& g1 = E.gl[1];
     const bool gcr = slot >= 0;
     if (part == 0 && gcr) return gcr_tail(E, slot);
-    if (part == 1 && gcr) CK(cudaMemsetAsync(E.gz[slot], 0, g1.elems() * sizeof(double), E.st));
     // the level-1 residual the levels below see (after the pre-smoothing of part 0, or the GCR
     // residual) and where the closing prolongation goes
     const double* r1 = E.res[1];
@@ -835,11 +848,10 @@ static int mixed_part(Engine& E, int part, int slot = -1) {
         }
         if (multi[p + 1] < multi[p]) {
             if (l == 2) {  // closing prolongation, added to x (or to z_slot) in FP64
-                if ((rc = launch_pdl("k_prolong_add", k_prolong_add, dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128),
-                                     0, E.st, xdst, (const float*)E.ferr[2], g1, g, g1.nx, g1.nz,
-                                     E.cfg.Vbc == 0 ? -1.0 : 1.0)))
-                    return rc;
-                return 0;
+                // GCR: z_slot = P e_2 is written, not added (its wall nodes are zero in every direction)
+                return launch_pdl("k_prolong_add", gcr ? k_prolong_add<true> : k_prolong_add<false>,
+                                  dim3(nblk(g1.nx - 1, 128), g1.nz - 1), dim3(128), 0, E.st, xdst,
+                                  (const float*)E.ferr[2], g1, g, g1.nx, g1.nz, E.cfg.Vbc == 0 ? -1.0 : 1.0);
             }
             const Geo& gf = E.gl[l - 1];
             if ((rc = launch_pdl("k_prolong_bc_f", k_prolong_bc_f, dim3(nblk(gf.nx - 1, 128), gf.nz - 1), dim3(128), 0,
@@ -874,39 +886,22 @@ static int gcr_tail(Engine& E, int slot) {
     }
     if (rc) return rc;
     if ((rc = smooth_f(E, 1, true, false))) return rc;
-    {
-        dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
-        if ((rc = launch_pdl("k_gcr_post", k_gcr_post, grd, blk, 0, E.st, E.gz[slot], E.gv[slot],
-                             (const double*)E.res[1], (const double*)E.gr1, (const float*)E.ferr[1], fop(E, 1), g, g.nx,
-                             g.nz, E.cfg.ivis, E.cfg.Vbc == 0 ? -1.0 : 1.0)))
-            return rc;
-    }
     GcrSet S{};
     for (int q = 0; q < slot; q++) {
         S.v[q] = E.gv[q];
         S.z[q] = E.gz[q];
     }
     const int R = g.nz + 2 * GH + 1;
-    if (slot > 0) {
-        if ((rc = launch_pdl("k_gcr_dots", k_gcr_dots, dim3(R), dim3(kGcrThreads), 0, E.st, (const double*)E.gv[slot], S,
-                             slot, g, g.nx, g.nz, E.gpart)))
-            return rc;
-        if ((rc = launch_pdl("k_gcr_coef", k_gcr_coef, dim3(1), dim3(kGcrThreads), 0, E.st, (const double*)E.gpart, R,
-                             slot, E.gsc)))
-            return rc;
-    }
-    if ((rc = launch_pdl("k_gcr_orth", k_gcr_orth, dim3(R), dim3(kGcrThreads), 0, E.st, E.gv[slot], E.gz[slot], S, slot,
-                         (const double*)E.gsc, (const double*)E.res[1], g, g.nx, g.nz, E.gpart)))
+    unsigned* cnt = reinterpret_cast<unsigned*>(E.gsc + kGcrSc);
+    if ((rc = launch_pdl("k_gcr_post", k_gcr_post, dim3(R), dim3(kGcrThreads), 0, E.st, E.gz[slot], E.gv[slot],
+                         (const double*)E.res[1], (const double*)E.gr1, (const float*)E.ferr[1], fop(E, 1), S, slot, g,
+                         g.nx, g.nz, E.cfg.ivis, E.cfg.Vbc == 0 ? -1.0 : 1.0, E.gpart, E.gsc, cnt)))
         return rc;
-    if ((rc = launch_pdl("k_gcr_alpha", k_gcr_alpha, dim3(1), dim3(kGcrThreads), 0, E.st, (const double*)E.gpart, R,
-                         slot, E.gsc)))
+    if (slot > 0 && (rc = launch_pdl("k_gcr_orth", k_gcr_orth, dim3(R), dim3(kGcrThreads), 0, E.st, E.gv[slot],
+                                     E.gz[slot], S, slot, E.gsc, (const double*)E.res[1], g, g.nx, g.nz, E.gpart, cnt)))
         return rc;
-    if ((rc = launch_pdl("k_gcr_update", k_gcr_update, dim3(R), dim3(kGcrThreads), 0, E.st, E.err[1], E.res[1],
-                         (const double*)E.gz[slot], (const double*)E.gv[slot], (const double*)E.gsc, g, g.nx, g.nz,
-                         E.gpart)))
-        return rc;
-    return launch_pdl("k_gcr_sum", k_gcr_sum, dim3(1), dim3(kGcrThreads), 0, E.st, (const double*)E.gpart, R,
-                      E.dscal + 8);
+    return launch_pdl("k_gcr_update", k_gcr_update, dim3(R), dim3(kGcrThreads), 0, E.st, E.err[1], E.res[1],
+                      (const double*)E.gz[slot], (const double*)E.gv[slot], E.gsc, g, g.nx, g.nz, E.gpart, cnt);
 }
 
 static int run_gcr(Engine& E, int part, int slot) {
@@ -958,8 +953,8 @@ static int run_mixed(Engine& E, int part) {
 }
 
 // |r| / |RHS| of the current residual: the sum written to dscal[8], read back
-static int read_ratio(Engine& E, double norm, double* ratio) {
-    CK(cudaMemcpyAsync(E.hscal, E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
+static int read_ratio(Engine& E, double norm, double* ratio, const double* sum = nullptr) {
+    CK(cudaMemcpyAsync(E.hscal, sum ? sum : E.dscal + 8, 8, cudaMemcpyDeviceToHost, E.st));
     CK(cudaStreamSynchronize(E.st));
     *ratio = E.hscal[0] / norm / E.res_ref[1];
     if (E.res_hist.size() < 100000) E.res_hist.push_back(*ratio);
@@ -988,7 +983,7 @@ static int gcr_solve(Engine& E, pt_solve_info* info, double norm) {
             PhaseTimer tp(E, PH_CYCLE_L1);
             if ((rc = run_gcr(E, 0, slot))) return rc;
         }
-        if ((rc = read_ratio(E, norm, &ratio))) return rc;
+        if ((rc = read_ratio(E, norm, &ratio, E.gsc + kGcrScRes))) return rc;
         harvest_graph_timer(E, 1);
         cycles++;
         if (trace_on()) fprintf(stderr, "[ptgpu] gcr iteration %d residual ratio %.4e\n", cycles, ratio);
@@ -1115,7 +1110,7 @@ int mixed_alloc(Engine& E) {
         for (int j = 0; j < E.cfg.krylov; j++)
             if ((rc = get(&E.gz[j], n)) || (rc = get(&E.gv[j], n))) return rc;
         if ((rc = get(&E.gr1, n)) || (rc = get(&E.gpart, (size_t)(kGcrMax + 2) * R)) ||
-            (rc = get(&E.gsc, 2 * kGcrMax + 1)))
+            (rc = get(&E.gsc, kGcrSc + 1)))  // the scalars, then the last-CTA counter
             return rc;
     }
     for (int f = 0; f < 3; f++) {
