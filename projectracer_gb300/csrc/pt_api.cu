@@ -265,7 +265,7 @@ static void engine_free(Engine& E) {
         if (E.gz[j]) cudaFree(E.gz[j]);
         if (E.gv[j]) cudaFree(E.gv[j]);
     }
-    for (double* p : {E.gr1, E.gpart, E.gsc})
+    for (double* p : {E.gr1, E.gzero, E.gpart, E.gsc})
         if (p) cudaFree(p);
     if (E.gA) cudaGraphExecDestroy(E.gA);
     if (E.gB) cudaGraphExecDestroy(E.gB);

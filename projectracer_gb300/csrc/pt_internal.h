@@ -130,11 +130,11 @@ struct Engine {
     cudaGraphExec_t gM1 = nullptr, gM2 = nullptr;
     int64_t nM1 = 0, nM2 = 0;
     // GCR acceleration of the mixed solve (krylov > 0): search directions z_j (FP64, with their
-    // ghost images) and v_j = -A z_j, the residual r - A P e_2 that the level-1 smoothing sees,
-    // per-row partial sums and the device scalars [|v_j|^2 (kGcrMax) | c_j (kGcrMax) | alpha];
-    // one pair of captured graphs per direction slot
+    // ghost images) and v_j = -A z_j, the residual r - A P e_2 that the level-1 smoothing sees, a
+    // zero right-hand side, per-row partial sums and the device scalars [|v_j|^2 (kGcrMax) | c_j
+    // (kGcrMax) | alpha | sum |r| | last-CTA counter]; one pair of captured graphs per slot
     double *gz[kGcrMax] = {}, *gv[kGcrMax] = {};
-    double *gr1 = nullptr, *gpart = nullptr, *gsc = nullptr;
+    double *gr1 = nullptr, *gzero = nullptr, *gpart = nullptr, *gsc = nullptr;
     cudaGraphExec_t gG0[kGcrMax] = {}, gG1[kGcrMax] = {};
     int64_t nG0[kGcrMax] = {}, nG1[kGcrMax] = {};
     double* psi_keep = nullptr;

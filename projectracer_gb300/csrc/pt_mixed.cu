@@ -483,14 +483,15 @@ __global__ void k_coarse_scatter_f(float* e, const double* B, Geo g, int nxc, in
 //                    because A applied to an unsmoothed prolongation is dominated by its grid-scale
 //                    interpolation error (the plain cycle, too, tests its residual after the level-1
 //                    smoothing, never right after a prolongation)
-//   v_j = -A z_j = (r_2 - A e_3) - r     (A e_3: FP32 stencil, FP64 update; e_3 was built from r_2,
-//                    so its rounding is relative to |r_2|)
+//   v_j = -A z_j     FP64, exact integer stencil sums on z_j: v_j must be exact to FP64 rounding,
+//                    since r is only ever updated through it (an FP32 A e_3 makes r drift from the
+//                    true residual by ~1e-4 of the starting residual over a solve at 1024x512)
 //   v_j -= sum_i c_i v_i,  z_j -= sum_i c_i z_i,  c_i = (v_j, v_i) / (v_i, v_i)    (i < j)
 //   alpha = -(r, v_j) / (v_j, v_j);   x += alpha z_j;   r += alpha v_j
 // so that r stays the residual of x (up to FP64 rounding) and |r| is minimised over the span of
-// the directions.  Three kernels after the smoothing, one CTA per padded grid row: k_gcr_post
-// (z_j, v_j, the dots (v_j, v_i)), k_gcr_orth (the orthogonalisation, (v_j, v_j), (r, v_j)) and
-// k_gcr_update (x, r, sum |r|).  Each writes per-row partial sums over the interior nodes, and its
+// the directions.  After the smoothing: k_gcr_zadd (z_j), the exact residual kernel (v_j), then
+// one CTA per padded grid row: k_gcr_dots (the dots (v_j, v_i)), k_gcr_orth (the
+// orthogonalisation, (v_j, v_j), (r, v_j)) and k_gcr_update (x, r, sum |r|).  Each writes per-row partial sums over the interior nodes, and its
 // last CTA to finish (a counter, reset by that CTA) reduces them in row order into the device
 // scalars gsc = [|v_i|^2 (kGcrMax) | c_i (kGcrMax) | alpha | sum |r|]: the iteration is
 // deterministic and the scalars never leave the device.
@@ -560,13 +561,20 @@ __device__ __forceinline__ void gcr_alpha(const double* tot, int j, double* sc) 
     }
 }
 
-// z += e (FP64, with the ghost images) and v = (r2 - A e) - r: the end of z_j = M r and -A z_j.
+// z += e (FP64, with the ghost images): the end of z_j = M r
+__global__ void __launch_bounds__(128) k_gcr_zadd(double* __restrict__ z, const float* __restrict__ e, Geo g, int nx,
+                                                  int nz, double sz) {
+    pdl_begin();
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx - 1 || k > nz - 1) return;
+    const size_t o = g.at(i, k);
+    store_ghosts_d(z, g, i, k, nx, nz, z[o] + (double)e[o], sz);
+}
+
 // nk > 0: partial dots (v, v_i), i < nk, then (last CTA) c_i = (v, v_i) / |v_i|^2;
 // nk = 0: partial (v, v) and (r, v), then (last CTA) alpha.
-__global__ void __launch_bounds__(kGcrThreads) k_gcr_post(double* __restrict__ z, double* __restrict__ v,
-                                                          const double* __restrict__ r, const double* __restrict__ r2,
-                                                          const float* __restrict__ e, FOp op, GcrSet S, int nk,
-                                                          Geo g, int nx, int nz, int ivis, double sz, double* part,
+__global__ void __launch_bounds__(kGcrThreads) k_gcr_dots(const double* __restrict__ v, const double* __restrict__ r,
+                                                          GcrSet S, int nk, Geo g, int nx, int nz, double* part,
                                                           double* sc, unsigned* count) {
     pdl_begin();
     const int R = gridDim.x, b = blockIdx.x, k = b - GH;
@@ -574,13 +582,10 @@ __global__ void __launch_bounds__(kGcrThreads) k_gcr_post(double* __restrict__ z
     if (k >= 1 && k <= nz - 1)
         for (int i = 1 + threadIdx.x; i <= nx - 1; i += kGcrThreads) {
             const size_t o = g.at(i, k);
-            const double rv = r[o];
-            const double vv = (r2[o] - (double)apply_A<float>(e, g, 1, op, i, k, ivis)) - rv;
-            v[o] = vv;
-            store_ghosts_d(z, g, i, k, nx, nz, z[o] + (double)e[o], sz);
+            const double vv = v[o];
             if (nk == 0) {
                 a[0] += vv * vv;
-                a[1] += rv * vv;
+                a[1] += r[o] * vv;
             } else {
 #pragma unroll
                 for (int q = 0; q < kGcrMax; q++)
@@ -886,6 +891,25 @@ static int gcr_tail(Engine& E, int slot) {
     }
     if (rc) return rc;
     if ((rc = smooth_f(E, 1, true, false))) return rc;
+    {
+        dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
+        if ((rc = launch_pdl("k_gcr_zadd", k_gcr_zadd, grd, blk, 0, E.st, E.gz[slot], (const float*)E.ferr[1], g, g.nx,
+                             g.nz, E.cfg.Vbc == 0 ? -1.0 : 1.0)))
+            return rc;
+    }
+    // v_j = 0 - A z_j
+    DOp op0{E.vis[1], E.vx[1], E.vz[1], E.vxz[1], E.vxxmzz[1], E.gzero};
+    if (E.res_int) {
+        dim3 blk(kRfTX, 8), grd(nblk(g.nx - 1, kRfTX), nblk(g.nz - 1, kRfTZ));
+        auto kern = E.resfx[1].square ? k_residual_fx<true> : k_residual_fx<false>;
+        rc = launch_pdl("k_residual_fx", kern, grd, blk, 0, E.st, E.gv[slot], (float*)nullptr,
+                        (const double*)E.gz[slot], op0, g, g.nx, g.nz, E.cfg.ivis, E.resfx[1]);
+    } else {
+        dim3 blk(32, 4), grd(nblk(g.nx - 1, 32), nblk(g.nz - 1, 4));
+        rc = launch_pdl("k_residual64", k_residual64, grd, blk, 0, E.st, E.gv[slot], (const double*)E.gz[slot], op0, g,
+                        g.nx, g.nz, E.cfg.ivis);
+    }
+    if (rc) return rc;
     GcrSet S{};
     for (int q = 0; q < slot; q++) {
         S.v[q] = E.gv[q];
@@ -893,9 +917,8 @@ static int gcr_tail(Engine& E, int slot) {
     }
     const int R = g.nz + 2 * GH + 1;
     unsigned* cnt = reinterpret_cast<unsigned*>(E.gsc + kGcrSc);
-    if ((rc = launch_pdl("k_gcr_post", k_gcr_post, dim3(R), dim3(kGcrThreads), 0, E.st, E.gz[slot], E.gv[slot],
-                         (const double*)E.res[1], (const double*)E.gr1, (const float*)E.ferr[1], fop(E, 1), S, slot, g,
-                         g.nx, g.nz, E.cfg.ivis, E.cfg.Vbc == 0 ? -1.0 : 1.0, E.gpart, E.gsc, cnt)))
+    if ((rc = launch_pdl("k_gcr_dots", k_gcr_dots, dim3(R), dim3(kGcrThreads), 0, E.st, (const double*)E.gv[slot],
+                         (const double*)E.res[1], S, slot, g, g.nx, g.nz, E.gpart, E.gsc, cnt)))
         return rc;
     if (slot > 0 && (rc = launch_pdl("k_gcr_orth", k_gcr_orth, dim3(R), dim3(kGcrThreads), 0, E.st, E.gv[slot],
                                      E.gz[slot], S, slot, E.gsc, (const double*)E.res[1], g, g.nx, g.nz, E.gpart, cnt)))
@@ -1109,7 +1132,7 @@ int mixed_alloc(Engine& E) {
         int rc;
         for (int j = 0; j < E.cfg.krylov; j++)
             if ((rc = get(&E.gz[j], n)) || (rc = get(&E.gv[j], n))) return rc;
-        if ((rc = get(&E.gr1, n)) || (rc = get(&E.gpart, (size_t)(kGcrMax + 2) * R)) ||
+        if ((rc = get(&E.gr1, n)) || (rc = get(&E.gzero, n)) || (rc = get(&E.gpart, (size_t)(kGcrMax + 2) * R)) ||
             (rc = get(&E.gsc, kGcrSc + 1)))  // the scalars, then the last-CTA counter
             return rc;
     }
