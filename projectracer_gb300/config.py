@@ -191,8 +191,13 @@ class PtConfig(ctypes.Structure):
 
 WORKLOADS = {
     # 128x128, isoviscous, Ra_T=1e5, Ra_C=0, H=0, 20 tracers per cell, Courant 0.5, 100 steps
+    # (mixed precision: the 1024x512 method's V-cycle and smoother, GCR with 8 directions around
+    # it, which at 1e-8 needs 5.9 instead of 9.3 cycles per solve; the FP64 path keeps the
+    # reference's solver)
     "C1": dict(nx=128, nz=128, aspect=1.0, RaT=1e5, RaC=0.0, comp=0, ivis=0, visT=1.0, visP=1.0,
-               tpc=20, courant=0.5, tolerance=1e-8, steps=100),
+               tpc=20, courant=0.5, tolerance=1e-8, steps=100,
+               mg_cycle=PT_CYCLE_V, mixed_nstageS=10, mixed_nstageC=8, mixed_dampingS=30.0,
+               mixed_guess=PT_GUESS_EXTRAPOLATE, mixed_krylov=8),
     # 256x128, thermochemical, eta = exp(-ln(1e3) T), 30 tracers per cell, 500 steps.  As at
     # 1024x512, Ra_C=5e5 on the projected composition interface moves tracers out of the domain
     # within two steps of the diffusive time step (CFL=0), so the run uses the reference's
@@ -200,7 +205,9 @@ WORKLOADS = {
     # first solve (oracle), so the run keeps the reference's cycle on 4 levels (grids=4, a
     # namelist option), which converges in 8-12 cycles.
     "C2": dict(nx=256, nz=128, aspect=2.0, RaT=1e6, RaC=5e5, comp=1, ivis=1, visT=1e3, visP=1.0,
-               tpc=30, courant=0.5, tolerance=1e-8, steps=500, CFL=1, grids=4),
+               tpc=30, courant=0.5, tolerance=1e-8, steps=500, CFL=1, grids=4,
+               mg_cycle=PT_CYCLE_V, mixed_nstageS=10, mixed_nstageC=8, mixed_dampingS=30.0,
+               mixed_guess=PT_GUESS_EXTRAPOLATE, mixed_krylov=8),
     # 1024x512, eta = exp(-ln(1e5) T + ln(10)(1-z)), 32 tracers per cell, 200 steps, 1e-8
     # The projected composition interface and Ra_C=2e6 drive velocities of order 1e5 from the
     # first step: the run needs the reference's velocity-limited time step (CFL=1) to keep tracers
