@@ -136,7 +136,16 @@ typedef struct pt_config {
                               psi (defect correction).  m in 1..8: the cycle is the preconditioner of
                               a flexible GCR iteration that keeps the last m search directions
                               (restarted after m); same convergence test */
-    int32_t pad_;
+    int32_t equalize;      /* &inputs equalize=1: tracer equalisation (equalize_tracers, composition.f90:
+                              266-763) at the start of every pt_step, as energy_time does
+                              (energy.f90:198-204); needs discrete types (comp=1) or comp=0 */
+    int32_t tpc;           /* &inputs tpc: tracers per cell corner (the comp=0 target count) */
+    int32_t pad2_;
+    double dist_factor;    /* &inputs dist_factor: dist_r = dist_factor dr, dist_s = dist_factor ds */
+    double Cinit;          /* Cinit(1): the average composition at time 0 (basics.f90:461), which sets the
+                              ideal tracer count per type, Nideal(1) = nint(Cinit ntr); < 0: taken from
+                              the state at the first equalisation */
+    uint64_t eq_seed;      /* seed of the equalisation's counter-based random numbers */
 } pt_config;
 
 /* Field identifiers for pt_set_field / pt_get_field / pt_field_extent. */
@@ -269,6 +278,25 @@ int pt_tracers_to_corners_noalloc(const double* T0, int smooth_vis);
  *   (4-byte length markers; records longer than 2^31-9 bytes split into sub-records).
  * pt_read_restart: the restart read (grid.f90:55-104) of those two files from dir, then
  *   pt_upload_state. */
+/* Tracer equalisation (equalize_tracers, composition.f90:266-763): tracers from nodes with more
+ * than their type's target count (donors; near-wall tracers of edge nodes first) are moved to the
+ * nodes that lack the most (one per node and pass, the poorest level first), jittered around the
+ * node, take the node's majority type and the temperature interpolated from Tratio; then the
+ * projection (smooth_vis=0).  The reference's shuffles and lottery order (mzran per OpenMP thread)
+ * are replaced by a counter-based hash of (eq_seed, call, tracer or node): the result does not
+ * depend on the tracer order or the thread count.  The columns of the reference's equalize.dat
+ * line are returned in info (nullable).  pt_step calls it first when cfg.equalize = 1. */
+typedef struct pt_equalize_info {
+    int32_t tpc_type[2];     /* target tracers per node, type 0 / type 1 */
+    int32_t minexcess[2];    /* after the moves (composition.f90:738-745) */
+    int64_t deficit;         /* sum of the negative excesses after the moves */
+    int64_t moved;           /* tracers moved (sum index_save) */
+    int64_t nfree;           /* donors found */
+    int64_t count_type[2];   /* tracers per type after the moves (the reference's count_display) */
+    int32_t passes, nequalize; /* lottery passes of this call; equalisations that moved tracers so far */
+} pt_equalize_info;
+int pt_equalize_tracers(pt_equalize_info* info);
+
 int pt_write_snapshot(const char* dir, int fcount);
 int pt_write_restart(const char* dir);
 int pt_read_restart(const char* dir);

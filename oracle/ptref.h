@@ -101,6 +101,8 @@ typedef struct ptref_state {
     double time, dt;
     double mass; int kent; int have_mass;
     int smooth_vis;
+    int64_t eq_calls; /* equalisations so far (the call index of the next one) */
+    int32_t eq_done;  /* equalisations that moved tracers (nequalize) */
     int status;
     char err_msg[256];
 } ptref_state;
@@ -131,6 +133,12 @@ int ptref_stats(ptref_state* s, pt_stats_row* out);
 int ptref_project(ptref_state* s, const double* r, const double* sv, const double* Tt,
                   const double* T0field, int smooth); /* tracers_to_corners */
 
+/* tracer equalisation (equalize_tracers, composition.f90:266-763) as the GPU library defines it:
+ * counter-based random numbers instead of mzran, see ptref_equalize.c.  call_index counts the
+ * calls of the run (the random numbers of call n are independent of every other call's); a negative
+ * call_index takes the next one of this state. */
+int ptref_equalize(ptref_state* s, int64_t call_index, pt_equalize_info* info);
+
 /* field exchange in the Fortran layout used by ptgpu.h */
 int ptref_get_field(ptref_state* s, int id, void* out);
 int ptref_set_field(ptref_state* s, int id, const void* in);
@@ -158,6 +166,9 @@ int ref_direct_solve(ptref_state* s, int rebuild);
 void ref_compute_velocities(ptref_state* s);
 int ref_project(ptref_state* s, const double* r, const double* sv, const double* Tt,
                 const rfld* T0, int smooth);
+void ref_extendT(ptref_state* s, const rfld* T0);
+void ref_compute_derivatives(ptref_state* s, const rfld* f, double* DERr);
+double ref_interpolate(ptref_state* s, double r, double sv, const double* DERr, const rfld* f);
 double ref_heating(ptref_state* s, int i, int k);
 int ref_coarse_bandwidth(ptref_state* s);
 rfld ref_fld_alloc(int nx, int nz, int g);

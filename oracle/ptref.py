@@ -43,6 +43,7 @@ def lib() -> ctypes.CDLL:
         L.ptref_set_types.argtypes = [vp, vp]
         L.ptref_solve_psi.argtypes = [vp]
         L.ptref_step.argtypes = [vp]
+        L.ptref_equalize.argtypes = [vp, ctypes.c_int64, vp]
         L.ptref_stats.argtypes = [vp, vp]
         L.ptref_project.argtypes = [vp, vp, vp, vp, vp, i32]
         L.ptref_get_field.argtypes = [vp, i32, vp]
@@ -144,6 +145,16 @@ class Oracle:
 
     def step(self):
         self.check(self.L.ptref_step(self.h))
+
+    def equalize(self, call_index: int | None = None) -> dict:
+        """ptref_equalize: the equalisation with call index `call_index` (default: the next one of
+        this run), then the projection."""
+        from projectracer_gb300.engine import EqualizeInfo
+
+        info = EqualizeInfo()
+        call_index = -1 if call_index is None else call_index
+        self.check(self.L.ptref_equalize(self.h, call_index, ctypes.byref(info)))
+        return info.as_dict()
 
     def stats(self) -> dict:
         row = StatsRow()

@@ -247,6 +247,13 @@ static double interpolate(ptref_state* s, double r, double sv, const double* DER
     return fi;
 }
 
+/* the three pieces the tracer equalisation uses to give moved tracers their temperature */
+void ref_extendT(ptref_state* s, const rfld* T0) { extendT(s, T0); }
+void ref_compute_derivatives(ptref_state* s, const rfld* f, double* DERr) { compute_derivatives(s, f, DERr); }
+double ref_interpolate(ptref_state* s, double r, double sv, const double* DERr, const rfld* f) {
+    return interpolate(s, r, sv, DERr, f);
+}
+
 /* shape_func, composition.f90:896-921 (bilinear): the x and z factors of one (i,k) pair. */
 static inline double shape_1d(double x, int i, double h) {
     double a = 1.0 - fabs(x - (double)i * h) / h;
@@ -717,6 +724,10 @@ int ptref_step(ptref_state* s) {
     double dt = stability_RK4(s);
     if (s->status) return s->status;
     s->dt = dt;
+    if (s->cfg.equalize) { /* energy.f90:198-204, after the time step */
+        int erc = ptref_equalize(s, -1, NULL);
+        if (erc) return erc;
+    }
     rfld C0 = ref_fld_alloc(nx, nz, 5);
     rfld T0 = ref_fld_alloc(nx, nz, 3);
     if (comp) copy_fld(&C0, &s->Cnew);

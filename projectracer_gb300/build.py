@@ -22,9 +22,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
           "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
 EXTRA = {"pt_fields.cu": ["--fmad=false"], "pt_mg.cu": ["--fmad=false"], "pt_direct.cu": ["--fmad=false"],
-         "pt_io.cu": ["--fmad=false"]}
+         "pt_io.cu": ["--fmad=false"], "pt_equalize.cu": ["--fmad=false"]}
 SOURCES = ["pt_setup.cpp", "pt_fields.cu", "pt_tracers.cu", "pt_mg.cu", "pt_mixed.cu", "pt_api.cu", "pt_unet.cu",
-           "pt_direct.cu", "pt_io.cu"]
+           "pt_direct.cu", "pt_io.cu", "pt_equalize.cu"]
 
 
 def nvcc() -> str:

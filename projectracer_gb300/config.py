@@ -80,7 +80,12 @@ class PtConfig(ctypes.Structure):
         ("damping", ctypes.c_double),
         ("aRK2", ctypes.c_double),
         ("krylov", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("equalize", ctypes.c_int32),
+        ("tpc", ctypes.c_int32),
+        ("pad2_", ctypes.c_int32),
+        ("dist_factor", ctypes.c_double),
+        ("Cinit", ctypes.c_double),
+        ("eq_seed", ctypes.c_uint64),
     ]
 
     @staticmethod
@@ -129,6 +134,9 @@ class PtConfig(ctypes.Structure):
         c.nstage = 3
         c.damping = 100.0
         c.aRK2 = 0.5
+        c.dist_factor = 1e-4
+        c.Cinit = -1.0
+        c.eq_seed = 1
         return c
 
     @staticmethod
@@ -143,10 +151,10 @@ class PtConfig(ctypes.Structure):
                     "nstageS", "comp", "Tbot", "Vbc", "CFL"):
             if key.lower() in inp:
                 setattr(c, key, int(inp[key.lower()]))
-        for key in ("nstage", "chebyshev"):
+        for key in ("nstage", "chebyshev", "equalize", "tpc"):
             if key in inp:
                 setattr(c, key, int(inp[key]))
-        for key in ("damping", "aRK2"):
+        for key in ("damping", "aRK2", "dist_factor"):
             if key.lower() in inp:
                 setattr(c, key, float(inp[key.lower()]))
         for key in ("aspect", "tolerance", "eig_ratio", "dampingS", "c_2", "c_1", "courant",
@@ -177,6 +185,7 @@ class PtConfig(ctypes.Structure):
         c.mg_cycle = int(gpu.get("mg_cycle", PT_CYCLE_REFERENCE))
         c.krylov = int(gpu.get("krylov", 0))
         tpc = int(inp.get("tpc", 0))
+        c.tpc = tpc
         c.ntr = ntr if ntr is not None else (c.nx + 1) * (c.nz + 1) * tpc
         return c
 
@@ -271,4 +280,5 @@ def workload(name: str, scale: float = 1.0, precision: int = PT_PREC_FP64) -> tu
         c.krylov = w.get("mixed_krylov", 0)
     c.precision = precision
     c.ntr = c.nx * c.nz * w["tpc"]
+    c.tpc = w["tpc"]
     return c, w

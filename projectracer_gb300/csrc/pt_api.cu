@@ -257,6 +257,7 @@ static void engine_free(Engine& E) {
     for (int q = 0; q < 2; q++)
         for (int j = 0; j < 2; j++)
             if (E.gev[q][j]) cudaEventDestroy(E.gev[q][j]);
+    equalize_free(E);
     if (E.gM1) cudaGraphExecDestroy(E.gM1);
     if (E.gM2) cudaGraphExecDestroy(E.gM2);
     for (int j = 0; j < kGcrMax; j++) {
@@ -373,6 +374,12 @@ int pt_init(const pt_config* cfg) {
     if (cfg->discrete_types != 0 && (cfg->discrete_types != 1 || cfg->comp != 1)) {
         delete E;
         return fail(PT_ERR_CONFIG, "discrete_types = 1 needs comp = 1 (one dense type, ntype = 1)");
+    }
+    if (cfg->equalize != 0 && (cfg->equalize != 1 || (cfg->comp == 1 && cfg->discrete_types != 1) ||
+                               cfg->dist_factor <= 0.0 || cfg->dist_factor >= 0.5 || (cfg->comp == 0 && cfg->tpc <= 0))) {
+        delete E;
+        return fail(PT_ERR_CONFIG, "equalize = 1 needs discrete_types = 1 (comp = 1) or tpc > 0 (comp = 0), "
+                                   "and 0 < dist_factor < 0.5");
     }
     if (cfg->krylov != 0 && (cfg->krylov < 0 || cfg->krylov > kGcrMax || cfg->precision != PT_PREC_MIXED)) {
         delete E;
@@ -668,6 +675,7 @@ static int velocity_tables(Engine& E) {
 static int step_rkc2(Engine& E, double* dt_out, pt_solve_info* info) {
     int rc;
     if ((rc = stability_dt(E, &E.dt))) return rc;
+    if (E.cfg.equalize && (rc = equalize_tracers(E, nullptr))) return rc;  // Chebyshev.f90:131-137
     const int comp = E.cfg.comp;
     if (comp && (rc = copy_field(E, E.C0, E.Cnew))) return rc;
     if ((rc = copy_field(E, E.T0, E.Tratio))) return rc;
@@ -704,6 +712,7 @@ int pt_step(double* dt_out, pt_solve_info* info) {
     int rc;
     if (E.want_resort && (rc = resort_tracers(E))) return rc;
     if ((rc = stability_dt(E, &E.dt))) return rc;
+    if (E.cfg.equalize && (rc = equalize_tracers(E, nullptr))) return rc;  // energy.f90:198-204
     const int comp = E.cfg.comp;
     if (comp && (rc = copy_field(E, E.C0, E.Cnew))) return rc;
     if ((rc = copy_field(E, E.T0, E.Tratio))) return rc;
@@ -737,6 +746,19 @@ int pt_step(double* dt_out, pt_solve_info* info) {
     CK(cudaStreamSynchronize(E.st));
     harvest_spans(E);
     return 0;
+}
+
+int pt_equalize_tracers(pt_equalize_info* info) {
+    if (int rc = need(g_eng != nullptr && g_eng->uploaded)) return rc;
+    Engine& E = *g_eng;
+    if (E.cfg.comp == 1 && !E.cfg.discrete_types)
+        return fail(PT_ERR_CONFIG, "tracer equalisation needs discrete tracer types (iC_continuous = 0)");
+    if (E.cfg.comp == 0 && E.cfg.tpc <= 0) return fail(PT_ERR_CONFIG, "tracer equalisation needs tpc > 0 (comp = 0)");
+    if (!(E.cfg.dist_factor > 0.0 && E.cfg.dist_factor < 0.5))
+        return fail(PT_ERR_CONFIG, "tracer equalisation needs 0 < dist_factor < 0.5");
+    int rc = equalize_tracers(E, info);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(E.st), "equalize");
+    return rc;
 }
 
 int pt_stats(pt_stats_row* out) {

@@ -116,6 +116,10 @@ struct Engine {
     void* dlu = nullptr;
     bool direct_ready = false;
     void* io = nullptr;  // snapshot / restart writer state (pt_io.cu)
+    void* eq = nullptr;  // tracer equalisation scratch (pt_equalize.cu)
+    int64_t eq_calls = 0;  // equalisations so far: the call index of the next one
+    int32_t eq_done = 0;   // equalisations that moved tracers (the reference's nequalize)
+    double eq_Cinit = -1;  // Cinit(1); < 0 until known
     // multigrid
     double *err[PT_MAXLEV] = {}, *S0[PT_MAXLEV] = {}, *S1[PT_MAXLEV] = {}, *S2[PT_MAXLEV] = {},
            *RHS[PT_MAXLEV] = {}, *res[PT_MAXLEV] = {}, *dtst[PT_MAXLEV] = {}, *ratio[PT_MAXLEV] = {},
@@ -285,6 +289,11 @@ int load_conductivity(Engine& E);                    // energy.f90:59-86
 int load_tracer_space(Engine& E);                    // energy.f90:154-179 (+extendT 595-630)
 int noalloc_scratch_setup(unsigned char** base);  // static scratch of the current device (before any capture)
 int project_noalloc(Engine& E, const double* T0f, int smooth);
+int sort_tracers_by_node(Engine& E, const double* r, const double* s);
+int exclusive_scan_i32(Engine& E, const int32_t* in, int32_t* out, int n);
+int interp_T_at(Engine& E, const int32_t* ids, int64_t m);
+int equalize_tracers(Engine& E, pt_equalize_info* info);  // pt_equalize.cu
+void equalize_free(Engine& E);
 // learned initial psi (pt_unet.cu): after mg_setup_solve; fallback check after the first cycle
 int unet_guess(Engine& E);
 int unet_check_fallback(Engine& E, double ratio);

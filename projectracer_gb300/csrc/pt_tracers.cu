@@ -1426,4 +1426,64 @@ int rk_stage(Engine& E, int stage) {
     return 0;
 }
 
+// ---------------------------------------------------------------- helpers of the tracer equalisation
+// Tracers grouped by their nearest node (the reference's nint cell): tcell, ccount (= nempty),
+// cstart (exclusive scan) and clist (tracer positions per node).  Out-of-domain tracers fail.
+int sort_tracers_by_node(Engine& E, const double* r, const double* s) {
+    const int ncell = (E.K.nx + 1) * (E.K.nz + 1);
+    const int64_t n = E.ntr;
+    CK(cudaMemsetAsync(E.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+    CK(cudaMemsetAsync(E.derr, 0, sizeof(int), E.st));
+    PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, E.tcell, E.ccount, E.derr);
+    if (int rc = exclusive_scan_i32(E, E.ccount, E.cstart, ncell)) return rc;
+    const int nb = (int)nblk(ncell, 1024);
+    int32_t* cursor = E.scan_tmp + nb + 32;
+    CK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)ncell, E.st));
+    PT_COUNT(), k_scatter<<<nblk(n, 256), 256, 0, E.st>>>(E.tcell, n, E.cstart, cursor, E.clist);
+    CKL("sort_tracers_by_node");
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, E.derr, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+    CK(cudaStreamSynchronize(E.st));
+    if (herr & 1) return fail(PT_ERR_TRACER_OUT_OF_DOMAIN, "Tracer advected outside of domain");
+    return 0;
+}
+
+// exclusive scan of n <= (nx+1)(nz+1) int32 values (block totals in E.scan_tmp)
+int exclusive_scan_i32(Engine& E, const int32_t* in, int32_t* out, int n) {
+    const int nb = (int)nblk(n, 1024);
+    PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(in, out, E.scan_tmp, n);
+    PT_COUNT(), k_scan_totals<<<1, kScanTotThreads, 0, E.st>>>(E.scan_tmp, nb);
+    PT_COUNT(), k_scan_add<<<nb, 1024, 0, E.st>>>(out, E.scan_tmp, n);
+    CKL("exclusive_scan_i32");
+    return 0;
+}
+
+// Ttr(p) = interpolate(rtr(p), str(p)) of Tratio (extendT, compute_derivatives, interpolate:
+// composition.f90:726-737) for the m tracers ids[0..m)
+__global__ void __launch_bounds__(256) k_interp_T_at(const int32_t* __restrict__ ids, int64_t m, Tables tb,
+                                                     const double* __restrict__ r, const double* __restrict__ s,
+                                                     double* __restrict__ Tt, Geo g) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int32_t p = ids[j];
+    const double rr = r[p], ss = s[p];
+    int i = cell_index(rr, cK.inv_dr, cK.dr, cK.exact_div, cK.p_inv_dr);
+    int k = cell_index(ss, cK.inv_ds, cK.ds, cK.exact_div, cK.p_inv_ds);
+    i = min(max(i, 0), cK.nx);
+    k = min(max(k, 0), cK.nz);
+    const double hr = rr - (double)i * cK.dr, hs = ss - (double)k * cK.ds;
+    const double a1 = hr * cK.inv_fact[1], a2 = hr * hr * cK.inv_fact[2], a3 = hr * hr * hr * cK.inv_fact[3];
+    const double b1 = hs * cK.inv_fact[1], b2 = hs * hs * cK.inv_fact[2], b3 = hs * hs * hs * cK.inv_fact[3];
+    Tt[p] = interp(tb, g, i, k, a1, a2, a3, b1, b2, b3);
+}
+int interp_T_at(Engine& E, const int32_t* ids, int64_t m) {
+    if (m <= 0) return 0;
+    if (int rc = extend_T(E)) return rc;
+    if (int rc = compute_derivatives(E, E.Text, 2)) return rc;
+    const Tables tb{E.Text, E.der[2][0], E.der[2][1], E.der[2][2]};
+    PT_COUNT(), k_interp_T_at<<<nblk(m, 256), 256, 0, E.st>>>(ids, m, tb, E.rtr, E.str, E.Ttr, E.g1);
+    CKL("k_interp_T_at");
+    return 0;
+}
+
 }  // namespace pt

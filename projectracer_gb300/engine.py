@@ -53,6 +53,20 @@ class StatsRow(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad"}
 
 
+class EqualizeInfo(ctypes.Structure):
+    """pt_equalize_info: the columns of the reference's equalize.dat line."""
+    _fields_ = [("tpc_type", ctypes.c_int32 * 2), ("minexcess", ctypes.c_int32 * 2), ("deficit", ctypes.c_int64),
+                ("moved", ctypes.c_int64), ("nfree", ctypes.c_int64), ("count_type", ctypes.c_int64 * 2),
+                ("passes", ctypes.c_int32), ("nequalize", ctypes.c_int32)]
+
+    def as_dict(self):
+        out = {}
+        for n, _ in self._fields_:
+            v = getattr(self, n)
+            out[n] = list(v) if isinstance(v, ctypes.Array) else v
+        return out
+
+
 _LIB = None
 
 
@@ -86,6 +100,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.pt_solve_psi.argtypes = [ctypes.POINTER(SolveInfo)]
     L.pt_step.argtypes = [ctypes.POINTER(f64), ctypes.POINTER(SolveInfo)]
     L.pt_stats.argtypes = [ctypes.POINTER(StatsRow)]
+    L.pt_equalize_tracers.argtypes = [ctypes.POINTER(EqualizeInfo)]
     L.pt_tracers_to_corners.argtypes = [vp, i32]
     L.pt_time.argtypes = [ctypes.POINTER(f64), ctypes.POINTER(f64)]
     L.pt_set_guess_mode.argtypes = [i32, ctypes.c_char_p]
@@ -163,6 +178,12 @@ class Engine:
         info = SolveInfo()
         self._check(self.L.pt_step(ctypes.byref(dt), ctypes.byref(info)))
         return dt.value, info.as_dict()
+
+    def equalize(self) -> dict:
+        """pt_equalize_tracers: one tracer equalisation and the projection that follows it."""
+        info = EqualizeInfo()
+        self._check(self.L.pt_equalize_tracers(ctypes.byref(info)))
+        return info.as_dict()
 
     def stats(self) -> dict:
         row = StatsRow()

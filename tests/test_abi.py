@@ -28,9 +28,13 @@ def test_library_exports_all_declared_symbols(lib):
 
 
 def test_config_struct_layout_matches_header():
-    # pt_config: 16 int32, one int64, 24 doubles, 9 int32, 4 bytes of padding, 2 doubles, 2 int32 (LP64)
-    assert ctypes.sizeof(PtConfig) == 16 * 4 + 8 + 24 * 8 + 9 * 4 + 4 + 2 * 8 + 2 * 4
-    assert PtConfig.krylov.offset == 16 * 4 + 8 + 24 * 8 + 9 * 4 + 4 + 2 * 8
+    # pt_config: 16 int32, one int64, 24 doubles, 9 int32, 4 bytes of padding, 2 doubles, 4 int32, 2 doubles,
+    # one uint64 (LP64)
+    tail = 16 * 4 + 8 + 24 * 8 + 9 * 4 + 4 + 2 * 8  # krylov
+    assert PtConfig.krylov.offset == tail
+    assert PtConfig.dist_factor.offset == tail + 4 * 4
+    assert PtConfig.eq_seed.offset == tail + 4 * 4 + 2 * 8
+    assert ctypes.sizeof(PtConfig) == tail + 4 * 4 + 3 * 8
     assert PtConfig.damping.offset == 16 * 4 + 8 + 24 * 8 + 9 * 4 + 4
     assert PtConfig.discrete_types.offset == 16 * 4 + 8 + 24 * 8 + 4 * 4
     assert PtConfig.reference_rounding.offset == 16 * 4 + 8 + 24 * 8 + 5 * 4
