@@ -46,6 +46,14 @@ int pt_unet_load(const char* path, int nz, int nx, int max_batch, pt_unet** out)
  * nodes i < nx, k < nz.  The FP64 solver's own output, written out for training. */
 int pt_training_pair(float* x4, float* psi);
 
+/* Training pairs of a time-evolved run: after pt_pair_capture(capacity), every converged psi solve
+ * (pt_solve_psi and the RK-stage solves inside pt_step) appends its pair (as pt_training_pair
+ * writes it) to a device buffer of `capacity` pairs; solves beyond capacity are not recorded.
+ * pt_pair_take copies up to max_pairs of them (x4: [n][4][nz][nx], psi: [n][nz][nx]), sets *taken,
+ * and empties the buffer.  capacity 0 stops capturing and frees the buffer. */
+int pt_pair_capture(int capacity);
+int pt_pair_take(float* x4, float* psi, int max_pairs, int* taken);
+
 /* Outcome of the last solve's learned guess (pt_set_guess_mode(PT_GUESS_UNET, path)).  The
  * network's psi shape is scaled by the least-squares factor fitted on the coarsest multigrid level;
  * the previous psi and the scaled guess each get the level-1 smoothing of a cycle and the one with

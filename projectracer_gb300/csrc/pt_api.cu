@@ -622,6 +622,7 @@ static int solve_psi(Engine& E, pt_solve_info* info) {
     rc = E.cfg.direct ? direct_solve(E, info)
                       : (E.cfg.precision == PT_PREC_MIXED) ? multigrid_mixed(E, info) : multigrid(E, info);
     if (!rc && E.cfg.guess_mode == PT_GUESS_EXTRAPOLATE) rc = record_psi(E);
+    if (!rc && E.pair_ring) rc = capture_pair(E);  // training pairs of a time-evolved run
     if (!rc) rc = compute_velocities(E);
     cudaEventRecord(b, E.st);
     cudaEventSynchronize(b);

@@ -174,6 +174,8 @@ struct Engine {
     void* unet = nullptr;        // pt_unet* of the learned guess (PT_GUESS_UNET)
     void* unet_core = nullptr;   // its network (pt::UNet*)
     float* pair_buf = nullptr;   // staging of pt_training_pair (5 planes of nz x nx)
+    float* pair_ring = nullptr;  // captured pairs of converged solves (pt_pair_capture), 5 planes each
+    int pair_cap = 0, pair_n = 0;
     int unet_used = 0;           // last solve started from the network's guess
     double unet_r_prev = 0.0, unet_r_net = 0.0;
     bool coarse_ready = false;  // coarse factorisation valid for coarse_time (mixed precision)
@@ -293,6 +295,7 @@ int sort_tracers_by_node(Engine& E, const double* r, const double* s);
 int exclusive_scan_i32(Engine& E, const int32_t* in, int32_t* out, int n);
 int interp_T_at(Engine& E, const int32_t* ids, int64_t m);
 int equalize_tracers(Engine& E, pt_equalize_info* info);  // pt_equalize.cu
+int capture_pair(Engine& E);                               // pt_unet.cu: append the solve's pair
 void equalize_free(Engine& E);
 // learned initial psi (pt_unet.cu): after mg_setup_solve; fallback check after the first cycle
 int unet_guess(Engine& E);

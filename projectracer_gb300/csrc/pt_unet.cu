@@ -827,6 +827,38 @@ int pt_training_pair(float* x4, float* psi) {
     return 0;
 }
 
+int pt_pair_capture(int capacity) {
+    if (!g_eng) return fail(PT_ERR_STATE, "call pt_init first");
+    if (capacity < 0 || capacity > 100000) return fail(PT_ERR_ARG, "pt_pair_capture: capacity must be 0..100000");
+    Engine& E = *g_eng;
+    if (E.pair_ring) cudaFree(E.pair_ring);
+    E.pair_ring = nullptr;
+    E.pair_cap = E.pair_n = 0;
+    if (capacity == 0) return 0;
+    const size_t plane = (size_t)E.cfg.nx * E.cfg.nz;
+    CK(cudaMalloc(&E.pair_ring, sizeof(float) * 5 * plane * (size_t)capacity));
+    E.pair_cap = capacity;
+    return 0;
+}
+
+int pt_pair_take(float* x4, float* psi, int max_pairs, int* taken) {
+    if (!g_eng) return fail(PT_ERR_STATE, "call pt_init first");
+    if ((!x4 || !psi) && max_pairs > 0) return fail(PT_ERR_ARG, "null pointer");
+    Engine& E = *g_eng;
+    const size_t plane = (size_t)E.cfg.nx * E.cfg.nz;
+    const int n = E.pair_n < max_pairs ? E.pair_n : (max_pairs > 0 ? max_pairs : 0);
+    for (int j = 0; j < n; j++) {
+        const float* src = E.pair_ring + (size_t)j * 5 * plane;
+        CK(cudaMemcpyAsync(x4 + (size_t)j * 4 * plane, src, sizeof(float) * 4 * plane, cudaMemcpyDeviceToHost, E.st));
+        CK(cudaMemcpyAsync(psi + (size_t)j * plane, src + 4 * plane, sizeof(float) * plane, cudaMemcpyDeviceToHost,
+                           E.st));
+    }
+    CK(cudaStreamSynchronize(E.st));
+    if (taken) *taken = n;
+    E.pair_n = 0;
+    return 0;
+}
+
 int pt_unet_guess_info(int* used, double* resid_prev, double* resid_net) {
     if (!g_eng) return fail(PT_ERR_STATE, "call pt_init first");
     Engine& E = *g_eng;
@@ -839,6 +871,15 @@ int pt_unet_guess_info(int* used, double* resid_prev, double* resid_net) {
 }  // extern "C"
 
 namespace pt {
+int capture_pair(Engine& E) {
+    if (!E.pair_ring || E.pair_n >= E.pair_cap) return 0;
+    const size_t plane = (size_t)E.cfg.nx * E.cfg.nz;
+    float* slot = E.pair_ring + (size_t)E.pair_n * 5 * plane;
+    if (int rc = engine_features(E, slot, slot + 4 * plane)) return rc;
+    E.pair_n++;
+    return 0;
+}
+
 int unet_engine_load(Engine& E, const char* path) {
     if (!path) return fail(PT_ERR_ARG, "PT_GUESS_UNET needs a weight file");
     pt_unet* net = nullptr;
@@ -854,6 +895,9 @@ int unet_engine_release(Engine& E) {
     E.unet_core = nullptr;
     if (E.pair_buf) cudaFree(E.pair_buf);
     E.pair_buf = nullptr;
+    if (E.pair_ring) cudaFree(E.pair_ring);
+    E.pair_ring = nullptr;
+    E.pair_cap = E.pair_n = 0;
     return 0;
 }
 }  // namespace pt

@@ -15,7 +15,7 @@ import math
 import numpy as np
 
 from . import engine as eng
-from .config import PT_GUESS_ZERO, PT_PREC_FP64, PtConfig, workload
+from .config import PT_GUESS_PREVIOUS, PT_GUESS_UNET, PT_GUESS_ZERO, PT_PREC_FP64, PtConfig, workload
 from .inputs import make_state
 
 _c = ctypes
@@ -38,6 +38,8 @@ def _bind(L):
     L.pt_training_pair.argtypes = [vp, vp]
     L.pt_unet_guess_info.argtypes = [_c.POINTER(i32), _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]
     L.pt_tc_gemm_check.argtypes = [vp, vp, vp, i32, i32, i32]
+    L.pt_pair_capture.argtypes = [i32]
+    L.pt_pair_take.argtypes = [vp, vp, i32, _c.POINTER(i32)]
     L._unet_bound = True
     return L
 
@@ -129,6 +131,71 @@ def training_pair(e: eng.Engine):
     return x, y
 
 
+def pair_capture(capacity: int):
+    """Record the training pair of every converged solve of the current engine (pt_pair_capture)."""
+    L = library()
+    rc = L.pt_pair_capture(int(capacity))
+    if rc:
+        raise eng.PtError(rc, L.pt_last_error().decode())
+
+
+def pair_take(e: eng.Engine, max_pairs: int):
+    """The pairs recorded since the last call: (X [n][4][nz][nx], Y [n][nz][nx]) float32."""
+    L = library()
+    X = np.zeros((max_pairs, 4, e.nz, e.nx), dtype=np.float32)
+    Y = np.zeros((max_pairs, e.nz, e.nx), dtype=np.float32)
+    n = _c.c_int(0)
+    rc = L.pt_pair_take(X.ctypes.data, Y.ctypes.data, int(max_pairs), _c.byref(n))
+    if rc:
+        raise eng.PtError(rc, L.pt_last_error().decode())
+    return X[: n.value], Y[: n.value]
+
+
+def run_pairs(cfg: PtConfig, st: dict, steps: int, warmup: int = 0):
+    """Training pairs of a time-evolved run: `warmup` unrecorded steps, then every converged solve of
+    `steps` steps (the top-of-step solve and the three RK-stage solves of each) -> (X, Y)."""
+    e = eng.Engine(cfg)
+    try:
+        e.upload(st)
+        for _ in range(warmup):
+            e.solve_psi()
+            e.step()
+        pair_capture(4 * steps + 4)
+        for _ in range(steps):
+            e.solve_psi()
+            e.step()
+        X, Y = pair_take(e, 4 * steps + 4)
+        pair_capture(0)
+    finally:
+        e.close()
+    return X, Y
+
+
+def write_shards(X: np.ndarray, Y: np.ndarray, out_dir: str, shard: int = 256, start: int = 0) -> list[str]:
+    """Pairs as .npy shards: x_<n>.npy ([m][4][nz][nx]) and y_<n>.npy ([m][nz][nx]), m <= shard."""
+    import os
+
+    os.makedirs(out_dir, exist_ok=True)
+    names = []
+    for q, a in enumerate(range(0, len(X), shard)):
+        tag = f"{start + q:05d}"
+        np.save(os.path.join(out_dir, f"x_{tag}.npy"), X[a:a + shard])
+        np.save(os.path.join(out_dir, f"y_{tag}.npy"), Y[a:a + shard])
+        names.append(tag)
+    return names
+
+
+def read_shards(in_dir: str):
+    """All shards of a directory written by write_shards, in order."""
+    import glob
+    import os
+
+    xs = sorted(glob.glob(os.path.join(in_dir, "x_*.npy")))
+    X = np.concatenate([np.load(f) for f in xs]) if xs else np.zeros((0,), np.float32)
+    Y = np.concatenate([np.load(f.replace(os.sep + "x_", os.sep + "y_")) for f in xs]) if xs else np.zeros((0,), np.float32)
+    return X, Y
+
+
 def guess_info():
     L = library()
     used, rp, rn = _c.c_int(), _c.c_double(), _c.c_double()
@@ -185,3 +252,104 @@ def train(net: UNet, X: np.ndarray, Y: np.ndarray, epochs: int, batch: int, lr: 
             losses.append(net.train_step(X[idx], Y[idx], lr))
         hist.append(float(np.mean(losses)))
     return hist
+
+
+def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run: int = 10, warmup: int = 2,
+             epochs: int = 10, batch: int = 8, lr: float = 1e-3, seed: int = 7, nx: int = 512, nz: int = 256,
+             tpc: int = 16, log=print) -> dict:
+    """The learned-guess evaluation of the 512x256 configuration.
+
+    Training pairs come from time-evolved FP64 runs of sampled physics (sample_config: Ra_T in
+    [1e5, 1e7], viscosity contrast in [1e2, 1e5]; `warmup` unrecorded steps, then every converged
+    solve of `steps_per_run` steps) and are written as .npy shards under out_dir/train.  The network
+    (4 levels, width 32) is trained on n_train of them.  Held-out: new runs of the same sampling; at
+    each top-of-step solve the FP64 solve to 1e-8 is run three times from the same state -- from
+    zero, from the previous step's psi (the reference's warm start) and from the network's guess
+    (with its fallback to the previous psi after one cycle) -- and the V-cycles are recorded, with
+    the network's error on psi / max|psi| against the zero guess's."""
+    import os
+    import time
+
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    Xs, Ys, runs = [], [], 0
+    while sum(len(x) for x in Xs) < n_train:
+        cfg = sample_config(rng, nx, nz, tpc)
+        st = make_state(cfg, int(rng.integers(1 << 30)), noise=1e-3)
+        x, y = run_pairs(cfg, st, steps_per_run, warmup)
+        Xs.append(x)
+        Ys.append(y)
+        runs += 1
+    X = np.concatenate(Xs)[:n_train]
+    Y = np.concatenate(Ys)[:n_train]
+    del Xs, Ys
+    shards = write_shards(X, Y, os.path.join(out_dir, "train"))
+    t_pairs = time.perf_counter() - t0
+    log(f"pairs: {len(X)} from {runs} runs in {t_pairs:.1f} s, {len(shards)} shards")
+    net = UNet(nz, nx, max_batch=batch, seed=seed)
+    t0 = time.perf_counter()
+    hist = train(net, X, Y, epochs, batch, lr, seed)
+    t_train = time.perf_counter() - t0
+    log(f"training: {epochs} epochs in {t_train:.1f} s, loss {hist[0]:.4g} -> {hist[-1]:.4g}")
+    wpath = os.path.join(out_dir, "unet_c4.bin")
+    net.save(wpath)
+    cyc = {"zero": [], "previous": [], "learned": []}
+    used, mse_net, mse_zero = [], [], []
+    test_runs = 0
+    while len(cyc["zero"]) < n_test:
+        cfg = sample_config(rng, nx, nz, tpc)
+        st = make_state(cfg, int(rng.integers(1 << 30)), noise=1e-3)
+        e = eng.Engine(cfg)
+        try:
+            e.upload(st)
+            for _ in range(warmup):
+                e.solve_psi()
+                e.step()
+            for _ in range(steps_per_run):
+                if len(cyc["zero"]) >= n_test:
+                    break
+                prev = e.get(eng.F_SF)
+                e.set_guess_mode(PT_GUESS_ZERO)
+                cyc["zero"].append(e.solve_psi()["cycles"])
+                xt, yt = training_pair(e)
+                pred = net.forward(xt[None])[0]
+                mse_net.append(float(np.mean((pred - yt) ** 2)))
+                mse_zero.append(float(np.mean(yt ** 2)))
+                e.set(eng.F_SF, prev)
+                e.set_guess_mode(PT_GUESS_UNET, wpath)
+                cyc["learned"].append(e.solve_psi()["cycles"])
+                used.append(guess_info()["used"])
+                e.set(eng.F_SF, prev)
+                e.set_guess_mode(PT_GUESS_PREVIOUS)
+                cyc["previous"].append(e.solve_psi()["cycles"])
+                e.step()
+        finally:
+            e.close()
+        test_runs += 1
+    net.close()
+    out = {"grid": f"{nx}x{nz}", "tracers_per_cell": tpc, "tolerance": 1e-8, "train_pairs": int(len(X)),
+           "train_runs": runs, "test_solves": len(cyc["zero"]), "test_runs": test_runs, "epochs": epochs,
+           "batch": batch, "lr": lr, "loss_history": hist, "seconds_pairs": t_pairs, "seconds_training": t_train,
+           "cycles_mean": {k: float(np.mean(v)) for k, v in cyc.items()},
+           "cycles_median": {k: float(np.median(v)) for k, v in cyc.items()},
+           "cycles_max": {k: int(np.max(v)) for k, v in cyc.items()},
+           "learned_guess_kept": float(np.mean(used)),
+           "heldout_mse_network": float(np.mean(mse_net)), "heldout_mse_zero_guess": float(np.mean(mse_zero))}
+    with open(os.path.join(out_dir, "c4_study.json"), "w") as fh:
+        import json
+
+        json.dump(out, fh, indent=1)
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="learned-guess evaluation at 512x256 (c4_study)")
+    ap.add_argument("out_dir")
+    ap.add_argument("--train", type=int, default=1000)
+    ap.add_argument("--test", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=10)
+    a = ap.parse_args()
+    print(json.dumps(c4_study(a.out_dir, n_train=a.train, n_test=a.test, epochs=a.epochs)))
