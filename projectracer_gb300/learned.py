@@ -153,17 +153,24 @@ def pair_take(e: eng.Engine, max_pairs: int):
 
 def run_pairs(cfg: PtConfig, st: dict, steps: int, warmup: int = 0):
     """Training pairs of a time-evolved run: `warmup` unrecorded steps, then every converged solve of
-    `steps` steps (the top-of-step solve and the three RK-stage solves of each) -> (X, Y)."""
+    `steps` steps (the top-of-step solve and the three RK-stage solves of each) -> (X, Y).  A solve
+    that fails to converge ends the run; the pairs of the solves before it are kept."""
     e = eng.Engine(cfg)
     try:
         e.upload(st)
-        for _ in range(warmup):
-            e.solve_psi()
-            e.step()
+        try:
+            for _ in range(warmup):
+                e.solve_psi()
+                e.step()
+        except eng.PtError:
+            return (np.zeros((0, 4, cfg.nz, cfg.nx), np.float32), np.zeros((0, cfg.nz, cfg.nx), np.float32))
         pair_capture(4 * steps + 4)
-        for _ in range(steps):
-            e.solve_psi()
-            e.step()
+        try:
+            for _ in range(steps):
+                e.solve_psi()
+                e.step()
+        except eng.PtError:
+            pass
         X, Y = pair_take(e, 4 * steps + 4)
         pair_capture(0)
     finally:
@@ -295,7 +302,7 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
     net.save(wpath)
     cyc = {"zero": [], "previous": [], "learned": []}
     used, mse_net, mse_zero = [], [], []
-    test_runs = 0
+    test_runs, skipped = 0, 0
     while len(cyc["zero"]) < n_test:
         cfg = sample_config(rng, nx, nz, tpc)
         st = make_state(cfg, int(rng.integers(1 << 30)), noise=1e-3)
@@ -310,25 +317,32 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
                     break
                 prev = e.get(eng.F_SF)
                 e.set_guess_mode(PT_GUESS_ZERO)
-                cyc["zero"].append(e.solve_psi()["cycles"])
+                cz = e.solve_psi()["cycles"]
                 xt, yt = training_pair(e)
                 pred = net.forward(xt[None])[0]
-                mse_net.append(float(np.mean((pred - yt) ** 2)))
-                mse_zero.append(float(np.mean(yt ** 2)))
                 e.set(eng.F_SF, prev)
                 e.set_guess_mode(PT_GUESS_UNET, wpath)
-                cyc["learned"].append(e.solve_psi()["cycles"])
-                used.append(guess_info()["used"])
+                cl = e.solve_psi()["cycles"]
+                ul = guess_info()["used"]
                 e.set(eng.F_SF, prev)
                 e.set_guess_mode(PT_GUESS_PREVIOUS)
-                cyc["previous"].append(e.solve_psi()["cycles"])
+                cp = e.solve_psi()["cycles"]
+                cyc["zero"].append(cz)
+                cyc["learned"].append(cl)
+                cyc["previous"].append(cp)
+                used.append(ul)
+                mse_net.append(float(np.mean((pred - yt) ** 2)))
+                mse_zero.append(float(np.mean(yt ** 2)))
                 e.step()
+        except eng.PtError:
+            skipped += 1  # a solve of this run did not converge (the rest of the run is dropped)
         finally:
             e.close()
         test_runs += 1
     net.close()
     out = {"grid": f"{nx}x{nz}", "tracers_per_cell": tpc, "tolerance": 1e-8, "train_pairs": int(len(X)),
-           "train_runs": runs, "test_solves": len(cyc["zero"]), "test_runs": test_runs, "epochs": epochs,
+           "train_runs": runs, "test_solves": len(cyc["zero"]), "test_runs": test_runs,
+           "test_runs_ended_by_a_failed_solve": skipped, "epochs": epochs,
            "batch": batch, "lr": lr, "loss_history": hist, "seconds_pairs": t_pairs, "seconds_training": t_train,
            "cycles_mean": {k: float(np.mean(v)) for k, v in cyc.items()},
            "cycles_median": {k: float(np.median(v)) for k, v in cyc.items()},
