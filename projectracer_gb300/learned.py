@@ -281,6 +281,8 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
     t0 = time.perf_counter()
     Xs, Ys, runs = [], [], 0
     while sum(len(x) for x in Xs) < n_train:
+        if runs > n_train:
+            raise RuntimeError("c4_study: too few converging runs for the training pairs")
         cfg = sample_config(rng, nx, nz, tpc)
         st = make_state(cfg, int(rng.integers(1 << 30)), noise=1e-3)
         x, y = run_pairs(cfg, st, steps_per_run, warmup)
@@ -304,6 +306,8 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
     used, mse_net, mse_zero = [], [], []
     test_runs, skipped = 0, 0
     while len(cyc["zero"]) < n_test:
+        if test_runs > n_test + 50:
+            break
         cfg = sample_config(rng, nx, nz, tpc)
         st = make_state(cfg, int(rng.integers(1 << 30)), noise=1e-3)
         e = eng.Engine(cfg)
