@@ -41,6 +41,10 @@ int pt_unet_train_step(pt_unet* net, const float* x, const float* target, int ba
 int pt_unet_save(pt_unet* net, const char* path);
 int pt_unet_load(const char* path, int nz, int nx, int max_batch, pt_unet** out);
 
+/* Device time of each of the 14 convolution GEMMs of one forward pass (CUDA events on the network's
+ * stream, after a warm-up pass): ms[l] for layer l (4 levels x width 32, see the weight layout). */
+int pt_unet_profile_forward(pt_unet* net, const float* x, int batch, float* ms);
+
 /* Training pair of the current engine state (after pt_solve_psi): the network's input planes
  * x4 [4][nz][nx] (T, C, log10(eta)/5, RHS/max|RHS|) and the target psi/max|psi| [nz][nx], on
  * nodes i < nx, k < nz.  The FP64 solver's own output, written out for training. */

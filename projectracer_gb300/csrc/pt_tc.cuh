@@ -6,8 +6,13 @@
 //     the canonical no-swizzle K-major layout: 8x8 "core matrices" of 128 contiguous bytes (8 rows
 //     of 16 bytes), LBO = 128 B between core matrices adjacent in K, SBO = 1024 B between the
 //     8-row groups (8 core matrices per 64-wide chunk);
-//   * one thread issues the four K=16 MMAs of the chunk (tcgen05.mma.cta_group::1.kind::f16) and
-//     commits them to an mbarrier; the next chunk's gather waits on that barrier (bounded spin);
+//   * two stages: while the MMAs of chunk c read one stage, the threads gather chunk c+1 into the
+//     other; a stage is overwritten only after the MMAs of the chunk two back have completed;
+//   * a problem with P::kVec gathers 8 consecutive K elements (one 16-byte core-matrix row) per
+//     call (gather_a8 / gather_b8), with the threads spread over rows first so that a warp's
+//     16-byte stores hit all 32 banks; otherwise one element per call;
+//   * one thread issues the four K=16 MMAs of a chunk (tcgen05.mma.cta_group::1.kind::f16) and
+//     commits them to the stage's mbarrier; waits on it are bounded spins;
 //   * the epilogue reads the accumulator with tcgen05.ld.32x32b (warp w owns TMEM lanes
 //     32w..32w+31 = tile rows) and hands each row's values to the problem's store functor.
 // A problem type supplies M, N, K, gather_a / gather_b (element (row, k) of A or B as BF16 bits,
@@ -112,10 +117,36 @@ __host__ __device__ constexpr uint32_t tmem_cols(int n) {
     return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : 256u;
 }
 
-// Dynamic shared memory: A tile (128 x 64 BF16 = 16 KB) | B tile (N x 64 BF16) | mbarrier | tmem
-// addr | 16 KB of slack, so that every core-matrix offset a descriptor can form from the tile
-// bases stays inside the allocation.
-__host__ __device__ constexpr size_t smem_bytes(int n) { return 16384 + (size_t)n * 128 + 64 + 16384; }
+// Dynamic shared memory: two stages of [A tile (128 x 64 BF16 = 16 KB) | B tile (N x 64 BF16)] |
+// two mbarriers | tmem addr | 16 KB of slack, so that every core-matrix offset a descriptor can
+// form from the tile bases stays inside the allocation.  Each stage starts on a 1024-byte boundary
+// (N is a multiple of 16).
+__host__ __device__ constexpr size_t stage_bytes(int n) { return 16384 + (size_t)n * 128; }
+__host__ __device__ constexpr size_t smem_bytes(int n) { return 2 * stage_bytes(n) + 64 + 16384; }
+
+template <class P>
+__device__ __forceinline__ void gather_chunk(const P& prob, unsigned char* sa, unsigned char* sb, int m0, int col0,
+                                             int n, int k0, int tid) {
+    if constexpr (P::kVec) {
+        for (int q = tid; q < kTileM * (kChunkK / 8); q += kThreads) {
+            const int r = q % kTileM, kg = q / kTileM;
+            *reinterpret_cast<uint4*>(sa + tile_off(r, kg * 8)) = prob.gather_a8(m0 + r, k0 + kg * 8);
+        }
+        for (int q = tid; q < n * (kChunkK / 8); q += kThreads) {
+            const int r = q % n, kg = q / n;
+            *reinterpret_cast<uint4*>(sb + tile_off(r, kg * 8)) = prob.gather_b8(col0 + r, k0 + kg * 8);
+        }
+    } else {
+        for (int q = tid; q < kTileM * kChunkK; q += kThreads) {
+            const int r = q / kChunkK, k = q % kChunkK;
+            *reinterpret_cast<uint16_t*>(sa + tile_off(r, k)) = prob.gather_a(m0 + r, k0 + k);
+        }
+        for (int q = tid; q < n * kChunkK; q += kThreads) {
+            const int r = q / kChunkK, k = q % kChunkK;
+            *reinterpret_cast<uint16_t*>(sb + tile_off(r, k)) = prob.gather_b(col0 + r, k0 + k);
+        }
+    }
+}
 
 // The GEMM tile.  Problem P: int M, N, K (matrix sizes), int Ntile (columns per CTA, a multiple
 // of 16 in [16, 256]), int kc_split (K chunks per CTA along grid z; 0 = all);
@@ -125,15 +156,19 @@ __host__ __device__ constexpr size_t smem_bytes(int n) { return 16384 + (size_t)
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sa = smem;
-    unsigned char* sb = smem + 16384;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 16384 + (size_t)prob.Ntile * 128);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int n = prob.Ntile, col0 = blockIdx.y * prob.Ntile;
+    const size_t sbytes = stage_bytes(n);
+    unsigned char* sa[2] = {smem, smem + sbytes};
+    unsigned char* sb[2] = {smem + 16384, smem + sbytes + 16384};
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * sbytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m0 = blockIdx.x * kTileM;
-    const int n = prob.Ntile, col0 = blockIdx.y * prob.Ntile;
     const uint32_t ncols = tmem_cols(n);
-    if (tid == 0) mbar_init(bar, 1);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+    }
     if (warp == 0) tmem_alloc(tslot, ncols);
     tc_fence_before();
     __syncthreads();
@@ -143,38 +178,46 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(P prob, int* err) {
     const int nall = (prob.K + kChunkK - 1) / kChunkK;
     const int per = prob.kc_split > 0 ? prob.kc_split : nall;
     const int cbeg = blockIdx.z * per, cend = min(nall, cbeg + per);
-    uint32_t phase = 0;
+    uint32_t phase[2] = {0u, 0u};
+    bool pending[2] = {false, false};
     bool ok = true;
     for (int c = cbeg; c < cend && ok; c++) {
-        const int k0 = c * kChunkK;
-        // gather the chunk: A rows m0..m0+127, B rows 0..n-1, k0..k0+63
-        for (int q = tid; q < kTileM * kChunkK; q += kThreads) {
-            const int r = q / kChunkK, k = q % kChunkK;
-            *reinterpret_cast<uint16_t*>(sa + tile_off(r, k)) = prob.gather_a(m0 + r, k0 + k);
+        const int st = (c - cbeg) & 1;
+        if (pending[st]) {  // the MMAs of chunk c - 2 read this stage: wait for them before overwriting
+            const int timed_out = __syncthreads_or(mbar_wait(bar + st, phase[st]) ? 0 : 1);
+            if (timed_out) {
+                if (tid == 0) atomicOr(err, 1);
+                ok = false;
+                break;
+            }
+            phase[st] ^= 1u;
+            pending[st] = false;
         }
-        for (int q = tid; q < n * kChunkK; q += kThreads) {
-            const int r = q / kChunkK, k = q % kChunkK;
-            *reinterpret_cast<uint16_t*>(sb + tile_off(r, k)) = prob.gather_b(col0 + r, k0 + k);
-        }
+        gather_chunk(prob, sa[st], sb[st], m0, col0, n, c * kChunkK, tid);
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            const uint32_t a0 = smem_u32(sa[st]), b0 = smem_u32(sb[st]);
 #pragma unroll
             for (int s = 0; s < kChunkK / 16; s++)
                 mma_bf16(taddr, smem_desc(a0 + s * 256, 128, 1024), smem_desc(b0 + s * 256, 128, 1024), idesc,
                          (c > cbeg || s > 0) ? 1u : 0u);
-            mma_commit(bar);
+            mma_commit(bar + st);
         }
-        // every thread waits for the chunk's MMAs before the tiles are overwritten; a timeout is
-        // agreed by the whole CTA so every thread leaves the loop together
-        const int timed_out = __syncthreads_or(mbar_wait(bar, phase) ? 0 : 1);
+        pending[st] = true;
+    }
+    // the outstanding commits, oldest first (each commit tracks every MMA issued before it)
+    for (int q = 0; q < 2 && ok; q++) {
+        const int st = ((cend - cbeg) + q) & 1;  // the stage of chunk cend - 2 first, then cend - 1
+        if (!pending[st]) continue;
+        const int timed_out = __syncthreads_or(mbar_wait(bar + st, phase[st]) ? 0 : 1);
         if (timed_out) {
             if (tid == 0) atomicOr(err, 1);
             ok = false;
         }
-        phase ^= 1u;
+        phase[st] ^= 1u;
+        pending[st] = false;
     }
     tc_fence_after();
     if (ok) {

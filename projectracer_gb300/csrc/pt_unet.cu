@@ -17,6 +17,7 @@ namespace pt {
 
 // plain GEMM problem: C (M x N, FP32) = A (M x K) * B (N x K)^T, BF16 row-major operands
 struct GemmProb {
+    static constexpr bool kVec = false;
     int M, N, K, Ntile, kc_split;
     const uint16_t* A;
     const uint16_t* B;
@@ -68,8 +69,16 @@ __device__ __forceinline__ bool tap_pixel(int p, int tap, int H, int W, int& b, 
     return y >= 0 && y < H && x >= 0 && x < W;
 }
 
-// forward: out[p][co] = relu(sum_{tap,ci} in(p+tap)[ci] w[co][tap][ci] + bias[co]) in BF16
+// 8 BF16 values from one 16-byte-aligned address
+__device__ __forceinline__ uint4 ld8(const uint16_t* p) { return *reinterpret_cast<const uint4*>(p); }
+__device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
+
+// forward: out[p][co] = relu(sum_{tap,ci} in(p+tap)[ci] w[co][tap][ci] + bias[co]) in BF16.
+// K = 9 cin, ordered (tap, ci): with cin a multiple of 8 the 8 values of a gather_a8 are 8
+// consecutive channels of one pixel (one 16-byte load of an NHWC tensor, four for a pooled view),
+// and those of a gather_b8 8 consecutive weights; the first layer (cin = 4) gathers element-wise.
 struct ConvFwd {
+    static constexpr bool kVec = true;
     int M, N, K, Ntile, kc_split;
     InView in;
     const uint16_t* w;
@@ -85,6 +94,56 @@ struct ConvFwd {
     }
     __device__ __forceinline__ uint16_t gather_b(int co, int k) const {
         return (co < N && k < K) ? w[(size_t)co * K + k] : (uint16_t)0;
+    }
+    __device__ __forceinline__ uint4 gather_a8(int p, int k0) const {
+        const int cin = in.C();
+        if ((cin & 7) || (in.C0 & 7) || k0 + 8 > K) {
+            uint16_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = gather_a(p, k0 + j);
+            return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+        }
+        if (p >= M) return make_uint4(0u, 0u, 0u, 0u);
+        const int tap = k0 / cin, ci = k0 - tap * cin;
+        int b, y, x;
+        if (!tap_pixel(p, tap, in.H, in.W, b, y, x)) return make_uint4(0u, 0u, 0u, 0u);
+        if (in.mode == 0) return ld8(in.t0 + (((size_t)b * in.H + y) * in.W + x) * in.C0 + ci);
+        if (in.mode == 2) {
+            if (ci < in.C0)
+                return ld8(in.t0 + (((size_t)b * (in.H >> 1) + (y >> 1)) * (in.W >> 1) + (x >> 1)) * in.C0 + ci);
+            return ld8(in.t1 + (((size_t)b * in.H + y) * in.W + x) * in.C1 + (ci - in.C0));
+        }
+        // 2x2 average of the finer tensor, summed in the order of InView::get
+        const size_t W2 = 2 * (size_t)in.W;
+        const uint16_t* q = in.t0 + (((size_t)b * 2 * in.H + 2 * y) * W2 + 2 * x) * in.C0 + ci;
+        const uint4 a = ld8(q), bq = ld8(q + in.C0), c = ld8(q + W2 * in.C0), d = ld8(q + W2 * in.C0 + in.C0);
+        const uint32_t* pa = &a.x;
+        const uint32_t* pb = &bq.x;
+        const uint32_t* pc = &c.x;
+        const uint32_t* pd = &d.x;
+        uint32_t o[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            uint16_t h[2];
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int sh = 16 * e;
+                const float sum = ((bf2f((uint16_t)(pa[j] >> sh)) + bf2f((uint16_t)(pb[j] >> sh))) +
+                                   bf2f((uint16_t)(pc[j] >> sh))) + bf2f((uint16_t)(pd[j] >> sh));
+                h[e] = f2bf(sum * 0.25f);
+            }
+            o[j] = pack2(h[0], h[1]);
+        }
+        return make_uint4(o[0], o[1], o[2], o[3]);
+    }
+    __device__ __forceinline__ uint4 gather_b8(int co, int k0) const {
+        if ((K & 7) || co >= N || k0 + 8 > K) {
+            uint16_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = gather_b(co, k0 + j);
+            return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+        }
+        return ld8(w + (size_t)co * K + k0);
     }
     __device__ __forceinline__ void store(int p, int co, int, float v) const {
         v += bias[co];
@@ -102,6 +161,7 @@ __device__ __forceinline__ uint16_t dz_bf(const float* dY, const uint16_t* Y, si
 
 // backward data: dX[q][ci] = sum_{t,co} dZ[q + tap t][co] w[co][8 - t][ci]  (FP32 out)
 struct ConvBwdData {
+    static constexpr bool kVec = false;
     int M, N, K, Ntile, kc_split;  // M pixels, N = Cin, K = 9 Cout
     int H, W, Cout;
     const float* dY;
@@ -125,6 +185,7 @@ struct ConvBwdData {
 
 // backward weights (split over pixels): part[z][tap*Cin + ci][co] = sum_{p in split z} in(p+tap)[ci] dZ[p][co]
 struct ConvBwdW {
+    static constexpr bool kVec = false;
     int M, N, K, Ntile, kc_split;  // M = 9 Cin, N = Cout, K = pixels
     InView in;
     const float* dY;
@@ -369,6 +430,8 @@ static int unet_build(UNet& U, int H, int W, int maxB, uint64_t seed) {
         U.tch[c.out] = c.cout;
         U.tlev[c.out] = c.level;
     }
+    for (auto& c : U.L)  // ConvFwd::gather_b8 reads 16-byte-aligned rows of the BF16 weights
+        if (c.woff % 8) return fail(PT_ERR_CONFIG, "U-Net: weight offsets must be multiples of 8");
     U.out_w = off;
     off += 32;
     U.out_b = off;
@@ -451,16 +514,20 @@ static InView view_of(const UNet& U, const UConv& c, int B) {
     return v;
 }
 
-// network input already in U.xin (device, NCHW FP32); output in U.y ([B][H][W] FP32)
-static int unet_forward(UNet& U, int B) {
+// network input already in U.xin (device, NCHW FP32); output in U.y ([B][H][W] FP32).
+// ev (optional): 15 CUDA events recorded around the 14 convolution GEMMs
+static int unet_forward(UNet& U, int B, cudaEvent_t* ev = nullptr) {
     const size_t P0 = (size_t)B * U.H * U.W;
     k_input_nhwc<<<nblk(P0 * 4, 256), 256, 0, U.st>>>(U.x0, U.xin, B, 4, U.H, U.W);
     CK(cudaGetLastError());
+    int li = 0;
+    if (ev) CK(cudaEventRecord(ev[0], U.st));
     for (auto& c : U.L) {
         const InView v = view_of(U, c, B);
         const int P = B * v.H * v.W;
         ConvFwd f{P, c.cout, 9 * c.cin, ntile_for(c.cout), 0, v, U.wbf + c.woff, U.w32 + c.boff, U.act[c.out], 1};
         if (int rc = run_gemm(U, f, 1)) return rc;
+        if (ev) CK(cudaEventRecord(ev[++li], U.st));
     }
     k_out_fwd<<<nblk(P0, 256), 256, 0, U.st>>>(U.y, U.act[13], U.w32 + U.out_w, U.w32 + U.out_b, (int)P0, 32);
     CK(cudaGetLastError());
@@ -811,6 +878,23 @@ int pt_unet_load(const char* path, int nz, int nx, int max_batch, pt_unet** out)
         return fail(PT_ERR_ARG, "U-Net weight file has a different parameter count");
     }
     return pt_unet_set_params(*out, h.data());
+}
+
+int pt_unet_profile_forward(pt_unet* net, const float* x, int batch, float* ms) {
+    if (!net || !x || !ms) return fail(PT_ERR_ARG, "null pointer");
+    UNet& U = net->u;
+    if (batch < 1 || batch > U.maxB) return fail(PT_ERR_ARG, "batch out of range");
+    const size_t P0 = (size_t)batch * U.H * U.W;
+    CK(cudaMemcpyAsync(U.xin, x, sizeof(float) * P0 * 4, cudaMemcpyHostToDevice, U.st));
+    if (int rc = unet_forward(U, batch)) return rc;  // warm-up
+    cudaEvent_t ev[15];
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    int rc = unet_forward(U, batch, ev);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(U.st), "pt_unet_profile_forward");
+    for (int l = 0; l < 14 && !rc; l++) cudaEventElapsedTime(&ms[l], ev[l], ev[l + 1]);
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (!rc) rc = gemm_error(U);
+    return rc;
 }
 
 int pt_training_pair(float* x4, float* psi) {

@@ -38,6 +38,7 @@ def _bind(L):
     L.pt_training_pair.argtypes = [vp, vp]
     L.pt_unet_guess_info.argtypes = [_c.POINTER(i32), _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]
     L.pt_tc_gemm_check.argtypes = [vp, vp, vp, i32, i32, i32]
+    L.pt_unet_profile_forward.argtypes = [vp, vp, i32, vp]
     L.pt_pair_capture.argtypes = [i32]
     L.pt_pair_take.argtypes = [vp, vp, i32, _c.POINTER(i32)]
     L._unet_bound = True
@@ -110,6 +111,13 @@ class UNet:
         loss = _c.c_float()
         self._ok(self.L.pt_unet_train_step(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], lr, _c.byref(loss)))
         return loss.value
+
+    def profile_forward(self, x: np.ndarray) -> np.ndarray:
+        """Device ms of each convolution GEMM of one forward pass (pt_unet_profile_forward)."""
+        x = _f32(x)
+        ms = np.zeros(14, dtype=np.float32)
+        self._ok(self.L.pt_unet_profile_forward(self.h, x.ctypes.data, x.shape[0], ms.ctypes.data))
+        return ms
 
     def save(self, path: str):
         self._ok(self.L.pt_unet_save(self.h, path.encode()))
@@ -371,3 +379,13 @@ if __name__ == "__main__":
     ap.add_argument("--epochs", type=int, default=10)
     a = ap.parse_args()
     print(json.dumps(c4_study(a.out_dir, n_train=a.train, n_test=a.test, epochs=a.epochs)))
+
+
+# (cin, cout, level) of the 14 convolutions, as built by the library (4 levels, width 32)
+LAYERS = [(4, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2), (128, 256, 3),
+          (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1), (64, 64, 1), (96, 32, 0), (32, 32, 0)]
+
+
+def conv_flops(nz: int, nx: int, batch: int) -> list[float]:
+    """FLOPs of each convolution GEMM of one forward pass (2 per multiply-add)."""
+    return [18.0 * ci * co * batch * nz * nx / 4 ** lv for ci, co, lv in LAYERS]
