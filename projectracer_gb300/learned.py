@@ -368,17 +368,51 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
     return out
 
 
+def profile(nz: int = 256, nx: int = 512, batch: int = 8, reps: int = 5) -> dict:
+    """Speed of the network's tensor-core GEMMs: per-layer device time of the forward convolutions
+    (CUDA events, pt_unet_profile_forward) with their TFLOP/s, and the host time of whole forward
+    passes and training steps on random inputs."""
+    import time
+
+    net = UNet(nz, nx, max_batch=batch, seed=1)
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((batch, 4, nz, nx)).astype(np.float32)
+    Y = (0.1 * rng.standard_normal((batch, nz, nx))).astype(np.float32)
+    ms = net.profile_forward(X)
+    fl = conv_flops(nz, nx, batch)
+    layers = [{"cin": LAYERS[q][0], "cout": LAYERS[q][1], "level": LAYERS[q][2], "ms": float(ms[q]),
+               "tflops": float(fl[q] / (ms[q] * 1e-3) / 1e12)} for q in range(len(LAYERS))]
+    net.forward(X)
+    net.train_step(X, Y, 1e-4)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        net.forward(X)
+    tf = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        net.train_step(X, Y, 1e-4)
+    tt = (time.perf_counter() - t0) / reps
+    net.close()
+    return {"grid": f"{nx}x{nz}", "batch": batch, "layers": layers, "forward_gemm_ms": float(ms.sum()),
+            "forward_gemm_tflops": float(sum(fl) / (ms.sum() * 1e-3) / 1e12), "forward_ms": tf * 1e3,
+            "train_step_ms": tt * 1e3, "train_step_tflops": 3 * sum(fl) / tt / 1e12}
+
+
 if __name__ == "__main__":
     import argparse
     import json
 
-    ap = argparse.ArgumentParser(description="learned-guess evaluation at 512x256 (c4_study)")
-    ap.add_argument("out_dir")
+    ap = argparse.ArgumentParser(description="learned-guess study at 512x256 (c4_study) or GEMM profile")
+    ap.add_argument("out_dir", nargs="?", default=None)
     ap.add_argument("--train", type=int, default=1000)
     ap.add_argument("--test", type=int, default=200)
     ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--profile", action="store_true", help="time the network's GEMMs instead")
     a = ap.parse_args()
-    print(json.dumps(c4_study(a.out_dir, n_train=a.train, n_test=a.test, epochs=a.epochs)))
+    if a.profile:
+        print(json.dumps(profile()))
+    else:
+        print(json.dumps(c4_study(a.out_dir, n_train=a.train, n_test=a.test, epochs=a.epochs)))
 
 
 # (cin, cout, level) of the 14 convolutions, as built by the library (4 levels, width 32)
