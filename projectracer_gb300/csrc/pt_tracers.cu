@@ -408,23 +408,18 @@ __device__ __forceinline__ bool locate(double rr, double ss, TracerCell& c) {
 
 // One CTA per chunk of kPjChunk consecutive tracers, kPjPer consecutive tracers per lane.  The
 // tracers are kept in cell order, so a lane's tracers mostly share a cell: it keeps the running
-// sums of its current cell (a run) in registers.  A finished run is appended to its warp's run
-// queue in shared memory (slots by ballot rank: all lanes that finish a run in the same step write
-// at once), and when the queue is full the whole warp drains it, one run per lane, into a
-// shared-memory window of the grid (64-bit integer shared atomics).  At the end the window is
-// added to the global sums with one integer atomic per non-zero value.  The window is the box of
-// the cells of every lane's first and last tracer plus one cell of margin; runs outside it (and
-// every run when the box is too large for the window) go to the global sums directly.
+// sums of its current cell (a run) in registers.  A lane that finishes a run adds it at once to a
+// shared-memory window of the grid (64-bit integer shared atomics; 8% faster than queueing the
+// runs of a warp and draining them together, which moved every run through shared memory twice).
+// At the end the window is added to the global sums with one integer atomic per non-zero value.
+// The window is the box of the cells of every lane's first and last tracer plus one cell of
+// margin; runs outside it (and every run when the box is too large for the window) go to the
+// global sums directly.
 // acc: [node][TS, CS, S, count] int64; window planes [TS | CS | S + (count << 44)] (a chunk's S
 // stays below 2^44, its counts below 2^20).  runs (optional): the number of runs.
 constexpr int kPjThreads = 256, kPjPer = 16, kPjChunk = kPjThreads * kPjPer, kPjWin = 1280;
 constexpr int kPjCountShift = 44;
-constexpr int kPjWarps = kPjThreads / 32;
 
-struct RunQueue {                   // one per warp, structure of arrays (conflict-free slots)
-    int node[32];                   // lower-left node of the run's cell
-    unsigned long long v[13][32];   // TS[4], CS[4], S[4], packed corner counts
-};
 
 template <bool EXACT, bool COMP>
 __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __restrict__ r, const double* __restrict__ s,
@@ -433,11 +428,9 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
                                                               unsigned long long* __restrict__ acc, int* err,
                                                               unsigned long long* runs) {
     __shared__ unsigned long long win[3 * kPjWin];  // planes [TS | CS | S + count << 44] of the window
-    __shared__ RunQueue rq[kPjWarps];
     __shared__ int box[4];
     const int nx1 = cK.nx + 1;
     const int lane = threadIdx.x & 31;
-    RunQueue& Q = rq[threadIdx.x >> 5];
     const int64_t t0 = (int64_t)blockIdx.x * kPjChunk + (int64_t)threadIdx.x * kPjPer;
     const int64_t t1 = t0 + kPjPer < n ? t0 + kPjPer : n;
     int bad = 0;
@@ -453,7 +446,7 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
     }
     __syncthreads();
     // window: cells box +- 1, i.e. nodes [imin-1, imax+2] x [kmin-1, kmax+2], odd row pitch; its
-    // geometry is re-derived from box[] in the drains (fewer live registers in the tracer loop)
+    // geometry is re-derived from box[] where a run is flushed (fewer live registers in the tracer loop)
     auto geometry = [&](int& wi, int& wk, int& W, int& H, int& P) {
         wi = box[0] - 1; wk = box[2] - 1;
         W = box[1] - box[0] + 4; H = box[3] - box[2] + 4; P = W | 1;
@@ -466,44 +459,7 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
             __syncthreads();
         }
     }
-    int nq = 0;              // queued runs of this warp (warp-uniform)
     unsigned nruns = 0;      // runs of this lane
-    // the warp adds its nq queued runs, one per lane
-    auto drain = [&]() {
-        __syncwarp();
-        if (lane < nq) {
-            int wi, wk, W, H, P;
-            const bool use_win = geometry(wi, wk, W, H, P);
-            const int nd = Q.node[lane];
-            const int ci = nd % nx1, ck = nd / nx1;
-            const int li = ci - wi, lk = ck - wk;
-            const unsigned cnt = (unsigned)Q.v[12][lane];
-            if (use_win && li >= 0 && lk >= 0 && li + 1 < W && lk + 1 < H) {
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const int o = (li + (j & 1)) + P * (lk + (j >> 1));
-                    const unsigned long long vT = Q.v[j][lane], vC = Q.v[4 + j][lane];
-                    const unsigned long long vS = Q.v[8 + j][lane] +
-                                                  ((unsigned long long)((cnt >> (8 * j)) & 255u) << kPjCountShift);
-                    if (vT) atomicAdd(&win[o], vT);
-                    if (vC) atomicAdd(&win[kPjWin + o], vC);
-                    if (vS) atomicAdd(&win[2 * kPjWin + o], vS);
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const size_t node = (size_t)(ci + (j & 1)) + (size_t)nx1 * (size_t)(ck + (j >> 1));
-                    const unsigned long long v[4] = {Q.v[j][lane], Q.v[4 + j][lane], Q.v[8 + j][lane],
-                                                     (cnt >> (8 * j)) & 255u};
-#pragma unroll
-                    for (int p = 0; p < 4; p++)
-                        if (v[p]) atomicAdd(&acc[4 * node + p], v[p]);
-                }
-            }
-        }
-        __syncwarp();
-        nq = 0;
-    };
     long long aT[4], aC[4], aS[4];
     uint32_t cnt = 0;  // four 8-bit counters, one per corner (a run holds at most kPjPer tracers)
     int ri = -1, rk = -1;
@@ -516,23 +472,34 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
             if (!inside) bad |= 1;
         }
         const bool close = ri >= 0 && (fin || (inside && (c.i0 != ri || c.k0 != rk)));
-        const unsigned m = __ballot_sync(0xffffffffu, close);
-        if (m) {
-            if (nq + __popc(m) > 32) drain();
-            if (close) {
-                const int slot = nq + __popc(m & ((1u << lane) - 1u));
-                Q.node[slot] = ri + nx1 * rk;
+        if (close) {  // the run's sums into the window (or the global sums)
+            int wi, wk, W, H, P;
+            const bool use_win = geometry(wi, wk, W, H, P);
+            const int li = ri - wi, lk = rk - wk;
+            if (use_win && li >= 0 && lk >= 0 && li + 1 < W && lk + 1 < H) {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    Q.v[j][slot] = (unsigned long long)aT[j];
-                    Q.v[4 + j][slot] = (unsigned long long)aC[j];
-                    Q.v[8 + j][slot] = (unsigned long long)aS[j];
+                    const int o = (li + (j & 1)) + P * (lk + (j >> 1));
+                    const unsigned long long vT = (unsigned long long)aT[j], vC = (unsigned long long)aC[j];
+                    const unsigned long long vS = (unsigned long long)aS[j] +
+                                                  ((unsigned long long)((cnt >> (8 * j)) & 255u) << kPjCountShift);
+                    if (vT) atomicAdd(&win[o], vT);
+                    if (vC) atomicAdd(&win[kPjWin + o], vC);
+                    if (vS) atomicAdd(&win[2 * kPjWin + o], vS);
                 }
-                Q.v[12][slot] = cnt;
-                nruns++;
-                ri = -1;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const size_t node = (size_t)(ri + (j & 1)) + (size_t)nx1 * (size_t)(rk + (j >> 1));
+                    const unsigned long long v4[4] = {(unsigned long long)aT[j], (unsigned long long)aC[j],
+                                                      (unsigned long long)aS[j], (cnt >> (8 * j)) & 255u};
+#pragma unroll
+                    for (int p = 0; p < 4; p++)
+                        if (v4[p]) atomicAdd(&acc[4 * node + p], v4[p]);
+                }
             }
-            nq += __popc(m);
+            nruns++;
+            ri = -1;
         }
         if (!inside) return;
         if (ri < 0) {
@@ -570,7 +537,6 @@ __global__ void __launch_bounds__(kPjThreads, 3) k_project_fx(const double* __re
         }
     }
     step(false, 0.0, 0.0, 0.0, 0.0, true);  // close the open runs
-    if (nq) drain();
     if (bad) atomicOr(err, bad);
     if (runs) {
         const unsigned wr = __reduce_add_sync(0xffffffffu, nruns);
