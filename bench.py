@@ -634,14 +634,14 @@ def algorithmic_bytes(kid: int, cfg) -> float:
 
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
-# each kernel class on the 1024x512 grid with 4 tracers per cell (the commands and figures are in
-# the profiles/ summaries named here).  Grid kernels are captured at full size; the tracer
+# each kernel class on the 1024x512 grid (the commands, tracer counts and figures are in the
+# profiles/ summaries named here).  Grid kernels are captured at full size; the tracer
 # kernels' traffic grows with the tracer count and is scaled by it.  Cold-cache figures: ncu
 # flushes the caches before each pass, so for the L2-resident stage kernel this is an upper bound.
 NCU_TRAFFIC = {
     1: ("per launch", 17.05e6, "profiles/k_rkc_stage_f_C3_1024x512.md"),
     2: ("per tracer", 109.9e6 / 2097152, "profiles/k_rk_stage_f_C3_1024x512.md"),
-    3: ("per tracer", (555.24e6 + 19.88e6) / 16777216, "profiles/k_project_fx_C3_1024x512.md"),
+    3: ("per tracer", (554.03e6 + 16.40e6) / 16777216, "profiles/k_project_fx_C3_1024x512.md"),
 }
 
 
@@ -655,22 +655,30 @@ def ncu_traffic(kid: int, cfg):
 
 def roofline(kinds: dict, cfg) -> dict | None:
     """Roofline of the kernel class with the largest share of the timed region, from the live
-    event timings (launch-averaged)."""
+    event timings (launch-averaged), and the same figures for every timed kernel class."""
     peaks = measured_peaks()
-    timed = {KERNEL_NAMES[k]: {"launches": c, "total_ms": ms, "avg_ms": ms / c} for k, (c, ms) in kinds.items() if c}
-    if not timed:
-        return None
-    kid, (cnt, ms) = max(((k, v) for k, v in kinds.items() if v[0]), key=lambda kv: kv[1][1])
-    avg_s = ms / cnt * 1e-3
-    per = algorithmic_bytes(kid, cfg)
-    achieved = per / avg_s / 1e9
     from projectracer_gb300.config import PT_PREC_MIXED
 
-    traffic, src = ncu_traffic(kid, cfg) if cfg.precision == PT_PREC_MIXED else (None, None)  # mixed-path kernels
-    return {"bound": "hbm", "kernel": KERNEL_NAMES[kid], "achieved": achieved, "peak": peaks["hbm_gbs"],
-            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)",
-            "traffic": traffic, "traffic_source": src, "algorithmic_bytes_per_launch": per,
-            "avg_launch_ms": avg_s * 1e3, "timed_kernels": timed}
+    per_kernel = {}
+    for k, (c, ms) in kinds.items():
+        if not c:
+            continue
+        avg_s = ms / c * 1e-3
+        per = algorithmic_bytes(k, cfg)
+        achieved = per / avg_s / 1e9
+        traffic, src = ncu_traffic(k, cfg) if cfg.precision == PT_PREC_MIXED else (None, None)  # mixed-path kernels
+        per_kernel[k] = {"launches": c, "total_ms": ms, "avg_ms": avg_s * 1e3, "algorithmic_bytes_per_launch": per,
+                         "achieved_gbs": achieved, "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                         "traffic_source": src}
+    if not per_kernel:
+        return None
+    kid = max(per_kernel, key=lambda k: per_kernel[k]["total_ms"])
+    d = per_kernel[kid]
+    return {"bound": "hbm", "kernel": KERNEL_NAMES[kid], "achieved": d["achieved_gbs"], "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": d["frac"], "peak_source": peaks["source"] + " (burst copy)",
+            "traffic": d["traffic"], "traffic_source": d["traffic_source"],
+            "algorithmic_bytes_per_launch": d["algorithmic_bytes_per_launch"], "avg_launch_ms": d["avg_ms"],
+            "timed_kernels": {KERNEL_NAMES[k]: v for k, v in per_kernel.items()}}
 
 
 if __name__ == "__main__":

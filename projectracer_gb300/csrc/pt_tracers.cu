@@ -598,7 +598,8 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
         if ((rc = copy_field(E, E.Tratio, T0f))) return rc;
     }
     {
-        KernelTimer kt(E, KT_PROJECT, 1);
+        // the kernel timer brackets k_project_fx alone on the mixed path (the roofline's dominant
+        // kernel), the whole sort-based sequence on the FP64 path
         CK(cudaMemsetAsync(W.ccount, 0, sizeof(int32_t) * (size_t)ncell, E.st));
         CK(cudaMemsetAsync(W.derr, 0, sizeof(int), E.st));
         dim3 grid(nblk(nx + 1, 128), nz + 1);
@@ -611,9 +612,14 @@ static int project_with(Engine& E, const ProjScratch& W, const double* r, const 
             auto kern = E.K.exact_div ? (E.cfg.comp ? k_project_fx<true, true> : k_project_fx<true, false>)
                                       : (E.cfg.comp ? k_project_fx<false, true> : k_project_fx<false, false>);
             if (W.runs) CK(cudaMemsetAsync(W.runs, 0, sizeof(unsigned long long), E.st));
-            PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, W.derr, W.runs);
+            {
+                KernelTimer kt(E, KT_PROJECT, 1);
+                PT_COUNT(), kern<<<nblk(n, kPjChunk), kPjThreads, 0, E.st>>>(r, s, Tt, E.Ctr, n, acc, W.derr,
+                                                                             W.runs);
+            }
             PT_COUNT(), k_node_fx<<<grid, 128, 0, E.st>>>(acc, E.Tratio, E.Cnew, E.nempty, E.g1, E.cfg.comp);
         } else {  // the reference's association: ascending tracer ID per cell, FP64
+            KernelTimer kt(E, KT_PROJECT, 1);
             PT_COUNT(), k_cells<<<nblk(n, 256), 256, 0, E.st>>>(r, s, n, W.tcell, W.ccount, W.derr);
             int nb = (int)nblk(ncell, 1024);
             PT_COUNT(), k_scan_block<<<nb, 1024, 0, E.st>>>(W.ccount, W.cstart, W.scan_tmp, ncell);
