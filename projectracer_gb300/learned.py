@@ -280,8 +280,10 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
     (4 levels, width 32) is trained on n_train of them.  Held-out: new runs of the same sampling; at
     each top-of-step solve the FP64 solve to 1e-8 is run three times from the same state -- from
     zero, from the previous step's psi (the reference's warm start) and from the network's guess
-    (with its fallback to the previous psi after one cycle) -- and the V-cycles are recorded, with
-    the network's error on psi / max|psi| against the zero guess's."""
+    (with its fallback to the previous psi after one cycle) -- and a fourth time from the network's
+    guess with psi zeroed first (a cold start: the fallback then compares against the zero guess);
+    the V-cycles are recorded, with the network's error on psi / max|psi| against the zero
+    guess's."""
     import os
     import time
 
@@ -310,8 +312,8 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
     log(f"training: {epochs} epochs in {t_train:.1f} s, loss {hist[0]:.4g} -> {hist[-1]:.4g}")
     wpath = os.path.join(out_dir, "unet_c4.bin")
     net.save(wpath)
-    cyc = {"zero": [], "previous": [], "learned": []}
-    used, mse_net, mse_zero = [], [], []
+    cyc = {"zero": [], "previous": [], "learned": [], "learned_cold": []}
+    used, used_cold, mse_net, mse_zero = [], [], [], []
     test_runs, skipped = 0, 0
     while len(cyc["zero"]) < n_test:
         if test_runs > n_test + 50:
@@ -332,8 +334,11 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
                 cz = e.solve_psi()["cycles"]
                 xt, yt = training_pair(e)
                 pred = net.forward(xt[None])[0]
-                e.set(eng.F_SF, prev)
+                e.set(eng.F_SF, np.zeros_like(prev))  # cold start: the network against zero
                 e.set_guess_mode(PT_GUESS_UNET, wpath)
+                cc = e.solve_psi()["cycles"]
+                uc = guess_info()["used"]
+                e.set(eng.F_SF, prev)
                 cl = e.solve_psi()["cycles"]
                 ul = guess_info()["used"]
                 e.set(eng.F_SF, prev)
@@ -341,8 +346,10 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
                 cp = e.solve_psi()["cycles"]
                 cyc["zero"].append(cz)
                 cyc["learned"].append(cl)
+                cyc["learned_cold"].append(cc)
                 cyc["previous"].append(cp)
                 used.append(ul)
+                used_cold.append(uc)
                 mse_net.append(float(np.mean((pred - yt) ** 2)))
                 mse_zero.append(float(np.mean(yt ** 2)))
                 e.step()
@@ -359,7 +366,7 @@ def c4_study(out_dir: str, n_train: int = 1000, n_test: int = 200, steps_per_run
            "cycles_mean": {k: float(np.mean(v)) for k, v in cyc.items()},
            "cycles_median": {k: float(np.median(v)) for k, v in cyc.items()},
            "cycles_max": {k: int(np.max(v)) for k, v in cyc.items()},
-           "learned_guess_kept": float(np.mean(used)),
+           "learned_guess_kept": float(np.mean(used)), "learned_cold_guess_kept": float(np.mean(used_cold)),
            "heldout_mse_network": float(np.mean(mse_net)), "heldout_mse_zero_guess": float(np.mean(mse_zero))}
     with open(os.path.join(out_dir, "c4_study.json"), "w") as fh:
         import json
