@@ -285,7 +285,9 @@ int pt_tracers_to_corners_noalloc(const double* T0, int smooth_vis);
  * projection (smooth_vis=0).  The reference's shuffles and lottery order (mzran per OpenMP thread)
  * are replaced by a counter-based hash of (eq_seed, call, tracer or node): the result does not
  * depend on the tracer order or the thread count.  The columns of the reference's equalize.dat
- * line are returned in info (nullable).  pt_step calls it first when cfg.equalize = 1. */
+ * line are returned in info (nullable).  pt_step calls it first when cfg.equalize = 1.  A rich node
+ * holding more than 8192 tracers is refused with PT_ERR_ARG (ranking its donors costs tracers x
+ * donors on one thread). */
 typedef struct pt_equalize_info {
     int32_t tpc_type[2];     /* target tracers per node, type 0 / type 1 */
     int32_t minexcess[2];    /* after the moves (composition.f90:738-745) */

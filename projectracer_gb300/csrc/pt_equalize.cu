@@ -150,21 +150,31 @@ __global__ void k_eq_excess(const int32_t* __restrict__ cnt0, const int32_t* __r
     warp_add(acc + 5, e != 0 ? 1 : 0);
 }
 
-// donations per node and type (a rich node's tracers are all of one type); acc[6], acc[7] totals
-__global__ void k_eq_donations(const int32_t* __restrict__ nexc, const int32_t* __restrict__ cnt1,
-                               int32_t* __restrict__ d0, int32_t* __restrict__ d1, int nn, unsigned long long* acc) {
+// donations per node and type (a rich node's tracers are all of one type); acc[6], acc[7] totals;
+// acc[15] = the most tracers on one rich node (the donor ranking costs tracers x donors per node)
+__global__ void k_eq_donations(const int32_t* __restrict__ nexc, const int32_t* __restrict__ cnt0,
+                               const int32_t* __restrict__ cnt1, int32_t* __restrict__ d0,
+                               int32_t* __restrict__ d1, int nn, unsigned long long* acc) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     int a = 0, b = 0;
+    unsigned long long m = 0;
     if (q < nn) {
         const int e = nexc[q] > 0 ? nexc[q] : 0;
         if (cnt1[q] > 0) b = e;
         else a = e;
         d0[q] = a;
         d1[q] = b;
+        if (e > 0) m = (unsigned long long)(cnt0[q] + cnt1[q]);
     }
     warp_add(acc + 6, a);
     warp_add(acc + 7, b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(acc + 15, m);
 }
+
+// a rich node holding more tracers than this is refused (its donor ranking would take seconds)
+constexpr int kEqMaxNode = 8192;
 
 // a rich node's donors: its nexc tracers of smallest (near-wall class, key(1, call, id), id), in
 // that order, into the donor list of their type at the node's offset; its excess becomes 0
@@ -450,9 +460,11 @@ int equalize_tracers(Engine& E, pt_equalize_info* info) {
     }
     E.eq_done++;
     // 3. donors
-    PT_COUNT(), k_eq_donations<<<nb, 256, 0, E.st>>>(S.nexc, S.cnt1, S.d0, S.d1, nn, S.acc);
+    PT_COUNT(), k_eq_donations<<<nb, 256, 0, E.st>>>(S.nexc, S.cnt0, S.cnt1, S.d0, S.d1, nn, S.acc);
     if ((rc = exclusive_scan_i32(E, S.d0, S.off0, nn)) || (rc = exclusive_scan_i32(E, S.d1, S.off1, nn))) return rc;
     if ((rc = read_acc(E, S))) return rc;
+    if (S.hacc[15] > (unsigned long long)kEqMaxNode)
+        return fail(PT_ERR_ARG, "tracer equalisation: a node holds more than 8192 tracers");
     const int64_t ndon[2] = {(int64_t)S.hacc[6], (int64_t)S.hacc[7]};
     const int64_t need_cap = ndon[0] > ndon[1] ? ndon[0] : ndon[1];
     if (need_cap > S.dcap) {
