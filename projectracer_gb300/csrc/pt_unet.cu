@@ -159,15 +159,57 @@ __device__ __forceinline__ uint16_t dz_bf(const float* dY, const uint16_t* Y, si
     return f2bf(g);
 }
 
-// backward data: dX[q][ci] = sum_{t,co} dZ[q + tap t][co] w[co][8 - t][ci]  (FP32 out)
+// backward data: dX[q][ci] = sum_{t,co} dZ[q + tap t][co] w[co][8 - t][ci]  (FP32 out).  K is
+// ordered (t, co): a gather_a8 takes 8 consecutive channels of dZ at one shifted pixel (two 16-byte
+// loads of dY, one of the ReLU mask), a gather_b8 8 consecutive weights of wbd[ci][t][co] =
+// w[co][8 - t][ci], the layout k_w_bwd_layout writes before the GEMM.
 struct ConvBwdData {
-    static constexpr bool kVec = false;
+    static constexpr bool kVec = true;
     int M, N, K, Ntile, kc_split;  // M pixels, N = Cin, K = 9 Cout
     int H, W, Cout;
     const float* dY;
     const uint16_t* Y;
     const uint16_t* w;
+    const uint16_t* wbd;
     float* dX;
+    __device__ __forceinline__ uint4 gather_a8(int q, int k0) const {
+        if ((Cout & 7) || k0 + 8 > K) {
+            uint16_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = gather_a(q, k0 + j);
+            return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+        }
+        if (q >= M) return make_uint4(0u, 0u, 0u, 0u);
+        const int t = k0 / Cout, co = k0 - t * Cout;
+        int b, y, x;
+        if (!tap_pixel(q, t, H, W, b, y, x)) return make_uint4(0u, 0u, 0u, 0u);
+        const size_t idx = (((size_t)b * H + y) * W + x) * Cout + co;
+        const float4 g0 = *reinterpret_cast<const float4*>(dY + idx), g1 = *reinterpret_cast<const float4*>(dY + idx + 4);
+        const float g[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+        uint16_t h[8];
+        if (Y) {
+            const uint4 m = ld8(Y + idx);
+            const uint32_t mm[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const uint16_t yb = (uint16_t)(mm[j >> 1] >> (16 * (j & 1)));
+                h[j] = bf2f(yb) > 0.f ? f2bf(g[j]) : (uint16_t)0;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) h[j] = f2bf(g[j]);
+        }
+        return make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+    }
+    __device__ __forceinline__ uint4 gather_b8(int ci, int k0) const {
+        if ((K & 7) || ci >= N || k0 + 8 > K) {
+            uint16_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = gather_b(ci, k0 + j);
+            return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+        }
+        return ld8(wbd + (size_t)ci * K + k0);
+    }
     __device__ __forceinline__ uint16_t gather_a(int q, int k) const {
         if (q >= M || k >= K) return 0;
         const int t = k / Cout, co = k - t * Cout;
@@ -205,6 +247,16 @@ struct ConvBwdW {
         part[((size_t)z * M + kk) * N + co] = v;
     }
 };
+
+// wbd[ci][t][co] = w[co][8 - t][ci]: the weights in the K order of the backward-data GEMM
+__global__ void k_w_bwd_layout(uint16_t* __restrict__ wbd, const uint16_t* __restrict__ w, int cin, int cout) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (size_t)cin * 9 * cout) return;
+    const int co = (int)(q % cout);
+    const int t = (int)((q / cout) % 9);
+    const int ci = (int)(q / ((size_t)cout * 9));
+    wbd[q] = w[((size_t)co * 9 + (8 - t)) * cin + ci];
+}
 
 // dW[co][kk] = sum_z part[z][kk][co], z ascending
 __global__ void k_wgrad_reduce(float* dW, const float* part, int nsplit, int M, int N) {
@@ -369,6 +421,7 @@ struct UNet {
     size_t nparams = 0, out_w = 0, out_b = 0;
     float *w32 = nullptr, *m = nullptr, *v = nullptr, *g = nullptr;
     uint16_t* wbf = nullptr;
+    uint16_t* wbd = nullptr;  // one layer's weights in the backward-data K order (k_w_bwd_layout)
     int step = 0;
     uint16_t* act[14] = {};
     float* grad[14] = {};
@@ -438,8 +491,11 @@ static int unet_build(UNet& U, int H, int W, int maxB, uint64_t seed) {
     off += 1;
     U.nparams = off;
     int rc;
+    size_t wmax = 0;
+    for (auto& c : U.L) wmax = std::max(wmax, (size_t)c.cout * 9 * c.cin);
     if ((rc = ualloc(U, &U.w32, off)) || (rc = ualloc(U, &U.m, off)) || (rc = ualloc(U, &U.v, off)) ||
-        (rc = ualloc(U, &U.g, off)) || (rc = ualloc(U, &U.wbf, off)) || (rc = ualloc(U, &U.derr, 1)))
+        (rc = ualloc(U, &U.g, off)) || (rc = ualloc(U, &U.wbf, off)) || (rc = ualloc(U, &U.wbd, wmax)) ||
+        (rc = ualloc(U, &U.derr, 1)))
         return rc;
     // He-normal initialisation from a portable generator; biases zero
     std::vector<float> h(off, 0.f);
@@ -570,7 +626,10 @@ static int unet_backward(UNet& U, int B, float* loss) {
         CK(cudaGetLastError());
         if (c.src0 < 0) continue;  // the network input needs no gradient
         if ((size_t)P * c.cin > U.dxg_cap) return fail(PT_ERR_STATE, "U-Net: view-gradient workspace too small");
-        ConvBwdData bd{P, c.cin, 9 * c.cout, ntile_for(c.cin), 0, v.H, v.W, c.cout, dY, Y, U.wbf + c.woff, U.dXg};
+        const size_t nw = (size_t)c.cin * 9 * c.cout;
+        k_w_bwd_layout<<<nblk(nw, 256), 256, 0, U.st>>>(U.wbd, U.wbf + c.woff, c.cin, c.cout);
+        ConvBwdData bd{P, c.cin, 9 * c.cout, ntile_for(c.cin), 0, v.H, v.W, c.cout, dY, Y, U.wbf + c.woff, U.wbd,
+                       U.dXg};
         if (int rc = run_gemm(U, bd, 1)) return rc;
         if (c.mode == 0) {
             const size_t n = (size_t)P * c.cin;
