@@ -405,6 +405,16 @@ def profile(nz: int = 256, nx: int = 512, batch: int = 8, reps: int = 5) -> dict
             "train_step_ms": tt * 1e3, "train_step_tflops": 3 * sum(fl) / tt / 1e12}
 
 
+# (cin, cout, level) of the 14 convolutions, as built by the library (4 levels, width 32)
+LAYERS = [(4, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2), (128, 256, 3),
+          (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1), (64, 64, 1), (96, 32, 0), (32, 32, 0)]
+
+
+def conv_flops(nz: int, nx: int, batch: int) -> list[float]:
+    """FLOPs of each convolution GEMM of one forward pass (2 per multiply-add)."""
+    return [18.0 * ci * co * batch * nz * nx / 4 ** lv for ci, co, lv in LAYERS]
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -421,12 +431,3 @@ if __name__ == "__main__":
     else:
         print(json.dumps(c4_study(a.out_dir, n_train=a.train, n_test=a.test, epochs=a.epochs)))
 
-
-# (cin, cout, level) of the 14 convolutions, as built by the library (4 levels, width 32)
-LAYERS = [(4, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2), (128, 256, 3),
-          (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1), (64, 64, 1), (96, 32, 0), (32, 32, 0)]
-
-
-def conv_flops(nz: int, nx: int, batch: int) -> list[float]:
-    """FLOPs of each convolution GEMM of one forward pass (2 per multiply-add)."""
-    return [18.0 * ci * co * batch * nz * nx / 4 ** lv for ci, co, lv in LAYERS]
