@@ -639,7 +639,7 @@ def algorithmic_bytes(kid: int, cfg) -> float:
 # kernels' traffic grows with the tracer count and is scaled by it.  Cold-cache figures: ncu
 # flushes the caches before each pass, so for the L2-resident stage kernel this is an upper bound.
 NCU_TRAFFIC = {
-    1: ("per launch", 17.05e6, "profiles/k_rkc_stage_f_C3_1024x512.md"),
+    1: ("per launch", 17.09e6, "profiles/k_rkc_stage_f2_C3_1024x512.md"),
     2: ("per tracer", 109.9e6 / 2097152, "profiles/k_rk_stage_f_C3_1024x512.md"),
     3: ("per tracer", (554.03e6 + 16.40e6) / 16777216, "profiles/k_project_fx_C3_1024x512.md"),
 }
