@@ -646,6 +646,10 @@ static int step_chebyshev(ptref_state* s) {
     double dt = stability_RK4(s);
     if (s->status) return s->status;
     s->dt = dt;
+    if (s->cfg.equalize) { /* Chebyshev.f90:131-137, after the time step */
+        int erc = ptref_equalize(s, -1, NULL);
+        if (erc) return erc;
+    }
     rfld C0 = ref_fld_alloc(nx, nz, 5);
     rfld T0 = ref_fld_alloc(nx, nz, 3);
     if (comp) copy_fld(&C0, &s->Cnew);

@@ -82,3 +82,21 @@ def test_equalize_config_checks():
     with pytest.raises(eng.PtError) as ex:
         eng.Engine(cfg)
     assert "equalize" in str(ex.value)
+
+
+def test_rkc2_step_with_equalize_matches_oracle():
+    """The RKC2 stepper equalises first too (Chebyshev.f90:131-137)."""
+    cfg, st = clustered("chem")
+    cfg.chebyshev, cfg.nstage = 1, 3
+    o = oracle_for(cfg, st)
+    e = eng.Engine(cfg)
+    e.upload(st)
+    e.solve_psi()
+    o.solve_psi()
+    dt, _ = e.step()
+    o.step()
+    assert dt == o.scalar("dt")
+    for fid, oid in ((eng.F_TRACER_R, 20), (eng.F_TRACER_S, 21), (eng.F_TRACER_T, 22)):
+        assert rel_err(e.get(fid), o.get(oid)) <= 1e-10, fid
+    assert np.array_equal(e.get(eng.F_TRACER_TYPE), o.get(24))
+    e.close()
