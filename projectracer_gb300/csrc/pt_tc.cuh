@@ -8,9 +8,12 @@
 //     8-row groups (8 core matrices per 64-wide chunk);
 //   * two stages: while the MMAs of chunk c read one stage, the threads gather chunk c+1 into the
 //     other; a stage is overwritten only after the MMAs of the chunk two back have completed;
-//   * a problem with P::kVec gathers 8 consecutive K elements (one 16-byte core-matrix row) per
-//     call (gather_a8 / gather_b8), with the threads spread over rows first so that a warp's
-//     16-byte stores hit all 32 banks; otherwise one element per call;
+//   * P::kGather says how a problem fills the tiles: kGatherElem one element per call;
+//     kGatherRow 8 consecutive K elements (one 16-byte core-matrix row) per call (gather_a8 /
+//     gather_b8), the threads spread over rows first so that a warp's 16-byte stores hit all 32
+//     banks; kGatherCol 8 consecutive rows at one K index per call (gather_col_a / gather_col_b,
+//     for operands whose K is strided in memory): 8 lanes load the 8 columns of a core matrix and
+//     transpose it among themselves with three shuffle stages, each lane then storing one row;
 //   * one thread issues the four K=16 MMAs of a chunk (tcgen05.mma.cta_group::1.kind::f16) and
 //     commits them to the stage's mbarrier; waits on it are bounded spins;
 //   * the epilogue reads the accumulator with tcgen05.ld.32x32b (warp w owns TMEM lanes
@@ -124,10 +127,59 @@ __host__ __device__ constexpr uint32_t tmem_cols(int n) {
 __host__ __device__ constexpr size_t stage_bytes(int n) { return 16384 + (size_t)n * 128; }
 __host__ __device__ constexpr size_t smem_bytes(int n) { return 2 * stage_bytes(n) + 64 + 16384; }
 
+constexpr int kGatherElem = 0, kGatherRow = 1, kGatherCol = 2;
+
+// 8 x 8 transpose of 16-bit values among the 8 lanes of an aligned lane group: lane j holds
+// column j (v = M[0..7][j], two values per word) on entry and row j (M[j][0..7]) on return
+// (butterfly stages exchanging 4-, 2- and 1-element blocks with lanes j^4, j^2, j^1)
+__device__ __forceinline__ uint4 transpose8(uint4 v, int j) {
+    uint32_t w0 = v.x, w1 = v.y, w2 = v.z, w3 = v.w;
+    {
+        const bool b = j & 4;
+        const uint32_t r0 = __shfl_xor_sync(0xffffffffu, b ? w0 : w2, 4);
+        const uint32_t r1 = __shfl_xor_sync(0xffffffffu, b ? w1 : w3, 4);
+        if (b) { w0 = r0; w1 = r1; } else { w2 = r0; w3 = r1; }
+    }
+    {
+        const bool b = j & 2;
+        const uint32_t r0 = __shfl_xor_sync(0xffffffffu, b ? w0 : w1, 2);
+        const uint32_t r1 = __shfl_xor_sync(0xffffffffu, b ? w2 : w3, 2);
+        if (b) { w0 = r0; w2 = r1; } else { w1 = r0; w3 = r1; }
+    }
+    {
+        const bool b = j & 1;
+        const uint32_t s0 = b ? __byte_perm(w0, w1, 0x5410) : __byte_perm(w0, w1, 0x7632);
+        const uint32_t s1 = b ? __byte_perm(w2, w3, 0x5410) : __byte_perm(w2, w3, 0x7632);
+        const uint32_t r0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+        const uint32_t r1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+        if (b) {
+            w0 = __byte_perm(w0, r0, 0x3254); w1 = __byte_perm(w1, r0, 0x3276);
+            w2 = __byte_perm(w2, r1, 0x3254); w3 = __byte_perm(w3, r1, 0x3276);
+        } else {
+            w0 = __byte_perm(w0, r0, 0x5410); w1 = __byte_perm(w1, r0, 0x7610);
+            w2 = __byte_perm(w2, r1, 0x5410); w3 = __byte_perm(w3, r1, 0x7610);
+        }
+    }
+    return make_uint4(w0, w1, w2, w3);
+}
+
 template <class P>
 __device__ __forceinline__ void gather_chunk(const P& prob, unsigned char* sa, unsigned char* sb, int m0, int col0,
                                              int n, int k0, int tid) {
-    if constexpr (P::kVec) {
+    if constexpr (P::kGather == kGatherCol) {
+        // core matrix cm = (row block cm / 8, K group cm % 8): 4 per warp at a time, 8 lanes each
+        const int lane = tid & 31, j = lane & 7, g = (tid >> 3);
+        for (int cm = g; cm < (kTileM / 8) * (kChunkK / 8); cm += kThreads / 8) {
+            const int rb = cm >> 3, kg = cm & 7;
+            const uint4 v = transpose8(prob.gather_col_a(m0 + rb * 8, k0 + kg * 8 + j), j);
+            *reinterpret_cast<uint4*>(sa + tile_off(rb * 8 + j, kg * 8)) = v;
+        }
+        for (int cm = g; cm < (n / 8) * (kChunkK / 8); cm += kThreads / 8) {
+            const int rb = cm >> 3, kg = cm & 7;
+            const uint4 v = transpose8(prob.gather_col_b(col0 + rb * 8, k0 + kg * 8 + j), j);
+            *reinterpret_cast<uint4*>(sb + tile_off(rb * 8 + j, kg * 8)) = v;
+        }
+    } else if constexpr (P::kGather == kGatherRow) {
         for (int q = tid; q < kTileM * (kChunkK / 8); q += kThreads) {
             const int r = q % kTileM, kg = q / kTileM;
             *reinterpret_cast<uint4*>(sa + tile_off(r, kg * 8)) = prob.gather_a8(m0 + r, k0 + kg * 8);

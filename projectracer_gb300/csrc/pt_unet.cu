@@ -17,7 +17,7 @@ namespace pt {
 
 // plain GEMM problem: C (M x N, FP32) = A (M x K) * B (N x K)^T, BF16 row-major operands
 struct GemmProb {
-    static constexpr bool kVec = false;
+    static constexpr int kGather = tc::kGatherElem;
     int M, N, K, Ntile, kc_split;
     const uint16_t* A;
     const uint16_t* B;
@@ -73,12 +73,63 @@ __device__ __forceinline__ bool tap_pixel(int p, int tap, int H, int W, int& b, 
 __device__ __forceinline__ uint4 ld8(const uint16_t* p) { return *reinterpret_cast<const uint4*>(p); }
 __device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
 
+// channels c..c+7 of a view at pixel (b, y, x) as 8 BF16 values (c, C0 and C1 multiples of 8):
+// one 16-byte load, or four averaged in the order of InView::get for a pooled view
+__device__ __forceinline__ uint4 view_load8(const InView& in, int b, int y, int x, int c) {
+    if (in.mode == 0) return ld8(in.t0 + (((size_t)b * in.H + y) * in.W + x) * in.C0 + c);
+    if (in.mode == 2) {
+        if (c < in.C0) return ld8(in.t0 + (((size_t)b * (in.H >> 1) + (y >> 1)) * (in.W >> 1) + (x >> 1)) * in.C0 + c);
+        return ld8(in.t1 + (((size_t)b * in.H + y) * in.W + x) * in.C1 + (c - in.C0));
+    }
+    const size_t W2 = 2 * (size_t)in.W;
+    const uint16_t* q = in.t0 + (((size_t)b * 2 * in.H + 2 * y) * W2 + 2 * x) * in.C0 + c;
+    const uint4 a = ld8(q), bq = ld8(q + in.C0), cq = ld8(q + W2 * in.C0), d = ld8(q + W2 * in.C0 + in.C0);
+    const uint32_t* pa = &a.x;
+    const uint32_t* pb = &bq.x;
+    const uint32_t* pc = &cq.x;
+    const uint32_t* pd = &d.x;
+    uint32_t o[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        uint16_t h[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            const int sh = 16 * e;
+            const float sum = ((bf2f((uint16_t)(pa[j] >> sh)) + bf2f((uint16_t)(pb[j] >> sh))) +
+                               bf2f((uint16_t)(pc[j] >> sh))) + bf2f((uint16_t)(pd[j] >> sh));
+            h[e] = f2bf(sum * 0.25f);
+        }
+        o[j] = pack2(h[0], h[1]);
+    }
+    return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+// channels c..c+7 of dZ (the ReLU-masked gradient, BF16) at flat index idx = pixel * C + c
+__device__ __forceinline__ uint4 dz_load8(const float* dY, const uint16_t* Y, size_t idx) {
+    const float4 g0 = *reinterpret_cast<const float4*>(dY + idx), g1 = *reinterpret_cast<const float4*>(dY + idx + 4);
+    const float g[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+    uint16_t h[8];
+    if (Y) {
+        const uint4 m = ld8(Y + idx);
+        const uint32_t mm[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint16_t yb = (uint16_t)(mm[j >> 1] >> (16 * (j & 1)));
+            h[j] = bf2f(yb) > 0.f ? f2bf(g[j]) : (uint16_t)0;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) h[j] = f2bf(g[j]);
+    }
+    return make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+}
+
 // forward: out[p][co] = relu(sum_{tap,ci} in(p+tap)[ci] w[co][tap][ci] + bias[co]) in BF16.
 // K = 9 cin, ordered (tap, ci): with cin a multiple of 8 the 8 values of a gather_a8 are 8
 // consecutive channels of one pixel (one 16-byte load of an NHWC tensor, four for a pooled view),
 // and those of a gather_b8 8 consecutive weights; the first layer (cin = 4) gathers element-wise.
 struct ConvFwd {
-    static constexpr bool kVec = true;
+    static constexpr int kGather = tc::kGatherRow;
     int M, N, K, Ntile, kc_split;
     InView in;
     const uint16_t* w;
@@ -107,34 +158,7 @@ struct ConvFwd {
         const int tap = k0 / cin, ci = k0 - tap * cin;
         int b, y, x;
         if (!tap_pixel(p, tap, in.H, in.W, b, y, x)) return make_uint4(0u, 0u, 0u, 0u);
-        if (in.mode == 0) return ld8(in.t0 + (((size_t)b * in.H + y) * in.W + x) * in.C0 + ci);
-        if (in.mode == 2) {
-            if (ci < in.C0)
-                return ld8(in.t0 + (((size_t)b * (in.H >> 1) + (y >> 1)) * (in.W >> 1) + (x >> 1)) * in.C0 + ci);
-            return ld8(in.t1 + (((size_t)b * in.H + y) * in.W + x) * in.C1 + (ci - in.C0));
-        }
-        // 2x2 average of the finer tensor, summed in the order of InView::get
-        const size_t W2 = 2 * (size_t)in.W;
-        const uint16_t* q = in.t0 + (((size_t)b * 2 * in.H + 2 * y) * W2 + 2 * x) * in.C0 + ci;
-        const uint4 a = ld8(q), bq = ld8(q + in.C0), c = ld8(q + W2 * in.C0), d = ld8(q + W2 * in.C0 + in.C0);
-        const uint32_t* pa = &a.x;
-        const uint32_t* pb = &bq.x;
-        const uint32_t* pc = &c.x;
-        const uint32_t* pd = &d.x;
-        uint32_t o[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            uint16_t h[2];
-#pragma unroll
-            for (int e = 0; e < 2; e++) {
-                const int sh = 16 * e;
-                const float sum = ((bf2f((uint16_t)(pa[j] >> sh)) + bf2f((uint16_t)(pb[j] >> sh))) +
-                                   bf2f((uint16_t)(pc[j] >> sh))) + bf2f((uint16_t)(pd[j] >> sh));
-                h[e] = f2bf(sum * 0.25f);
-            }
-            o[j] = pack2(h[0], h[1]);
-        }
-        return make_uint4(o[0], o[1], o[2], o[3]);
+        return view_load8(in, b, y, x, ci);
     }
     __device__ __forceinline__ uint4 gather_b8(int co, int k0) const {
         if ((K & 7) || co >= N || k0 + 8 > K) {
@@ -164,7 +188,7 @@ __device__ __forceinline__ uint16_t dz_bf(const float* dY, const uint16_t* Y, si
 // loads of dY, one of the ReLU mask), a gather_b8 8 consecutive weights of wbd[ci][t][co] =
 // w[co][8 - t][ci], the layout k_w_bwd_layout writes before the GEMM.
 struct ConvBwdData {
-    static constexpr bool kVec = true;
+    static constexpr int kGather = tc::kGatherRow;
     int M, N, K, Ntile, kc_split;  // M pixels, N = Cin, K = 9 Cout
     int H, W, Cout;
     const float* dY;
@@ -183,23 +207,7 @@ struct ConvBwdData {
         const int t = k0 / Cout, co = k0 - t * Cout;
         int b, y, x;
         if (!tap_pixel(q, t, H, W, b, y, x)) return make_uint4(0u, 0u, 0u, 0u);
-        const size_t idx = (((size_t)b * H + y) * W + x) * Cout + co;
-        const float4 g0 = *reinterpret_cast<const float4*>(dY + idx), g1 = *reinterpret_cast<const float4*>(dY + idx + 4);
-        const float g[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
-        uint16_t h[8];
-        if (Y) {
-            const uint4 m = ld8(Y + idx);
-            const uint32_t mm[4] = {m.x, m.y, m.z, m.w};
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const uint16_t yb = (uint16_t)(mm[j >> 1] >> (16 * (j & 1)));
-                h[j] = bf2f(yb) > 0.f ? f2bf(g[j]) : (uint16_t)0;
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < 8; j++) h[j] = f2bf(g[j]);
-        }
-        return make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+        return dz_load8(dY, Y, (((size_t)b * H + y) * W + x) * Cout + co);
     }
     __device__ __forceinline__ uint4 gather_b8(int ci, int k0) const {
         if ((K & 7) || ci >= N || k0 + 8 > K) {
@@ -227,7 +235,7 @@ struct ConvBwdData {
 
 // backward weights (split over pixels): part[z][tap*Cin + ci][co] = sum_{p in split z} in(p+tap)[ci] dZ[p][co]
 struct ConvBwdW {
-    static constexpr bool kVec = false;
+    static constexpr int kGather = tc::kGatherCol;
     int M, N, K, Ntile, kc_split;  // M = 9 Cin, N = Cout, K = pixels
     InView in;
     const float* dY;
@@ -242,6 +250,32 @@ struct ConvBwdW {
     }
     __device__ __forceinline__ uint16_t gather_b(int co, int p) const {
         return (co < N && p < K) ? dz_bf(dY, Y, (size_t)p * N + co) : (uint16_t)0;
+    }
+    // A[kk0..kk0+7][p]: channels ci..ci+7 of the input at pixel p shifted by the rows' tap
+    __device__ __forceinline__ uint4 gather_col_a(int kk0, int p) const {
+        const int cin = in.C();
+        if ((cin & 7) || (in.C0 & 7)) {
+            uint16_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = gather_a(kk0 + j, p);
+            return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+        }
+        if (kk0 >= M || p >= K) return make_uint4(0u, 0u, 0u, 0u);
+        const int tap = kk0 / cin, ci = kk0 - tap * cin;
+        int b, y, x;
+        if (!tap_pixel(p, tap, in.H, in.W, b, y, x)) return make_uint4(0u, 0u, 0u, 0u);
+        return view_load8(in, b, y, x, ci);
+    }
+    // B[co0..co0+7][p]: channels co0..co0+7 of dZ at pixel p
+    __device__ __forceinline__ uint4 gather_col_b(int co0, int p) const {
+        if (N & 7) {
+            uint16_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = gather_b(co0 + j, p);
+            return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+        }
+        if (co0 >= N || p >= K) return make_uint4(0u, 0u, 0u, 0u);
+        return dz_load8(dY, Y, (size_t)p * N + co0);
     }
     __device__ __forceinline__ void store(int kk, int co, int z, float v) const {
         part[((size_t)z * M + kk) * N + co] = v;
