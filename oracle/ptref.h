@@ -1,6 +1,6 @@
 /*
  * ptref -- CPU oracle: a plain-C restatement of the ProjecTracer hot path, used ONLY as test
- * infrastructure (parity checker) and as the timed CPU baseline ("port").  The product library
+ * infrastructure (the parity tests compare against it) and as the timed CPU baseline ("port").  The product library
  * never links, loads or calls anything in this directory.
  *
  * Every function cites the reference routine it follows (ProjecTracer_Source/<file>:<lines>).

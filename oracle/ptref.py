@@ -1,6 +1,6 @@
 """ctypes wrapper of the CPU oracle (libptref.so).
 
-Test infrastructure only: imported by tests/, by __graft_entry__.smoke() as the checker, and by
+Test infrastructure only: imported by tests/, by __graft_entry__.smoke() to check its GPU result, and by
 bench.py's CPU-baseline leg.  The product package never imports this module.
 """
 
