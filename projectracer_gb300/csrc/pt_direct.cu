@@ -305,64 +305,139 @@ __global__ void __launch_bounds__(kLuThreads) k_direct_lu(double* ab, int* ipiv,
 }
 
 // DGBTRS (TRANS='N', one right-hand side): forward substitution with the interchanges and L,
-// back substitution with U (dtbsv), one warp carrying the sequential column steps, the band
-// columns staged through shared memory `chunk` at a time by the whole CTA.  Same operations in the
-// same order as the column-by-column DGBTRS; zero entries are divided and propagated too, like the
-// optimized BLAS of the shipped run (psi = -0 on the non-corner wall nodes of its snapshots).
-constexpr int kDsThreads = 128;
-static size_t direct_solve_smem(int n, int kl, int ku, int chunk) {
-    return sizeof(double) * ((size_t)n + (size_t)chunk * (size_t)(kl + ku + 1)) + sizeof(int) * (size_t)chunk;
+// back substitution with U (dtbsv).  Same operations in the same order for every element as the
+// column-by-column DGBTRS; zero entries are divided and propagated too, like the optimized BLAS of
+// the shipped run (psi = -0 on the non-corner wall nodes of its snapshots).
+//
+// The column steps are sequential, so one CTA carries them, with b in shared memory.  Every
+// element of b has one owner thread (element i: thread (i - 1) mod kDsThreads), which alone
+// writes it: in a column step each thread applies the column to the elements it owns, and the
+// value the next step needs first (the pivot row's b for the forward step, the next x = b / U_jj
+// for the back substitution) is published by its owner at the end of the step, so a step needs
+// one barrier.  The band columns stream through a ring of kDsRing shared-memory slots, filled by
+// cp.async kDsAhead columns ahead of their step (16-byte copies from the 16-byte boundary at or
+// below the column's first entry; `off` is the column's position in its slot).  On this part a
+// step is bound by the SM's FP64 pipe: forward kl, backward kl + ku multiply-subtract pairs.
+constexpr int kDsThreads = 256, kDsAhead = 8, kDsRing = kDsAhead + 1;
+static __host__ __device__ int direct_slot_len(int kl, int ku) { return (kl + ku + 3) & ~1; }
+static size_t direct_solve_smem(int n, int kl, int ku) {
+    return sizeof(double) * ((size_t)kDsRing * (size_t)direct_slot_len(kl, ku) + (size_t)n + 4) +
+           sizeof(int) * (size_t)kDsRing;
 }
-__global__ void __launch_bounds__(kDsThreads) k_direct_solve(const double* ab, const int* ipiv, double* bg, int n,
-                                                           int kl, int ku, int chunk) {
-    extern __shared__ double b[];
-    const int ldab = 2 * kl + ku + 1, kd = ku + kl + 1, kp1 = kl + ku + 1, k = kl + ku;
-    double* cb = b + n;
-    int* cp = reinterpret_cast<int*>(cb + (size_t)chunk * kp1);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+__device__ __forceinline__ void ds_cp16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void ds_cp4(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void ds_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void ds_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// copies band entries [s0, s0 + len) into a slot from the even index at or below s0 (the slot
+// then holds entry s0 at position s0 & 1); every thread commits one group, empty or not
+__device__ __forceinline__ void ds_issue(double* slot, const double* ab, size_t s0, int len, bool live, int tid) {
+    if (live) {
+        const size_t a0 = s0 & ~(size_t)1;
+        const int pairs = (int)((s0 - a0) + (size_t)len + 1) >> 1;
+        for (int q = tid; q < pairs; q += kDsThreads) ds_cp16(slot + 2 * q, ab + a0 + 2 * (size_t)q);
+    }
+    ds_commit();
+}
+
+__global__ void __launch_bounds__(kDsThreads, 1) k_direct_solve(const double* __restrict__ ab, const int* __restrict__ ipiv,
+                                                               double* __restrict__ bg, int n, int kl, int ku) {
+    extern __shared__ __align__(16) double dsm[];
+    const int SL = direct_slot_len(kl, ku);
+    double* ring = dsm;                                  // kDsRing slots of SL doubles
+    double* b = ring + (size_t)kDsRing * SL;             // n
+    double* pub = b + n;                                 // [2]: published values, by step parity
+    int* ipr = reinterpret_cast<int*>(pub + 4);          // pivots of the columns in the ring
+    const int ldab = 2 * kl + ku + 1, kd = kl + ku + 1, kp1 = kl + ku + 1, k = kl + ku;
+    const int tid = threadIdx.x;
+    // the first element >= a that this thread owns
+    auto first_owned = [&](int a) {
+        int r = (tid - (a - 1)) % kDsThreads;
+        if (r < 0) r += kDsThreads;
+        return a + r;
+    };
+    auto owns = [&](int i) { return (i - 1) % kDsThreads == tid; };
+
+    // ---- forward: for j = 1 .. n-1, b(j) <-> b(ipiv(j)), then b(j+1 .. j+lm) += L(., j) * (-b(j))
+    auto issue_fwd = [&](int c) {  // column c's multipliers AB(kd+1 .. kd+kl, c) and its pivot
+        const bool live = c <= n - 1;
+        double* slot = ring + (size_t)(c % kDsRing) * SL;
+        if (live && tid == 0) ds_cp4(ipr + c % kDsRing, ipiv + (c - 1));
+        ds_issue(slot, ab, (size_t)kd + (size_t)(c - 1) * (size_t)ldab, kl, live, tid);
+    };
+    for (int c = 1; c <= kDsAhead; c++) issue_fwd(c);
     for (int q = tid; q < n; q += kDsThreads) b[q] = bg[q];
-#define AB(r, c) ab[(size_t)((r) - 1) + (size_t)((c) - 1) * (size_t)ldab]
-    for (int c0 = 1; c0 <= n - 1; c0 += chunk) {
-        const int cn = min(chunk, n - c0);
-        __syncthreads();
-        for (int q = tid; q < cn * kl; q += kDsThreads) {
-            const int jc = c0 + q / kl, i = q % kl + 1;
-            cb[q] = (i <= n - jc) ? AB(kd + i, jc) : 0.0;
-        }
-        for (int q = tid; q < cn; q += kDsThreads) cp[q] = ipiv[c0 + q - 1];
-        __syncthreads();
-        if (warp == 0) {
-            for (int jj = 0; jj < cn; jj++) {
-                const int j = c0 + jj;
-                const int lm = kl < n - j ? kl : n - j;
-                const int l = cp[jj];
-                if (l != j && lane == 0) { const double t = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = t; }
-                __syncwarp();
-                const double temp = -1.0 * b[j - 1];
-                for (int i = 1 + lane; i <= lm; i += 32) b[j + i - 1] = b[j + i - 1] + cb[jj * kl + i - 1] * temp;
-                __syncwarp();
-            }
-        }
+    ds_wait<kDsAhead - 1>();  // column 1
+    __syncthreads();
+    if (n >= 2 && tid == 0) {
+        pub[1] = b[ipr[1 % kDsRing] - 1];  // the value the first step swaps into b(1)
+        pub[3] = b[0];
     }
-    for (int c1 = n; c1 >= 1; c1 -= chunk) {
-        const int cn = min(chunk, c1);
+    for (int j = 1; j <= n - 1; j++) {
+        ds_wait<kDsAhead - 2>();  // columns j and j + 1
         __syncthreads();
-        for (int q = tid; q < cn * kp1; q += kDsThreads) cb[q] = AB(1 + q % kp1, c1 - q / kp1);
-        __syncthreads();
-        if (warp == 0) {
-            for (int jj = 0; jj < cn; jj++) {
-                const int j = c1 - jj;
-                const double* col = cb + (size_t)jj * kp1;
-                const double x = b[j - 1] / col[kp1 - 1];
-                __syncwarp();
-                if (lane == 0) b[j - 1] = x;
-                const int l = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
-                for (int i = j - 1 - lane; i >= i0; i -= 32) b[i - 1] = b[i - 1] - x * col[l + i - 1];
-                __syncwarp();
-            }
+        const int sl = j % kDsRing;
+        const double* L = ring + (size_t)sl * SL + (((size_t)kd + (size_t)(j - 1) * (size_t)ldab) & 1);
+        const int l = ipr[sl];
+        const double T = pub[j & 1], S = pub[2 + (j & 1)];
+        if (owns(j)) b[j - 1] = T;
+        if (l != j && owns(l)) b[l - 1] = S;
+        const double temp = -T;  // -1.0 * T, exactly
+        const int lm = kl < n - j ? kl : n - j;
+        for (int i = first_owned(j + 1); i <= j + lm; i += kDsThreads) b[i - 1] = b[i - 1] + L[i - j - 1] * temp;
+        if (j + 1 <= n - 1) {
+            const int l1 = ipr[(j + 1) % kDsRing];
+            if (owns(l1)) pub[(j + 1) & 1] = b[l1 - 1];
+            if (owns(j + 1)) pub[2 + ((j + 1) & 1)] = b[j];
         }
+        issue_fwd(j + kDsAhead);
     }
-#undef AB
+    __syncthreads();
+
+    // ---- back substitution: for j = n .. 1, x = b(j) / U(j,j), b(j) = x, b(i0 .. j-1) -= x U(., j)
+    // (step m handles column j = n - m + 1)
+    auto issue_bwd = [&](int m) {  // column n - m + 1: AB(1 .. kp1, j)
+        const int c = n - m + 1;
+        ds_issue(ring + (size_t)(m % kDsRing) * SL, ab, (size_t)(c - 1) * (size_t)ldab, kp1, c >= 1, tid);
+    };
+    auto ucol = [&](int m) {
+        const int c = n - m + 1;
+        return ring + (size_t)(m % kDsRing) * SL + (((size_t)(c - 1) * (size_t)ldab) & 1);
+    };
+    for (int m = 1; m <= kDsAhead; m++) issue_bwd(m);
+    ds_wait<kDsAhead - 1>();  // column n
+    __syncthreads();
+    if (owns(n)) {
+        const double x = b[n - 1] / ucol(1)[kp1 - 1];
+        b[n - 1] = x;
+        pub[1] = x;
+    }
+    for (int m = 1; m <= n; m++) {
+        const int j = n - m + 1;
+        ds_wait<kDsAhead - 2>();  // columns j and j - 1
+        __syncthreads();
+        const double* U = ucol(m);
+        const double x = pub[m & 1];
+        const int lo = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
+        for (int i = first_owned(i0); i <= j - 1; i += kDsThreads) b[i - 1] = b[i - 1] - x * U[lo + i - 1];
+        if (j >= 2 && owns(j - 1)) {
+            const double x1 = b[j - 2] / ucol(m + 1)[kp1 - 1];
+            b[j - 2] = x1;
+            pub[(m + 1) & 1] = x1;
+        }
+        issue_bwd(m + kDsAhead);
+    }
+    ds_wait<0>();
     __syncthreads();
     for (int q = tid; q < n; q += kDsThreads) bg[q] = b[q];
 }
@@ -457,14 +532,11 @@ int direct_alloc(Engine& E) {
     E.dkl = kl;
     E.dku = ku;
     E.dn = n;
-    // the largest staging chunk of the substitution kernel that fits the shared memory
-    int chunk = 32;
-    while (chunk > 1 && direct_solve_smem(n, kl, ku, chunk) > 200 * 1024) chunk--;
-    if (direct_solve_smem(n, kl, ku, chunk) > 200 * 1024)
+    // the substitution kernel keeps b and its column ring in shared memory (227 KB per CTA)
+    if (direct_solve_smem(n, kl, ku) > 227 * 1024)
         return fail(PT_ERR_CONFIG, "direct solve: the grid is too large for the banded substitution kernel");
-    E.dchunk = chunk;
     CK(cudaFuncSetAttribute(k_direct_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)direct_solve_smem(n, kl, ku, chunk)));
+                            (int)direct_solve_smem(n, kl, ku)));
     CK(cudaMalloc(&E.dMB, sizeof(double) * (size_t)ldab * (size_t)n));
     CK(cudaMalloc(&E.dRow, sizeof(double) * (size_t)n));
     CK(cudaMalloc(&E.dB, sizeof(double) * (size_t)n));
@@ -550,8 +622,7 @@ int direct_solve(Engine& E, pt_solve_info* info) {
     const int n = E.dn, kl = E.dkl, ku = E.dku;
     PT_COUNT(), k_direct_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.dB, E.Tbuoy, E.Cbuoy, E.dRow, E.g1, n, E.cfg.comp,
                                                             E.cfg.RaT, E.cfg.RaC);
-    PT_COUNT(), k_direct_solve<<<1, kDsThreads, direct_solve_smem(n, kl, ku, E.dchunk), E.st>>>(E.dMB, E.dipiv, E.dB, n,
-                                                                                              kl, ku, E.dchunk);
+    PT_COUNT(), k_direct_solve<<<1, kDsThreads, direct_solve_smem(n, kl, ku), E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku);
     PT_COUNT(), k_direct_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.SF, E.dB, E.g1, E.K.nx, E.K.nz);
     PT_COUNT(), k_direct_images_x<<<nblk(3 * (E.K.nz + 1), 128), 128, 0, E.st>>>(E.SF, E.g1, E.K.nx, E.K.nz);
     PT_COUNT(), k_direct_images_z<<<nblk(3 * (E.K.nx + 7), 128), 128, 0, E.st>>>(E.SF, E.g1, E.K.nx, E.K.nz,
