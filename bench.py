@@ -214,13 +214,21 @@ def main():
                     help="GCR directions of the mixed solve (default: the workload's setting; 0 = defect correction)")
     ap.add_argument("--tpc", type=int, default=0,
                     help="tracers per cell override (profiling captures of a smaller tracer state only)")
-    ap.add_argument("--rows", action="store_true",
-                    help="also time the follow-on rows (direct solve, equalisation, RKC2 stepper, discrete "
-                         "types, file writers) on the GPU with the oracle beside them (extended_rows)")
+    ap.add_argument("--rows", nargs="*", default=None, choices=list(ROW_NAMES),
+                    help="also time the follow-on rows (all, or the ones named) on the GPU with the oracle beside "
+                         "them (extended_rows): f-1 file writers, f-2 direct solve, f-3 equalisation, f-4 RKC2 "
+                         "stepper, A9 discrete types")
+    ap.add_argument("--only-rows", action="store_true", help="with --rows: print only the rows' JSON object")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.only_rows:
+        from projectracer_gb300 import engine as eng
+
+        if rank == 0:
+            print(json.dumps({"extended_rows": extended_rows(eng, args.rows or list(ROW_NAMES))}), flush=True)
         return
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
@@ -296,11 +304,11 @@ def main():
             e = None
         extra["psi_solve_at_1e-8"] = psi_at_1e8(eng)
         extra["per_config"] = per_config(eng)
-    if args.rows and rank == 0:
+    if args.rows is not None and rank == 0:
         if e is not None:
             e.close()
             e = None
-        extra["extended_rows"] = extended_rows(eng)
+        extra["extended_rows"] = extended_rows(eng, args.rows or list(ROW_NAMES))
     line = {"metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": args.steps,
             "warmup": W, "ms_per_step": elapsed / args.steps * 1e3, "host_ms_per_step": host_s / args.steps * 1e3,
             "higher_is_better": True,
@@ -529,10 +537,14 @@ def psi_at_1e8(eng, steps: int = 2) -> dict:
     return res
 
 
-def extended_rows(eng) -> dict:
-    """The follow-on rows on the GPU, each with the oracle timed beside it on all host cores (the
-    file writer against the package's numpy writer of the same records).  GPU times are host-timed
-    around calls that return synchronised (the writers: until pt_io_wait returns)."""
+ROW_NAMES = ("f-1", "f-2", "f-3", "f-4", "A9")
+
+
+def extended_rows(eng, which) -> dict:
+    """The follow-on rows named in `which` on the GPU, each with the oracle timed beside it on all
+    host cores (the file writer against the package's numpy writer of the same records).  GPU
+    times are host-timed around calls that return synchronised (the writers: until pt_io_wait
+    returns)."""
     import shutil
     import tempfile
 
@@ -546,7 +558,6 @@ def extended_rows(eng) -> dict:
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     clock = time.perf_counter
-    out = {}
 
     def oracle_for(cfg, st, iterate=1, types=None):
         o = Oracle(cfg, iterate=iterate, nparts=cores)
@@ -561,116 +572,124 @@ def extended_rows(eng) -> dict:
             fn()
         return (clock() - t0) / reps * 1e3
 
-    # f-2: the banded direct psi solve (iterate=0) on the 128x128 isoviscous grid; the first solve
-    # of a run assembles, equilibrates and factors, later ones substitute
-    cfg, _ = workload("C1", 1.0, PT_PREC_FP64)
-    cfg.direct, cfg.ntr = 1, 128 * 128 * 20
-    st = make_state(cfg, 3)
-    e = eng.Engine(cfg)
-    e.upload(st)
-    g_first = timed(e.solve_psi)
-    g_solve = timed(e.solve_psi, 5)
-    e.close()
-    o = oracle_for(cfg, st, iterate=0)
-    c_first = timed(o.solve_psi)
-    o.step()
-    c_solve = timed(o.solve_psi)
-    del o
-    n = (cfg.nx + 1) * (cfg.nz + 1)
-    out["f-2 direct banded psi solve"] = {
-        "case": f"128x128 isoviscous, {n} unknowns, band widths {3 * (cfg.nz + 1)}/{3 * (cfg.nz + 1)}",
-        "gpu_ms": {"factor_and_solve": g_first, "solve": g_solve},
-        "cpu_ms": {"factor_and_solve": c_first, "solve": c_solve}, "cpu_cores": cores}
-
-    # f-3: tracer equalisation after 5% of the tracers gathered into a small box (512x512, 20 per
-    # cell, 5.2M tracers)
-    cfg, _ = workload("C1", 1.0, PT_PREC_FP64)
-    cfg.nx = cfg.nz = 512
-    cfg.ntr = 512 * 512 * 20
-    cfg.equalize, cfg.tpc = 1, 20
-    st = make_state(cfg, 3)
-    rng = np.random.default_rng(5)
-    idx = rng.choice(cfg.ntr, cfg.ntr // 20, replace=False)
-    st["rtr"][idx] = 0.3 + 0.05 * rng.random(len(idx))
-    st["str"][idx] = 0.5 + 0.05 * rng.random(len(idx))
-    e = eng.Engine(cfg)
-    e.upload(st)
-    e.equalize()  # first call: allocations
-    e.upload(st)
-    info = {}
-    g_eq = timed(lambda: info.update(e.equalize()))
-    e.close()
-    o = oracle_for(cfg, st)
-    c_eq = timed(o.equalize)
-    del o
-    out["f-3 tracer equalisation"] = {"case": f"512x512, {cfg.ntr} tracers, 5% gathered into a 0.05 x 0.05 box",
-                                      "moved": int(info.get("moved", 0)), "gpu_ms": g_eq, "cpu_ms": c_eq,
-                                      "cpu_cores": cores, "cpu_note": "the oracle's equalisation is serial"}
-
-    # f-4: the RKC2 energy stepper (Chebyshev=1, 3 stages) on the 128x128 isoviscous grid, FP64
-    cfg, _ = workload("C1", 1.0, PT_PREC_FP64)
-    cfg.ntr = 128 * 128 * 20
-    cfg.chebyshev, cfg.nstage, cfg.damping, cfg.aRK2 = 1, 3, 100.0, 0.5
-    st = make_state(cfg, 3)
-
     def one_step(x):
         x.solve_psi()
         x.step()
 
-    e = eng.Engine(cfg)
-    e.upload(st)
-    one_step(e)
-    g_step = timed(lambda: one_step(e), 3)
-    e.close()
-    o = oracle_for(cfg, st)
-    one_step(o)
-    c_step = timed(lambda: one_step(o))
-    del o
-    out["f-4 RKC2 energy stepper"] = {"case": "128x128 isoviscous, 327,680 tracers, nstage 3, tolerance 1e-8",
-                                      "gpu_ms_per_step": g_step, "cpu_ms_per_step": c_step, "cpu_cores": cores}
-
-    # A9: discrete tracer types (projection by type counts) in the FP64 step, 256x128 thermochemical
-    cfg, w = workload("C2", 1.0, PT_PREC_FP64)
-    cfg.ntr = 256 * 128 * 30
-    cfg.discrete_types = 1
-    st = make_state(cfg, 3, noise=w.get("noise", 1e-3))
-    types = (st["Ctr"] > 0.5).astype(np.int32)
-    st_e = dict(st, Ttype=types)
-    e = eng.Engine(cfg)
-    e.upload(st_e)
-    one_step(e)
-    g_step = timed(lambda: one_step(e), 3)
-    e.close()
-    o = oracle_for(cfg, st, types=types)
-    one_step(o)
-    c_step = timed(lambda: one_step(o))
-    del o
-    out["A9 discrete tracer types"] = {"case": "256x128 thermochemical, 983,040 tracers, FP64 step (4 projections)",
-                                       "gpu_ms_per_step": g_step, "cpu_ms_per_step": c_step, "cpu_cores": cores}
-
-    # f-1: snapshot (T/P text) and restart (gfortran records) files of the 1024x512 state
-    cfg, w = workload("C3", 1.0, PT_PREC_MIXED)
-    st = make_state(cfg, 3, noise=w.get("noise", 1e-3))
-    d1, d2 = tempfile.mkdtemp(), tempfile.mkdtemp()
-    try:
+    def f2():
+        """the banded direct psi solve (iterate=0) on the 128x128 isoviscous grid; the first solve
+        of a run assembles, equilibrates and factors, later ones substitute"""
+        cfg, _ = workload("C1", 1.0, PT_PREC_FP64)
+        cfg.direct, cfg.ntr = 1, 128 * 128 * 20
+        st = make_state(cfg, 3)
         e = eng.Engine(cfg)
         e.upload(st)
-        g_snap = timed(lambda: (e.write_snapshot(d1, 0), e.io_wait()))
-        g_rst = timed(lambda: (e.write_restart(d1), e.io_wait()))
+        g_first = timed(e.solve_psi)
+        g_solve = timed(e.solve_psi, 5)
         e.close()
-        sizes = {f: os.path.getsize(os.path.join(d1, f)) for f in sorted(os.listdir(d1))}
-        c_rst = timed(lambda: write_restart(d2, st, cfg.comp))
-    finally:
-        shutil.rmtree(d1, ignore_errors=True)
-        shutil.rmtree(d2, ignore_errors=True)
-    rst_bytes = sizes.get("Trestart", 0) + sizes.get("restart_tracers", 0)
-    out["f-1 snapshot and restart files"] = {
-        "case": f"1024x512, {cfg.ntr} tracers", "bytes": sizes,
-        "gpu_ms": {"snapshot": g_snap, "restart": g_rst},
-        "gpu_restart_gbs": rst_bytes / (g_rst * 1e-3) / 1e9,
-        "cpu_ms": {"restart_numpy_writer": c_rst},
-        "cpu_note": "the package's numpy writer of the same restart records from host arrays "
-                    "(no Fortran compiler here for the reference's own writer)"}
+        o = oracle_for(cfg, st, iterate=0)
+        c_first = timed(o.solve_psi)
+        o.step()
+        c_solve = timed(o.solve_psi)
+        n = (cfg.nx + 1) * (cfg.nz + 1)
+        return "f-2 direct banded psi solve", {
+            "case": f"128x128 isoviscous, {n} unknowns, band widths {3 * (cfg.nz + 1)}/{3 * (cfg.nz + 1)}",
+            "gpu_ms": {"factor_and_solve": g_first, "solve": g_solve},
+            "cpu_ms": {"factor_and_solve": c_first, "solve": c_solve}, "cpu_cores": cores,
+            "cpu_note": "the oracle's band factorisation and substitutions are serial"}
+
+    def f3():
+        """tracer equalisation after 5% of the tracers gathered into a small box (512x512, 20 per
+        cell, 5.2M tracers)"""
+        cfg, _ = workload("C1", 1.0, PT_PREC_FP64)
+        cfg.nx = cfg.nz = 512
+        cfg.ntr = 512 * 512 * 20
+        cfg.equalize, cfg.tpc = 1, 20
+        st = make_state(cfg, 3)
+        rng = np.random.default_rng(5)
+        idx = rng.choice(cfg.ntr, cfg.ntr // 20, replace=False)
+        st["rtr"][idx] = 0.3 + 0.05 * rng.random(len(idx))
+        st["str"][idx] = 0.5 + 0.05 * rng.random(len(idx))
+        e = eng.Engine(cfg)
+        e.upload(st)
+        e.equalize()  # first call: allocations
+        e.upload(st)
+        info = {}
+        g_eq = timed(lambda: info.update(e.equalize()))
+        e.close()
+        o = oracle_for(cfg, st)
+        c_eq = timed(o.equalize)
+        return "f-3 tracer equalisation", {
+            "case": f"512x512, {cfg.ntr} tracers, 5% gathered into a 0.05 x 0.05 box", "moved": int(info.get("moved", 0)),
+            "gpu_ms": g_eq, "cpu_ms": c_eq, "cpu_cores": cores, "cpu_note": "the oracle's equalisation is serial"}
+
+    def f4():
+        """the RKC2 energy stepper (Chebyshev=1, 3 stages) on the 128x128 isoviscous grid, FP64"""
+        cfg, _ = workload("C1", 1.0, PT_PREC_FP64)
+        cfg.ntr = 128 * 128 * 20
+        cfg.chebyshev, cfg.nstage, cfg.damping, cfg.aRK2 = 1, 3, 100.0, 0.5
+        st = make_state(cfg, 3)
+        e = eng.Engine(cfg)
+        e.upload(st)
+        one_step(e)
+        g_step = timed(lambda: one_step(e), 3)
+        e.close()
+        o = oracle_for(cfg, st)
+        one_step(o)
+        c_step = timed(lambda: one_step(o))
+        return "f-4 RKC2 energy stepper", {
+            "case": "128x128 isoviscous, 327,680 tracers, nstage 3, tolerance 1e-8", "gpu_ms_per_step": g_step,
+            "cpu_ms_per_step": c_step, "cpu_cores": cores}
+
+    def a9():
+        """discrete tracer types (projection by type counts) in the FP64 step, 256x128
+        thermochemical"""
+        cfg, w = workload("C2", 1.0, PT_PREC_FP64)
+        cfg.ntr = 256 * 128 * 30
+        cfg.discrete_types = 1
+        st = make_state(cfg, 3, noise=w.get("noise", 1e-3))
+        types = (st["Ctr"] > 0.5).astype(np.int32)
+        e = eng.Engine(cfg)
+        e.upload(dict(st, Ttype=types))
+        one_step(e)
+        g_step = timed(lambda: one_step(e), 3)
+        e.close()
+        o = oracle_for(cfg, st, types=types)
+        one_step(o)
+        c_step = timed(lambda: one_step(o))
+        return "A9 discrete tracer types", {
+            "case": "256x128 thermochemical, 983,040 tracers, FP64 step (4 projections)", "gpu_ms_per_step": g_step,
+            "cpu_ms_per_step": c_step, "cpu_cores": cores}
+
+    def f1():
+        """snapshot (T/P text) and restart (gfortran records) files of the 1024x512 state"""
+        cfg, w = workload("C3", 1.0, PT_PREC_MIXED)
+        st = make_state(cfg, 3, noise=w.get("noise", 1e-3))
+        d1, d2 = tempfile.mkdtemp(), tempfile.mkdtemp()
+        try:
+            e = eng.Engine(cfg)
+            e.upload(st)
+            g_snap = timed(lambda: (e.write_snapshot(d1, 0), e.io_wait()))
+            g_rst = timed(lambda: (e.write_restart(d1), e.io_wait()))
+            e.close()
+            sizes = {f: os.path.getsize(os.path.join(d1, f)) for f in sorted(os.listdir(d1))}
+            c_rst = timed(lambda: write_restart(d2, st, cfg.comp))
+        finally:
+            shutil.rmtree(d1, ignore_errors=True)
+            shutil.rmtree(d2, ignore_errors=True)
+        rst_bytes = sizes.get("Trestart", 0) + sizes.get("restart_tracers", 0)
+        return "f-1 snapshot and restart files", {
+            "case": f"1024x512, {cfg.ntr} tracers", "bytes": sizes, "gpu_ms": {"snapshot": g_snap, "restart": g_rst},
+            "gpu_restart_gbs": rst_bytes / (g_rst * 1e-3) / 1e9, "cpu_ms": {"restart_numpy_writer": c_rst},
+            "cpu_note": "the package's numpy writer of the same restart records from host arrays "
+                        "(no Fortran compiler here for the reference's own writer)"}
+
+    rows = {"f-1": f1, "f-2": f2, "f-3": f3, "f-4": f4, "A9": a9}
+    out = {}
+    for name in ROW_NAMES:
+        if name in which:
+            key, val = rows[name]()
+            out[key] = val
     return out
 
 
