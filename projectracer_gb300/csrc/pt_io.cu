@@ -12,6 +12,7 @@
 // order after the work that produced the state and before any later step, into pinned staging;
 // a host thread then formats and writes the files while the caller keeps stepping.  pt_io_wait
 // joins it and returns its status.
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -365,31 +366,53 @@ int pt_write_snapshot(const char* dir, int fcount) {
         auto at5 = [&](int q, int i, int k) {
             return F[7 * n3 + n5 * q + (size_t)(i + 5) + (size_t)(k + 5) * (nx + 11)];
         };
-        std::string out;
-        out.reserve((size_t)(nx + 1) * (nz + 2) * 200);
-        for (int i = 0; i <= nx; i++) {
-            for (int k = 0; k <= nz; k++) {
-                put_g14_5e3(out, xg[(size_t)i + 6]);
-                put_g14_5e3(out, zg[(size_t)k + 6]);
-                put_g14_5e3(out, at3(0, i, k));
-                put_g14_5e3(out, at3(1, i, k));
-                put_g14_5e3(out, at3(2, i, k));
-                put_g14_5e3(out, at3(3, i, k));
-                put_g14_5e3(out, 2.0 * at3(5, i, k) * at3(4, i, k));
-                put_g14_5e3(out, at3(5, i, k));
-                put_g14_5e3(out, at3(6, i, k));
-                put_i6(out, ne[(size_t)i + (size_t)k * (nx + 1)]);
-                if (comp) {
-                    put_g14_5e3(out, at5(0, i, k));
-                    put_g14_5e3(out, at5(1, i, k));
+        // the lines of columns i0 .. i1-1 (one block of lines per column, then a blank record)
+        auto columns = [&](std::string& out, int i0, int i1) {
+            out.reserve((size_t)(i1 - i0) * (nz + 2) * 200);
+            for (int i = i0; i < i1; i++) {
+                for (int k = 0; k <= nz; k++) {
+                    put_g14_5e3(out, xg[(size_t)i + 6]);
+                    put_g14_5e3(out, zg[(size_t)k + 6]);
+                    put_g14_5e3(out, at3(0, i, k));
+                    put_g14_5e3(out, at3(1, i, k));
+                    put_g14_5e3(out, at3(2, i, k));
+                    put_g14_5e3(out, at3(3, i, k));
+                    put_g14_5e3(out, 2.0 * at3(5, i, k) * at3(4, i, k));
+                    put_g14_5e3(out, at3(5, i, k));
+                    put_g14_5e3(out, at3(6, i, k));
+                    put_i6(out, ne[(size_t)i + (size_t)k * (nx + 1)]);
+                    if (comp) {
+                        put_g14_5e3(out, at5(0, i, k));
+                        put_g14_5e3(out, at5(1, i, k));
+                    }
+                    out += '\n';
                 }
-                out += '\n';
+                out += "  \n";  // write(101,*) " "
             }
-            out += "  \n";  // write(101,*) " "
+        };
+        // formatted by up to 16 host threads, column blocks in order
+        const unsigned hc = std::thread::hardware_concurrency();
+        const int nth = std::max(1, std::min({16, nx + 1, hc ? (int)hc : 1}));
+        std::vector<std::string> parts((size_t)nth);
+        {
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nth; t++) {
+                const int a = (int)((long long)(nx + 1) * t / nth), c = (int)((long long)(nx + 1) * (t + 1) / nth);
+                try {
+                    pool.emplace_back(columns, std::ref(parts[(size_t)t]), a, c);
+                } catch (...) {  // no thread to be had: this one formats the block
+                    columns(parts[(size_t)t], a, c);
+                }
+            }
+            columns(parts[0], 0, (int)((long long)(nx + 1) / nth));
+            for (std::thread& th : pool) th.join();
         }
         FILE* f = std::fopen(ftn.c_str(), "w");
-        int bad = !f || std::fwrite(out.data(), 1, out.size(), f) != out.size();
+        int bad = !f;
+        for (const std::string& part : parts)
+            if (!bad && std::fwrite(part.data(), 1, part.size(), f) != part.size()) bad = 1;
         if (f && std::fclose(f) != 0) bad = 1;
+        std::string out;
         // lateral averages: integrate1Dx (basics.f90:494-515, trapezoids) over each row
         out.clear();
         auto lat = [&](auto fn, int k) {
