@@ -314,15 +314,17 @@ __global__ void __launch_bounds__(kLuThreads) k_direct_lu(double* ab, int* ipiv,
 // writes it: in a column step each thread applies the column to the elements it owns, and the
 // value the next step needs first (the pivot row's b for the forward step, the next x = b / U_jj
 // for the back substitution) is published by its owner at the end of the step, so a step needs
-// one barrier.  The band columns stream through a ring of kDsRing shared-memory slots, filled by
-// cp.async kDsAhead columns ahead of their step (16-byte copies from the 16-byte boundary at or
+// one barrier.  The band columns stream through a ring of AHEAD + 1 shared-memory slots, filled by
+// cp.async AHEAD columns ahead of their step (16-byte copies from the 16-byte boundary at or
 // below the column's first entry; `off` is the column's position in its slot).  On this part a
 // step is bound by the SM's FP64 pipe: forward kl, backward kl + ku multiply-subtract pairs.
-constexpr int kDsThreads = 256, kDsAhead = 8, kDsRing = kDsAhead + 1;
+// AHEAD = 8 where the ring fits beside b, else 2 (no lookahead beyond the next column, for the
+// largest grids).
+constexpr int kDsThreads = 256;
 static __host__ __device__ int direct_slot_len(int kl, int ku) { return (kl + ku + 3) & ~1; }
-static size_t direct_solve_smem(int n, int kl, int ku) {
-    return sizeof(double) * ((size_t)kDsRing * (size_t)direct_slot_len(kl, ku) + (size_t)n + 4) +
-           sizeof(int) * (size_t)kDsRing;
+static size_t direct_solve_smem(int n, int kl, int ku, int ahead) {
+    return sizeof(double) * ((size_t)(ahead + 1) * (size_t)direct_slot_len(kl, ku) + (size_t)n + 4) +
+           sizeof(int) * (size_t)(ahead + 1);
 }
 
 __device__ __forceinline__ void ds_cp16(void* dst, const void* src) {
@@ -350,8 +352,10 @@ __device__ __forceinline__ void ds_issue(double* slot, const double* ab, size_t 
     ds_commit();
 }
 
+template <int kDsAhead>
 __global__ void __launch_bounds__(kDsThreads, 1) k_direct_solve(const double* __restrict__ ab, const int* __restrict__ ipiv,
                                                                double* __restrict__ bg, int n, int kl, int ku) {
+    constexpr int kDsRing = kDsAhead + 1;
     extern __shared__ __align__(16) double dsm[];
     const int SL = direct_slot_len(kl, ku);
     double* ring = dsm;                                  // kDsRing slots of SL doubles
@@ -533,10 +537,12 @@ int direct_alloc(Engine& E) {
     E.dku = ku;
     E.dn = n;
     // the substitution kernel keeps b and its column ring in shared memory (227 KB per CTA)
-    if (direct_solve_smem(n, kl, ku) > 227 * 1024)
+    E.dahead = direct_solve_smem(n, kl, ku, 8) <= 227 * 1024 ? 8 : 2;
+    if (direct_solve_smem(n, kl, ku, E.dahead) > 227 * 1024)
         return fail(PT_ERR_CONFIG, "direct solve: the grid is too large for the banded substitution kernel");
-    CK(cudaFuncSetAttribute(k_direct_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)direct_solve_smem(n, kl, ku)));
+    const int smem = (int)direct_solve_smem(n, kl, ku, E.dahead);
+    if (E.dahead == 8) CK(cudaFuncSetAttribute(k_direct_solve<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    else CK(cudaFuncSetAttribute(k_direct_solve<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CK(cudaMalloc(&E.dMB, sizeof(double) * (size_t)ldab * (size_t)n));
     CK(cudaMalloc(&E.dRow, sizeof(double) * (size_t)n));
     CK(cudaMalloc(&E.dB, sizeof(double) * (size_t)n));
@@ -622,7 +628,9 @@ int direct_solve(Engine& E, pt_solve_info* info) {
     const int n = E.dn, kl = E.dkl, ku = E.dku;
     PT_COUNT(), k_direct_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.dB, E.Tbuoy, E.Cbuoy, E.dRow, E.g1, n, E.cfg.comp,
                                                             E.cfg.RaT, E.cfg.RaC);
-    PT_COUNT(), k_direct_solve<<<1, kDsThreads, direct_solve_smem(n, kl, ku), E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku);
+    const size_t smem = direct_solve_smem(n, kl, ku, E.dahead);
+    if (E.dahead == 8) PT_COUNT(), k_direct_solve<8><<<1, kDsThreads, smem, E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku);
+    else PT_COUNT(), k_direct_solve<2><<<1, kDsThreads, smem, E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku);
     PT_COUNT(), k_direct_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.SF, E.dB, E.g1, E.K.nx, E.K.nz);
     PT_COUNT(), k_direct_images_x<<<nblk(3 * (E.K.nz + 1), 128), 128, 0, E.st>>>(E.SF, E.g1, E.K.nx, E.K.nz);
     PT_COUNT(), k_direct_images_z<<<nblk(3 * (E.K.nx + 7), 128), 128, 0, E.st>>>(E.SF, E.g1, E.K.nx, E.K.nz,

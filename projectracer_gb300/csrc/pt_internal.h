@@ -110,7 +110,7 @@ struct Engine {
     int32_t* count1 = nullptr;  // discrete types: count_type(1, 0:nx, 0:nz) of the last projection
     // direct banded solve (cfg.direct, pt_direct.cu): band matrix and LU, row factors, right-hand
     // side, pivots, the LU kernel's barrier state and error words
-    int dn = 0, dkl = 0, dku = 0;
+    int dn = 0, dkl = 0, dku = 0, dahead = 8;  // dahead: the substitution kernel's column lookahead
     double *dMB = nullptr, *dRow = nullptr, *dB = nullptr;
     int *dipiv = nullptr, *dluerr = nullptr;
     void* dlu = nullptr;
