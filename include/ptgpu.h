@@ -125,10 +125,10 @@ typedef struct pt_config {
                               build_SF_matrix/solve_SF_equation (momentum.f90:319-653): assembly,
                               row equilibration and band LU once (the operator of an isoviscous run
                               does not change), then per solve the banded substitutions.  FP64,
-                              ivis=0 only; the substitutions keep the right-hand side and a ring
-                              of band columns in one CTA's shared memory (227 KB), which bounds
-                              the grid at about 160 x 160 cells (pt_init fails with
-                              PT_ERR_CONFIG past it).  0: multigrid (iterate=1, MG=1) */
+                              ivis=0 only; the substitutions keep a window of the right-hand side
+                              and a ring of band columns (band width 3 (nz+1)) in one CTA's
+                              shared memory (227 KB), which bounds nz at about 1,150 (pt_init
+                              fails with PT_ERR_CONFIG past it).  0: multigrid (iterate=1, MG=1) */
     int32_t chebyshev;     /* &inputs Chebyshev=1: the energy step is the nstage-stage RKC2 Chebyshev
                               method of energy_time_Chebyshev (Chebyshev.f90:113-243) with the RK2
                               time step (torder=2, energy.f90:787-793); 0: RK4 (energy_time).  FP64

@@ -309,21 +309,30 @@ __global__ void __launch_bounds__(kLuThreads) k_direct_lu(double* ab, int* ipiv,
 // column-by-column DGBTRS; zero entries are divided and propagated too, like the optimized BLAS of
 // the shipped run (psi = -0 on the non-corner wall nodes of its snapshots).
 //
-// The column steps are sequential, so one CTA carries them, with b in shared memory.  Every
-// element of b has one owner thread (element i: thread (i - 1) mod kDsThreads), which alone
-// writes it: in a column step each thread applies the column to the elements it owns, and the
-// value the next step needs first (the pivot row's b for the forward step, the next x = b / U_jj
-// for the back substitution) is published by its owner at the end of the step, so a step needs
-// one barrier.  The band columns stream through a ring of AHEAD + 1 shared-memory slots, filled by
-// cp.async AHEAD columns ahead of their step (16-byte copies from the 16-byte boundary at or
-// below the column's first entry; `off` is the column's position in its slot).  On this part a
-// step is bound by the SM's FP64 pipe: forward kl, backward kl + ku multiply-subtract pairs.
-// AHEAD = 8 where the ring fits beside b, else 2 (no lookahead beyond the next column, for the
-// largest grids).
+// The column steps are sequential, so one CTA carries them.  Every element of b has one owner
+// thread (element i: thread (i - 1) mod kDsThreads), which alone writes it: in a column step each
+// thread applies the column to the elements it owns, and the value the next step needs first (the
+// pivot row's b for the forward step, the next x = b / U_jj for the back substitution) is
+// published by its owner, so a step needs one barrier.
+//   * b stays in global memory; the elements a step touches (j .. j+kl forward, j-k .. j back)
+//     live in a window of W shared-memory slots (W a power of two >= k + 4, element i in slot
+//     (i - 1) mod W).  An element enters two steps before its first use: its owner loads it into
+//     a register one step, stores it into its slot the next.  An element is written back by its
+//     owner in the step it becomes final (forward: when swapped into b(j); back: as x).
+//   * The band columns stream through a ring of AHEAD + 1 shared-memory slots, filled by
+//     cp.async AHEAD columns ahead of their step (16-byte copies from the 16-byte boundary at or
+//     below the column's first entry; the column sits at offset s0 & 1 in its slot).
+// On this part a step is bound by the SM's FP64 pipe: forward kl, backward kl + ku
+// multiply-subtract pairs.  AHEAD = 8 where that ring fits, else 2.
 constexpr int kDsThreads = 256;
 static __host__ __device__ int direct_slot_len(int kl, int ku) { return (kl + ku + 3) & ~1; }
-static size_t direct_solve_smem(int n, int kl, int ku, int ahead) {
-    return sizeof(double) * ((size_t)(ahead + 1) * (size_t)direct_slot_len(kl, ku) + (size_t)n + 4) +
+static int direct_window(int kl, int ku) {
+    int w = 64;
+    while (w < kl + ku + 4) w *= 2;
+    return w;
+}
+static size_t direct_solve_smem(int kl, int ku, int ahead) {
+    return sizeof(double) * ((size_t)(ahead + 1) * (size_t)direct_slot_len(kl, ku) + (size_t)direct_window(kl, ku) + 4) +
            sizeof(int) * (size_t)(ahead + 1);
 }
 
@@ -354,16 +363,17 @@ __device__ __forceinline__ void ds_issue(double* slot, const double* ab, size_t 
 
 template <int kDsAhead>
 __global__ void __launch_bounds__(kDsThreads, 1) k_direct_solve(const double* __restrict__ ab, const int* __restrict__ ipiv,
-                                                               double* __restrict__ bg, int n, int kl, int ku) {
+                                                               double* __restrict__ bg, int n, int kl, int ku, int W) {
     constexpr int kDsRing = kDsAhead + 1;
     extern __shared__ __align__(16) double dsm[];
-    const int SL = direct_slot_len(kl, ku);
+    const int SL = direct_slot_len(kl, ku), mask = W - 1;
     double* ring = dsm;                                  // kDsRing slots of SL doubles
-    double* b = ring + (size_t)kDsRing * SL;             // n
-    double* pub = b + n;                                 // [2]: published values, by step parity
+    double* win = ring + (size_t)kDsRing * SL;           // W: the window of b
+    double* pub = win + W;                               // [4]: published values, by step parity
     int* ipr = reinterpret_cast<int*>(pub + 4);          // pivots of the columns in the ring
     const int ldab = 2 * kl + ku + 1, kd = kl + ku + 1, kp1 = kl + ku + 1, k = kl + ku;
     const int tid = threadIdx.x;
+    auto B = [&](int i) -> double& { return win[(i - 1) & mask]; };
     // the first element >= a that this thread owns
     auto first_owned = [&](int a) {
         int r = (tid - (a - 1)) % kDsThreads;
@@ -371,8 +381,11 @@ __global__ void __launch_bounds__(kDsThreads, 1) k_direct_solve(const double* __
         return a + r;
     };
     auto owns = [&](int i) { return (i - 1) % kDsThreads == tid; };
+    double pend = 0.0;  // the element this thread loaded for the window, stored the next step
+    int pend_i = 0;
 
-    // ---- forward: for j = 1 .. n-1, b(j) <-> b(ipiv(j)), then b(j+1 .. j+lm) += L(., j) * (-b(j))
+    // ---- forward: for j = 1 .. n-1, b(j) <-> b(ipiv(j)), then b(j+1 .. j+lm) += L(., j) * (-b(j));
+    // the window holds b(j .. j+kl) at step j
     auto issue_fwd = [&](int c) {  // column c's multipliers AB(kd+1 .. kd+kl, c) and its pivot
         const bool live = c <= n - 1;
         double* slot = ring + (size_t)(c % kDsRing) * SL;
@@ -380,36 +393,53 @@ __global__ void __launch_bounds__(kDsThreads, 1) k_direct_solve(const double* __
         ds_issue(slot, ab, (size_t)kd + (size_t)(c - 1) * (size_t)ldab, kl, live, tid);
     };
     for (int c = 1; c <= kDsAhead; c++) issue_fwd(c);
-    for (int q = tid; q < n; q += kDsThreads) b[q] = bg[q];
+    for (int i = 1 + tid; i <= n && i <= kl + 1; i += kDsThreads) B(i) = bg[i - 1];
+    if (kl + 2 <= n && owns(kl + 2)) {  // needed from step 2
+        pend = bg[kl + 1];
+        pend_i = kl + 2;
+    }
     ds_wait<kDsAhead - 1>();  // column 1
     __syncthreads();
     if (n >= 2 && tid == 0) {
-        pub[1] = b[ipr[1 % kDsRing] - 1];  // the value the first step swaps into b(1)
-        pub[3] = b[0];
+        pub[1] = B(ipr[1 % kDsRing]);  // the value the first step swaps into b(1)
+        pub[3] = B(1);
     }
     for (int j = 1; j <= n - 1; j++) {
         ds_wait<kDsAhead - 2>();  // columns j and j + 1
         __syncthreads();
+        if (pend_i) {  // b(j + kl + 1), first used in step j + 1
+            B(pend_i) = pend;
+            pend_i = 0;
+        }
         const int sl = j % kDsRing;
         const double* L = ring + (size_t)sl * SL + (((size_t)kd + (size_t)(j - 1) * (size_t)ldab) & 1);
         const int l = ipr[sl];
         const double T = pub[j & 1], S = pub[2 + (j & 1)];
-        if (owns(j)) b[j - 1] = T;
-        if (l != j && owns(l)) b[l - 1] = S;
+        if (owns(j)) {
+            B(j) = T;
+            bg[j - 1] = T;  // final for the forward substitution
+        }
+        if (l != j && owns(l)) B(l) = S;
         const double temp = -T;  // -1.0 * T, exactly
         const int lm = kl < n - j ? kl : n - j;
-        for (int i = first_owned(j + 1); i <= j + lm; i += kDsThreads) b[i - 1] = b[i - 1] + L[i - j - 1] * temp;
+        for (int i = first_owned(j + 1); i <= j + lm; i += kDsThreads) B(i) = B(i) + L[i - j - 1] * temp;
         if (j + 1 <= n - 1) {
             const int l1 = ipr[(j + 1) % kDsRing];
-            if (owns(l1)) pub[(j + 1) & 1] = b[l1 - 1];
-            if (owns(j + 1)) pub[2 + ((j + 1) & 1)] = b[j];
+            if (owns(l1)) pub[(j + 1) & 1] = B(l1);
+            if (owns(j + 1)) pub[2 + ((j + 1) & 1)] = B(j + 1);
+        }
+        const int f = j + kl + 2;  // first used in step j + 2
+        if (f <= n && owns(f)) {
+            pend = bg[f - 1];
+            pend_i = f;
         }
         issue_fwd(j + kDsAhead);
     }
-    __syncthreads();
+    if (owns(n)) bg[n - 1] = B(n);
+    __syncthreads();  // the forward results in bg are visible to the whole CTA
 
     // ---- back substitution: for j = n .. 1, x = b(j) / U(j,j), b(j) = x, b(i0 .. j-1) -= x U(., j)
-    // (step m handles column j = n - m + 1)
+    // (step m handles column j = n - m + 1); the window holds b(j-k .. j) at step j
     auto issue_bwd = [&](int m) {  // column n - m + 1: AB(1 .. kp1, j)
         const int c = n - m + 1;
         ds_issue(ring + (size_t)(m % kDsRing) * SL, ab, (size_t)(c - 1) * (size_t)ldab, kp1, c >= 1, tid);
@@ -419,31 +449,46 @@ __global__ void __launch_bounds__(kDsThreads, 1) k_direct_solve(const double* __
         return ring + (size_t)(m % kDsRing) * SL + (((size_t)(c - 1) * (size_t)ldab) & 1);
     };
     for (int m = 1; m <= kDsAhead; m++) issue_bwd(m);
+    pend_i = 0;
+    for (int i = n - tid; i >= 1 && i >= n - k; i -= kDsThreads) B(i) = bg[i - 1];
+    if (n - k - 1 >= 1 && owns(n - k - 1)) {  // needed from step j = n - 1
+        pend = bg[n - k - 2];
+        pend_i = n - k - 1;
+    }
     ds_wait<kDsAhead - 1>();  // column n
     __syncthreads();
     if (owns(n)) {
-        const double x = b[n - 1] / ucol(1)[kp1 - 1];
-        b[n - 1] = x;
+        const double x = B(n) / ucol(1)[kp1 - 1];
+        B(n) = x;
+        bg[n - 1] = x;
         pub[1] = x;
     }
     for (int m = 1; m <= n; m++) {
         const int j = n - m + 1;
         ds_wait<kDsAhead - 2>();  // columns j and j - 1
         __syncthreads();
+        if (pend_i) {  // b(j - k - 1), first used in step j - 1
+            B(pend_i) = pend;
+            pend_i = 0;
+        }
         const double* U = ucol(m);
         const double x = pub[m & 1];
         const int lo = kp1 - j, i0 = 1 > j - k ? 1 : j - k;
-        for (int i = first_owned(i0); i <= j - 1; i += kDsThreads) b[i - 1] = b[i - 1] - x * U[lo + i - 1];
+        for (int i = first_owned(i0); i <= j - 1; i += kDsThreads) B(i) = B(i) - x * U[lo + i - 1];
         if (j >= 2 && owns(j - 1)) {
-            const double x1 = b[j - 2] / ucol(m + 1)[kp1 - 1];
-            b[j - 2] = x1;
+            const double x1 = B(j - 1) / ucol(m + 1)[kp1 - 1];
+            B(j - 1) = x1;
+            bg[j - 2] = x1;
             pub[(m + 1) & 1] = x1;
+        }
+        const int f = j - k - 2;  // first used in step j - 2
+        if (f >= 1 && owns(f)) {
+            pend = bg[f - 1];
+            pend_i = f;
         }
         issue_bwd(m + kDsAhead);
     }
     ds_wait<0>();
-    __syncthreads();
-    for (int q = tid; q < n; q += kDsThreads) bg[q] = b[q];
 }
 
 // buoyancy (momentum.f90:258-289): Bvec(p) = (Ra_T T_x - Ra_C C_x) r(p) on interior nodes, 0 on
@@ -536,11 +581,11 @@ int direct_alloc(Engine& E) {
     E.dkl = kl;
     E.dku = ku;
     E.dn = n;
-    // the substitution kernel keeps b and its column ring in shared memory (227 KB per CTA)
-    E.dahead = direct_solve_smem(n, kl, ku, 8) <= 227 * 1024 ? 8 : 2;
-    if (direct_solve_smem(n, kl, ku, E.dahead) > 227 * 1024)
-        return fail(PT_ERR_CONFIG, "direct solve: the grid is too large for the banded substitution kernel");
-    const int smem = (int)direct_solve_smem(n, kl, ku, E.dahead);
+    // the substitution kernel keeps its window of b and its column ring in shared memory
+    E.dahead = direct_solve_smem(kl, ku, 8) <= 227 * 1024 ? 8 : 2;
+    if (direct_solve_smem(kl, ku, E.dahead) > 227 * 1024)
+        return fail(PT_ERR_CONFIG, "direct solve: the band is too wide for the banded substitution kernel");
+    const int smem = (int)direct_solve_smem(kl, ku, E.dahead);
     if (E.dahead == 8) CK(cudaFuncSetAttribute(k_direct_solve<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     else CK(cudaFuncSetAttribute(k_direct_solve<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CK(cudaMalloc(&E.dMB, sizeof(double) * (size_t)ldab * (size_t)n));
@@ -628,9 +673,10 @@ int direct_solve(Engine& E, pt_solve_info* info) {
     const int n = E.dn, kl = E.dkl, ku = E.dku;
     PT_COUNT(), k_direct_rhs<<<nblk(n, 128), 128, 0, E.st>>>(E.dB, E.Tbuoy, E.Cbuoy, E.dRow, E.g1, n, E.cfg.comp,
                                                             E.cfg.RaT, E.cfg.RaC);
-    const size_t smem = direct_solve_smem(n, kl, ku, E.dahead);
-    if (E.dahead == 8) PT_COUNT(), k_direct_solve<8><<<1, kDsThreads, smem, E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku);
-    else PT_COUNT(), k_direct_solve<2><<<1, kDsThreads, smem, E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku);
+    const size_t smem = direct_solve_smem(kl, ku, E.dahead);
+    const int W = direct_window(kl, ku);
+    if (E.dahead == 8) PT_COUNT(), k_direct_solve<8><<<1, kDsThreads, smem, E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku, W);
+    else PT_COUNT(), k_direct_solve<2><<<1, kDsThreads, smem, E.st>>>(E.dMB, E.dipiv, E.dB, n, kl, ku, W);
     PT_COUNT(), k_direct_scatter<<<nblk(n, 128), 128, 0, E.st>>>(E.SF, E.dB, E.g1, E.K.nx, E.K.nz);
     PT_COUNT(), k_direct_images_x<<<nblk(3 * (E.K.nz + 1), 128), 128, 0, E.st>>>(E.SF, E.g1, E.K.nx, E.K.nz);
     PT_COUNT(), k_direct_images_z<<<nblk(3 * (E.K.nx + 7), 128), 128, 0, E.st>>>(E.SF, E.g1, E.K.nx, E.K.nz,
